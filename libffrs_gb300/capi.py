@@ -1,0 +1,139 @@
+"""ctypes view of the C ABI in include/ffgpu.h (libffgpu.so).
+
+This is the boundary a non-Python caller binds; tests and
+bench.py use it to drive the kernels with device pointers (e.g. torch tensors'
+data_ptr()) and CUDA streams.
+"""
+
+import ctypes
+import os
+import re
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libffgpu.so")
+HEADER = os.path.join(os.path.dirname(_HERE), "include", "ffgpu.h")
+
+OK = 0
+EINVAL = -1
+ECUDA = -2
+ENOMEM = -3
+EASSERT = -4
+ETIMEOUT = -5
+STATUS_ASSERT = 0xFF
+
+
+class FFGPUError(RuntimeError):
+    def __init__(self, rc, msg):
+        super().__init__(f"ffgpu error {rc}: {msg}")
+        self.rc = rc
+
+
+_lib = None
+
+
+def declared_symbols():
+    """Function names declared in include/ffgpu.h."""
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w[\w\s\*]*?\b(ffgpu_\w+)\s*\(", text, re.M)))
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libffgpu.so is not built")
+        L = ctypes.CDLL(LIB_PATH)
+        _declare(L)
+        _lib = L
+    return _lib
+
+
+_P = ctypes.c_void_p
+_SZ = ctypes.c_size_t
+_I = ctypes.c_int
+_U32 = ctypes.c_uint32
+_PP = ctypes.POINTER(ctypes.c_void_p)
+
+
+def _declare(L):
+    sig = {
+        "ffgpu_last_error": (ctypes.c_char_p, []),
+        "ffgpu_version": (ctypes.c_char_p, []),
+        "ffgpu_init": (_I, [_I]),
+        "ffgpu_kernel_launches": (ctypes.c_uint64, []),
+        "ffgpu_default_stream": (_P, []),
+        "ffgpu_synchronize": (_I, [_P]),
+        "ffgpu_host_alloc": (_I, [_SZ, _PP]),
+        "ffgpu_host_free": (_I, [_P]),
+        "ffgpu_rs256_create": (_I, [_I, _I, _I, _PP]),
+        "ffgpu_rs256_destroy": (_I, [_P]),
+        "ffgpu_rs256_generator": (_I, [_P, _P, _P]),
+        "ffgpu_rs256_encode": (_I, [_P, _P, _SZ, _SZ, _P, _P]),
+        "ffgpu_rs256_decode": (_I, [_P, _P, _P, _SZ, _SZ, _P, _P]),
+        "ffgpu_rs256_synds": (_I, [_P, _P, _P, _SZ, _SZ, _P, _P]),
+        "ffgpu_rs256_encode_host": (_I, [_P, _P, _SZ, _SZ, _P]),
+        "ffgpu_rs256_decode_host": (_I, [_P, _P, _P, _SZ, _SZ, _P]),
+        "ffgpu_rs256_synds_host": (_I, [_P, _P, _P, _SZ, _SZ, _P]),
+        "ffgpu_rsi16_create": (_I, [_SZ, _SZ, _U32, _PP]),
+        "ffgpu_rsi16_destroy": (_I, [_P]),
+        "ffgpu_rsi16_info": (_I, [_P, ctypes.POINTER(_U32), ctypes.POINTER(_SZ)]),
+        "ffgpu_rsi16_encode": (_I, [_P, _P, _SZ, _P, _P]),
+        "ffgpu_rsi16_encode_interleaved": (_I, [_P, _P, _SZ, _SZ, _P, _P]),
+        "ffgpu_rsi16_repair": (_I, [_P, _P, _P, _SZ, _P, _P]),
+        "ffgpu_rsi16_repair_interleaved": (_I, [_P, _P, _P, _SZ, _P, _SZ, _P, _P]),
+        "ffgpu_rsi16_repair_known": (_I, [_P, _P, _P, _SZ, _P, _SZ, _P, _P]),
+        "ffgpu_rsi16_synd": (_I, [_P, _P, _P, _SZ, _P, _P]),
+        "ffgpu_rsi16_sugiyama": (_I, [_P, _P, _SZ, _P, _P, _P, _P]),
+        "ffgpu_rsi16_roots": (_I, [_P, _P, _P, _P]),
+        "ffgpu_rsi16_encode_host": (_I, [_P, _P, _SZ, _SZ, _P]),
+        "ffgpu_rsi16_repair_host": (_I, [_P, _P, _P, _SZ, _SZ, _P, ctypes.c_long, _P]),
+        "ffgpu_circ16_create": (_I, [_SZ, _SZ, _SZ, _SZ, _SZ, _U32, _PP]),
+        "ffgpu_circ16_destroy": (_I, [_P]),
+        "ffgpu_circ16_info": (_I, [_P, ctypes.POINTER(_SZ), ctypes.POINTER(_SZ)]),
+        "ffgpu_circ16_encode": (_I, [_P, _P, _SZ, _P, _P]),
+        "ffgpu_circ16_repair": (_I, [_P, _P, _P, _SZ, _P, _P]),
+        "ffgpu_circ16_find_outer_error_locations": (_I, [_P, _P, _P, _SZ, _P, _P]),
+        "ffgpu_circ16_encode_host": (_I, [_P, _P, _SZ, _P]),
+        "ffgpu_circ16_repair_host": (_I, [_P, _P, _P, _SZ, _P]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name, None)
+        if f is None:
+            continue
+        f.restype = res
+        f.argtypes = args
+
+
+def check(rc):
+    if rc != OK:
+        raise FFGPUError(rc, lib().ffgpu_last_error().decode())
+    return rc
+
+
+def call(name, *args):
+    return check(getattr(lib(), name)(*args))
+
+
+class RS256Code:
+    """Device-resident RS256 code handle (ffgpu_rs256)."""
+
+    def __init__(self, ecc_len, primitive=2, polynomial=0x11D):
+        h = ctypes.c_void_p()
+        call("ffgpu_rs256_create", ecc_len, primitive, polynomial, ctypes.byref(h))
+        self.h = h
+        self.ecc_len = ecc_len
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.ffgpu_rs256_destroy(self.h)
+            self.h = None
+
+    def encode(self, data_ptr, nblocks, message_len, parity_ptr, stream=None):
+        call("ffgpu_rs256_encode", self.h, data_ptr, nblocks, message_len, parity_ptr, stream)
+
+    def decode(self, data_ptr, parity_ptr, nblocks, message_len, status_ptr, stream=None):
+        call("ffgpu_rs256_decode", self.h, data_ptr, parity_ptr, nblocks, message_len, status_ptr, stream)
+
+
+def kernel_launches():
+    return int(lib().ffgpu_kernel_launches())

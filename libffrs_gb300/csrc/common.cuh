@@ -1,0 +1,111 @@
+// Shared runtime pieces of libffgpu: error reporting, launch accounting, the
+// library stream and reusable device / pinned staging buffers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+
+#include "../../include/ffgpu.h"
+
+namespace ffgpu {
+
+void set_error(const std::string &msg);
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+#define FFGPU_CHECK_CUDA(expr)                                                                        \
+    do {                                                                                              \
+        cudaError_t _e = (expr);                                                                      \
+        if (_e != cudaSuccess)                                                                        \
+            throw ::ffgpu::Error(FFGPU_ECUDA, std::string(#expr) + ": " + cudaGetErrorString(_e)); \
+    } while (0)
+
+#define FFGPU_REQUIRE(cond, msg)                                      \
+    do {                                                              \
+        if (!(cond)) throw ::ffgpu::Error(FFGPU_EINVAL, (msg));        \
+    } while (0)
+
+// Every kernel launch in the library goes through this counter so callers can
+// report how many kernels ran inside a timed region.
+extern std::atomic<uint64_t> g_launches;
+
+inline void launched(int n = 1) { g_launches.fetch_add((uint64_t)n, std::memory_order_relaxed); }
+
+inline void check_launch(const char *what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) throw Error(FFGPU_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    launched();
+}
+
+cudaStream_t lib_stream();
+
+// Grow-only device scratch owned by one code object (not thread-safe by
+// design: one code object is used from one host thread at a time).
+struct DeviceBuffer {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    void *get(size_t need) {
+        if (need > bytes) {
+            if (ptr) cudaFree(ptr);
+            ptr = nullptr;
+            bytes = 0;
+            size_t want = need < 256 ? 256 : need;
+            if (cudaMalloc(&ptr, want) != cudaSuccess) throw Error(FFGPU_ENOMEM, "cudaMalloc failed");
+            bytes = want;
+        }
+        return ptr;
+    }
+    ~DeviceBuffer() {
+        if (ptr) cudaFree(ptr);
+    }
+};
+
+struct PinnedBuffer {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    void *get(size_t need) {
+        if (need > bytes) {
+            if (ptr) cudaFreeHost(ptr);
+            ptr = nullptr;
+            bytes = 0;
+            size_t want = need < 4096 ? 4096 : need;
+            if (cudaMallocHost(&ptr, want) != cudaSuccess) throw Error(FFGPU_ENOMEM, "cudaMallocHost failed");
+            bytes = want;
+        }
+        return ptr;
+    }
+    ~PinnedBuffer() {
+        if (ptr) cudaFreeHost(ptr);
+    }
+};
+
+// Runs `f` and converts exceptions into a status code + last-error message.
+template <typename F>
+int guarded(F &&f) {
+    try {
+        f();
+        return FFGPU_OK;
+    } catch (const Error &e) {
+        set_error(e.what());
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        set_error("out of host memory");
+        return FFGPU_ENOMEM;
+    } catch (const std::exception &e) {
+        set_error(e.what());
+        return FFGPU_EINVAL;
+    }
+}
+
+inline unsigned grid_for(size_t n, unsigned block) { return (unsigned)((n + block - 1) / block); }
+
+}  // namespace ffgpu

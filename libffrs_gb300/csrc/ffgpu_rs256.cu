@@ -1,0 +1,210 @@
+// C ABI: runtime helpers and the RS256 entry points.
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+
+#include "common.cuh"
+#include "rs256.cuh"
+
+namespace ffgpu {
+
+std::atomic<uint64_t> g_launches{0};
+static thread_local std::string t_last_error;
+void set_error(const std::string &msg) { t_last_error = msg; }
+
+static std::mutex g_stream_mu;
+static cudaStream_t g_stream = nullptr;
+static int g_device = 0;
+
+cudaStream_t lib_stream() {
+    std::lock_guard<std::mutex> lk(g_stream_mu);
+    if (!g_stream) {
+        FFGPU_CHECK_CUDA(cudaSetDevice(g_device));
+        FFGPU_CHECK_CUDA(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking));
+    }
+    return g_stream;
+}
+
+}  // namespace ffgpu
+
+using namespace ffgpu;
+
+struct ffgpu_rs256 {
+    std::unique_ptr<Rs256Code> code;
+    std::mutex mu;
+    DeviceBuffer d_data, d_parity, d_status;
+};
+
+extern "C" {
+
+const char *ffgpu_last_error(void) { return t_last_error.c_str(); }
+const char *ffgpu_version(void) { return "libffrs-gb300 0.1.0 (sm_103a)"; }
+uint64_t ffgpu_kernel_launches(void) { return g_launches.load(); }
+
+int ffgpu_init(int device) {
+    return guarded([&] {
+        int n = 0;
+        FFGPU_CHECK_CUDA(cudaGetDeviceCount(&n));
+        FFGPU_REQUIRE(device >= 0 && device < n, "no such CUDA device");
+        g_device = device;
+        FFGPU_CHECK_CUDA(cudaSetDevice(device));
+    });
+}
+
+void *ffgpu_default_stream(void) {
+    void *s = nullptr;
+    guarded([&] { s = (void *)lib_stream(); });
+    return s;
+}
+
+int ffgpu_synchronize(void *stream) {
+    return guarded([&] { FFGPU_CHECK_CUDA(cudaStreamSynchronize(stream ? (cudaStream_t)stream : lib_stream())); });
+}
+
+int ffgpu_host_alloc(size_t bytes, void **out) {
+    return guarded([&] {
+        FFGPU_REQUIRE(out, "out is NULL");
+        void *p = nullptr;
+        if (cudaHostAlloc(&p, bytes ? bytes : 1, cudaHostAllocPortable) != cudaSuccess)
+            throw Error(FFGPU_ENOMEM, "cudaHostAlloc failed");
+        std::memset(p, 0, bytes);
+        *out = p;
+    });
+}
+
+int ffgpu_host_free(void *ptr) {
+    return guarded([&] {
+        if (ptr) FFGPU_CHECK_CUDA(cudaFreeHost(ptr));
+    });
+}
+
+int ffgpu_rs256_create(int ecc_len, int primitive, int polynomial, ffgpu_rs256 **out) {
+    return guarded([&] {
+        FFGPU_REQUIRE(out, "out is NULL");
+        lib_stream();
+        auto h = std::make_unique<ffgpu_rs256>();
+        h->code = std::make_unique<Rs256Code>(ecc_len, primitive, polynomial);
+        *out = h.release();
+    });
+}
+
+int ffgpu_rs256_destroy(ffgpu_rs256 *code) {
+    return guarded([&] { delete code; });
+}
+
+int ffgpu_rs256_generator(const ffgpu_rs256 *code, uint8_t *generator, uint8_t *roots) {
+    return guarded([&] {
+        FFGPU_REQUIRE(code, "code is NULL");
+        const Rs256Code &c = *code->code;
+        if (generator) std::memcpy(generator, c.generator, (size_t)c.ecc + 1);
+        if (roots) std::memcpy(roots, c.roots, (size_t)c.ecc);
+    });
+}
+
+static void check_rs_geometry(const Rs256Code &c, size_t message_len) {
+    FFGPU_REQUIRE(message_len >= 1 && message_len + (size_t)c.ecc <= 255, "block_len must be <= 255");
+}
+
+int ffgpu_rs256_encode(const ffgpu_rs256 *code, const uint8_t *data, size_t nblocks, size_t message_len,
+                       uint8_t *parity, void *stream) {
+    return guarded([&] {
+        FFGPU_REQUIRE(code, "code is NULL");
+        check_rs_geometry(*code->code, message_len);
+        rs256_encode(*code->code, data, nblocks, (int)message_len, parity,
+                     stream ? (cudaStream_t)stream : lib_stream());
+    });
+}
+
+int ffgpu_rs256_decode(const ffgpu_rs256 *code, uint8_t *data, uint8_t *parity, size_t nblocks, size_t message_len,
+                       uint8_t *status, void *stream) {
+    return guarded([&] {
+        FFGPU_REQUIRE(code, "code is NULL");
+        check_rs_geometry(*code->code, message_len);
+        rs256_decode(*code->code, data, parity, nblocks, (int)message_len, status,
+                     stream ? (cudaStream_t)stream : lib_stream());
+    });
+}
+
+int ffgpu_rs256_synds(const ffgpu_rs256 *code, const uint8_t *data, const uint8_t *parity, size_t nblocks,
+                      size_t message_len, uint8_t *synds, void *stream) {
+    return guarded([&] {
+        FFGPU_REQUIRE(code, "code is NULL");
+        check_rs_geometry(*code->code, message_len);
+        rs256_decode_table(*code->code, const_cast<uint8_t *>(data), const_cast<uint8_t *>(parity), nblocks,
+                           (int)message_len, nullptr, synds, stream ? (cudaStream_t)stream : lib_stream());
+    });
+}
+
+int ffgpu_rs256_encode_host(const ffgpu_rs256 *code, const uint8_t *buf, size_t len, size_t message_len,
+                            uint8_t *out) {
+    return guarded([&] {
+        FFGPU_REQUIRE(code, "code is NULL");
+        ffgpu_rs256 *h = const_cast<ffgpu_rs256 *>(code);
+        const Rs256Code &c = *h->code;
+        check_rs_geometry(c, message_len);
+        if (len == 0) return;
+        std::lock_guard<std::mutex> lk(h->mu);
+        cudaStream_t st = lib_stream();
+        const size_t full = len / message_len, tail = len - full * message_len;
+        const size_t nout = (full + (tail ? 1 : 0)) * (size_t)c.ecc;
+        uint8_t *d_in = (uint8_t *)h->d_data.get(len);
+        uint8_t *d_out = (uint8_t *)h->d_parity.get(nout);
+        FFGPU_CHECK_CUDA(cudaMemcpyAsync(d_in, buf, len, cudaMemcpyHostToDevice, st));
+        rs256_encode(c, d_in, full, (int)message_len, d_out, st);
+        if (tail) rs256_encode(c, d_in + full * message_len, 1, (int)tail, d_out + full * (size_t)c.ecc, st);
+        FFGPU_CHECK_CUDA(cudaMemcpyAsync(out, d_out, nout, cudaMemcpyDeviceToHost, st));
+        FFGPU_CHECK_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+int ffgpu_rs256_decode_host(const ffgpu_rs256 *code, uint8_t *data, uint8_t *parity, size_t nblocks,
+                            size_t message_len, uint8_t *status) {
+    return guarded([&] {
+        FFGPU_REQUIRE(code, "code is NULL");
+        ffgpu_rs256 *h = const_cast<ffgpu_rs256 *>(code);
+        const Rs256Code &c = *h->code;
+        check_rs_geometry(c, message_len);
+        if (nblocks == 0) return;
+        std::lock_guard<std::mutex> lk(h->mu);
+        cudaStream_t st = lib_stream();
+        const size_t nd = nblocks * message_len, np = nblocks * (size_t)c.ecc;
+        uint8_t *d_d = (uint8_t *)h->d_data.get(nd);
+        uint8_t *d_p = (uint8_t *)h->d_parity.get(np);
+        uint8_t *d_s = (uint8_t *)h->d_status.get(nblocks);
+        FFGPU_CHECK_CUDA(cudaMemcpyAsync(d_d, data, nd, cudaMemcpyHostToDevice, st));
+        FFGPU_CHECK_CUDA(cudaMemcpyAsync(d_p, parity, np, cudaMemcpyHostToDevice, st));
+        rs256_decode(c, d_d, d_p, nblocks, (int)message_len, d_s, st);
+        FFGPU_CHECK_CUDA(cudaMemcpyAsync(data, d_d, nd, cudaMemcpyDeviceToHost, st));
+        FFGPU_CHECK_CUDA(cudaMemcpyAsync(parity, d_p, np, cudaMemcpyDeviceToHost, st));
+        FFGPU_CHECK_CUDA(cudaMemcpyAsync(status, d_s, nblocks, cudaMemcpyDeviceToHost, st));
+        FFGPU_CHECK_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+int ffgpu_rs256_synds_host(const ffgpu_rs256 *code, const uint8_t *data, const uint8_t *parity, size_t nblocks,
+                           size_t message_len, uint8_t *synds) {
+    return guarded([&] {
+        FFGPU_REQUIRE(code, "code is NULL");
+        ffgpu_rs256 *h = const_cast<ffgpu_rs256 *>(code);
+        const Rs256Code &c = *h->code;
+        check_rs_geometry(c, message_len);
+        if (nblocks == 0) return;
+        std::lock_guard<std::mutex> lk(h->mu);
+        cudaStream_t st = lib_stream();
+        const size_t nd = nblocks * message_len, np = nblocks * (size_t)c.ecc;
+        uint8_t *d_d = (uint8_t *)h->d_data.get(nd);
+        uint8_t *d_p = (uint8_t *)h->d_parity.get(np);
+        uint8_t *d_s = (uint8_t *)h->d_status.get(np);
+        FFGPU_CHECK_CUDA(cudaMemcpyAsync(d_d, data, nd, cudaMemcpyHostToDevice, st));
+        FFGPU_CHECK_CUDA(cudaMemcpyAsync(d_p, parity, np, cudaMemcpyHostToDevice, st));
+        rs256_decode_table(c, d_d, d_p, nblocks, (int)message_len, nullptr, d_s, st);
+        FFGPU_CHECK_CUDA(cudaMemcpyAsync(synds, d_s, np, cudaMemcpyDeviceToHost, st));
+        FFGPU_CHECK_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+}  // extern "C"

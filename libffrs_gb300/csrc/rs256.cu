@@ -1,0 +1,358 @@
+// RS256: Reed-Solomon over GF(2^8) -- code objects and the table-driven
+// kernels that serve every (ecc_len, primitive, polynomial, length).
+//
+// Encoder (reed_solomon.hpp:169-297): a byte-serial LFSR over the row table
+// lut[v] = v * x^ecc mod g held in shared memory as 32-bit words, one thread
+// per block.  The reference's slicing-by-N loops combine N rows of this same
+// linear table, so for a field the parity is identical.
+//
+// Decoder (reed_solomon.hpp:559-595): one thread per block.  The remainder
+// R = r(x) * x^ecc mod g is formed with the same LFSR; R == 0 exactly when all
+// syndromes vanish.  Otherwise S_j = r(a^j) = sum_m R[m] a^{-j(m+1)}, followed
+// by the reference's Berlekamp-Massey (:655-702), its root search over
+// positions [0, size + ecc) (:516-537), Forney (:704-743) and the in-place
+// correction (:583-592).  A block whose decode fails is left untouched.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <vector>
+
+#include "common.cuh"
+#include "gf256.h"
+#include "rs256.cuh"
+
+namespace ffgpu {
+
+// ---------------------------------------------------------------- device
+
+// multiply with a 512-entry exp table (ex[i] = a^(i mod 255), i <= 510)
+__device__ __forceinline__ uint32_t gmul(const uint8_t *ex, const uint8_t *lg, uint32_t a, uint32_t b) {
+    return (a && b) ? ex[lg[a] + lg[b]] : 0u;
+}
+__device__ __forceinline__ uint32_t gdiv(const uint8_t *ex, const uint8_t *lg, uint32_t a, uint32_t b) {
+    return a ? ex[lg[a] + 255u - lg[b]] : 0u;
+}
+__device__ __forceinline__ uint32_t ginv(const uint8_t *ex, const uint8_t *lg, uint32_t a) {
+    return ex[255u - lg[a]];
+}
+
+// Cooperative byte copy global -> shared (coalesced, any alignment).
+__device__ __forceinline__ void stage_bytes(uint8_t *dst, const uint8_t *src, size_t n) {
+    for (size_t i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+}
+
+// One LFSR step: rem <- (rem >> 8) ^ lut[(rem & 0xff) ^ in], rem held as W words.
+template <int W>
+__device__ __forceinline__ void lfsr_step(uint32_t (&rem)[W], uint32_t in, const uint32_t *s_lut) {
+    const uint32_t fb = (rem[0] & 0xffu) ^ in;
+    const uint32_t *row = s_lut + fb * W;
+#pragma unroll
+    for (int w = 0; w < W - 1; ++w) rem[w] = __funnelshift_r(rem[w], rem[w + 1], 8) ^ row[w];
+    rem[W - 1] = (rem[W - 1] >> 8) ^ row[W - 1];
+}
+
+template <int W>
+__device__ __forceinline__ uint32_t rem_byte(const uint32_t (&rem)[W], int j) {
+    uint32_t v = 0;
+#pragma unroll
+    for (int w = 0; w < W; ++w)
+        if (w == (j >> 2)) v = rem[w];
+    return (v >> ((j & 3) * 8)) & 0xffu;
+}
+
+template <int W>
+__global__ void __launch_bounds__(128) rs256_encode_table_kernel(const uint8_t *__restrict__ data, size_t nblocks,
+                                                                 int msg_len, const uint32_t *__restrict__ lut,
+                                                                 int ecc, uint8_t *__restrict__ parity) {
+    extern __shared__ uint32_t smem[];
+    uint32_t *s_lut = smem;
+    uint8_t *s_data = reinterpret_cast<uint8_t *>(smem + 256 * W);
+    for (int i = threadIdx.x; i < 256 * W; i += blockDim.x) s_lut[i] = lut[i];
+    const size_t first = (size_t)blockIdx.x * blockDim.x;
+    const size_t nb = min((size_t)blockDim.x, nblocks - first);
+    stage_bytes(s_data, data + first * (size_t)msg_len, nb * (size_t)msg_len);
+    __syncthreads();
+    if (threadIdx.x >= nb) return;
+    uint32_t rem[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) rem[w] = 0;
+    const uint8_t *my = s_data + (size_t)threadIdx.x * msg_len;
+    for (int i = 0; i < msg_len; ++i) lfsr_step<W>(rem, my[i], s_lut);
+    uint8_t *out = parity + (first + threadIdx.x) * (size_t)ecc;
+    for (int j = 0; j < ecc; ++j) out[j] = (uint8_t)rem_byte<W>(rem, j);
+}
+
+struct DecodeScratch {
+    uint8_t S[256], lam[256], prev[256], tmp[256], pos[256], mag[256], ev[512];
+};
+
+// Syndromes from the remainder: S_j = sum_m R[m] a^{-j(m+1)}.
+template <int W>
+__device__ void synds_from_rem(const uint32_t (&rem)[W], int ecc, const uint8_t *ex, const uint8_t *lg, uint8_t *S) {
+    for (int j = 0; j < ecc; ++j) S[j] = 0;
+    for (int m = 0; m < ecc; ++m) {
+        const uint32_t r = rem_byte<W>(rem, m);
+        if (!r) continue;
+        const int step = (m + 1) % 255;
+        int e = lg[r] % 255;
+        for (int j = 0; j < ecc; ++j) {
+            S[j] ^= ex[e];
+            e -= step;
+            if (e < 0) e += 255;
+        }
+    }
+}
+
+// rs_decode::berlekamp_massey (reed_solomon.hpp:655-702); err_poly is
+// right-aligned and reversed: err_poly[ecc-1-i] holds Lambda_i.
+__device__ int rs_bm(const uint8_t *S, int ecc, const uint8_t *ex, const uint8_t *lg, uint8_t *err_poly, uint8_t *prev,
+                     uint8_t *temp) {
+    for (int i = 0; i < ecc; ++i) {
+        prev[i] = 0;
+        err_poly[i] = 0;
+    }
+    prev[ecc - 1] = 1;
+    err_poly[ecc - 1] = 1;
+    int errors = 0, m = 1;
+    uint32_t b = 1;
+    for (int n = 0; n < ecc; ++n) {
+        uint32_t d = S[n];
+        for (int i = 1; i < errors + 1; ++i) d ^= gmul(ex, lg, err_poly[ecc - 1 - i], S[n - i]);
+        if (d == 0) {
+            m = m + 1;
+        } else if (2 * errors <= n) {
+            for (int i = 0; i < ecc; ++i) temp[i] = err_poly[i];
+            const uint32_t s = gdiv(ex, lg, d, b);
+            for (int i = 0; i < ecc; ++i) {
+                const uint32_t p = (i < ecc - m) ? prev[i + m] : 0u;
+                err_poly[i] ^= gmul(ex, lg, s, p);
+            }
+            errors = n + 1 - errors;
+            for (int i = 0; i < ecc; ++i) prev[i] = temp[i];
+            b = d;
+            m = 1;
+        } else {
+            const uint32_t s = gdiv(ex, lg, d, b);
+            for (int i = 0; i < ecc; ++i) {
+                const uint32_t p = (i < ecc - m) ? prev[i + m] : 0u;
+                err_poly[i] ^= gmul(ex, lg, s, p);
+            }
+            m = m + 1;
+        }
+    }
+    return errors;
+}
+
+__device__ __forceinline__ uint32_t poly_eval(const uint8_t *p, int n, uint32_t x, const uint8_t *ex,
+                                              const uint8_t *lg) {
+    uint32_t r = 0;
+    for (int i = 0; i < n; ++i) r = gmul(ex, lg, r, x) ^ p[i];
+    return r;
+}
+
+template <int W>
+__global__ void __launch_bounds__(128) rs256_decode_table_kernel(uint8_t *__restrict__ data,
+                                                                 uint8_t *__restrict__ parity, size_t nblocks,
+                                                                 int msg_len, const uint32_t *__restrict__ lut,
+                                                                 const uint8_t *__restrict__ exp512,
+                                                                 const uint8_t *__restrict__ log256, int ecc,
+                                                                 uint8_t *__restrict__ status,
+                                                                 uint8_t *__restrict__ synds_out) {
+    extern __shared__ uint32_t smem[];
+    uint32_t *s_lut = smem;
+    uint8_t *ex = reinterpret_cast<uint8_t *>(smem + 256 * W);
+    uint8_t *lg = ex + 512;
+    for (int i = threadIdx.x; i < 256 * W; i += blockDim.x) s_lut[i] = lut[i];
+    for (int i = threadIdx.x; i < 512; i += blockDim.x) ex[i] = exp512[i];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) lg[i] = log256[i];
+    __syncthreads();
+    const size_t blk = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (blk >= nblocks) return;
+    uint8_t *d = data + blk * (size_t)msg_len;
+    uint8_t *p = parity + blk * (size_t)ecc;
+
+    uint32_t rem[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) rem[w] = 0;
+    for (int i = 0; i < msg_len; ++i) lfsr_step<W>(rem, d[i], s_lut);
+    for (int i = 0; i < ecc; ++i) lfsr_step<W>(rem, p[i], s_lut);
+
+    uint32_t any = 0;
+#pragma unroll
+    for (int w = 0; w < W; ++w) any |= rem[w];
+
+    DecodeScratch sc;
+    if (synds_out) {
+        if (any)
+            synds_from_rem<W>(rem, ecc, ex, lg, sc.S);
+        else
+            for (int j = 0; j < ecc; ++j) sc.S[j] = 0;
+        for (int j = 0; j < ecc; ++j) synds_out[blk * (size_t)ecc + j] = sc.S[j];
+        return;
+    }
+    if (!any) {
+        status[blk] = 1;
+        return;
+    }
+    synds_from_rem<W>(rem, ecc, ex, lg, sc.S);
+    const int errors = rs_bm(sc.S, ecc, ex, lg, sc.lam, sc.prev, sc.tmp);
+    if (errors > ecc / 2) {
+        status[blk] = 0;
+        return;
+    }
+    const uint8_t *loc = &sc.lam[ecc - errors - 1];
+    const int size = msg_len + ecc;
+    int roots = 0;
+    for (int i = 0; i < size && i < 256; ++i) {
+        const uint32_t x = ex[(255 - i) % 255];
+        if (poly_eval(loc, errors + 1, x, ex, lg) == 0) sc.pos[roots++] = (uint8_t)i;
+        if (roots > errors) break;
+    }
+    if (roots != errors) {
+        status[blk] = 0;
+        return;
+    }
+    // Forney: omega = (S reversed * Lambda) mod x^ecc, highest degree first
+    const int esize = ecc + errors;
+    for (int i = 0; i < esize; ++i) sc.ev[i] = 0;
+    for (int i = 0; i < ecc; ++i)
+        for (int j = 0; j < errors + 1; ++j) sc.ev[i + j] ^= gmul(ex, lg, sc.S[ecc - 1 - i], loc[j]);
+    int begin = errors;
+    while (begin < esize && sc.ev[begin] == 0) ++begin;
+    if (begin >= esize) {
+        status[blk] = 0;
+        return;
+    }
+    // formal derivative in place (gf_poly_deriv_pw2, galois.hpp:725-734)
+    uint8_t *lp = &sc.lam[ecc - errors - 1];
+    const int psize = errors + 1;
+    for (int i = 1; i < psize; ++i) lp[psize - i] = (i & 1) ? lp[psize - i - 1] : 0;
+    for (int i = 0; i < errors; ++i) {
+        const uint32_t xi = ex[sc.pos[i]];
+        const uint32_t xinv = ginv(ex, lg, xi);
+        const uint32_t num = poly_eval(&sc.ev[begin], esize - begin, xinv, ex, lg);
+        const uint32_t den = poly_eval(lp + 1, errors, xinv, ex, lg);
+        sc.mag[i] = (uint8_t)gmul(ex, lg, xi, gdiv(ex, lg, num, den));
+    }
+    for (int i = 0; i < errors; ++i) {
+        const int pos = size - 1 - sc.pos[i];
+        if (pos < msg_len)
+            d[pos] ^= sc.mag[i];
+        else
+            p[pos - msg_len] ^= sc.mag[i];
+    }
+    status[blk] = 1;
+}
+
+// ---------------------------------------------------------------- host
+
+static int bucket_words(int ecc) {
+    const int w = (ecc + 3) / 4;
+    int b = 1;
+    while (b < w) b *= 2;
+    return b;
+}
+
+Rs256Code::Rs256Code(int ecc_, int primitive_, int polynomial_)
+    : gf((uint8_t)primitive_, (uint8_t)(polynomial_ & 0xff)), ecc(ecc_), primitive(primitive_),
+      polynomial(polynomial_) {
+    FFGPU_REQUIRE(ecc_ >= 1 && ecc_ <= 254, "ecc_len must be in [1, 254]");
+    FFGPU_REQUIRE(gf.is_field(), "primitive does not generate GF(2^8) with this polynomial");
+    rs256_generator(gf, ecc, generator, roots);
+    std::vector<uint8_t> lut;
+    rs256_lut(gf, ecc, generator, lut);
+    W = bucket_words(ecc);
+    lut_words.assign((size_t)256 * W, 0);
+    for (int v = 0; v < 256; ++v)
+        for (int j = 0; j < ecc; ++j)
+            lut_words[(size_t)v * W + j / 4] |= (uint32_t)lut[(size_t)v * ecc + j] << (8 * (j % 4));
+    uint8_t exp512[512], log256[256];
+    for (int i = 0; i < 512; ++i) exp512[i] = gf.exp[i % 255];
+    std::memcpy(log256, gf.log, 256);
+    FFGPU_CHECK_CUDA(cudaMalloc(&d_lut, lut_words.size() * 4));
+    FFGPU_CHECK_CUDA(cudaMalloc(&d_exp512, 512));
+    FFGPU_CHECK_CUDA(cudaMalloc(&d_log256, 256));
+    FFGPU_CHECK_CUDA(cudaMemcpy(d_lut, lut_words.data(), lut_words.size() * 4, cudaMemcpyHostToDevice));
+    FFGPU_CHECK_CUDA(cudaMemcpy(d_exp512, exp512, 512, cudaMemcpyHostToDevice));
+    FFGPU_CHECK_CUDA(cudaMemcpy(d_log256, log256, 256, cudaMemcpyHostToDevice));
+    fast = rs256_fast_init(*this);
+}
+
+Rs256Code::~Rs256Code() {
+    rs256_fast_free(*this);
+    if (d_lut) cudaFree(d_lut);
+    if (d_exp512) cudaFree(d_exp512);
+    if (d_log256) cudaFree(d_log256);
+}
+
+template <int W>
+static void launch_encode_table(const Rs256Code &c, const uint8_t *data, size_t nblocks, int msg_len, uint8_t *parity,
+                                cudaStream_t st) {
+    const unsigned threads = 128;
+    const size_t smem = (size_t)256 * W * 4 + (size_t)threads * msg_len + 16;
+    static bool attr = false;
+    if (!attr) {
+        FFGPU_CHECK_CUDA(cudaFuncSetAttribute(rs256_encode_table_kernel<W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              200 * 1024));
+        attr = true;
+    }
+    rs256_encode_table_kernel<W><<<grid_for(nblocks, threads), threads, smem, st>>>(data, nblocks, msg_len, c.d_lut,
+                                                                                    c.ecc, parity);
+    check_launch("rs256_encode_table_kernel");
+}
+
+template <int W>
+static void launch_decode_table(const Rs256Code &c, uint8_t *data, uint8_t *parity, size_t nblocks, int msg_len,
+                                uint8_t *status, uint8_t *synds, cudaStream_t st) {
+    const unsigned threads = 128;
+    const size_t smem = (size_t)256 * W * 4 + 768;
+    static bool attr = false;
+    if (!attr) {
+        FFGPU_CHECK_CUDA(cudaFuncSetAttribute(rs256_decode_table_kernel<W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              200 * 1024));
+        attr = true;
+    }
+    rs256_decode_table_kernel<W><<<grid_for(nblocks, threads), threads, smem, st>>>(
+        data, parity, nblocks, msg_len, c.d_lut, c.d_exp512, c.d_log256, c.ecc, status, synds);
+    check_launch("rs256_decode_table_kernel");
+}
+
+#define FFGPU_W_DISPATCH(W, CALL)          \
+    switch (W) {                           \
+        case 1: { constexpr int w_ = 1; CALL; } break;   \
+        case 2: { constexpr int w_ = 2; CALL; } break;   \
+        case 4: { constexpr int w_ = 4; CALL; } break;   \
+        case 8: { constexpr int w_ = 8; CALL; } break;   \
+        case 16: { constexpr int w_ = 16; CALL; } break; \
+        case 32: { constexpr int w_ = 32; CALL; } break; \
+        default: { constexpr int w_ = 64; CALL; } break; \
+    }
+
+void rs256_encode_table(const Rs256Code &c, const uint8_t *data, size_t nblocks, int msg_len, uint8_t *parity,
+                        cudaStream_t st) {
+    if (nblocks == 0) return;
+    FFGPU_W_DISPATCH(c.W, (launch_encode_table<w_>(c, data, nblocks, msg_len, parity, st)));
+}
+
+void rs256_decode_table(const Rs256Code &c, uint8_t *data, uint8_t *parity, size_t nblocks, int msg_len,
+                        uint8_t *status, uint8_t *synds, cudaStream_t st) {
+    if (nblocks == 0) return;
+    FFGPU_W_DISPATCH(c.W, (launch_decode_table<w_>(c, data, parity, nblocks, msg_len, status, synds, st)));
+}
+
+void rs256_encode(const Rs256Code &c, const uint8_t *data, size_t nblocks, int msg_len, uint8_t *parity,
+                  cudaStream_t st) {
+    if (nblocks == 0) return;
+    if (c.fast && rs256_fast_encode(c, data, nblocks, msg_len, parity, st)) return;
+    rs256_encode_table(c, data, nblocks, msg_len, parity, st);
+}
+
+void rs256_decode(const Rs256Code &c, uint8_t *data, uint8_t *parity, size_t nblocks, int msg_len, uint8_t *status,
+                  cudaStream_t st) {
+    if (nblocks == 0) return;
+    if (c.fast && rs256_fast_decode(c, data, parity, nblocks, msg_len, status, st)) return;
+    rs256_decode_table(c, data, parity, nblocks, msg_len, status, nullptr, st);
+}
+
+}  // namespace ffgpu
