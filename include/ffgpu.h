@@ -19,6 +19,12 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#if defined(__GNUC__)
+#define FFGPU_API __attribute__((visibility("default")))
+#else
+#define FFGPU_API
+#endif
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -44,120 +50,120 @@ typedef struct ffgpu_rsi16 ffgpu_rsi16;
 typedef struct ffgpu_circ16 ffgpu_circ16;
 
 /* ---------------------------------------------------------------- runtime */
-const char *ffgpu_last_error(void);
-const char *ffgpu_version(void);
+FFGPU_API const char *ffgpu_last_error(void);
+FFGPU_API const char *ffgpu_version(void);
 /* select the device used by later calls on this process (default 0) */
-int ffgpu_init(int device);
+FFGPU_API int ffgpu_init(int device);
 /* number of kernels this library has launched since load (for accounting) */
-uint64_t ffgpu_kernel_launches(void);
+FFGPU_API uint64_t ffgpu_kernel_launches(void);
 /* the library's own stream (cudaStream_t) */
-void *ffgpu_default_stream(void);
-int ffgpu_synchronize(void *stream);
+FFGPU_API void *ffgpu_default_stream(void);
+FFGPU_API int ffgpu_synchronize(void *stream);
 
 /* create_buffer (libffrs/pyffrs.cpp:41-98): zeroed, page-locked host memory */
-int ffgpu_host_alloc(size_t bytes, void **out);
-int ffgpu_host_free(void *ptr);
+FFGPU_API int ffgpu_host_alloc(size_t bytes, void **out);
+FFGPU_API int ffgpu_host_free(void *ptr);
 
 /* ---------------------------------------------------------------- RS256 */
 /* PyRS256 ctor (libffrs/pyrs256.hpp:63-97): GF(2^8) tables, generator and the
  * encoder's table, resident on the device.  ecc_len in [1, 254]. */
-int ffgpu_rs256_create(int ecc_len, int primitive, int polynomial, ffgpu_rs256 **out);
-int ffgpu_rs256_destroy(ffgpu_rs256 *code);
+FFGPU_API int ffgpu_rs256_create(int ecc_len, int primitive, int polynomial, ffgpu_rs256 **out);
+FFGPU_API int ffgpu_rs256_destroy(ffgpu_rs256 *code);
 /* generator (ecc_len + 1 bytes) and generator_roots (ecc_len bytes),
  * pyrs256.hpp:165-169 */
-int ffgpu_rs256_generator(const ffgpu_rs256 *code, uint8_t *generator, uint8_t *roots);
+FFGPU_API int ffgpu_rs256_generator(const ffgpu_rs256 *code, uint8_t *generator, uint8_t *roots);
 
 /* nblocks messages of message_len bytes, back to back, -> nblocks x ecc_len
  * parity bytes (rs_encode_slice_pw2_dispatch::encode, reed_solomon.hpp:335-337,
  * looped as in PyRS256::py_encode, pyrs256.hpp:118-120) */
-int ffgpu_rs256_encode(const ffgpu_rs256 *code, const uint8_t *data, size_t nblocks, size_t message_len,
+FFGPU_API int ffgpu_rs256_encode(const ffgpu_rs256 *code, const uint8_t *data, size_t nblocks, size_t message_len,
                        uint8_t *parity, void *stream);
 /* in-place repair of nblocks (data, parity) pairs; status[i] = 1 (true) or 0
  * (false) exactly as rs_decode::decode (reed_solomon.hpp:559-595) called by
  * PyRS256::py_repair (pyrs256.hpp:129-131) once per block */
-int ffgpu_rs256_decode(const ffgpu_rs256 *code, uint8_t *data, uint8_t *parity, size_t nblocks, size_t message_len,
+FFGPU_API int ffgpu_rs256_decode(const ffgpu_rs256 *code, uint8_t *data, uint8_t *parity, size_t nblocks, size_t message_len,
                        uint8_t *status, void *stream);
 /* syndromes of nblocks blocks, ecc_len bytes each (PyRS256::py_synds, pyrs256.hpp:133-140) */
-int ffgpu_rs256_synds(const ffgpu_rs256 *code, const uint8_t *data, const uint8_t *parity, size_t nblocks,
+FFGPU_API int ffgpu_rs256_synds(const ffgpu_rs256 *code, const uint8_t *data, const uint8_t *parity, size_t nblocks,
                       size_t message_len, uint8_t *synds, void *stream);
 
 /* host-buffer forms: RS256.encode(buffer) including the shortened tail block
  * (pyrs256.hpp:99-127); out must hold ceil(len / message_len) * ecc_len bytes */
-int ffgpu_rs256_encode_host(const ffgpu_rs256 *code, const uint8_t *buf, size_t len, size_t message_len, uint8_t *out);
-int ffgpu_rs256_decode_host(const ffgpu_rs256 *code, uint8_t *data, uint8_t *parity, size_t nblocks,
+FFGPU_API int ffgpu_rs256_encode_host(const ffgpu_rs256 *code, const uint8_t *buf, size_t len, size_t message_len, uint8_t *out);
+FFGPU_API int ffgpu_rs256_decode_host(const ffgpu_rs256 *code, uint8_t *data, uint8_t *parity, size_t nblocks,
                             size_t message_len, uint8_t *status);
-int ffgpu_rs256_synds_host(const ffgpu_rs256 *code, const uint8_t *data, const uint8_t *parity, size_t nblocks,
+FFGPU_API int ffgpu_rs256_synds_host(const ffgpu_rs256 *code, const uint8_t *data, const uint8_t *parity, size_t nblocks,
                            size_t message_len, uint8_t *synds);
 
 /* ---------------------------------------------------------------- RSi16 */
 /* PyRSi16 ctor (libffrs/pyrsi16.hpp:41-125), NTT ctor (libffrs/ntt.hpp:55-123),
  * RSi16v ctor (libffrs/rsi16v_impl.hpp:68-86). */
-int ffgpu_rsi16_create(size_t block_len, size_t ecc_len, uint32_t primitive, ffgpu_rsi16 **out);
-int ffgpu_rsi16_destroy(ffgpu_rsi16 *code);
+FFGPU_API int ffgpu_rsi16_create(size_t block_len, size_t ecc_len, uint32_t primitive, ffgpu_rsi16 **out);
+FFGPU_API int ffgpu_rsi16_destroy(ffgpu_rsi16 *code);
 /* root, ntt_len */
-int ffgpu_rsi16_info(const ffgpu_rsi16 *code, uint32_t *root, size_t *ntt_len);
+FFGPU_API int ffgpu_rsi16_info(const ffgpu_rsi16 *code, uint32_t *root, size_t *ntt_len);
 
 /* nblocks x message_len uint16 words -> nblocks x ecc_len uint16 parity words
  * (RSi16v::_encode, rsi16v_impl.hpp:93-119, via PyRSi16::encode_blocks,
  * pyrsi16.hpp:127-140; parity truncated to 16 bits as pyrsi16.hpp:370) */
-int ffgpu_rsi16_encode(const ffgpu_rsi16 *code, const uint16_t *msg, size_t nblocks, uint16_t *parity, void *stream);
+FFGPU_API int ffgpu_rsi16_encode(const ffgpu_rsi16 *code, const uint16_t *msg, size_t nblocks, uint16_t *parity, void *stream);
 /* interleaved encode of nblocks interleaved blocks (PyRSi16::_encode_interleaved,
  * pyrsi16.hpp:323-361): msg is message_len x interleave words per block,
  * parity ecc_len x interleave words per block */
-int ffgpu_rsi16_encode_interleaved(const ffgpu_rsi16 *code, const uint16_t *msg, size_t nblocks, size_t interleave,
+FFGPU_API int ffgpu_rsi16_encode_interleaved(const ffgpu_rsi16 *code, const uint16_t *msg, size_t nblocks, size_t interleave,
                                    uint16_t *parity, void *stream);
 /* unknown-location repair of nblocks blocks in place, W = 1 semantics
  * (RSi16v::_repair, rsi16v_impl.hpp:122-168, as PyRSi16::py_repair,
  * pyrsi16.hpp:588-631); status[i] is a RepairStatus or FFGPU_STATUS_ASSERT */
-int ffgpu_rsi16_repair(const ffgpu_rsi16 *code, uint16_t *msg, uint16_t *parity, size_t nblocks, uint8_t *status,
+FFGPU_API int ffgpu_rsi16_repair(const ffgpu_rsi16 *code, uint16_t *msg, uint16_t *parity, size_t nblocks, uint8_t *status,
                        void *stream);
 /* interleaved repair (PyRSi16::repair_interleaved, pyrsi16.hpp:160-176, with
  * W = 1 semantics): one interleaved block; error_pos == NULL selects unknown
  * locations.  *status receives the max over columns. */
-int ffgpu_rsi16_repair_interleaved(const ffgpu_rsi16 *code, uint16_t *msg, uint16_t *parity, size_t interleave,
+FFGPU_API int ffgpu_rsi16_repair_interleaved(const ffgpu_rsi16 *code, uint16_t *msg, uint16_t *parity, size_t interleave,
                                    const uint32_t *error_pos, size_t error_count, uint8_t *status, void *stream);
 /* known-location repair of nblocks blocks sharing one error position list
  * (RSi16v::_repair with positions, rsi16v_impl.hpp:171-231) */
-int ffgpu_rsi16_repair_known(const ffgpu_rsi16 *code, uint16_t *msg, uint16_t *parity, size_t nblocks,
+FFGPU_API int ffgpu_rsi16_repair_known(const ffgpu_rsi16 *code, uint16_t *msg, uint16_t *parity, size_t nblocks,
                              const uint32_t *error_pos, size_t error_count, uint8_t *status, void *stream);
 /* syndromes, ecc_len uint32 words per block (PyRSi16::py_synd, pyrsi16.hpp:633-651) */
-int ffgpu_rsi16_synd(const ffgpu_rsi16 *code, const uint16_t *msg, const uint16_t *parity, size_t nblocks,
+FFGPU_API int ffgpu_rsi16_synd(const ffgpu_rsi16 *code, const uint16_t *msg, const uint16_t *parity, size_t nblocks,
                      uint32_t *synds, void *stream);
 /* Sugiyama on nblocks syndrome vectors (PyRSi16::py_sugiyama<1>, pyrsi16.hpp:653-674) */
-int ffgpu_rsi16_sugiyama(const ffgpu_rsi16 *code, const uint32_t *synds, size_t nblocks, uint32_t *locator,
+FFGPU_API int ffgpu_rsi16_sugiyama(const ffgpu_rsi16 *code, const uint32_t *synds, size_t nblocks, uint32_t *locator,
                          uint32_t *evaluator, uint8_t *status, void *stream);
 /* zeros of pintt_ecc(poly) (PyRSi16::py_roots, pyrsi16.hpp:676-691): out
  * receives block_len flags (1 = zero) */
-int ffgpu_rsi16_roots(const ffgpu_rsi16 *code, const uint32_t *poly, uint8_t *is_zero, void *stream);
+FFGPU_API int ffgpu_rsi16_roots(const ffgpu_rsi16 *code, const uint32_t *poly, uint8_t *is_zero, void *stream);
 
-int ffgpu_rsi16_encode_host(const ffgpu_rsi16 *code, const uint16_t *msg, size_t nblocks, size_t interleave,
+FFGPU_API int ffgpu_rsi16_encode_host(const ffgpu_rsi16 *code, const uint16_t *msg, size_t nblocks, size_t interleave,
                             uint16_t *parity);
-int ffgpu_rsi16_repair_host(const ffgpu_rsi16 *code, uint16_t *msg, uint16_t *parity, size_t nblocks,
+FFGPU_API int ffgpu_rsi16_repair_host(const ffgpu_rsi16 *code, uint16_t *msg, uint16_t *parity, size_t nblocks,
                             size_t interleave, const uint32_t *error_pos, long error_count, uint8_t *status);
 
 /* ---------------------------------------------------------------- CIRC16 */
 /* PyCIRC16 ctor (libffrs/pycirc16.hpp:46-65) */
-int ffgpu_circ16_create(size_t inner_block_len, size_t inner_ecc_len, size_t outer_block_len, size_t outer_ecc_len,
+FFGPU_API int ffgpu_circ16_create(size_t inner_block_len, size_t inner_ecc_len, size_t outer_block_len, size_t outer_ecc_len,
                         size_t interleave, uint32_t primitive, ffgpu_circ16 **out);
-int ffgpu_circ16_destroy(ffgpu_circ16 *code);
+FFGPU_API int ffgpu_circ16_destroy(ffgpu_circ16 *code);
 /* message_len, ecc_len of one CIRC16 block in uint16 words */
-int ffgpu_circ16_info(const ffgpu_circ16 *code, size_t *message_len, size_t *ecc_len);
+FFGPU_API int ffgpu_circ16_info(const ffgpu_circ16 *code, size_t *message_len, size_t *ecc_len);
 /* nblocks CIRC16 blocks: [rso_ecc | rsi_ecc | rsio_ecc] per block
  * (PyCIRC16::py_encode / encode_block, pycirc16.hpp:337-363) */
-int ffgpu_circ16_encode(const ffgpu_circ16 *code, const uint16_t *msg, size_t nblocks, uint16_t *ecc, void *stream);
+FFGPU_API int ffgpu_circ16_encode(const ffgpu_circ16 *code, const uint16_t *msg, size_t nblocks, uint16_t *ecc, void *stream);
 /* in-place repair of one CIRC16 block (CircRepair, pycirc16.hpp:135-335,
  * PyCIRC16::py_repair :365-384); *assert_fail is set when the reference
  * would raise RuntimeError */
-int ffgpu_circ16_repair(const ffgpu_circ16 *code, uint16_t *msg, uint16_t *ecc, size_t nblocks, uint8_t *status,
+FFGPU_API int ffgpu_circ16_repair(const ffgpu_circ16 *code, uint16_t *msg, uint16_t *ecc, size_t nblocks, uint8_t *status,
                         void *stream);
 /* outer error rows of interleave k after the zero heuristics
  * (PyCIRC16::py_find_outer_error_locations, pycirc16.hpp:386-405); flags has
  * outer_block_len entries */
-int ffgpu_circ16_find_outer_error_locations(const ffgpu_circ16 *code, const uint16_t *msg, const uint16_t *ecc,
+FFGPU_API int ffgpu_circ16_find_outer_error_locations(const ffgpu_circ16 *code, const uint16_t *msg, const uint16_t *ecc,
                                             size_t k, uint8_t *flags, void *stream);
 
-int ffgpu_circ16_encode_host(const ffgpu_circ16 *code, const uint16_t *msg, size_t nblocks, uint16_t *ecc);
-int ffgpu_circ16_repair_host(const ffgpu_circ16 *code, uint16_t *msg, uint16_t *ecc, size_t nblocks, uint8_t *status);
+FFGPU_API int ffgpu_circ16_encode_host(const ffgpu_circ16 *code, const uint16_t *msg, size_t nblocks, uint16_t *ecc);
+FFGPU_API int ffgpu_circ16_repair_host(const ffgpu_circ16 *code, uint16_t *msg, uint16_t *ecc, size_t nblocks, uint8_t *status);
 
 #ifdef __cplusplus
 }

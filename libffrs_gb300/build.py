@@ -11,6 +11,7 @@ parallel and are skipped when up to date.  No cmake.
 import concurrent.futures as cf
 import glob
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -20,7 +21,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 HOST = os.path.join(HERE, "host")
-OBJ = os.path.join(HERE, "_build")
+OBJ = os.path.join(HERE, "_build", platform.machine())
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 LIB_GPU = os.path.join(HERE, "libffgpu.so")
 

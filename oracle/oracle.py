@@ -7,13 +7,14 @@ It never runs on the product path.
 
 import ctypes
 import os
+import platform
 import subprocess
 import threading
 
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-_BUILD = os.path.join(_HERE, "_build")
+_BUILD = os.path.join(_HERE, "_build", platform.machine())
 _LIB_PATH = os.path.join(_BUILD, "liboracle.so")
 _lock = threading.Lock()
 _lib = None

@@ -36,9 +36,9 @@ def pytest_collection_modifyitems(config, items):
 @pytest.fixture(scope="session")
 def built():
     """Build the native libraries once per session (no-op when up to date)."""
-    from libffrs_gb300 import build
+    import __graft_entry__
 
-    build.build()
+    __graft_entry__._build_module().build()
     return True
 
 
