@@ -138,6 +138,11 @@ FFGPU_API int ffgpu_rsi16_roots(const ffgpu_rsi16 *code, const uint32_t *poly, u
 
 FFGPU_API int ffgpu_rsi16_encode_host(const ffgpu_rsi16 *code, const uint16_t *msg, size_t nblocks, size_t interleave,
                             uint16_t *parity);
+FFGPU_API int ffgpu_rsi16_synd_host(const ffgpu_rsi16 *code, const uint16_t *msg, const uint16_t *parity,
+                                    size_t nblocks, uint32_t *synds);
+FFGPU_API int ffgpu_rsi16_sugiyama_host(const ffgpu_rsi16 *code, const uint32_t *synds, size_t nblocks,
+                                       uint32_t *locator, uint32_t *evaluator, uint8_t *status);
+FFGPU_API int ffgpu_rsi16_roots_host(const ffgpu_rsi16 *code, const uint32_t *poly, uint8_t *is_zero);
 FFGPU_API int ffgpu_rsi16_repair_host(const ffgpu_rsi16 *code, uint16_t *msg, uint16_t *parity, size_t nblocks,
                             size_t interleave, const uint32_t *error_pos, long error_count, uint8_t *status);
 
@@ -163,6 +168,10 @@ FFGPU_API int ffgpu_circ16_find_outer_error_locations(const ffgpu_circ16 *code, 
                                             size_t k, uint8_t *flags, void *stream);
 
 FFGPU_API int ffgpu_circ16_encode_host(const ffgpu_circ16 *code, const uint16_t *msg, size_t nblocks, uint16_t *ecc);
+/* rows (outer_block_len capacity) receives the outer error rows of group k */
+FFGPU_API int ffgpu_circ16_find_outer_error_locations_host(const ffgpu_circ16 *code, const uint16_t *msg,
+                                                           const uint16_t *ecc, size_t k, uint32_t *rows,
+                                                           size_t *count);
 FFGPU_API int ffgpu_circ16_repair_host(const ffgpu_circ16 *code, uint16_t *msg, uint16_t *ecc, size_t nblocks, uint8_t *status);
 
 #ifdef __cplusplus

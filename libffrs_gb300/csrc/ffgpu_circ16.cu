@@ -1,0 +1,193 @@
+// C ABI: CIRC16 entry points.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <vector>
+
+#include "circ16.cuh"
+#include "common.cuh"
+
+using namespace ffgpu;
+
+struct ffgpu_circ16 {
+    std::unique_ptr<Circ16Code> code;
+    std::mutex mu;
+    DeviceBuffer d_msg, d_ecc;
+};
+
+static cudaStream_t pick(void *stream) { return stream ? (cudaStream_t)stream : lib_stream(); }
+
+// Runs the repair of one block already on the device; returns the first
+// raising outer column or SIZE_MAX, and writes the ecc back only when no
+// column raised (the reference's exception skips dump_ecc).
+static size_t repair_device(Circ16Code &c, uint16_t *dm, uint16_t *de, cudaStream_t st) {
+    std::vector<uint8_t> cst(c.rso_interleave);
+    circ16_repair_one(c, dm, de, st, false, 0, nullptr, nullptr, cst.data());
+    FFGPU_CHECK_CUDA(cudaStreamSynchronize(st));
+    for (size_t i = 0; i < cst.size(); ++i)
+        if (cst[i] == FFGPU_STATUS_ASSERT) return i;
+    circ16_dump_ecc(c, de, st);
+    return (size_t)-1;
+}
+
+extern "C" {
+
+int ffgpu_circ16_create(size_t inner_block_len, size_t inner_ecc_len, size_t outer_block_len, size_t outer_ecc_len,
+                        size_t interleave, uint32_t primitive, ffgpu_circ16 **out) {
+    return guarded([&] {
+        FFGPU_REQUIRE(out, "out is NULL");
+        lib_stream();
+        auto h = std::make_unique<ffgpu_circ16>();
+        h->code = std::make_unique<Circ16Code>(inner_block_len, inner_ecc_len, outer_block_len, outer_ecc_len,
+                                               interleave, primitive);
+        *out = h.release();
+    });
+}
+
+int ffgpu_circ16_destroy(ffgpu_circ16 *code) {
+    return guarded([&] { delete code; });
+}
+
+int ffgpu_circ16_info(const ffgpu_circ16 *code, size_t *message_len, size_t *ecc_len) {
+    return guarded([&] {
+        FFGPU_REQUIRE(code, "code is NULL");
+        if (message_len) *message_len = code->code->message_len;
+        if (ecc_len) *ecc_len = code->code->ecc_len;
+    });
+}
+
+int ffgpu_circ16_encode(const ffgpu_circ16 *code, const uint16_t *msg, size_t nblocks, uint16_t *ecc, void *stream) {
+    return guarded([&] {
+        FFGPU_REQUIRE(code, "code is NULL");
+        ffgpu_circ16 *h = const_cast<ffgpu_circ16 *>(code);
+        std::lock_guard<std::mutex> lk(h->mu);
+        circ16_encode(*h->code, msg, nblocks, ecc, pick(stream));
+    });
+}
+
+// status[i]: 0 when block i was repaired as the reference does (which always
+// returns False), FFGPU_STATUS_ASSERT when the reference raises RuntimeError
+// for it (its message is then left as the reference leaves it and its ecc is
+// not written back).
+int ffgpu_circ16_repair(const ffgpu_circ16 *code, uint16_t *msg, uint16_t *ecc, size_t nblocks, uint8_t *status,
+                        void *stream) {
+    return guarded([&] {
+        FFGPU_REQUIRE(code, "code is NULL");
+        ffgpu_circ16 *h = const_cast<ffgpu_circ16 *>(code);
+        std::lock_guard<std::mutex> lk(h->mu);
+        Circ16Code &c = *h->code;
+        cudaStream_t st = pick(stream);
+        for (size_t b = 0; b < nblocks; ++b) {
+            uint16_t *dm = msg + b * c.message_len, *de = ecc + b * c.ecc_len;
+            // keep the message of this block in case a column raises
+            uint16_t *saved = (uint16_t *)h->d_msg.get(c.message_len * 2);
+            FFGPU_CHECK_CUDA(cudaMemcpyAsync(saved, dm, c.message_len * 2, cudaMemcpyDeviceToDevice, st));
+            const size_t fail = repair_device(c, dm, de, st);
+            if (fail != (size_t)-1) {
+                // columns from the raising one on keep their original words
+                const size_t ncols = c.rso_interleave - fail;
+                FFGPU_CHECK_CUDA(cudaMemcpy2DAsync(dm + fail, c.rso_interleave * 2, saved + fail,
+                                                   c.rso_interleave * 2, ncols * 2, c.rso->message_len,
+                                                   cudaMemcpyDeviceToDevice, st));
+            }
+            const uint8_t s = fail == (size_t)-1 ? 0 : FFGPU_STATUS_ASSERT;
+            if (status) FFGPU_CHECK_CUDA(cudaMemcpyAsync(status + b, &s, 1, cudaMemcpyHostToDevice, st));
+            FFGPU_CHECK_CUDA(cudaStreamSynchronize(st));
+        }
+    });
+}
+
+int ffgpu_circ16_find_outer_error_locations(const ffgpu_circ16 *code, const uint16_t *msg, const uint16_t *ecc,
+                                            size_t k, uint8_t *flags, void *stream) {
+    return guarded([&] {
+        FFGPU_REQUIRE(code, "code is NULL");
+        ffgpu_circ16 *h = const_cast<ffgpu_circ16 *>(code);
+        std::lock_guard<std::mutex> lk(h->mu);
+        Circ16Code &c = *h->code;
+        FFGPU_REQUIRE(k < c.interleave, "interleave index out of range");
+        cudaStream_t st = pick(stream);
+        std::vector<uint32_t> locs(c.rso->block_len);
+        uint32_t n = 0;
+        circ16_repair_one(c, const_cast<uint16_t *>(msg), const_cast<uint16_t *>(ecc), st, true, k, locs.data(), &n,
+                          nullptr);
+        FFGPU_CHECK_CUDA(cudaStreamSynchronize(st));
+        std::vector<uint8_t> f(c.rso->block_len, 0);
+        for (uint32_t i = 0; i < n; ++i) f[locs[i]] = 1;
+        FFGPU_CHECK_CUDA(cudaMemcpy(flags, f.data(), f.size(), cudaMemcpyHostToDevice));
+    });
+}
+
+int ffgpu_circ16_encode_host(const ffgpu_circ16 *code, const uint16_t *msg, size_t nblocks, uint16_t *ecc) {
+    return guarded([&] {
+        FFGPU_REQUIRE(code, "code is NULL");
+        ffgpu_circ16 *h = const_cast<ffgpu_circ16 *>(code);
+        std::lock_guard<std::mutex> lk(h->mu);
+        Circ16Code &c = *h->code;
+        if (!nblocks) return;
+        cudaStream_t st = lib_stream();
+        uint16_t *dm = (uint16_t *)h->d_msg.get(nblocks * c.message_len * 2);
+        uint16_t *de = (uint16_t *)h->d_ecc.get(nblocks * c.ecc_len * 2);
+        FFGPU_CHECK_CUDA(cudaMemcpyAsync(dm, msg, nblocks * c.message_len * 2, cudaMemcpyHostToDevice, st));
+        circ16_encode(c, dm, nblocks, de, st);
+        FFGPU_CHECK_CUDA(cudaMemcpyAsync(ecc, de, nblocks * c.ecc_len * 2, cudaMemcpyDeviceToHost, st));
+        FFGPU_CHECK_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+int ffgpu_circ16_find_outer_error_locations_host(const ffgpu_circ16 *code, const uint16_t *msg, const uint16_t *ecc,
+                                                 size_t k, uint32_t *rows, size_t *count) {
+    return guarded([&] {
+        FFGPU_REQUIRE(code, "code is NULL");
+        ffgpu_circ16 *h = const_cast<ffgpu_circ16 *>(code);
+        std::lock_guard<std::mutex> lk(h->mu);
+        Circ16Code &c = *h->code;
+        if (k >= c.interleave) throw Error(FFGPU_EASSERT, "Assertion failed: interleave < this->interleave");
+        cudaStream_t st = lib_stream();
+        uint16_t *dm = (uint16_t *)h->d_msg.get(c.message_len * 2 * 2);
+        uint16_t *de = (uint16_t *)h->d_ecc.get(c.ecc_len * 2);
+        FFGPU_CHECK_CUDA(cudaMemcpyAsync(dm, msg, c.message_len * 2, cudaMemcpyHostToDevice, st));
+        FFGPU_CHECK_CUDA(cudaMemcpyAsync(de, ecc, c.ecc_len * 2, cudaMemcpyHostToDevice, st));
+        uint32_t n = 0;
+        circ16_repair_one(c, dm, de, st, true, k, rows, &n, nullptr);
+        FFGPU_CHECK_CUDA(cudaStreamSynchronize(st));
+        *count = n;
+    });
+}
+
+int ffgpu_circ16_repair_host(const ffgpu_circ16 *code, uint16_t *msg, uint16_t *ecc, size_t nblocks,
+                             uint8_t *status) {
+    return guarded([&] {
+        FFGPU_REQUIRE(code, "code is NULL");
+        ffgpu_circ16 *h = const_cast<ffgpu_circ16 *>(code);
+        std::lock_guard<std::mutex> lk(h->mu);
+        Circ16Code &c = *h->code;
+        if (!nblocks) return;
+        cudaStream_t st = lib_stream();
+        uint16_t *dm = (uint16_t *)h->d_msg.get(c.message_len * 2 * 2);
+        uint16_t *de = (uint16_t *)h->d_ecc.get(c.ecc_len * 2);
+        for (size_t b = 0; b < nblocks; ++b) {
+            uint16_t *hm = msg + b * c.message_len, *he = ecc + b * c.ecc_len;
+            FFGPU_CHECK_CUDA(cudaMemcpyAsync(dm, hm, c.message_len * 2, cudaMemcpyHostToDevice, st));
+            FFGPU_CHECK_CUDA(cudaMemcpyAsync(de, he, c.ecc_len * 2, cudaMemcpyHostToDevice, st));
+            const size_t fail = repair_device(c, dm, de, st);
+            if (fail == (size_t)-1) {
+                FFGPU_CHECK_CUDA(cudaMemcpyAsync(hm, dm, c.message_len * 2, cudaMemcpyDeviceToHost, st));
+                FFGPU_CHECK_CUDA(cudaMemcpyAsync(he, de, c.ecc_len * 2, cudaMemcpyDeviceToHost, st));
+                FFGPU_CHECK_CUDA(cudaStreamSynchronize(st));
+                if (status) status[b] = 0;
+            } else {
+                std::vector<uint16_t> tmp(c.message_len);
+                FFGPU_CHECK_CUDA(cudaMemcpyAsync(tmp.data(), dm, c.message_len * 2, cudaMemcpyDeviceToHost, st));
+                FFGPU_CHECK_CUDA(cudaStreamSynchronize(st));
+                for (size_t r = 0; r < c.rso->message_len; ++r)
+                    for (size_t col = 0; col < fail; ++col)
+                        hm[r * c.rso_interleave + col] = tmp[r * c.rso_interleave + col];
+                if (status) status[b] = FFGPU_STATUS_ASSERT;
+            }
+        }
+    });
+}
+
+}  // extern "C"

@@ -232,6 +232,8 @@ public:
     uint32_t log(uint32_t a) const { return log_.at(a); }
 };
 
+py::object make_gfi16(uint32_t primitive) { return py::cast(PyGFi16(primitive)); }
+
 void register_gf(py::module &m) {
     py::class_<PyGF256>(m, "GF256")
         .def(py::init<uint8_t, uint16_t>(), "primitive"_a = 2, "poly1"_a = 0x11d)

@@ -38,7 +38,6 @@ public:
         }
         if (ecc < 1 || ecc > 254) throw py::value_error("ecc_len must be in [1, 254]");
         ecc_len = ecc;
-        ffgpu_check(ffgpu_rs256_create((int)ecc, primitive_, polynomial_, &code));
         set_block_len(block_len_ ? *block_len_ : 255);
         if (ecc_len_ && message_len_) {
             if (block_len_ && (size_t)*message_len_ + *ecc_len_ != *block_len_)
@@ -46,6 +45,8 @@ public:
             else if (!block_len_)
                 set_block_len((size_t)*message_len_ + (size_t)*ecc_len_);
         }
+        // device tables last: every argument error above is raised first
+        ffgpu_check(ffgpu_rs256_create((int)ecc, primitive_, polynomial_, &code));
     }
     ~PyRS256() {
         if (code) ffgpu_rs256_destroy(code);
