@@ -311,7 +311,170 @@ def cpu_baseline_rs256_encode(threads, nblocks):
     return nblocks * 255 / dt / 1e9, dt
 
 
+def make_rsi16_inputs(torch, nb, seed, corrupt):
+    """C3 inputs on the device: RSi16(1024, 64) messages (960 uint16 words),
+    parity from our encoder, and (corrupt=True) 0-32 symbol errors per block,
+    (v + d) mod 65537 with d uniform in [1, 65536], never producing 65536."""
+    from libffrs_gb300 import capi
+
+    bl, ecc = 1024, 64
+    ml = bl - ecc
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    msg = torch.randint(-32768, 32768, (nb, ml), dtype=torch.int16, device="cuda", generator=g)
+    par = torch.zeros((nb, ecc), dtype=torch.int16, device="cuda")
+    code = capi.RSi16Code(bl, ecc)
+    code.encode(msg.data_ptr(), nb, par.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    if not corrupt:
+        return msg, par
+    cw = torch.cat([msg, par], dim=1)
+    ks = torch.randint(0, 33, (nb,), device="cuda", generator=g)
+    chunk = 1 << 16
+    for s in range(0, nb, chunk):
+        e = min(nb, s + chunk)
+        n = e - s
+        pos = torch.rand((n, bl), device="cuda", generator=g).argsort(dim=1)[:, :32]
+        mask = torch.arange(32, device="cuda")[None, :] < ks[s:e, None]
+        rows = torch.arange(s, e, device="cuda")[:, None].expand(n, 32)
+        v = cw[rows, pos].to(torch.int64) & 0xFFFF
+        d = torch.randint(1, 65537, (n, 32), device="cuda", generator=g)
+        nv = (v + d) % 65537
+        alt = torch.where(d > 1, (v + d - 1) % 65537, (v + 2) % 65537)
+        nv = torch.where(nv == 65536, alt, nv)
+        nv = torch.where(mask, nv, v)
+        cw[rows, pos] = nv.to(torch.int32).to(torch.int16)
+    torch.cuda.synchronize()
+    return cw[:, :ml].contiguous(), cw[:, ml:].contiguous()
+
+
+def bench_rsi16(args, torch, rank, world, decode):
+    from libffrs_gb300 import capi
+    import libffrs_gb300
+
+    nb, bl, ecc = 262144, 1024, 64
+    ml = bl - ecc
+    msg0, par0 = make_rsi16_inputs(torch, nb, 3000 + rank, decode)
+    code = capi.RSi16Code(bl, ecc)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    nbuf = 2
+    if decode:
+        bufs = [(msg0.clone(), par0.clone(), torch.zeros(nb, dtype=torch.uint8, device="cuda")) for _ in range(nbuf)]
+    else:
+        bufs = [(msg0 if i == 0 else msg0.clone(), torch.zeros_like(par0), None) for i in range(nbuf)]
+
+    def run(i):
+        m, p, s = bufs[i % nbuf]
+        if decode:
+            code.repair(m.data_ptr(), p.data_ptr(), nb, s.data_ptr(), sp)
+        else:
+            code.encode(m.data_ptr(), nb, p.data_ptr(), sp)
+
+    for i in range(args.warmup):
+        if decode:
+            bufs[i % nbuf][0].copy_(msg0)
+            bufs[i % nbuf][1].copy_(par0)
+        run(i)
+    torch.cuda.synchronize()
+    total_ms, kern_ms = 0.0, []
+    launches0 = capi.kernel_launches()
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        done = 0
+        while done < args.steps:
+            batch = min(nbuf, args.steps - done)
+            if decode:
+                for j in range(batch):
+                    bufs[j][0].copy_(msg0)
+                    bufs[j][1].copy_(par0)
+            torch.cuda.synchronize()
+            if world > 1:
+                torch.distributed.barrier()
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(batch + 1)]
+            ev[0].record(stream)
+            for j in range(batch):
+                run(j)
+                ev[j + 1].record(stream)
+            torch.cuda.synchronize()
+            total_ms += ev[0].elapsed_time(ev[batch])
+            kern_ms += [ev[j].elapsed_time(ev[j + 1]) for j in range(batch)]
+            done += batch
+    launches = capi.kernel_launches() - launches0
+    algo = nb * (2048 if not decode else 2048 + 4)
+    lf = libffrs_gb300.libffrs
+    rs = lf.RSi16(bl, ecc)
+    hm = lf.create_buffer(nb * ml * 2)
+    hm[:] = msg0.cpu().numpy().tobytes()
+    e2e_t = []
+    if decode:
+        hp = lf.create_buffer(nb * ecc * 2)
+        p0 = par0.cpu().numpy().tobytes()
+        m0 = bytes(hm)
+    for i in range(max(1, args.e2e_steps) + 1):
+        if decode:
+            hm[:] = m0
+            hp[:] = p0
+        t0 = time.perf_counter()
+        if decode:
+            rs.repair_blocks(hm, hp)
+        else:
+            rs.encode(hm)
+        t1 = time.perf_counter()
+        if i:
+            e2e_t.append(t1 - t0)
+    if decode:
+        e2e = {"value": algo * world / statistics.median(e2e_t) / 1e9, "unit": "GB/s",
+               "h2d_bytes_per_step": nb * bl * 2, "d2h_bytes_per_step": nb * bl * 2 + nb,
+               "api": "libffrs.RSi16.repair_blocks(create_buffer, create_buffer)"}
+    else:
+        e2e = {"value": algo * world / statistics.median(e2e_t) / 1e9, "unit": "GB/s",
+               "h2d_bytes_per_step": nb * ml * 2, "d2h_bytes_per_step": nb * ecc * 2, "api": "libffrs.RSi16.encode"}
+    out = {
+        "workload": "rsi16-decode" if decode else "rsi16-encode", "total_ms": total_ms, "kern_ms": kern_ms,
+        "algo_bytes_per_step": algo, "launches": launches, "clocks": clk.summary(), "e2e": e2e,
+        "config": {"workload": ("RSi16(1024, 64) decode, 262144 blocks, 0-32 symbol errors/block" if decode else
+                                "RSi16(1024, 64) encode, 262144 blocks x 960 uint16 words"),
+                   "blocks": nb, "l2": "inputs larger than L2 (503 MB per step)"},
+        "dtype": "u32 mod 65537",
+    }
+    if decode:
+        st = bufs[0][2]
+        out["status_ok_fraction"] = float((st == 2).float().mean().item())
+    return out
+
+
+def cpu_baseline_rsi16(threads, nblocks, decode):
+    from oracle import oracle as O
+
+    rng = np.random.Generator(np.random.PCG64(79))
+    o = O.RSi16(1024, 64)
+    msg = rng.integers(0, 65536, size=(nblocks, 960), dtype=np.uint16)
+    t0 = time.perf_counter()
+    par = o.encode_blocks(msg, threads=threads)
+    dt = time.perf_counter() - t0
+    if not decode:
+        return nblocks * 2048 / dt / 1e9, dt
+    cw = np.concatenate([msg, par], axis=1).astype(np.int64)
+    ks = rng.integers(0, 33, size=nblocks)
+    for i in range(nblocks):
+        for q in rng.choice(1024, size=int(ks[i]), replace=False):
+            while True:
+                v = (cw[i, q] + int(rng.integers(1, 65537))) % 65537
+                if v != 65536:
+                    break
+            cw[i, q] = v
+    m = np.ascontiguousarray(cw[:, :960].astype(np.uint16))
+    p = np.ascontiguousarray(cw[:, 960:].astype(np.uint16))
+    t0 = time.perf_counter()
+    o.repair_blocks(m, p, threads=threads)
+    dt = time.perf_counter() - t0
+    return nblocks * 2052 / dt / 1e9, dt
+
+
 WORKLOADS = {
+    "rsi16-encode": (lambda a, t, r, w: bench_rsi16(a, t, r, w, False),
+                     lambda th, n: cpu_baseline_rsi16(th, n, False), 65536, "GB/s"),
+    "rsi16-decode": (lambda a, t, r, w: bench_rsi16(a, t, r, w, True),
+                     lambda th, n: cpu_baseline_rsi16(th, n, True), 4096, "GB/s"),
     "rs256-decode": (bench_rs256_decode, cpu_baseline_rs256_decode, 262144, "GB/s"),
     "rs256-encode": (bench_rs256_encode, cpu_baseline_rs256_encode, 65536 * 8, "GB/s"),
 }

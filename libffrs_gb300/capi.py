@@ -135,5 +135,51 @@ class RS256Code:
         call("ffgpu_rs256_decode", self.h, data_ptr, parity_ptr, nblocks, message_len, status_ptr, stream)
 
 
+class RSi16Code:
+    """Device-resident RSi16 code handle (ffgpu_rsi16)."""
+
+    def __init__(self, block_len, ecc_len, primitive=3):
+        h = ctypes.c_void_p()
+        call("ffgpu_rsi16_create", block_len, ecc_len, primitive, ctypes.byref(h))
+        self.h = h
+        self.block_len = block_len
+        self.ecc_len = ecc_len
+        self.message_len = block_len - ecc_len
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.ffgpu_rsi16_destroy(self.h)
+            self.h = None
+
+    def encode(self, msg_ptr, nblocks, parity_ptr, stream=None):
+        call("ffgpu_rsi16_encode", self.h, msg_ptr, nblocks, parity_ptr, stream)
+
+    def repair(self, msg_ptr, parity_ptr, nblocks, status_ptr, stream=None):
+        call("ffgpu_rsi16_repair", self.h, msg_ptr, parity_ptr, nblocks, status_ptr, stream)
+
+
+class CIRC16Code:
+    """Device-resident CIRC16 code handle (ffgpu_circ16)."""
+
+    def __init__(self, ib, ie, ob, oe, interleave=1, primitive=3):
+        h = ctypes.c_void_p()
+        call("ffgpu_circ16_create", ib, ie, ob, oe, interleave, primitive, ctypes.byref(h))
+        self.h = h
+        ml, el = _SZ(), _SZ()
+        call("ffgpu_circ16_info", h, ctypes.byref(ml), ctypes.byref(el))
+        self.message_len, self.ecc_len = ml.value, el.value
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.ffgpu_circ16_destroy(self.h)
+            self.h = None
+
+    def encode(self, msg_ptr, nblocks, ecc_ptr, stream=None):
+        call("ffgpu_circ16_encode", self.h, msg_ptr, nblocks, ecc_ptr, stream)
+
+    def repair(self, msg_ptr, ecc_ptr, nblocks, status_ptr, stream=None):
+        call("ffgpu_circ16_repair", self.h, msg_ptr, ecc_ptr, nblocks, status_ptr, stream)
+
+
 def kernel_launches():
     return int(lib().ffgpu_kernel_launches())

@@ -83,13 +83,32 @@ __global__ void __launch_bounds__(128) rs256_encode_table_kernel(const uint8_t *
     for (int j = 0; j < ecc; ++j) out[j] = (uint8_t)rem_byte<W>(rem, j);
 }
 
-struct DecodeScratch {
-    uint8_t S[256], lam[256], prev[256], tmp[256], pos[256], mag[256], ev[512];
+// Per-thread decode scratch in global memory, interleaved across the threads
+// of the launch so that lock-step accesses of a warp coalesce.
+struct ScratchBytes {
+    uint8_t *base;
+    size_t stride;
+    __device__ __forceinline__ uint8_t &operator[](int k) const { return base[(size_t)k * stride]; }
+    __device__ __forceinline__ ScratchBytes operator+(int k) const { return {base + (size_t)k * stride, stride}; }
 };
+struct DecodeScratchG {
+    ScratchBytes S, lam, prev, tmp, pos, mag, ev;
+    __device__ DecodeScratchG(uint8_t *g, size_t tid, size_t nthreads) {
+        uint8_t *b = g + tid;
+        S = {b, nthreads};
+        lam = {b + 256 * nthreads, nthreads};
+        prev = {b + 512 * nthreads, nthreads};
+        tmp = {b + 768 * nthreads, nthreads};
+        pos = {b + 1024 * nthreads, nthreads};
+        mag = {b + 1280 * nthreads, nthreads};
+        ev = {b + 1536 * nthreads, nthreads};
+    }
+};
+constexpr size_t kDecodeScratchBytes = 2048;
 
 // Syndromes from the remainder: S_j = sum_m R[m] a^{-j(m+1)}.
-template <int W>
-__device__ void synds_from_rem(const uint32_t (&rem)[W], int ecc, const uint8_t *ex, const uint8_t *lg, uint8_t *S) {
+template <int W, typename A>
+__device__ void synds_from_rem(const uint32_t (&rem)[W], int ecc, const uint8_t *ex, const uint8_t *lg, A S) {
     for (int j = 0; j < ecc; ++j) S[j] = 0;
     for (int m = 0; m < ecc; ++m) {
         const uint32_t r = rem_byte<W>(rem, m);
@@ -106,8 +125,8 @@ __device__ void synds_from_rem(const uint32_t (&rem)[W], int ecc, const uint8_t 
 
 // rs_decode::berlekamp_massey (reed_solomon.hpp:655-702); err_poly is
 // right-aligned and reversed: err_poly[ecc-1-i] holds Lambda_i.
-__device__ int rs_bm(const uint8_t *S, int ecc, const uint8_t *ex, const uint8_t *lg, uint8_t *err_poly, uint8_t *prev,
-                     uint8_t *temp) {
+template <typename A>
+__device__ int rs_bm(A S, int ecc, const uint8_t *ex, const uint8_t *lg, A err_poly, A prev, A temp) {
     for (int i = 0; i < ecc; ++i) {
         prev[i] = 0;
         err_poly[i] = 0;
@@ -144,64 +163,45 @@ __device__ int rs_bm(const uint8_t *S, int ecc, const uint8_t *ex, const uint8_t
     return errors;
 }
 
-__device__ __forceinline__ uint32_t poly_eval(const uint8_t *p, int n, uint32_t x, const uint8_t *ex,
-                                              const uint8_t *lg) {
+template <typename A>
+__device__ __forceinline__ uint32_t poly_eval(A p, int n, uint32_t x, const uint8_t *ex, const uint8_t *lg) {
     uint32_t r = 0;
     for (int i = 0; i < n; ++i) r = gmul(ex, lg, r, x) ^ p[i];
     return r;
 }
 
+// One block: rs_decode::decode (reed_solomon.hpp:559-595).  Writes the
+// status (1/0) or, when synds_out is set, only the syndromes.
 template <int W>
-__global__ void __launch_bounds__(128) rs256_decode_table_kernel(uint8_t *__restrict__ data,
-                                                                 uint8_t *__restrict__ parity, size_t nblocks,
-                                                                 int msg_len, const uint32_t *__restrict__ lut,
-                                                                 const uint8_t *__restrict__ exp512,
-                                                                 const uint8_t *__restrict__ log256, int ecc,
-                                                                 uint8_t *__restrict__ status,
-                                                                 uint8_t *__restrict__ synds_out) {
-    extern __shared__ uint32_t smem[];
-    uint32_t *s_lut = smem;
-    uint8_t *ex = reinterpret_cast<uint8_t *>(smem + 256 * W);
-    uint8_t *lg = ex + 512;
-    for (int i = threadIdx.x; i < 256 * W; i += blockDim.x) s_lut[i] = lut[i];
-    for (int i = threadIdx.x; i < 512; i += blockDim.x) ex[i] = exp512[i];
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) lg[i] = log256[i];
-    __syncthreads();
-    const size_t blk = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (blk >= nblocks) return;
-    uint8_t *d = data + blk * (size_t)msg_len;
-    uint8_t *p = parity + blk * (size_t)ecc;
-
+__device__ void decode_one(uint8_t *d, uint8_t *p, int msg_len, int ecc, const uint32_t *s_lut, const uint8_t *ex,
+                           const uint8_t *lg, const DecodeScratchG &sc, uint8_t *status, uint8_t *synds_out) {
     uint32_t rem[W];
 #pragma unroll
     for (int w = 0; w < W; ++w) rem[w] = 0;
     for (int i = 0; i < msg_len; ++i) lfsr_step<W>(rem, d[i], s_lut);
     for (int i = 0; i < ecc; ++i) lfsr_step<W>(rem, p[i], s_lut);
-
     uint32_t any = 0;
 #pragma unroll
     for (int w = 0; w < W; ++w) any |= rem[w];
-
-    DecodeScratch sc;
     if (synds_out) {
         if (any)
             synds_from_rem<W>(rem, ecc, ex, lg, sc.S);
         else
             for (int j = 0; j < ecc; ++j) sc.S[j] = 0;
-        for (int j = 0; j < ecc; ++j) synds_out[blk * (size_t)ecc + j] = sc.S[j];
+        for (int j = 0; j < ecc; ++j) synds_out[j] = sc.S[j];
         return;
     }
     if (!any) {
-        status[blk] = 1;
+        *status = 1;
         return;
     }
     synds_from_rem<W>(rem, ecc, ex, lg, sc.S);
     const int errors = rs_bm(sc.S, ecc, ex, lg, sc.lam, sc.prev, sc.tmp);
     if (errors > ecc / 2) {
-        status[blk] = 0;
+        *status = 0;
         return;
     }
-    const uint8_t *loc = &sc.lam[ecc - errors - 1];
+    const ScratchBytes loc = sc.lam + (ecc - errors - 1);
     const int size = msg_len + ecc;
     int roots = 0;
     for (int i = 0; i < size && i < 256; ++i) {
@@ -210,7 +210,7 @@ __global__ void __launch_bounds__(128) rs256_decode_table_kernel(uint8_t *__rest
         if (roots > errors) break;
     }
     if (roots != errors) {
-        status[blk] = 0;
+        *status = 0;
         return;
     }
     // Forney: omega = (S reversed * Lambda) mod x^ecc, highest degree first
@@ -221,17 +221,17 @@ __global__ void __launch_bounds__(128) rs256_decode_table_kernel(uint8_t *__rest
     int begin = errors;
     while (begin < esize && sc.ev[begin] == 0) ++begin;
     if (begin >= esize) {
-        status[blk] = 0;
+        *status = 0;
         return;
     }
     // formal derivative in place (gf_poly_deriv_pw2, galois.hpp:725-734)
-    uint8_t *lp = &sc.lam[ecc - errors - 1];
+    const ScratchBytes lp = loc;
     const int psize = errors + 1;
     for (int i = 1; i < psize; ++i) lp[psize - i] = (i & 1) ? lp[psize - i - 1] : 0;
     for (int i = 0; i < errors; ++i) {
         const uint32_t xi = ex[sc.pos[i]];
         const uint32_t xinv = ginv(ex, lg, xi);
-        const uint32_t num = poly_eval(&sc.ev[begin], esize - begin, xinv, ex, lg);
+        const uint32_t num = poly_eval(sc.ev + begin, esize - begin, xinv, ex, lg);
         const uint32_t den = poly_eval(lp + 1, errors, xinv, ex, lg);
         sc.mag[i] = (uint8_t)gmul(ex, lg, xi, gdiv(ex, lg, num, den));
     }
@@ -242,7 +242,32 @@ __global__ void __launch_bounds__(128) rs256_decode_table_kernel(uint8_t *__rest
         else
             p[pos - msg_len] ^= sc.mag[i];
     }
-    status[blk] = 1;
+    *status = 1;
+}
+
+template <int W>
+__global__ void __launch_bounds__(128) rs256_decode_table_kernel(uint8_t *__restrict__ data,
+                                                                 uint8_t *__restrict__ parity, size_t nblocks,
+                                                                 int msg_len, const uint32_t *__restrict__ lut,
+                                                                 const uint8_t *__restrict__ exp512,
+                                                                 const uint8_t *__restrict__ log256, int ecc,
+                                                                 uint8_t *__restrict__ status,
+                                                                 uint8_t *__restrict__ synds_out,
+                                                                 uint8_t *__restrict__ gscratch) {
+    extern __shared__ uint32_t smem[];
+    uint32_t *s_lut = smem;
+    uint8_t *ex = reinterpret_cast<uint8_t *>(smem + 256 * W);
+    uint8_t *lg = ex + 512;
+    for (int i = threadIdx.x; i < 256 * W; i += blockDim.x) s_lut[i] = lut[i];
+    for (int i = threadIdx.x; i < 512; i += blockDim.x) ex[i] = exp512[i];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) lg[i] = log256[i];
+    __syncthreads();
+    const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t nthreads = (size_t)gridDim.x * blockDim.x;
+    const DecodeScratchG sc(gscratch, tid, nthreads);
+    for (size_t blk = tid; blk < nblocks; blk += nthreads)
+        decode_one<W>(data + blk * (size_t)msg_len, parity + blk * (size_t)ecc, msg_len, ecc, s_lut, ex, lg, sc,
+                      status ? status + blk : nullptr, synds_out ? synds_out + blk * (size_t)ecc : nullptr);
 }
 
 // ---------------------------------------------------------------- host
@@ -313,9 +338,19 @@ static void launch_decode_table(const Rs256Code &c, uint8_t *data, uint8_t *pari
                                               200 * 1024));
         attr = true;
     }
-    rs256_decode_table_kernel<W><<<grid_for(nblocks, threads), threads, smem, st>>>(
-        data, parity, nblocks, msg_len, c.d_lut, c.d_exp512, c.d_log256, c.ecc, status, synds);
-    check_launch("rs256_decode_table_kernel");
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const size_t grid = std::min<size_t>(grid_for(nblocks, threads), (size_t)(sms > 0 ? sms : 132) * 8);
+    void *scratch = nullptr;
+    FFGPU_CHECK_CUDA(cudaMallocAsync(&scratch, grid * threads * kDecodeScratchBytes, st));
+    rs256_decode_table_kernel<W><<<(unsigned)grid, threads, smem, st>>>(data, parity, nblocks, msg_len, c.d_lut,
+                                                                        c.d_exp512, c.d_log256, c.ecc, status, synds,
+                                                                        (uint8_t *)scratch);
+    cudaError_t le = cudaGetLastError();
+    cudaFreeAsync(scratch, st);
+    if (le != cudaSuccess) throw Error(FFGPU_ECUDA, std::string("rs256_decode_table_kernel: ") + cudaGetErrorString(le));
+    launched();
 }
 
 #define FFGPU_W_DISPATCH(W, CALL)          \
