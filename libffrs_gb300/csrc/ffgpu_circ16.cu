@@ -17,7 +17,8 @@ struct ffgpu_circ16 {
     DeviceBuffer d_msg, d_ecc;
 };
 
-static cudaStream_t pick(void *stream) { return stream ? (cudaStream_t)stream : lib_stream(); }
+// NULL is the CUDA default stream, as everywhere in the CUDA runtime
+static cudaStream_t pick(void *stream) { return (cudaStream_t)stream; }
 
 // Runs the repair of one block already on the device; returns the first
 // raising outer column or SIZE_MAX, and writes the ecc back only when no

@@ -62,7 +62,7 @@ void *ffgpu_default_stream(void) {
 }
 
 int ffgpu_synchronize(void *stream) {
-    return guarded([&] { FFGPU_CHECK_CUDA(cudaStreamSynchronize(stream ? (cudaStream_t)stream : lib_stream())); });
+    return guarded([&] { FFGPU_CHECK_CUDA(cudaStreamSynchronize((cudaStream_t)stream)); });
 }
 
 int ffgpu_host_alloc(size_t bytes, void **out) {
@@ -115,7 +115,7 @@ int ffgpu_rs256_encode(const ffgpu_rs256 *code, const uint8_t *data, size_t nblo
         FFGPU_REQUIRE(code, "code is NULL");
         check_rs_geometry(*code->code, message_len);
         rs256_encode(*code->code, data, nblocks, (int)message_len, parity,
-                     stream ? (cudaStream_t)stream : lib_stream());
+                     (cudaStream_t)stream);
     });
 }
 
@@ -125,7 +125,7 @@ int ffgpu_rs256_decode(const ffgpu_rs256 *code, uint8_t *data, uint8_t *parity, 
         FFGPU_REQUIRE(code, "code is NULL");
         check_rs_geometry(*code->code, message_len);
         rs256_decode(*code->code, data, parity, nblocks, (int)message_len, status,
-                     stream ? (cudaStream_t)stream : lib_stream());
+                     (cudaStream_t)stream);
     });
 }
 
@@ -135,7 +135,7 @@ int ffgpu_rs256_synds(const ffgpu_rs256 *code, const uint8_t *data, const uint8_
         FFGPU_REQUIRE(code, "code is NULL");
         check_rs_geometry(*code->code, message_len);
         rs256_decode_table(*code->code, const_cast<uint8_t *>(data), const_cast<uint8_t *>(parity), nblocks,
-                           (int)message_len, nullptr, synds, stream ? (cudaStream_t)stream : lib_stream());
+                           (int)message_len, nullptr, synds, (cudaStream_t)stream);
     });
 }
 

@@ -18,7 +18,8 @@ struct ffgpu_rsi16 {
     DeviceBuffer d_msg, d_par, d_status, d_pos;
 };
 
-static cudaStream_t pick(void *stream) { return stream ? (cudaStream_t)stream : lib_stream(); }
+// NULL is the CUDA default stream, as everywhere in the CUDA runtime
+static cudaStream_t pick(void *stream) { return (cudaStream_t)stream; }
 
 static void check_positions(const Rsi16Code &c, const uint32_t *pos, size_t count) {
     // py_repair asserts error_pos.size() <= ecc_len (pyrsi16.hpp:605, 623); a
