@@ -94,6 +94,12 @@ FFGPU_API int ffgpu_rs256_decode_host(const ffgpu_rs256 *code, uint8_t *data, ui
                             size_t message_len, uint8_t *status);
 FFGPU_API int ffgpu_rs256_synds_host(const ffgpu_rs256 *code, const uint8_t *data, const uint8_t *parity, size_t nblocks,
                            size_t message_len, uint8_t *synds);
+/* No reference counterpart.  table_only != 0 makes this code use the
+ * byte-table kernels only (the bitsliced kernels are otherwise chosen for
+ * ecc_len 16/32 with primitive 2 and 4-byte aligned buffers); results are
+ * identical either way, the switch exists to cross-check the two kernel
+ * families. */
+FFGPU_API int ffgpu_rs256_set_table_only(ffgpu_rs256 *code, int table_only);
 
 /* ---------------------------------------------------------------- RSi16 */
 /* PyRSi16 ctor (libffrs/pyrsi16.hpp:41-125), NTT ctor (libffrs/ntt.hpp:55-123),

@@ -79,6 +79,8 @@ def build_gpu_lib(verbose=False):
         "-lineinfo",
         "-std=c++17",
         "--expt-relaxed-constexpr",
+        "-Xcudafe",
+        "--max_cost_constexpr_call=400000000",
         "-Xcompiler",
         "-fPIC",
         "-Xcompiler",

@@ -74,6 +74,7 @@ def _declare(L):
         "ffgpu_rs256_encode_host": (_I, [_P, _P, _SZ, _SZ, _P]),
         "ffgpu_rs256_decode_host": (_I, [_P, _P, _P, _SZ, _SZ, _P]),
         "ffgpu_rs256_synds_host": (_I, [_P, _P, _P, _SZ, _SZ, _P]),
+        "ffgpu_rs256_set_table_only": (_I, [_P, _I]),
         "ffgpu_rsi16_create": (_I, [_SZ, _SZ, _U32, _PP]),
         "ffgpu_rsi16_destroy": (_I, [_P]),
         "ffgpu_rsi16_info": (_I, [_P, ctypes.POINTER(_U32), ctypes.POINTER(_SZ)]),
@@ -133,6 +134,13 @@ class RS256Code:
 
     def decode(self, data_ptr, parity_ptr, nblocks, message_len, status_ptr, stream=None):
         call("ffgpu_rs256_decode", self.h, data_ptr, parity_ptr, nblocks, message_len, status_ptr, stream)
+
+    def synds(self, data_ptr, parity_ptr, nblocks, message_len, synds_ptr, stream=None):
+        call("ffgpu_rs256_synds", self.h, data_ptr, parity_ptr, nblocks, message_len, synds_ptr, stream)
+
+    def set_table_only(self, on=True):
+        """Use the byte-table kernels only (cross-check of the bitsliced ones)."""
+        call("ffgpu_rs256_set_table_only", self.h, 1 if on else 0)
 
 
 class RSi16Code:

@@ -134,8 +134,7 @@ int ffgpu_rs256_synds(const ffgpu_rs256 *code, const uint8_t *data, const uint8_
     return guarded([&] {
         FFGPU_REQUIRE(code, "code is NULL");
         check_rs_geometry(*code->code, message_len);
-        rs256_decode_table(*code->code, const_cast<uint8_t *>(data), const_cast<uint8_t *>(parity), nblocks,
-                           (int)message_len, nullptr, synds, (cudaStream_t)stream);
+        rs256_synds(*code->code, data, parity, nblocks, (int)message_len, synds, (cudaStream_t)stream);
     });
 }
 
@@ -201,9 +200,17 @@ int ffgpu_rs256_synds_host(const ffgpu_rs256 *code, const uint8_t *data, const u
         uint8_t *d_s = (uint8_t *)h->d_status.get(np);
         FFGPU_CHECK_CUDA(cudaMemcpyAsync(d_d, data, nd, cudaMemcpyHostToDevice, st));
         FFGPU_CHECK_CUDA(cudaMemcpyAsync(d_p, parity, np, cudaMemcpyHostToDevice, st));
-        rs256_decode_table(c, d_d, d_p, nblocks, (int)message_len, nullptr, d_s, st);
+        rs256_synds(c, d_d, d_p, nblocks, (int)message_len, d_s, st);
         FFGPU_CHECK_CUDA(cudaMemcpyAsync(synds, d_s, np, cudaMemcpyDeviceToHost, st));
         FFGPU_CHECK_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+int ffgpu_rs256_set_table_only(ffgpu_rs256 *code, int table_only) {
+    return guarded([&] {
+        FFGPU_REQUIRE(code, "code is NULL");
+        std::lock_guard<std::mutex> lk(code->mu);
+        code->code->table_only = table_only != 0;
     });
 }
 

@@ -170,6 +170,9 @@ __device__ __forceinline__ uint32_t poly_eval(A p, int n, uint32_t x, const uint
     return r;
 }
 
+__device__ void decode_solve(uint8_t *d, uint8_t *p, int msg_len, int ecc, const uint8_t *ex, const uint8_t *lg,
+                             const DecodeScratchG &sc, uint8_t *status);
+
 // One block: rs_decode::decode (reed_solomon.hpp:559-595).  Writes the
 // status (1/0) or, when synds_out is set, only the syndromes.
 template <int W>
@@ -196,6 +199,13 @@ __device__ void decode_one(uint8_t *d, uint8_t *p, int msg_len, int ecc, const u
         return;
     }
     synds_from_rem<W>(rem, ecc, ex, lg, sc.S);
+    decode_solve(d, p, msg_len, ecc, ex, lg, sc, status);
+}
+
+// The part of rs_decode::decode after the syndromes (reed_solomon.hpp:568-594),
+// with sc.S holding non-zero syndromes.
+__device__ void decode_solve(uint8_t *d, uint8_t *p, int msg_len, int ecc, const uint8_t *ex, const uint8_t *lg,
+                             const DecodeScratchG &sc, uint8_t *status) {
     const int errors = rs_bm(sc.S, ecc, ex, lg, sc.lam, sc.prev, sc.tmp);
     if (errors > ecc / 2) {
         *status = 0;
@@ -268,6 +278,65 @@ __global__ void __launch_bounds__(128) rs256_decode_table_kernel(uint8_t *__rest
     for (size_t blk = tid; blk < nblocks; blk += nthreads)
         decode_one<W>(data + blk * (size_t)msg_len, parity + blk * (size_t)ecc, msg_len, ecc, s_lut, ex, lg, sc,
                       status ? status + blk : nullptr, synds_out ? synds_out + blk * (size_t)ecc : nullptr);
+}
+
+// Decode from precomputed syndromes (ecc bytes per block).
+__global__ void __launch_bounds__(128) rs256_solve_kernel(uint8_t *__restrict__ data, uint8_t *__restrict__ parity,
+                                                          size_t nblocks, int msg_len,
+                                                          const uint8_t *__restrict__ exp512,
+                                                          const uint8_t *__restrict__ log256, int ecc,
+                                                          const uint8_t *__restrict__ synds,
+                                                          uint8_t *__restrict__ status,
+                                                          uint8_t *__restrict__ gscratch) {
+    __shared__ uint8_t ex[512], lg[256];
+    for (int i = threadIdx.x; i < 512; i += blockDim.x) ex[i] = exp512[i];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) lg[i] = log256[i];
+    __syncthreads();
+    const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t nthreads = (size_t)gridDim.x * blockDim.x;
+    const DecodeScratchG sc(gscratch, tid, nthreads);
+    for (size_t blk = tid; blk < nblocks; blk += nthreads) {
+        const uint8_t *s = synds + blk * (size_t)ecc;
+        uint32_t any = 0;
+        if ((ecc & 3) == 0) {
+            for (int j = 0; j < ecc; j += 4) {
+                const uint32_t w = *reinterpret_cast<const uint32_t *>(s + j);
+                any |= w;
+                sc.S[j] = (uint8_t)w;
+                sc.S[j + 1] = (uint8_t)(w >> 8);
+                sc.S[j + 2] = (uint8_t)(w >> 16);
+                sc.S[j + 3] = (uint8_t)(w >> 24);
+            }
+        } else {
+            for (int j = 0; j < ecc; ++j) {
+                any |= s[j];
+                sc.S[j] = s[j];
+            }
+        }
+        if (!any) {
+            status[blk] = 1;
+            continue;
+        }
+        decode_solve(data + blk * (size_t)msg_len, parity + blk * (size_t)ecc, msg_len, ecc, ex, lg, sc,
+                     status + blk);
+    }
+}
+
+void rs256_solve(const Rs256Code &c, uint8_t *data, uint8_t *parity, size_t nblocks, int msg_len, const uint8_t *synds,
+                 uint8_t *status, cudaStream_t st) {
+    const unsigned threads = 128;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const size_t grid = std::min<size_t>(grid_for(nblocks, threads), (size_t)(sms > 0 ? sms : 132) * 8);
+    void *scratch = nullptr;
+    FFGPU_CHECK_CUDA(cudaMallocAsync(&scratch, grid * threads * kDecodeScratchBytes, st));
+    rs256_solve_kernel<<<(unsigned)grid, threads, 0, st>>>(data, parity, nblocks, msg_len, c.d_exp512, c.d_log256,
+                                                          c.ecc, synds, status, (uint8_t *)scratch);
+    cudaError_t le = cudaGetLastError();
+    cudaFreeAsync(scratch, st);
+    if (le != cudaSuccess) throw Error(FFGPU_ECUDA, std::string("rs256_solve_kernel: ") + cudaGetErrorString(le));
+    launched();
 }
 
 // ---------------------------------------------------------------- host
@@ -381,6 +450,14 @@ void rs256_encode(const Rs256Code &c, const uint8_t *data, size_t nblocks, int m
     if (nblocks == 0) return;
     if (c.fast && rs256_fast_encode(c, data, nblocks, msg_len, parity, st)) return;
     rs256_encode_table(c, data, nblocks, msg_len, parity, st);
+}
+
+void rs256_synds(const Rs256Code &c, const uint8_t *data, const uint8_t *parity, size_t nblocks, int msg_len,
+                 uint8_t *synds, cudaStream_t st) {
+    if (nblocks == 0) return;
+    if (c.fast && rs256_fast_synds(c, data, parity, nblocks, msg_len, synds, st)) return;
+    rs256_decode_table(c, const_cast<uint8_t *>(data), const_cast<uint8_t *>(parity), nblocks, msg_len, nullptr,
+                       synds, st);
 }
 
 void rs256_decode(const Rs256Code &c, uint8_t *data, uint8_t *parity, size_t nblocks, int msg_len, uint8_t *status,

@@ -24,6 +24,7 @@ struct Rs256Code {
     uint8_t *d_log256 = nullptr;
     bool fast = false;       // bitsliced kernels available for this code
     void *fast_state = nullptr;
+    bool table_only = false;  // force the table kernels (cross-checks)
 
     Rs256Code(int ecc, int primitive, int polynomial);
     ~Rs256Code();
@@ -39,6 +40,16 @@ void rs256_encode_table(const Rs256Code &c, const uint8_t *data, size_t nblocks,
                         cudaStream_t st);
 void rs256_decode_table(const Rs256Code &c, uint8_t *data, uint8_t *parity, size_t nblocks, int msg_len,
                         uint8_t *status, uint8_t *synds, cudaStream_t st);
+
+// syndromes (ecc bytes per block, S_0 first), bitsliced kernel when it covers
+// the request, else the table kernel
+void rs256_synds(const Rs256Code &c, const uint8_t *data, const uint8_t *parity, size_t nblocks, int msg_len,
+                 uint8_t *synds, cudaStream_t st);
+// decode from syndromes already computed (ecc bytes per block)
+void rs256_solve(const Rs256Code &c, uint8_t *data, uint8_t *parity, size_t nblocks, int msg_len, const uint8_t *synds,
+                 uint8_t *status, cudaStream_t st);
+bool rs256_fast_synds(const Rs256Code &c, const uint8_t *data, const uint8_t *parity, size_t nblocks, int msg_len,
+                      uint8_t *synds, cudaStream_t st);
 
 // bitsliced fast path (rs256_bitsliced.cu); the *_encode/_decode functions
 // return false when they do not cover the request

@@ -1,12 +1,700 @@
-// Bitsliced RS256 kernels (filled in by the fast-path implementation).
+// Bitsliced RS256 kernels for the default field (primitive 2, polynomial
+// 0x11d) with ecc_len in {2, 4, 8, 16, 32}.
+//
+// Layout: a "group" is 32 consecutive blocks; bit j of a 32-bit plane word
+// belongs to block j.  Byte position i of the group is 8 planes (one per bit).
+// A GF(2^8) multiplication by a constant is then a fixed XOR network over the
+// 8 planes, computed for all 32 blocks at once with LOP3.
+//
+// The generator g(x) = prod_{j<ecc}(x - a^j) is split into factors
+// g_t(x) = prod_{16t <= j < 16t+d}(x - a^j) of degree d <= 16; one thread per
+// (group, factor) runs the byte-serial LFSR of the reference's encoder
+// (rem <- (rem >> 8) ^ lut[rem0 ^ in], reed_solomon.hpp:194-195) modulo g_t.
+// Its update needs the products g_t[m] * fb for every coefficient m; the
+// "four Russians" trick forms the 15 XOR combinations of each nibble of fb once
+// and every output plane is then old_plane ^ lo[c1] ^ hi[c2], one LOP3.
+//
+// Encode recovers the parity (data * x^ecc mod g) from the factor remainders
+// with a fixed GF(2)-linear map (Chinese remainders); decode turns each factor
+// remainder R = r * x^d mod g_t into its syndromes S_j = r(a^j) = R(a^j) a^{-jd}.
+// All selector tables are computed at compile time and reach the code as
+// template constants, so every plane index is resolved to a register.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <utility>
+
 #include "common.cuh"
 #include "rs256.cuh"
 
 namespace ffgpu {
+namespace bs {
 
-bool rs256_fast_init(Rs256Code &) { return false; }
-void rs256_fast_free(Rs256Code &) {}
-bool rs256_fast_encode(const Rs256Code &, const uint8_t *, size_t, int, uint8_t *, cudaStream_t) { return false; }
-bool rs256_fast_decode(const Rs256Code &, uint8_t *, uint8_t *, size_t, int, uint8_t *, cudaStream_t) { return false; }
+// ---------------------------------------------------------------- compile-time field
+
+struct Field {
+    uint8_t exp[512];
+    uint8_t log[256];
+};
+
+constexpr uint8_t mul_serial(uint8_t a, uint8_t b) {
+    uint8_t r = 0;
+    for (int i = 7; i >= 0; --i) {
+        r = (r & 0x80) ? (uint8_t)((r << 1) ^ 0x1d) : (uint8_t)(r << 1);
+        if (a & (1 << i)) r ^= b;
+    }
+    return r;
+}
+
+constexpr Field make_field() {
+    Field f{};
+    uint8_t x = 1;
+    for (int i = 0; i < 255; ++i) {
+        f.exp[i] = x;
+        f.log[x] = (uint8_t)i;
+        x = mul_serial(x, 2);
+    }
+    for (int i = 255; i < 512; ++i) f.exp[i] = f.exp[i - 255];
+    return f;
+}
+
+constexpr Field F = make_field();
+
+constexpr uint8_t gm(uint8_t a, uint8_t b) { return (a && b) ? F.exp[F.log[a] + F.log[b]] : 0; }
+constexpr uint8_t apow(int e) {
+    e %= 255;
+    if (e < 0) e += 255;
+    return F.exp[e];
+}
+// input-bit mask of output bit o of the multiplication by c: bit b set when
+// bit o of c * 2^b is set
+constexpr uint8_t sel_of(uint8_t c, int o) {
+    uint8_t s = 0;
+    for (int b = 0; b < 8; ++b)
+        if ((gm(c, (uint8_t)(1 << b)) >> o) & 1) s |= (uint8_t)(1 << b);
+    return s;
+}
+
+// g_t = prod_{j=J0}^{J0+D-1} (x - a^j), highest degree first
+template <int D>
+struct Poly {
+    uint8_t c[D + 1];
+};
+template <int D>
+constexpr Poly<D> factor_poly(int J0) {
+    Poly<D> g{};
+    g.c[0] = 1;
+    int len = 1;
+    for (int j = J0; j < J0 + D; ++j) {
+        uint8_t r = apow(j);
+        uint8_t ng[D + 1] = {};
+        for (int a = 0; a < len; ++a) {
+            ng[a] ^= g.c[a];
+            ng[a + 1] ^= gm(g.c[a], r);
+        }
+        ++len;
+        for (int a = 0; a < len; ++a) g.c[a] = ng[a];
+    }
+    return g;
+}
+
+// LFSR selectors: new R[m][o] = R[m+1][o] ^ (g[m+1] * fb)[o]
+template <int D>
+struct LfsrSel {
+    uint8_t s[D][8];
+};
+template <int D>
+constexpr LfsrSel<D> make_lfsr_sel(int J0) {
+    LfsrSel<D> L{};
+    const Poly<D> g = factor_poly<D>(J0);
+    for (int m = 0; m < D; ++m)
+        for (int o = 0; o < 8; ++o) L.s[m][o] = sel_of(g.c[m + 1], o);
+    return L;
+}
+
+// remainder -> syndromes: S_{J0+j} = sum_m R[m] a^{-(J0+j)(m+1)}
+template <int D>
+struct SyndSel {
+    uint8_t s[D][D][8];  // [m][j][o]
+};
+template <int D>
+constexpr SyndSel<D> make_synd_sel(int J0) {
+    SyndSel<D> S{};
+    for (int m = 0; m < D; ++m)
+        for (int j = 0; j < D; ++j)
+            for (int o = 0; o < 8; ++o) S.s[m][j][o] = sel_of(apow(-(J0 + j) * (m + 1)), o);
+    return S;
+}
+
+// ---- polynomial helpers over GF(2^8) (compile time), highest degree first
+template <int N>
+struct P {
+    int n;  // number of coefficients
+    uint8_t c[N];
+};
+
+// a mod b, b monic of degree db (db + 1 coefficients)
+template <int N, int M>
+constexpr P<N> pmod(P<N> a, const P<M> &b) {
+    const int db = b.n - 1;
+    for (int i = 0; i + db < a.n; ++i) {
+        uint8_t q = a.c[i];
+        if (!q) continue;
+        for (int k = 0; k <= db; ++k) a.c[i + k] ^= gm(q, b.c[k]);
+    }
+    // keep the low db coefficients
+    P<N> r{};
+    r.n = db;
+    for (int k = 0; k < db; ++k) r.c[k] = a.c[a.n - db + k];
+    return r;
+}
+
+template <int N>
+constexpr P<N> pmul(const P<N> &a, const P<N> &b) {
+    P<N> r{};
+    r.n = a.n + b.n - 1;
+    for (int i = 0; i < a.n; ++i)
+        for (int j = 0; j < b.n; ++j) r.c[i + j] ^= gm(a.c[i], b.c[j]);
+    return r;
+}
+
+// Chinese-remainder map for ecc = 32 (two degree-16 factors): the parity
+// coefficient vector P (32 bytes, highest first) is linear in the two factor
+// remainders R0 = data * x^16 mod g0, R1 = data * x^16 mod g1:
+//   P = data * x^32 mod g = sum_t [x^16 * R_t * E_t mod g_t] * G_t
+// with G_t = g / g_t and E_t = G_t^{-1} mod g_t.  The selector table gives,
+// for every input byte (t, m) and output bit (p, o), the input-bit mask.
+struct CrtSel {
+    uint8_t s[2][16][32][8];  // [t][m][p][o]
+};
+
+template <int N>
+constexpr P<N> pinv_mod(const P<N> &a, const P<N> &m) {
+    // inverse of a modulo m by exhaustive linear solve over the remainders:
+    // a * e = 1 mod m with deg e < deg m; solved by Gaussian elimination on
+    // the 16x16 GF(2^8) system
+    const int d = m.n - 1;
+    uint8_t A[16][17] = {};
+    for (int k = 0; k < d; ++k) {
+        // column k: a * x^(d-1-k) mod m
+        P<N> xk{};
+        xk.n = d - k;
+        xk.c[0] = 1;
+        P<N> prod = pmul(a, xk);
+        P<N> r = pmod(prod, m);
+        // r has d coefficients, highest first
+        for (int row = 0; row < d; ++row) A[row][k] = r.c[row];
+    }
+    for (int row = 0; row < d; ++row) A[row][d] = (row == d - 1) ? 1 : 0;  // target polynomial 1
+    for (int col = 0; col < d; ++col) {
+        int piv = col;
+        while (piv < d && A[piv][col] == 0) ++piv;
+        for (int k = 0; k <= d; ++k) {
+            uint8_t t = A[col][k];
+            A[col][k] = A[piv][k];
+            A[piv][k] = t;
+        }
+        uint8_t inv = F.exp[255 - F.log[A[col][col]]];
+        for (int k = 0; k <= d; ++k) A[col][k] = gm(A[col][k], inv);
+        for (int row = 0; row < d; ++row)
+            if (row != col && A[row][col]) {
+                uint8_t f = A[row][col];
+                for (int k = 0; k <= d; ++k) A[row][k] ^= gm(f, A[col][k]);
+            }
+    }
+    P<N> e{};
+    e.n = d;
+    for (int k = 0; k < d; ++k) e.c[k] = A[k][d];
+    return e;
+}
+
+constexpr CrtSel make_crt_sel() {
+    CrtSel C{};
+    using Q = P<80>;
+    Q g[2] = {};
+    for (int t = 0; t < 2; ++t) {
+        Poly<16> f = factor_poly<16>(16 * t);
+        g[t].n = 17;
+        for (int k = 0; k < 17; ++k) g[t].c[k] = f.c[k];
+    }
+    Q G[2] = {g[1], g[0]};  // g / g_t
+    Q E[2] = {pinv_mod(pmod(G[0], g[0]), g[0]), pinv_mod(pmod(G[1], g[1]), g[1])};
+    for (int t = 0; t < 2; ++t) {
+        for (int m = 0; m < 16; ++m) {
+            for (int b = 0; b < 8; ++b) {
+                // basis input: R_t = 2^b at coefficient m (x^(15-m))
+                Q r{};
+                r.n = 16;
+                r.c[m] = (uint8_t)(1 << b);
+                Q x16{};
+                x16.n = 17;
+                x16.c[0] = 1;
+                Q u = pmod(pmul(pmul(r, x16), E[t]), g[t]);  // 16 coefficients
+                Q p = pmul(u, G[t]);                            // degree <= 31: up to 32 coefficients
+                // align to 32 coefficients, highest first
+                uint8_t out[32] = {};
+                for (int k = 0; k < p.n; ++k) out[32 - p.n + k] = p.c[k];
+                for (int pp = 0; pp < 32; ++pp)
+                    for (int o = 0; o < 8; ++o)
+                        if ((out[pp] >> o) & 1) C.s[t][m][pp][o] |= (uint8_t)(1 << b);
+            }
+        }
+    }
+    return C;
+}
+
+template <int E>
+struct Code {
+    static constexpr int T = E > 16 ? E / 16 : 1;  // factors (threads per group)
+    static constexpr int D = E > 16 ? 16 : E;       // factor degree
+    static constexpr LfsrSel<D> lfsr0 = make_lfsr_sel<D>(0);
+    static constexpr LfsrSel<D> lfsr1 = make_lfsr_sel<D>(D);
+    static constexpr SyndSel<D> synd0 = make_synd_sel<D>(0);
+    static constexpr SyndSel<D> synd1 = make_synd_sel<D>(D);
+    template <int t>
+    static constexpr const LfsrSel<D> &lfsr() {
+        if constexpr (t == 0)
+            return lfsr0;
+        else
+            return lfsr1;
+    }
+    template <int t>
+    static constexpr const SyndSel<D> &synd() {
+        if constexpr (t == 0)
+            return synd0;
+        else
+            return synd1;
+    }
+};
+
+struct CrtHolder {
+    static constexpr CrtSel crt = make_crt_sel();
+};
+
+// ---------------------------------------------------------------- device helpers
+
+// 32x32 bit transpose in registers: afterwards a[c] bit r == old a[r] bit c
+__device__ __forceinline__ void transpose32(uint32_t (&a)[32]) {
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+        const uint32_t x = a[k], y = a[k + 16];
+        a[k] = __byte_perm(x, y, 0x5410);
+        a[k + 16] = __byte_perm(x, y, 0x7632);
+    }
+#pragma unroll
+    for (int k0 = 0; k0 < 32; k0 += 16)
+#pragma unroll
+        for (int k = k0; k < k0 + 8; ++k) {
+            const uint32_t x = a[k], y = a[k + 8];
+            a[k] = __byte_perm(x, y, 0x6240);
+            a[k + 8] = __byte_perm(x, y, 0x7351);
+        }
+#pragma unroll
+    for (int j = 4, sh = 0; j >= 1; j >>= 1, ++sh) {
+        const uint32_t m = j == 4 ? 0x0F0F0F0Fu : (j == 2 ? 0x33333333u : 0x55555555u);
+#pragma unroll
+        for (int k = 0; k < 32; ++k) {
+            if (k & j) continue;
+            const uint32_t t = ((a[k] >> j) ^ a[k + j]) & m;
+            a[k + j] ^= t;
+            a[k] ^= t << j;
+        }
+    }
+}
+
+// nibble combinations of 8 planes: lo[c] = XOR of f[b] for bits b of c (b < 4),
+// hi[c] the same over f[4..7]
+__device__ __forceinline__ void combos(const uint32_t (&f)[8], uint32_t (&lo)[16], uint32_t (&hi)[16]) {
+    lo[0] = 0u;
+    hi[0] = 0u;
+#pragma unroll
+    for (int c = 1; c < 16; ++c) {
+        const int low = c & -c;
+        const int bit = low == 1 ? 0 : (low == 2 ? 1 : (low == 4 ? 2 : 3));
+        lo[c] = (c == low) ? f[bit] : (lo[c ^ low] ^ f[bit]);
+        hi[c] = (c == low) ? f[bit + 4] : (hi[c ^ low] ^ f[bit + 4]);
+    }
+}
+
+template <uint8_t S>
+__device__ __forceinline__ uint32_t pick(const uint32_t (&lo)[16], const uint32_t (&hi)[16]) {
+    constexpr int a = S & 15, h = S >> 4;
+    if constexpr (a && h)
+        return lo[a] ^ hi[h];
+    else if constexpr (a)
+        return lo[a];
+    else if constexpr (h)
+        return hi[h];
+    else
+        return 0u;
+}
+
+// one LFSR step of factor t: R[m] <- R[m+1] ^ g[m+1] * (R[0] ^ in)
+template <int E, int t, int... K>
+__device__ __forceinline__ void lfsr_apply(uint32_t (&R)[Code<E>::D][8], const uint32_t (&lo)[16],
+                                           const uint32_t (&hi)[16], std::integer_sequence<int, K...>) {
+    constexpr int D = Code<E>::D;
+    ((R[K / 8][K % 8] = ((K / 8 + 1 < D) ? R[(K / 8 + 1 < D) ? K / 8 + 1 : 0][K % 8] : 0u) ^
+                        pick<Code<E>::template lfsr<t>().s[K / 8][K % 8]>(lo, hi)),
+     ...);
+}
+
+template <int E, int t>
+__device__ __forceinline__ void lfsr_step(uint32_t (&R)[Code<E>::D][8], const uint32_t (&in)[8]) {
+    constexpr int D = Code<E>::D;
+    uint32_t f[8];
+#pragma unroll
+    for (int b = 0; b < 8; ++b) f[b] = R[0][b] ^ in[b];
+    uint32_t lo[16], hi[16];
+    combos(f, lo, hi);
+    lfsr_apply<E, t>(R, lo, hi, std::make_integer_sequence<int, D * 8>{});
+}
+
+// S[j][o] ^= (c_{m,j} * r)[o] for one remainder byte m
+template <int E, int t, int M, int... K>
+__device__ __forceinline__ void synd_accum(uint32_t (&S)[Code<E>::D][8], const uint32_t (&lo)[16],
+                                           const uint32_t (&hi)[16], std::integer_sequence<int, K...>) {
+    ((S[K / 8][K % 8] ^= pick<Code<E>::template synd<t>().s[M][K / 8][K % 8]>(lo, hi)), ...);
+}
+
+template <int E, int t, int... M>
+__device__ __forceinline__ void rem_to_synd(const uint32_t *rs, int stride, uint32_t (&S)[Code<E>::D][8],
+                                            std::integer_sequence<int, M...>) {
+    constexpr int D = Code<E>::D;
+    auto one = [&](auto mc) {
+        constexpr int m = decltype(mc)::value;
+        uint32_t r[8];
+#pragma unroll
+        for (int b = 0; b < 8; ++b) r[b] = rs[(m * 8 + b) * stride];
+        uint32_t lo[16], hi[16];
+        combos(r, lo, hi);
+        synd_accum<E, t, m>(S, lo, hi, std::make_integer_sequence<int, D * 8>{});
+    };
+    (one(std::integral_constant<int, M>{}), ...);
+}
+
+// parity half p0 .. p0+15 (ecc 32): P[pp][o] ^= crt(t, m)[pp][o] over all (t, m)
+template <int T, int M, int P0, int... K>
+__device__ __forceinline__ void crt_accum(uint32_t (&Pp)[16][8], const uint32_t (&lo)[16], const uint32_t (&hi)[16],
+                                          std::integer_sequence<int, K...>) {
+    ((Pp[K / 8][K % 8] ^= pick<CrtHolder::crt.s[T][M][P0 + K / 8][K % 8]>(lo, hi)), ...);
+}
+
+template <int P0, int... TM>
+__device__ __forceinline__ void crt_map(const uint32_t *rs, int stride, uint32_t (&Pp)[16][8],
+                                        std::integer_sequence<int, TM...>) {
+    auto one = [&](auto tc) {
+        constexpr int tm = decltype(tc)::value;
+        constexpr int t = tm / 16, m = tm % 16;
+        uint32_t r[8];
+#pragma unroll
+        for (int b = 0; b < 8; ++b) r[b] = rs[((t * 16 + m) * 8 + b) * stride];
+        uint32_t lo[16], hi[16];
+        combos(r, lo, hi);
+        crt_accum<t, m, P0>(Pp, lo, hi, std::make_integer_sequence<int, 128>{});
+    };
+    (one(std::integral_constant<int, TM>{}), ...);
+}
+
+// ---------------------------------------------------------------- window loader
+
+// Tile geometry: G groups of 32 blocks per CTA.  A window is 32 consecutive
+// codeword positions of every block of the tile, held as 8 words per block.
+// Column q (bytes 4q .. 4q+3 of the window) of group g lives in words
+// [g*256 + q*32, +32), with word j (block j) stored at j ^ (g & 31): a warp
+// always works on 32 consecutive groups (or 32 blocks of one group), so every
+// shared-memory access below touches 32 different banks.
+__device__ __forceinline__ int swz(int g) { return g & 31; }
+
+// Load window bytes [p0, p0 + 32) of every block of the tile from the segment
+// `base` (block b at base + b * seg_len; total bytes of the segment array in
+// `total`).  Positions at or beyond seg_len are never consumed.
+__device__ __forceinline__ void load_window(uint32_t *buf, const uint8_t *__restrict__ base, size_t seg_len,
+                                            size_t total, size_t first_block, int nblocks_tile, int p0, int G) {
+    for (int b = threadIdx.x; b < G * 32; b += blockDim.x) {
+        const int g = b >> 5, j = b & 31;
+        uint32_t w[9];
+        uint32_t sh = 0;
+        if (b < nblocks_tile) {
+            const size_t start = (first_block + b) * seg_len + p0;
+            const size_t a0 = start & ~(size_t)3;
+            sh = (uint32_t)(start & 3) * 8;
+#pragma unroll
+            for (int i = 0; i < 9; ++i)
+                w[i] = (a0 + 4 * i < total) ? __ldg(reinterpret_cast<const uint32_t *>(base + a0 + 4 * i)) : 0u;
+        } else {
+#pragma unroll
+            for (int i = 0; i < 9; ++i) w[i] = 0u;
+        }
+        uint32_t *dst = buf + g * 256 + (j ^ swz(g));
+#pragma unroll
+        for (int k = 0; k < 8; ++k) dst[k * 32] = __funnelshift_r(w[k], w[k + 1], sh);
+    }
+}
+
+// transpose the columns this thread owns (q = t, t + T, ...) in place
+template <int T>
+__device__ __forceinline__ void transpose_window(uint32_t *buf, int g, int t) {
+    const int s = swz(g);
+#pragma unroll 1
+    for (int q = t; q < 8; q += T) {
+        uint32_t *col = buf + g * 256 + q * 32;
+        uint32_t a[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) a[j] = col[j ^ s];
+        transpose32(a);
+#pragma unroll
+        for (int c = 0; c < 32; ++c) col[c ^ s] = a[c];
+    }
+}
+
+// planes of window position i (0..31) of group g
+template <int T>
+__device__ __forceinline__ void read_planes(const uint32_t *buf, int g, int i, uint32_t (&in)[8]) {
+    const int q = i >> 2, qb = i & 3;
+    const int s = swz(g);
+    const uint32_t *col = buf + g * 256 + q * 32;
+#pragma unroll
+    for (int b = 0; b < 8; ++b) in[b] = col[(qb * 8 + b) ^ s];
+}
+
+// ---------------------------------------------------------------- kernels
+
+constexpr int kGroups = 64;  // groups per CTA tile (2048 blocks)
+
+template <int E, int t>
+__device__ __forceinline__ void run_lfsr_window(const uint32_t *buf, int g, int npos, uint32_t (&R)[Code<E>::D][8]) {
+    constexpr int T = Code<E>::T;
+#pragma unroll 2
+    for (int i = 0; i < npos; ++i) {
+        uint32_t in[8];
+        read_planes<T>(buf, g, i, in);
+        lfsr_step<E, t>(R, in);
+    }
+}
+
+// Factor remainders R_t = (codeword segment) * x^d mod g_t over the segments
+// (data, message_len bytes per block) then optionally (parity, E bytes).
+template <int E>
+__device__ __forceinline__ size_t total_bytes_e(int seg, size_t nblocks, int msg_len) {
+    return seg == 0 ? nblocks * (size_t)msg_len : nblocks * (size_t)E;
+}
+
+template <int E, int t>
+__device__ __forceinline__ void factor_remainder(uint32_t *buf, const uint8_t *data, int msg_len,
+                                                 const uint8_t *parity, size_t first, int nb_tile, int g,
+                                                 size_t nblocks_total, uint32_t (&R)[Code<E>::D][8]) {
+    auto total_bytes = [](int seg, size_t nb, int ml) { return total_bytes_e<E>(seg, nb, ml); };
+    constexpr int T = Code<E>::T;
+#pragma unroll
+    for (int m = 0; m < Code<E>::D; ++m)
+#pragma unroll
+        for (int b = 0; b < 8; ++b) R[m][b] = 0u;
+    for (int seg = 0; seg < (parity ? 2 : 1); ++seg) {
+        const uint8_t *base = seg == 0 ? data : parity;
+        const int len = seg == 0 ? msg_len : E;
+        for (int p0 = 0; p0 < len; p0 += 32) {
+            __syncthreads();
+            load_window(buf, base, (size_t)len, total_bytes(seg, nblocks_total, msg_len), first, nb_tile, p0,
+                        kGroups);
+            __syncthreads();
+            transpose_window<T>(buf, g, t);
+            __syncthreads();
+            run_lfsr_window<E, t>(buf, g, min(32, len - p0), R);
+        }
+    }
+}
+
+template <int E>
+__global__ void __launch_bounds__(kGroups * Code<E>::T) bs_synd_kernel(const uint8_t *__restrict__ data,
+                                                                         const uint8_t *__restrict__ parity,
+                                                                         size_t nblocks, int msg_len,
+                                                                         uint8_t *__restrict__ synds) {
+    constexpr int T = Code<E>::T, D = Code<E>::D;
+    __shared__ uint32_t buf[kGroups * 256];
+    const int tid = threadIdx.x;
+    // one factor per warp: warps (2w, 2w+1) share the 32 groups 32w .. 32w+31
+    const int warp = tid >> 5, lane = tid & 31;
+    const int t = warp % T, g = (warp / T) * 32 + lane;
+    const size_t ntiles = (nblocks + kGroups * 32 - 1) / (kGroups * 32);
+    for (size_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const size_t first = tile * kGroups * 32;
+        const int nb_tile = (int)min((size_t)kGroups * 32, nblocks - first);
+        uint32_t R[D][8];
+        uint32_t S[D][8];
+        if (t == 0)
+            factor_remainder<E, 0>(buf, data, msg_len, parity, first, nb_tile, g, nblocks, R);
+        else if constexpr (T > 1)
+            factor_remainder<E, 1>(buf, data, msg_len, parity, first, nb_tile, g, nblocks, R);
+        // stash remainders, interleaved by thread
+        __syncthreads();
+        const int stride = kGroups * T;
+#pragma unroll
+        for (int m = 0; m < D; ++m)
+#pragma unroll
+            for (int b = 0; b < 8; ++b) buf[(m * 8 + b) * stride + tid] = R[m][b];
+#pragma unroll
+        for (int m = 0; m < D; ++m)
+#pragma unroll
+            for (int b = 0; b < 8; ++b) S[m][b] = 0u;
+        if (t == 0)
+            rem_to_synd<E, 0>(buf + tid, stride, S, std::make_integer_sequence<int, D>{});
+        else if constexpr (T > 1)
+            rem_to_synd<E, 1>(buf + tid, stride, S, std::make_integer_sequence<int, D>{});
+        // S planes -> per-block syndrome bytes: 4 syndromes per transpose
+#pragma unroll
+        for (int q = 0; q < (D + 3) / 4; ++q) {
+            uint32_t a[32];
+#pragma unroll
+            for (int k = 0; k < 32; ++k) a[k] = (q * 4 + k / 8 < D) ? S[(q * 4 + k / 8 < D) ? q * 4 + k / 8 : 0][k % 8] : 0u;
+            transpose32(a);
+            const int jb = t * D + q * 4;  // first syndrome index of this word
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                const size_t blk = first + (size_t)g * 32 + j;
+                if ((int)(g * 32 + j) < nb_tile) {
+                    uint8_t *o = synds + blk * E + jb;
+                    if (D >= 4) {
+                        *reinterpret_cast<uint32_t *>(o) = a[j];
+                    } else {
+                        for (int k = 0; k < D; ++k) o[k] = (uint8_t)(a[j] >> (8 * k));
+                    }
+                }
+            }
+        }
+    }
+}
+
+// encode, ecc 32 only (two factors): parity = CRT(R0, R1)
+__global__ void __launch_bounds__(kGroups * 2) bs_encode32_kernel(const uint8_t *__restrict__ data, size_t nblocks,
+                                                                  int msg_len, uint8_t *__restrict__ parity) {
+    constexpr int E = 32, T = 2, D = 16;
+    __shared__ uint32_t buf[kGroups * 256];
+    const int tid = threadIdx.x;
+    const int warp = tid >> 5, lane = tid & 31;
+    const int t = warp % T, g = (warp / T) * 32 + lane;
+    const size_t ntiles = (nblocks + kGroups * 32 - 1) / (kGroups * 32);
+    for (size_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const size_t first = tile * kGroups * 32;
+        const int nb_tile = (int)min((size_t)kGroups * 32, nblocks - first);
+        uint32_t R[D][8];
+        if (t == 0)
+            factor_remainder<E, 0>(buf, data, msg_len, nullptr, first, nb_tile, g, nblocks, R);
+        else
+            factor_remainder<E, 1>(buf, data, msg_len, nullptr, first, nb_tile, g, nblocks, R);
+        __syncthreads();
+        // stash: group g's two factor remainders, [(t*16+m)*8+b] * stride + g
+        const int stride = kGroups;
+#pragma unroll
+        for (int m = 0; m < D; ++m)
+#pragma unroll
+            for (int b = 0; b < 8; ++b) buf[((t * 16 + m) * 8 + b) * stride + g] = R[m][b];
+        __syncthreads();
+        // thread t computes parity bytes 16t .. 16t+15 from all 32 remainder bytes
+        uint32_t Pp[16][8];
+#pragma unroll
+        for (int p = 0; p < 16; ++p)
+#pragma unroll
+            for (int o = 0; o < 8; ++o) Pp[p][o] = 0u;
+        if (t == 0)
+            crt_map<0>(buf + g, stride, Pp, std::make_integer_sequence<int, 32>{});
+        else
+            crt_map<16>(buf + g, stride, Pp, std::make_integer_sequence<int, 32>{});
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            uint32_t a[32];
+#pragma unroll
+            for (int k = 0; k < 32; ++k) a[k] = Pp[q * 4 + k / 8][k % 8];
+            transpose32(a);
+            const int pb = t * 16 + q * 4;
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                if ((int)(g * 32 + j) < nb_tile)
+                    *reinterpret_cast<uint32_t *>(parity + (first + (size_t)g * 32 + j) * E + pb) = a[j];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace bs
+
+// ---------------------------------------------------------------- dispatch
+
+struct FastState {
+    int ecc;
+};
+
+bool rs256_fast_init(Rs256Code &c) {
+    if (c.primitive != 2 || (c.polynomial & 0xff) != 0x1d) return false;
+    if (c.ecc != 32 && c.ecc != 16 && c.ecc != 8 && c.ecc != 4 && c.ecc != 2) return false;
+    c.fast_state = new FastState{c.ecc};
+    return true;
+}
+
+void rs256_fast_free(Rs256Code &c) {
+    delete static_cast<FastState *>(c.fast_state);
+    c.fast_state = nullptr;
+}
+
+static int sm_count() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 132;
+    }
+    return n;
+}
+
+static unsigned tiles_grid(size_t nblocks) {
+    const size_t tiles = (nblocks + bs::kGroups * 32 - 1) / (bs::kGroups * 32);
+    return (unsigned)std::max<size_t>(1, std::min<size_t>(tiles, (size_t)sm_count() * 4));
+}
+
+static bool aligned4(const void *p) { return ((uintptr_t)p & 3) == 0; }
+
+bool rs256_fast_encode(const Rs256Code &c, const uint8_t *data, size_t nblocks, int msg_len, uint8_t *parity,
+                       cudaStream_t st) {
+    if (!c.fast || c.table_only || c.ecc != 32 || !aligned4(data) || !aligned4(parity)) return false;
+    if (!nblocks) return true;
+    bs::bs_encode32_kernel<<<tiles_grid(nblocks), bs::kGroups * 2, 0, st>>>(data, nblocks, msg_len, parity);
+    check_launch("bs_encode32_kernel");
+    return true;
+}
+
+// syndromes of nblocks blocks, ecc bytes each
+bool rs256_fast_synds(const Rs256Code &c, const uint8_t *data, const uint8_t *parity, size_t nblocks, int msg_len,
+                      uint8_t *synds, cudaStream_t st) {
+    if (!c.fast || c.table_only || (c.ecc != 32 && c.ecc != 16)) return false;
+    if (!aligned4(data) || !aligned4(parity) || !aligned4(synds)) return false;
+    if (!nblocks) return true;
+    if (c.ecc == 32)
+        bs::bs_synd_kernel<32><<<tiles_grid(nblocks), bs::kGroups * 2, 0, st>>>(data, parity, nblocks, msg_len, synds);
+    else
+        bs::bs_synd_kernel<16><<<tiles_grid(nblocks), bs::kGroups, 0, st>>>(data, parity, nblocks, msg_len, synds);
+    check_launch("bs_synd_kernel");
+    return true;
+}
+
+bool rs256_fast_decode(const Rs256Code &c, uint8_t *data, uint8_t *parity, size_t nblocks, int msg_len,
+                       uint8_t *status, cudaStream_t st) {
+    if (!c.fast || c.table_only || (c.ecc != 32 && c.ecc != 16)) return false;
+    if (!aligned4(data) || !aligned4(parity)) return false;
+    if (!nblocks) return true;
+    void *synds = nullptr;
+    FFGPU_CHECK_CUDA(cudaMallocAsync(&synds, nblocks * (size_t)c.ecc, st));
+    try {
+        rs256_fast_synds(c, data, parity, nblocks, msg_len, (uint8_t *)synds, st);
+        rs256_solve(c, data, parity, nblocks, msg_len, (const uint8_t *)synds, status, st);
+    } catch (...) {
+        cudaFreeAsync(synds, st);
+        throw;
+    }
+    FFGPU_CHECK_CUDA(cudaFreeAsync(synds, st));
+    return true;
+}
 
 }  // namespace ffgpu
