@@ -506,7 +506,12 @@ __device__ __forceinline__ void factor_remainder(uint32_t *buf, const uint8_t *d
     }
 }
 
-template <int E>
+// Syndromes of every block.  PLANES = false: E bytes per block, S_0 first.
+// PLANES = true: bitsliced, for the solve kernel: group G (blocks 32G ..
+// 32G+31) keeps plane word k = 8j + b (bit b of S_j) at
+// planes[(G / 32) * (E * 8 * 32) + k * 32 + G % 32], so that 32 consecutive
+// groups read or write one plane word with one coalesced access.
+template <int E, bool PLANES>
 __global__ void __launch_bounds__(kGroups * Code<E>::T) bs_synd_kernel(const uint8_t *__restrict__ data,
                                                                          const uint8_t *__restrict__ parity,
                                                                          size_t nblocks, int msg_len,
@@ -542,23 +547,34 @@ __global__ void __launch_bounds__(kGroups * Code<E>::T) bs_synd_kernel(const uin
             rem_to_synd<E, 0>(buf + tid, stride, S, std::make_integer_sequence<int, D>{});
         else if constexpr (T > 1)
             rem_to_synd<E, 1>(buf + tid, stride, S, std::make_integer_sequence<int, D>{});
-        // S planes -> per-block syndrome bytes: 4 syndromes per transpose
+        if constexpr (PLANES) {
+            const size_t G = first / 32 + g;
+            if ((int)(g * 32) < nb_tile) {
+                uint32_t *o = reinterpret_cast<uint32_t *>(synds) + (G / 32) * (size_t)(E * 8 * 32) + G % 32;
 #pragma unroll
-        for (int q = 0; q < (D + 3) / 4; ++q) {
-            uint32_t a[32];
+                for (int m = 0; m < D; ++m)
 #pragma unroll
-            for (int k = 0; k < 32; ++k) a[k] = (q * 4 + k / 8 < D) ? S[(q * 4 + k / 8 < D) ? q * 4 + k / 8 : 0][k % 8] : 0u;
-            transpose32(a);
-            const int jb = t * D + q * 4;  // first syndrome index of this word
+                    for (int b = 0; b < 8; ++b) o[((t * D + m) * 8 + b) * 32] = S[m][b];
+            }
+        } else {
+            // S planes -> per-block syndrome bytes: 4 syndromes per transpose
 #pragma unroll
-            for (int j = 0; j < 32; ++j) {
-                const size_t blk = first + (size_t)g * 32 + j;
-                if ((int)(g * 32 + j) < nb_tile) {
-                    uint8_t *o = synds + blk * E + jb;
-                    if (D >= 4) {
-                        *reinterpret_cast<uint32_t *>(o) = a[j];
-                    } else {
-                        for (int k = 0; k < D; ++k) o[k] = (uint8_t)(a[j] >> (8 * k));
+            for (int q = 0; q < (D + 3) / 4; ++q) {
+                uint32_t a[32];
+#pragma unroll
+                for (int k = 0; k < 32; ++k) a[k] = (q * 4 + k / 8 < D) ? S[(q * 4 + k / 8 < D) ? q * 4 + k / 8 : 0][k % 8] : 0u;
+                transpose32(a);
+                const int jb = t * D + q * 4;  // first syndrome index of this word
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const size_t blk = first + (size_t)g * 32 + j;
+                    if ((int)(g * 32 + j) < nb_tile) {
+                        uint8_t *o = synds + blk * E + jb;
+                        if (D >= 4) {
+                            *reinterpret_cast<uint32_t *>(o) = a[j];
+                        } else {
+                            for (int k = 0; k < D; ++k) o[k] = (uint8_t)(a[j] >> (8 * k));
+                        }
                     }
                 }
             }
@@ -618,6 +634,403 @@ __global__ void __launch_bounds__(kGroups * 2) bs_encode32_kernel(const uint8_t 
     }
 }
 
+
+// ---------------------------------------------------------------- bitsliced solve
+//
+// Decoding from the bitsliced syndromes, 32 blocks per plane word, following
+// rs_decode::decode (reed_solomon.hpp:559-595) step by step:
+//   * Berlekamp-Massey (berlekamp_massey, reed_solomon.hpp:655-702) in its
+//     normalised form C <- C - (d / b) x^m B, with x^m B kept pre-shifted and
+//     1 / b kept next to it; the length L is a 6-plane bitsliced counter;
+//   * error evaluator Omega = S * C mod x^t (its degree is below L whenever
+//     the decoder succeeds, so t coefficients are exact);
+//   * Chien search over the positions 0 .. size-1 with x = a^{-i}, as the
+//     reference scans them, counting the roots of every block;
+//   * Forney: e = Omega(x) / Lodd(x) with Lodd the odd-degree part of C, which
+//     equals X * Omega(X^-1) / C'(X^-1) of the reference in characteristic 2.
+// A block is repaired when its syndromes are non-zero, L <= ecc/2 and the
+// number of roots equals L; this is exactly when the reference returns true
+// (with roots == L, C has L distinct roots and Omega != 0).
+//
+// One CTA = 32 groups (1024 blocks) and two warps: warp h keeps the
+// coefficients C_i, i = hK+1 .. hK+K (K = t/2) and the evaluator terms
+// Omega_k, k = 2v+h; the two halves meet through shared memory.
+
+__device__ __forceinline__ void reduce15(uint32_t (&p)[15], uint32_t (&r)[8]) {
+#pragma unroll
+    for (int k = 14; k >= 8; --k) {  // x^8 = x^4 + x^3 + x^2 + 1
+        p[k - 8] ^= p[k];
+        p[k - 6] ^= p[k];
+        p[k - 5] ^= p[k];
+        p[k - 4] ^= p[k];
+    }
+#pragma unroll
+    for (int o = 0; o < 8; ++o) r[o] = p[o];
+}
+
+// r = a * b (r may alias a or b)
+__device__ __forceinline__ void vmul(const uint32_t (&a)[8], const uint32_t (&b)[8], uint32_t (&r)[8]) {
+    uint32_t p[15];
+#pragma unroll
+    for (int k = 0; k < 15; ++k) p[k] = 0u;
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) p[i + j] ^= a[i] & b[j];
+    reduce15(p, r);
+}
+
+__device__ __forceinline__ void vsqr(const uint32_t (&a)[8], uint32_t (&r)[8]) {
+    uint32_t p[15];
+#pragma unroll
+    for (int k = 0; k < 15; ++k) p[k] = (k & 1) ? 0u : a[k >> 1];
+    reduce15(p, r);
+}
+
+// r = x^254 = 1 / x (0 for x = 0): x^240 * x^14 with x^240 = (x^15)^16
+__device__ __forceinline__ void vinv(const uint32_t (&x)[8], uint32_t (&r)[8]) {
+    uint32_t x2[8], x3[8], x12[8], x14[8], y[8];
+    vsqr(x, x2);
+    vmul(x2, x, x3);
+    vsqr(x3, y);
+    vsqr(y, x12);
+    vmul(x12, x2, x14);
+    vmul(x12, x3, y);  // x^15
+#pragma unroll
+    for (int k = 0; k < 4; ++k) vsqr(y, y);
+    vmul(y, x14, r);
+}
+
+template <uint8_t S>
+__device__ __forceinline__ uint32_t xsel(const uint32_t (&in)[8]) {
+    uint32_t r = 0u;
+    if constexpr ((S & 1) != 0) r ^= in[0];
+    if constexpr ((S & 2) != 0) r ^= in[1];
+    if constexpr ((S & 4) != 0) r ^= in[2];
+    if constexpr ((S & 8) != 0) r ^= in[3];
+    if constexpr ((S & 16) != 0) r ^= in[4];
+    if constexpr ((S & 32) != 0) r ^= in[5];
+    if constexpr ((S & 64) != 0) r ^= in[6];
+    if constexpr ((S & 128) != 0) r ^= in[7];
+    return r;
+}
+
+template <uint8_t C, int... O>
+__device__ __forceinline__ void cmul_(const uint32_t (&in)[8], uint32_t (&out)[8], std::integer_sequence<int, O...>) {
+    ((out[O] = xsel<sel_of(C, O)>(in)), ...);
+}
+
+// x <- C * x, C a compile-time constant
+template <uint8_t C>
+__device__ __forceinline__ void cmul_inplace(uint32_t (&x)[8]) {
+    uint32_t o[8];
+    cmul_<C>(x, o, std::make_integer_sequence<int, 8>{});
+#pragma unroll
+    for (int b = 0; b < 8; ++b) x[b] = o[b];
+}
+
+// per-block L <= c for a warp-uniform constant c
+__device__ __forceinline__ uint32_t le_const(const uint32_t (&L)[6], int c) {
+    uint32_t gt = 0u, eq = ~0u;
+#pragma unroll
+    for (int b = 5; b >= 0; --b) {
+        const uint32_t cb = ((c >> b) & 1) ? ~0u : 0u;
+        gt |= eq & L[b] & ~cb;
+        eq &= ~(L[b] ^ cb);
+    }
+    return ~gt;
+}
+
+// L <- cond ? a - L : L (6 bits, a warp-uniform constant)
+__device__ __forceinline__ void l_update(uint32_t (&L)[6], int a, uint32_t cond) {
+    uint32_t carry = ~0u;  // a + ~L + 1
+#pragma unroll
+    for (int b = 0; b < 6; ++b) {
+        const uint32_t ab = ((a >> b) & 1) ? ~0u : 0u;
+        const uint32_t x = ~L[b];
+        const uint32_t s = ab ^ x ^ carry;
+        carry = (ab & x) | (carry & (ab ^ x));
+        L[b] = (cond & s) | (~cond & L[b]);
+    }
+}
+
+template <int E>
+struct SolveGeom {
+    static constexpr int t = E / 2;
+    static constexpr int K = t / 2;          // coefficients per warp
+    static constexpr int kS = E * 8 * 32;    // words: syndrome planes of 32 groups
+    static constexpr int kC = t * 8 * 32;    // words: C_1..C_t planes of 32 groups (also the BM exchange)
+    static constexpr int kX = 2 * 2 * 2 * 24 * 32;  // words: Chien exchange (2 buffers x 2 positions x 2 warps)
+    static constexpr int kSX = kS > kX ? kS : kX;
+    static constexpr size_t smem = (size_t)(kSX + kC) * 4 + 2 * 32 * 32 + 768;
+};
+
+// C_i <- C_i a^{-i}, Omega_k <- Omega_k a^{-k}
+template <int E, int H, int... U>
+__device__ __forceinline__ void chien_advance(uint32_t (&Ct)[SolveGeom<E>::K][8], uint32_t (&Ot)[SolveGeom<E>::K][8],
+                                              std::integer_sequence<int, U...>) {
+    constexpr int K = SolveGeom<E>::K;
+    (cmul_inplace<apow(-(H * K + 1 + U))>(Ct[U]), ...);
+    (cmul_inplace<apow(-(2 * U + H))>(Ot[U]), ...);
+}
+
+// One Chien position for warp H: partial sums of the even / odd C terms and of
+// the Omega terms, then every term advances by its constant a^{-i}.
+template <int E, int H>
+__device__ __forceinline__ void chien_step(uint32_t (&Ct)[SolveGeom<E>::K][8], uint32_t (&Ot)[SolveGeom<E>::K][8],
+                                           uint32_t *out, int stride) {
+    constexpr int K = SolveGeom<E>::K;
+    uint32_t pe[8], po[8], pw[8];
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+        pe[b] = (H == 0 && b == 0) ? ~0u : 0u;  // C_0 = 1
+        po[b] = 0u;
+        pw[b] = 0u;
+    }
+#pragma unroll
+    for (int u = 0; u < K; ++u) {
+        const int i = H * K + 1 + u;
+#pragma unroll
+        for (int b = 0; b < 8; ++b) {
+            if (i & 1)
+                po[b] ^= Ct[u][b];
+            else
+                pe[b] ^= Ct[u][b];
+        }
+    }
+#pragma unroll
+    for (int v = 0; v < K; ++v)
+#pragma unroll
+        for (int b = 0; b < 8; ++b) pw[b] ^= Ot[v][b];
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+        out[b * stride] = pe[b];
+        out[(8 + b) * stride] = po[b];
+        out[(16 + b) * stride] = pw[b];
+    }
+    chien_advance<E, H>(Ct, Ot, std::make_integer_sequence<int, K>{});
+}
+
+template <int E>
+__global__ void __launch_bounds__(64) bs_solve_kernel(uint8_t *__restrict__ data, uint8_t *__restrict__ parity,
+                                                      size_t nblocks, int msg_len, uint32_t *__restrict__ planes,
+                                                      uint8_t *__restrict__ status,
+                                                      const uint8_t *__restrict__ exp512,
+                                                      const uint8_t *__restrict__ log256) {
+    using G = SolveGeom<E>;
+    constexpr int t = G::t, K = G::K;
+    extern __shared__ __align__(16) uint32_t sm[];
+    uint32_t *Ssm = sm;                    // [E*8][32] syndrome planes; later the Chien exchange
+    uint32_t *Csm = sm + G::kSX;           // [t*8][32] C planes; earlier the BM exchange
+    uint8_t *cnt = reinterpret_cast<uint8_t *>(Csm + G::kC);  // [2][32 blocks][32 groups]
+    uint8_t *ex = cnt + 2 * 32 * 32;       // exp[512], log[256]
+    uint8_t *lg = ex + 512;
+
+    const int lane = threadIdx.x & 31, h = threadIdx.x >> 5;
+    const size_t ngroups = (nblocks + 31) / 32;
+    const size_t tile = blockIdx.x;
+    const size_t grp = tile * 32 + lane;
+    const bool valid = grp < ngroups;
+    uint32_t *tplanes = planes + tile * (size_t)G::kS;
+
+    for (int i = threadIdx.x; i < 512; i += 64) ex[i] = exp512[i];
+    for (int i = threadIdx.x; i < 256; i += 64) lg[i] = log256[i];
+    for (int i = threadIdx.x; i < 2 * 32 * 32; i += 64) cnt[i] = 0;
+    // phase 0: syndrome planes of the 32 groups
+    for (int k = h; k < E * 8; k += 2) Ssm[k * 32 + lane] = valid ? tplanes[k * 32 + lane] : 0u;
+    __syncthreads();
+    uint32_t anyS = 0u;
+    for (int k = 0; k < E * 8; ++k) anyS |= Ssm[k * 32 + lane];
+    const size_t blk0 = grp * 32;
+    const uint32_t vmask = !valid ? 0u : (nblocks - blk0 >= 32 ? ~0u : ((1u << (nblocks - blk0)) - 1u));
+
+    // phase 1: Berlekamp-Massey
+    uint32_t C[K][8], Bs[K][8], binv[8], L[6];
+#pragma unroll
+    for (int u = 0; u < K; ++u)
+#pragma unroll
+        for (int b = 0; b < 8; ++b) {
+            C[u][b] = 0u;
+            Bs[u][b] = (h == 0 && u == 0 && b == 0) ? ~0u : 0u;  // x^1 * B, B = 1
+        }
+#pragma unroll
+    for (int b = 0; b < 8; ++b) binv[b] = b == 0 ? ~0u : 0u;
+#pragma unroll
+    for (int b = 0; b < 6; ++b) L[b] = 0u;
+    uint32_t *Xb = Csm;  // [2 buffers][4 x 8 words][32]
+#pragma unroll 1
+    for (int n = 0; n < E; ++n) {
+        uint32_t dp[8];
+#pragma unroll
+        for (int b = 0; b < 8; ++b) dp[b] = h == 0 ? Ssm[(n * 8 + b) * 32 + lane] : 0u;
+#pragma unroll
+        for (int u = 0; u < K; ++u) {
+            const int j = n - (h * K + 1 + u);
+            if (j >= 0) {
+                uint32_t sj[8], pr[8];
+#pragma unroll
+                for (int b = 0; b < 8; ++b) sj[b] = Ssm[(j * 8 + b) * 32 + lane];
+                vmul(C[u], sj, pr);
+#pragma unroll
+                for (int b = 0; b < 8; ++b) dp[b] ^= pr[b];
+            }
+        }
+        uint32_t *X = Xb + (n & 1) * (32 * 32);
+#pragma unroll
+        for (int b = 0; b < 8; ++b) X[(h * 8 + b) * 32 + lane] = dp[b];
+        if (h == 0) {
+#pragma unroll
+            for (int b = 0; b < 8; ++b) {
+                X[(16 + b) * 32 + lane] = C[K - 1][b];
+                X[(24 + b) * 32 + lane] = Bs[K - 1][b];
+            }
+        }
+        __syncthreads();
+        uint32_t d[8], nzd = 0u;
+#pragma unroll
+        for (int b = 0; b < 8; ++b) {
+            d[b] = X[b * 32 + lane] ^ X[(8 + b) * 32 + lane];
+            nzd |= d[b];
+        }
+        const uint32_t cond = nzd & le_const(L, n >> 1);
+        uint32_t q[8], dinv[8];
+        vmul(d, binv, q);
+        vinv(d, dinv);
+        // C_i ^= q * Bs_i and Bs_i <- cond ? C_{i-1} : Bs_{i-1}, from the top down
+#pragma unroll
+        for (int u = K - 1; u >= 0; --u) {
+            uint32_t pr[8];
+            vmul(q, Bs[u], pr);
+#pragma unroll
+            for (int b = 0; b < 8; ++b) {
+                uint32_t lc, lb;
+                if (u > 0) {
+                    lc = C[u - 1][b];
+                    lb = Bs[u - 1][b];
+                } else if (h == 0) {
+                    lc = b == 0 ? ~0u : 0u;  // C_0 = 1, Bs_0 = 0
+                    lb = 0u;
+                } else {
+                    lc = X[(16 + b) * 32 + lane];
+                    lb = X[(24 + b) * 32 + lane];
+                }
+                C[u][b] ^= pr[b];
+                Bs[u][b] = (cond & lc) | (~cond & lb);
+            }
+        }
+#pragma unroll
+        for (int b = 0; b < 8; ++b) binv[b] = (cond & dinv[b]) | (~cond & binv[b]);
+        l_update(L, n + 1, cond);
+    }
+    __syncthreads();  // BM exchange reads done before Csm is rewritten
+
+    // phase 2: Omega_k = S_k + sum_{i=1}^{k} C_i S_{k-i}, k = 2v + h
+#pragma unroll
+    for (int u = 0; u < K; ++u)
+#pragma unroll
+        for (int b = 0; b < 8; ++b) Csm[((h * K + u) * 8 + b) * 32 + lane] = C[u][b];
+    __syncthreads();
+    uint32_t Ot[K][8];
+#pragma unroll
+    for (int v = 0; v < K; ++v) {
+        const int k = 2 * v + h;
+#pragma unroll
+        for (int b = 0; b < 8; ++b) Ot[v][b] = Ssm[(k * 8 + b) * 32 + lane];
+        for (int i = 1; i <= k; ++i) {
+            uint32_t ci[8], sj[8], pr[8];
+#pragma unroll
+            for (int b = 0; b < 8; ++b) {
+                ci[b] = Csm[((i - 1) * 8 + b) * 32 + lane];
+                sj[b] = Ssm[((k - i) * 8 + b) * 32 + lane];
+            }
+            vmul(ci, sj, pr);
+#pragma unroll
+            for (int b = 0; b < 8; ++b) Ot[v][b] ^= pr[b];
+        }
+    }
+    __syncthreads();  // Ssm becomes the Chien exchange
+
+    // phase 3: Chien search and Forney, two positions per exchange
+    const int size = msg_len + E;
+    uint8_t *corr = reinterpret_cast<uint8_t *>(tplanes) + (size_t)lane * (E * 32);  // [32 blocks][t][2]
+    uint8_t *mycnt = cnt + h * 1024;
+    const uint32_t live = anyS & vmask;
+#pragma unroll 1
+    for (int base = 0, it = 0; base < size; base += 2, ++it) {
+        uint32_t *Xc = Ssm + (it & 1) * (2 * 2 * 24 * 32);  // [2 positions][2 warps][24][32]
+        if (h == 0) {
+            chien_step<E, 0>(C, Ot, Xc + (0 * 2 + 0) * 24 * 32 + lane, 32);
+            chien_step<E, 0>(C, Ot, Xc + (1 * 2 + 0) * 24 * 32 + lane, 32);
+        } else {
+            chien_step<E, 1>(C, Ot, Xc + (0 * 2 + 1) * 24 * 32 + lane, 32);
+            chien_step<E, 1>(C, Ot, Xc + (1 * 2 + 1) * 24 * 32 + lane, 32);
+        }
+        __syncthreads();
+        const int i = base + h;  // warp h takes position base + h
+        if (i < size) {
+            const uint32_t *A = Xc + (h * 2 + 0) * 24 * 32 + lane;
+            const uint32_t *B = Xc + (h * 2 + 1) * 24 * 32 + lane;
+            uint32_t lo[8], om[8], nz = 0u;
+#pragma unroll
+            for (int b = 0; b < 8; ++b) {
+                const uint32_t o = A[(8 + b) * 32] ^ B[(8 + b) * 32];
+                nz |= A[b * 32] ^ B[b * 32] ^ o;
+                lo[b] = o;
+                om[b] = A[(16 + b) * 32] ^ B[(16 + b) * 32];
+            }
+            uint32_t roots = ~nz & live;
+            const int pos = size - 1 - i;
+            while (roots) {
+                const int j = __ffs(roots) - 1;
+                roots &= roots - 1;
+                uint32_t ob = 0u, lb = 0u;
+#pragma unroll
+                for (int b = 0; b < 8; ++b) {
+                    ob |= ((om[b] >> j) & 1u) << b;
+                    lb |= ((lo[b] >> j) & 1u) << b;
+                }
+                const uint32_t e = (ob && lb) ? ex[lg[ob] + 255 - lg[lb]] : 0u;
+                const int c = mycnt[j * 32 + lane];
+                mycnt[j * 32 + lane] = (uint8_t)(c + 1);
+                const int slot = h == 0 ? c : t - 1 - c;
+                if (slot >= 0 && slot < t) {
+                    corr[(j * t + slot) * 2] = (uint8_t)pos;
+                    corr[(j * t + slot) * 2 + 1] = (uint8_t)e;
+                }
+            }
+        }
+    }
+    __syncthreads();
+
+    // phase 4: status and corrections, warp h takes blocks 16h .. 16h+15
+    for (int j = h * 16; j < h * 16 + 16; ++j) {
+        if (!((vmask >> j) & 1u)) continue;
+        const size_t blk = blk0 + j;
+        if (!((anyS >> j) & 1u)) {
+            status[blk] = 1;
+            continue;
+        }
+        int l = 0;
+#pragma unroll
+        for (int b = 0; b < 6; ++b) l |= (int)((L[b] >> j) & 1u) << b;
+        const int c0 = cnt[j * 32 + lane], c1 = cnt[1024 + j * 32 + lane];
+        if (l > t || c0 + c1 != l) {
+            status[blk] = 0;
+            continue;
+        }
+        for (int s = 0; s < t; ++s) {
+            if (s >= c0 && s < t - c1) continue;
+            const int p = corr[(j * t + s) * 2];
+            const uint8_t e = corr[(j * t + s) * 2 + 1];
+            if (p < msg_len)
+                data[blk * (size_t)msg_len + p] ^= e;
+            else
+                parity[blk * (size_t)E + (p - msg_len)] ^= e;
+        }
+        status[blk] = 1;
+    }
+}
+
 }  // namespace bs
 
 // ---------------------------------------------------------------- dispatch
@@ -672,10 +1085,45 @@ bool rs256_fast_synds(const Rs256Code &c, const uint8_t *data, const uint8_t *pa
     if (!aligned4(data) || !aligned4(parity) || !aligned4(synds)) return false;
     if (!nblocks) return true;
     if (c.ecc == 32)
-        bs::bs_synd_kernel<32><<<tiles_grid(nblocks), bs::kGroups * 2, 0, st>>>(data, parity, nblocks, msg_len, synds);
+        bs::bs_synd_kernel<32, false><<<tiles_grid(nblocks), bs::kGroups * 2, 0, st>>>(data, parity, nblocks, msg_len, synds);
     else
-        bs::bs_synd_kernel<16><<<tiles_grid(nblocks), bs::kGroups, 0, st>>>(data, parity, nblocks, msg_len, synds);
+        bs::bs_synd_kernel<16, false><<<tiles_grid(nblocks), bs::kGroups, 0, st>>>(data, parity, nblocks, msg_len, synds);
     check_launch("bs_synd_kernel");
+    return true;
+}
+
+// bytes of the bitsliced syndrome planes (and, later, the corrections) of
+// nblocks blocks: whole tiles of 32 groups
+size_t rs256_fast_scratch_bytes(int ecc, size_t nblocks) {
+    const size_t ngroups = (nblocks + 31) / 32, ntiles = (ngroups + 31) / 32;
+    return ntiles * (size_t)ecc * 8 * 32 * 4;
+}
+
+template <int E>
+static void launch_bs_decode(const Rs256Code &c, uint8_t *data, uint8_t *parity, size_t nblocks, int msg_len,
+                             uint8_t *status, uint32_t *planes, cudaStream_t st) {
+    constexpr int T = bs::Code<E>::T;
+    bs::bs_synd_kernel<E, true><<<tiles_grid(nblocks), bs::kGroups * T, 0, st>>>(data, parity, nblocks, msg_len,
+                                                                                 reinterpret_cast<uint8_t *>(planes));
+    check_launch("bs_synd_kernel");
+    FFGPU_CHECK_CUDA(cudaFuncSetAttribute(bs::bs_solve_kernel<E>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)bs::SolveGeom<E>::smem));
+    const size_t ntiles = ((nblocks + 31) / 32 + 31) / 32;
+    bs::bs_solve_kernel<E><<<(unsigned)ntiles, 64, bs::SolveGeom<E>::smem, st>>>(
+        data, parity, nblocks, msg_len, planes, status, c.d_exp512, c.d_log256);
+    check_launch("bs_solve_kernel");
+}
+
+// decode with caller-provided scratch of rs256_fast_scratch_bytes(ecc, nblocks)
+bool rs256_fast_decode_with(const Rs256Code &c, uint8_t *data, uint8_t *parity, size_t nblocks, int msg_len,
+                            uint8_t *status, void *scratch, cudaStream_t st) {
+    if (!c.fast || c.table_only || (c.ecc != 32 && c.ecc != 16)) return false;
+    if (!aligned4(data) || !aligned4(parity) || !aligned4(scratch)) return false;
+    if (!nblocks) return true;
+    if (c.ecc == 32)
+        launch_bs_decode<32>(c, data, parity, nblocks, msg_len, status, (uint32_t *)scratch, st);
+    else
+        launch_bs_decode<16>(c, data, parity, nblocks, msg_len, status, (uint32_t *)scratch, st);
     return true;
 }
 
@@ -684,16 +1132,15 @@ bool rs256_fast_decode(const Rs256Code &c, uint8_t *data, uint8_t *parity, size_
     if (!c.fast || c.table_only || (c.ecc != 32 && c.ecc != 16)) return false;
     if (!aligned4(data) || !aligned4(parity)) return false;
     if (!nblocks) return true;
-    void *synds = nullptr;
-    FFGPU_CHECK_CUDA(cudaMallocAsync(&synds, nblocks * (size_t)c.ecc, st));
+    void *scratch = nullptr;
+    FFGPU_CHECK_CUDA(cudaMallocAsync(&scratch, rs256_fast_scratch_bytes(c.ecc, nblocks), st));
     try {
-        rs256_fast_synds(c, data, parity, nblocks, msg_len, (uint8_t *)synds, st);
-        rs256_solve(c, data, parity, nblocks, msg_len, (const uint8_t *)synds, status, st);
+        rs256_fast_decode_with(c, data, parity, nblocks, msg_len, status, scratch, st);
     } catch (...) {
-        cudaFreeAsync(synds, st);
+        cudaFreeAsync(scratch, st);
         throw;
     }
-    FFGPU_CHECK_CUDA(cudaFreeAsync(synds, st));
+    FFGPU_CHECK_CUDA(cudaFreeAsync(scratch, st));
     return true;
 }
 
