@@ -143,7 +143,7 @@ def bench_rs256_decode(args, torch, rank, world):
     from libffrs_gb300 import capi
     import libffrs_gb300
 
-    nb, ml, ecc = 1 << 20, 223, 32
+    nb, ml, ecc = args.blocks or (1 << 20), 223, 32
     data0, par0 = make_rs256_decode_inputs(torch, nb, 1000 + rank)
     code = capi.RS256Code(ecc)
     nbuf = max(1, min(args.steps, 4))
@@ -165,6 +165,8 @@ def bench_rs256_decode(args, torch, rank, world):
     total_ms = 0.0
     kern_ms = []
     launches0 = capi.kernel_launches()
+    capi.timing_collect()
+    capi.timing_enable(True)
     with ClockSampler(torch.cuda.current_device()) as clk:
         done = 0
         while done < args.steps:
@@ -186,6 +188,8 @@ def bench_rs256_decode(args, torch, rank, world):
             kern_ms += [ev[j].elapsed_time(ev[j + 1]) for j in range(batch)]
             done += batch
     launches = capi.kernel_launches() - launches0
+    kernels = capi.timing_collect()
+    capi.timing_enable(False)
     # correctness spot check of the last step against the golden property
     st = bufs[0][2]
     algo_bytes = nb * 256  # read 255 B + write 1 B status per block
@@ -197,7 +201,7 @@ def bench_rs256_decode(args, torch, rank, world):
     d0 = data0.cpu().numpy().tobytes()
     p0 = par0.cpu().numpy().tobytes()
     e2e_t = []
-    for i in range(max(1, args.e2e_steps) + 1):
+    for i in range(0 if args.no_e2e else max(1, args.e2e_steps) + 1):
         hd[:] = d0
         hp[:] = p0
         t0 = time.perf_counter()
@@ -205,7 +209,7 @@ def bench_rs256_decode(args, torch, rank, world):
         t1 = time.perf_counter()
         if i > 0:
             e2e_t.append(t1 - t0)
-    e2e = {"value": algo_bytes * world / statistics.median(e2e_t) / 1e9, "unit": "GB/s",
+    e2e = {"value": algo_bytes * world / statistics.median(e2e_t) / 1e9 if e2e_t else None, "unit": "GB/s",
            "h2d_bytes_per_step": nb * (ml + ecc), "d2h_bytes_per_step": nb * (ml + ecc) + nb,
            "api": "libffrs.RS256.repair_blocks(create_buffer, create_buffer)"}
     return {
@@ -214,6 +218,7 @@ def bench_rs256_decode(args, torch, rank, world):
         "kern_ms": kern_ms,
         "algo_bytes_per_step": algo_bytes,
         "launches": launches,
+        "kernels": kernels,
         "clocks": clk.summary(),
         "e2e": e2e,
         "config": {"workload": "RS256 decode ecc_len=32, 1048576 blocks x (223+32) B, 0-16 errors/block, "
@@ -251,7 +256,7 @@ def bench_rs256_encode(args, torch, rank, world):
     from libffrs_gb300 import capi
     import libffrs_gb300
 
-    nb, ml, ecc = 65536, 223, 32
+    nb, ml, ecc = args.blocks or 65536, 223, 32
     nbuf = 10  # 10 x 16.7 MB rotating inputs > L2
     g = torch.Generator(device="cuda")
     g.manual_seed(2000 + rank)
@@ -266,6 +271,8 @@ def bench_rs256_encode(args, torch, rank, world):
     if world > 1:
         torch.distributed.barrier()
     launches0 = capi.kernel_launches()
+    capi.timing_collect()
+    capi.timing_enable(True)
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
     with ClockSampler(torch.cuda.current_device()) as clk:
         ev[0].record(stream)
@@ -274,6 +281,8 @@ def bench_rs256_encode(args, torch, rank, world):
             ev[i + 1].record(stream)
         torch.cuda.synchronize()
     launches = capi.kernel_launches() - launches0
+    kernels = capi.timing_collect()
+    capi.timing_enable(False)
     total_ms = ev[0].elapsed_time(ev[-1])
     kern_ms = [ev[i].elapsed_time(ev[i + 1]) for i in range(args.steps)]
     algo = nb * 255
@@ -282,7 +291,7 @@ def bench_rs256_encode(args, torch, rank, world):
     hb = lf.create_buffer(nb * ml)
     hb[:] = ins[0].cpu().numpy().tobytes()
     e2e_t = []
-    for i in range(max(1, args.e2e_steps) + 1):
+    for i in range(0 if args.no_e2e else max(1, args.e2e_steps) + 1):
         t0 = time.perf_counter()
         rs.encode(hb)
         t1 = time.perf_counter()
@@ -290,8 +299,8 @@ def bench_rs256_encode(args, torch, rank, world):
             e2e_t.append(t1 - t0)
     return {
         "workload": "rs256-encode", "total_ms": total_ms, "kern_ms": kern_ms, "algo_bytes_per_step": algo,
-        "launches": launches, "clocks": clk.summary(),
-        "e2e": {"value": algo * world / statistics.median(e2e_t) / 1e9, "unit": "GB/s",
+        "launches": launches, "kernels": kernels, "clocks": clk.summary(),
+        "e2e": {"value": algo * world / statistics.median(e2e_t) / 1e9 if e2e_t else None, "unit": "GB/s",
                 "h2d_bytes_per_step": nb * ml, "d2h_bytes_per_step": nb * ecc, "api": "libffrs.RS256.encode"},
         "config": {"workload": "RS256 encode ecc_len=32, 65536 blocks x 223 B", "blocks": nb,
                    "l2": "10 rotating 16.7 MB inputs (167 MB > L2)"},
@@ -351,7 +360,7 @@ def bench_rsi16(args, torch, rank, world, decode):
     from libffrs_gb300 import capi
     import libffrs_gb300
 
-    nb, bl, ecc = 262144, 1024, 64
+    nb, bl, ecc = args.blocks or 262144, 1024, 64
     ml = bl - ecc
     msg0, par0 = make_rsi16_inputs(torch, nb, 3000 + rank, decode)
     code = capi.RSi16Code(bl, ecc)
@@ -378,6 +387,8 @@ def bench_rsi16(args, torch, rank, world, decode):
     torch.cuda.synchronize()
     total_ms, kern_ms = 0.0, []
     launches0 = capi.kernel_launches()
+    capi.timing_collect()
+    capi.timing_enable(True)
     with ClockSampler(torch.cuda.current_device()) as clk:
         done = 0
         while done < args.steps:
@@ -399,6 +410,8 @@ def bench_rsi16(args, torch, rank, world, decode):
             kern_ms += [ev[j].elapsed_time(ev[j + 1]) for j in range(batch)]
             done += batch
     launches = capi.kernel_launches() - launches0
+    kernels = capi.timing_collect()
+    capi.timing_enable(False)
     algo = nb * (2048 if not decode else 2048 + 4)
     lf = libffrs_gb300.libffrs
     rs = lf.RSi16(bl, ecc)
@@ -409,7 +422,7 @@ def bench_rsi16(args, torch, rank, world, decode):
         hp = lf.create_buffer(nb * ecc * 2)
         p0 = par0.cpu().numpy().tobytes()
         m0 = bytes(hm)
-    for i in range(max(1, args.e2e_steps) + 1):
+    for i in range(0 if args.no_e2e else max(1, args.e2e_steps) + 1):
         if decode:
             hm[:] = m0
             hp[:] = p0
@@ -422,15 +435,15 @@ def bench_rsi16(args, torch, rank, world, decode):
         if i:
             e2e_t.append(t1 - t0)
     if decode:
-        e2e = {"value": algo * world / statistics.median(e2e_t) / 1e9, "unit": "GB/s",
+        e2e = {"value": algo * world / statistics.median(e2e_t) / 1e9 if e2e_t else None, "unit": "GB/s",
                "h2d_bytes_per_step": nb * bl * 2, "d2h_bytes_per_step": nb * bl * 2 + nb,
                "api": "libffrs.RSi16.repair_blocks(create_buffer, create_buffer)"}
     else:
-        e2e = {"value": algo * world / statistics.median(e2e_t) / 1e9, "unit": "GB/s",
+        e2e = {"value": algo * world / statistics.median(e2e_t) / 1e9 if e2e_t else None, "unit": "GB/s",
                "h2d_bytes_per_step": nb * ml * 2, "d2h_bytes_per_step": nb * ecc * 2, "api": "libffrs.RSi16.encode"}
     out = {
         "workload": "rsi16-decode" if decode else "rsi16-encode", "total_ms": total_ms, "kern_ms": kern_ms,
-        "algo_bytes_per_step": algo, "launches": launches, "clocks": clk.summary(), "e2e": e2e,
+        "algo_bytes_per_step": algo, "launches": launches, "kernels": kernels, "clocks": clk.summary(), "e2e": e2e,
         "config": {"workload": ("RSi16(1024, 64) decode, 262144 blocks, 0-32 symbol errors/block" if decode else
                                 "RSi16(1024, 64) encode, 262144 blocks x 960 uint16 words"),
                    "blocks": nb, "l2": "inputs larger than L2 (503 MB per step)"},
@@ -521,6 +534,9 @@ def main():
     ap.add_argument("--workload", default="rs256-decode", choices=sorted(WORKLOADS))
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--blocks", type=int, default=0,
+                    help="override the block count (small cases for profiling; not a bench line)")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer pass (profiling)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -563,8 +579,18 @@ def main():
         return
     steps = args.steps
     value = r["algo_bytes_per_step"] * steps * world / (total_ms / 1e3) / 1e9
-    kern = statistics.median(r["kern_ms"])
-    achieved = r["algo_bytes_per_step"] / (kern / 1e3) / 1e9
+    # dominant kernel: the one with the largest share of the timed region's
+    # kernel time (CUDA events around each launch, on its stream)
+    kernels = r.get("kernels") or {}
+    ktot = sum(ms for ms, _ in kernels.values()) or 1.0
+    if kernels:
+        dom = max(kernels, key=lambda k: kernels[k][0])
+        dom_ms = kernels[dom][0] / kernels[dom][1]
+        dom_launch_per_step = kernels[dom][1] / steps
+    else:
+        dom, dom_ms, dom_launch_per_step = None, statistics.median(r["kern_ms"]), 1.0
+    # algorithmic bytes per launch = per-unit bytes x units one launch processes
+    achieved = r["algo_bytes_per_step"] / dom_launch_per_step / (dom_ms / 1e3) / 1e9
     peak, peak_src = load_peaks()
     line = {
         "metric": METRIC if args.workload == "rs256-decode" else f"{args.workload} GB/s bit-exact",
@@ -574,7 +600,8 @@ def main():
         "e2e": r["e2e"], "gpu_launches": r["launches"], "clocks": r["clocks"],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_src, "traffic": load_traffic(args.workload),
-                     "kernel_ms_median": kern},
+                     "kernel": dom, "kernel_ms_per_launch": dom_ms},
+        "kernels": {k: {"ms_per_launch": ms / n, "launches": n, "share": ms / ktot} for k, (ms, n) in kernels.items()},
     }
     if "status_ok_fraction" in r:
         line["status_ok_fraction"] = r["status_ok_fraction"]

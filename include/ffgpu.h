@@ -56,6 +56,13 @@ FFGPU_API const char *ffgpu_version(void);
 FFGPU_API int ffgpu_init(int device);
 /* number of kernels this library has launched since load (for accounting) */
 FFGPU_API uint64_t ffgpu_kernel_launches(void);
+/* No reference counterpart (measurement support).  While enabled, every
+ * kernel launch is bracketed by a CUDA event pair on its stream;
+ * ffgpu_timing_collect waits for the recorded launches and writes one line
+ * "<kernel> <total ms> <launches>" per kernel into out (NUL-terminated,
+ * truncated to cap), the full length into *len, and forgets them. */
+FFGPU_API int ffgpu_timing_enable(int on);
+FFGPU_API int ffgpu_timing_collect(char *out, size_t cap, size_t *len);
 /* the library's own stream (cudaStream_t) */
 FFGPU_API void *ffgpu_default_stream(void);
 FFGPU_API int ffgpu_synchronize(void *stream);

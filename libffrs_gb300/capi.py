@@ -63,6 +63,8 @@ def _declare(L):
         "ffgpu_kernel_launches": (ctypes.c_uint64, []),
         "ffgpu_default_stream": (_P, []),
         "ffgpu_synchronize": (_I, [_P]),
+        "ffgpu_timing_enable": (_I, [_I]),
+        "ffgpu_timing_collect": (_I, [ctypes.c_char_p, _SZ, ctypes.POINTER(_SZ)]),
         "ffgpu_host_alloc": (_I, [_SZ, _PP]),
         "ffgpu_host_free": (_I, [_P]),
         "ffgpu_rs256_create": (_I, [_I, _I, _I, _PP]),
@@ -187,6 +189,22 @@ class CIRC16Code:
 
     def repair(self, msg_ptr, ecc_ptr, nblocks, status_ptr, stream=None):
         call("ffgpu_circ16_repair", self.h, msg_ptr, ecc_ptr, nblocks, status_ptr, stream)
+
+
+def timing_enable(on=True):
+    call("ffgpu_timing_enable", 1 if on else 0)
+
+
+def timing_collect():
+    """{kernel name: (total ms, launches)} of the launches timed since the last call."""
+    n = _SZ(0)
+    buf = ctypes.create_string_buffer(1 << 16)
+    call("ffgpu_timing_collect", buf, 1 << 16, ctypes.byref(n))
+    out = {}
+    for line in buf.value.decode().splitlines():
+        name, ms, cnt = line.rsplit(" ", 2)
+        out[name] = (float(ms), int(cnt))
+    return out
 
 
 def kernel_launches():

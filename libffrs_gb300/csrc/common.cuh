@@ -48,6 +48,34 @@ inline void check_launch(const char *what) {
 
 cudaStream_t lib_stream();
 
+// Optional per-kernel timing (ffgpu_timing_enable): while it is on, a
+// KernelTimer records a CUDA event pair around one launch on the launching
+// stream, and ffgpu_timing_collect adds the elapsed times up per kernel name.
+bool timing_on();
+cudaEvent_t timing_event();
+void timing_push(const char *name, cudaEvent_t start, cudaEvent_t stop);
+
+struct KernelTimer {
+    const char *name;
+    cudaStream_t st;
+    cudaEvent_t start = nullptr;
+    KernelTimer(const char *n, cudaStream_t s) : name(n), st(s) {
+        if (timing_on()) {
+            start = timing_event();
+            cudaEventRecord(start, st);
+        }
+    }
+    ~KernelTimer() {
+        if (start) {
+            cudaEvent_t stop = timing_event();
+            cudaEventRecord(stop, st);
+            timing_push(name, start, stop);
+        }
+    }
+    KernelTimer(const KernelTimer &) = delete;
+    KernelTimer &operator=(const KernelTimer &) = delete;
+};
+
 // Grow-only device scratch owned by one code object (not thread-safe by
 // design: one code object is used from one host thread at a time).
 struct DeviceBuffer {

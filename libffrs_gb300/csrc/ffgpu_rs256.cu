@@ -6,6 +6,8 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <vector>
+#include <algorithm>
 
 #include "common.cuh"
 #include "rs256.cuh"
@@ -29,6 +31,35 @@ cudaStream_t lib_stream() {
     return g_stream;
 }
 
+// ---- per-kernel timing
+static std::atomic<bool> g_timing{false};
+static std::mutex g_timing_mu;
+static std::vector<cudaEvent_t> g_event_pool;
+struct Timed {
+    std::string name;
+    cudaEvent_t start, stop;
+};
+static std::vector<Timed> g_timed;
+
+bool timing_on() { return g_timing.load(std::memory_order_relaxed); }
+
+cudaEvent_t timing_event() {
+    std::lock_guard<std::mutex> lk(g_timing_mu);
+    if (!g_event_pool.empty()) {
+        cudaEvent_t e = g_event_pool.back();
+        g_event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    FFGPU_CHECK_CUDA(cudaEventCreate(&e));
+    return e;
+}
+
+void timing_push(const char *name, cudaEvent_t start, cudaEvent_t stop) {
+    std::lock_guard<std::mutex> lk(g_timing_mu);
+    g_timed.push_back({name, start, stop});
+}
+
 }  // namespace ffgpu
 
 using namespace ffgpu;
@@ -44,6 +75,50 @@ extern "C" {
 const char *ffgpu_last_error(void) { return t_last_error.c_str(); }
 const char *ffgpu_version(void) { return "libffrs-gb300 0.1.0 (sm_103a)"; }
 uint64_t ffgpu_kernel_launches(void) { return g_launches.load(); }
+
+int ffgpu_timing_enable(int on) {
+    return guarded([&] { g_timing.store(on != 0); });
+}
+
+int ffgpu_timing_collect(char *out, size_t cap, size_t *len) {
+    return guarded([&] {
+        std::vector<Timed> done;
+        {
+            std::lock_guard<std::mutex> lk(g_timing_mu);
+            done.swap(g_timed);
+        }
+        std::vector<std::pair<std::string, std::pair<double, long>>> acc;
+        for (auto &t : done) {
+            FFGPU_CHECK_CUDA(cudaEventSynchronize(t.stop));
+            float ms = 0.f;
+            FFGPU_CHECK_CUDA(cudaEventElapsedTime(&ms, t.start, t.stop));
+            bool found = false;
+            for (auto &a : acc)
+                if (a.first == t.name) {
+                    a.second.first += ms;
+                    a.second.second += 1;
+                    found = true;
+                }
+            if (!found) acc.push_back({t.name, {ms, 1}});
+        }
+        {
+            std::lock_guard<std::mutex> lk(g_timing_mu);
+            for (auto &t : done) {
+                g_event_pool.push_back(t.start);
+                g_event_pool.push_back(t.stop);
+            }
+        }
+        std::string text;
+        for (auto &a : acc)
+            text += a.first + " " + std::to_string(a.second.first) + " " + std::to_string(a.second.second) + "\n";
+        if (len) *len = text.size();
+        if (out && cap) {
+            const size_t n = std::min(cap - 1, text.size());
+            std::memcpy(out, text.data(), n);
+            out[n] = 0;
+        }
+    });
+}
 
 int ffgpu_init(int device) {
     return guarded([&] {

@@ -331,6 +331,7 @@ void rs256_solve(const Rs256Code &c, uint8_t *data, uint8_t *parity, size_t nblo
     const size_t grid = std::min<size_t>(grid_for(nblocks, threads), (size_t)(sms > 0 ? sms : 132) * 8);
     void *scratch = nullptr;
     FFGPU_CHECK_CUDA(cudaMallocAsync(&scratch, grid * threads * kDecodeScratchBytes, st));
+    KernelTimer kt_timer("rs256_solve_kernel", st);
     rs256_solve_kernel<<<(unsigned)grid, threads, 0, st>>>(data, parity, nblocks, msg_len, c.d_exp512, c.d_log256,
                                                           c.ecc, synds, status, (uint8_t *)scratch);
     cudaError_t le = cudaGetLastError();
@@ -391,6 +392,7 @@ static void launch_encode_table(const Rs256Code &c, const uint8_t *data, size_t 
                                               200 * 1024));
         attr = true;
     }
+    KernelTimer kt_timer("rs256_encode_table_kernel", st);
     rs256_encode_table_kernel<W><<<grid_for(nblocks, threads), threads, smem, st>>>(data, nblocks, msg_len, c.d_lut,
                                                                                     c.ecc, parity);
     check_launch("rs256_encode_table_kernel");
@@ -413,6 +415,7 @@ static void launch_decode_table(const Rs256Code &c, uint8_t *data, uint8_t *pari
     const size_t grid = std::min<size_t>(grid_for(nblocks, threads), (size_t)(sms > 0 ? sms : 132) * 8);
     void *scratch = nullptr;
     FFGPU_CHECK_CUDA(cudaMallocAsync(&scratch, grid * threads * kDecodeScratchBytes, st));
+    KernelTimer kt_timer("rs256_decode_table_kernel", st);
     rs256_decode_table_kernel<W><<<(unsigned)grid, threads, smem, st>>>(data, parity, nblocks, msg_len, c.d_lut,
                                                                         c.d_exp512, c.d_log256, c.ecc, status, synds,
                                                                         (uint8_t *)scratch);

@@ -1073,6 +1073,7 @@ bool rs256_fast_encode(const Rs256Code &c, const uint8_t *data, size_t nblocks, 
                        cudaStream_t st) {
     if (!c.fast || c.table_only || c.ecc != 32 || !aligned4(data) || !aligned4(parity)) return false;
     if (!nblocks) return true;
+    KernelTimer kt_timer("bs_encode32_kernel", st);
     bs::bs_encode32_kernel<<<tiles_grid(nblocks), bs::kGroups * 2, 0, st>>>(data, nblocks, msg_len, parity);
     check_launch("bs_encode32_kernel");
     return true;
@@ -1084,6 +1085,7 @@ bool rs256_fast_synds(const Rs256Code &c, const uint8_t *data, const uint8_t *pa
     if (!c.fast || c.table_only || (c.ecc != 32 && c.ecc != 16)) return false;
     if (!aligned4(data) || !aligned4(parity) || !aligned4(synds)) return false;
     if (!nblocks) return true;
+    KernelTimer kt_timer("bs_synd_kernel", st);
     if (c.ecc == 32)
         bs::bs_synd_kernel<32, false><<<tiles_grid(nblocks), bs::kGroups * 2, 0, st>>>(data, parity, nblocks, msg_len, synds);
     else
@@ -1103,12 +1105,16 @@ template <int E>
 static void launch_bs_decode(const Rs256Code &c, uint8_t *data, uint8_t *parity, size_t nblocks, int msg_len,
                              uint8_t *status, uint32_t *planes, cudaStream_t st) {
     constexpr int T = bs::Code<E>::T;
-    bs::bs_synd_kernel<E, true><<<tiles_grid(nblocks), bs::kGroups * T, 0, st>>>(data, parity, nblocks, msg_len,
-                                                                                 reinterpret_cast<uint8_t *>(planes));
-    check_launch("bs_synd_kernel");
+    {
+        KernelTimer kt_timer("bs_synd_kernel", st);
+        bs::bs_synd_kernel<E, true><<<tiles_grid(nblocks), bs::kGroups * T, 0, st>>>(
+            data, parity, nblocks, msg_len, reinterpret_cast<uint8_t *>(planes));
+        check_launch("bs_synd_kernel");
+    }
     FFGPU_CHECK_CUDA(cudaFuncSetAttribute(bs::bs_solve_kernel<E>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)bs::SolveGeom<E>::smem));
     const size_t ntiles = ((nblocks + 31) / 32 + 31) / 32;
+    KernelTimer kt_timer("bs_solve_kernel", st);
     bs::bs_solve_kernel<E><<<(unsigned)ntiles, 64, bs::SolveGeom<E>::smem, st>>>(
         data, parity, nblocks, msg_len, planes, status, c.d_exp512, c.d_log256);
     check_launch("bs_solve_kernel");

@@ -841,6 +841,7 @@ Launch plan(K kernel, size_t nblocks, uint32_t ws_words) {
 void rsi16_encode(const Rsi16Code &c, const BlockView &v, size_t nblocks, cudaStream_t st) {
     if (!nblocks) return;
     Launch L = plan(rsi16_encode_warp_kernel, nblocks, (uint32_t)c.block_len);
+    KernelTimer kt_timer("rsi16_encode_warp_kernel", st);
     rsi16_encode_warp_kernel<<<L.grid, L.threads, L.smem, st>>>(c.dev, v, nblocks, L.gscratch, L.ws_words);
     check_launch("rsi16_encode_warp_kernel");
 }
@@ -848,6 +849,7 @@ void rsi16_encode(const Rsi16Code &c, const BlockView &v, size_t nblocks, cudaSt
 void rsi16_synd(const Rsi16Code &c, const BlockView &v, size_t nblocks, uint32_t *synds, cudaStream_t st) {
     if (!nblocks) return;
     Launch L = plan(rsi16_synd_warp_kernel, nblocks, (uint32_t)c.block_len);
+    KernelTimer kt_timer("rsi16_synd_warp_kernel", st);
     rsi16_synd_warp_kernel<<<L.grid, L.threads, L.smem, st>>>(c.dev, v, nblocks, synds, L.gscratch, L.ws_words);
     check_launch("rsi16_synd_warp_kernel");
 }
@@ -856,6 +858,7 @@ void rsi16_repair(const Rsi16Code &c, const BlockView &v, size_t nblocks, uint8_
                   const uint8_t *active) {
     if (!nblocks) return;
     Launch L = plan(rsi16_repair_warp_kernel, nblocks, c.dev.temp_len + 1);
+    KernelTimer kt_timer("rsi16_repair_warp_kernel", st);
     rsi16_repair_warp_kernel<<<L.grid, L.threads, L.smem, st>>>(c.dev, v, nblocks, status, active, L.gscratch,
                                                                 L.ws_words);
     check_launch("rsi16_repair_warp_kernel");
@@ -866,6 +869,7 @@ void rsi16_repair_known(const Rsi16Code &c, const BlockView &v, size_t nblocks, 
                         uint8_t *status, cudaStream_t st) {
     if (!nblocks) return;
     Launch L = plan(rsi16_repair_known_warp_kernel, nblocks, c.dev.temp_len + 1);
+    KernelTimer kt_timer("rsi16_repair_known_warp_kernel", st);
     rsi16_repair_known_warp_kernel<<<L.grid, L.threads, L.smem, st>>>(c.dev, v, nblocks, pos, pos_off, pos_cnt,
                                                                          count_all, active, status, L.gscratch,
                                                                          L.ws_words);
@@ -876,6 +880,7 @@ void rsi16_sugiyama(const Rsi16Code &c, const uint32_t *synds, size_t nblocks, u
                     uint8_t *status, cudaStream_t st) {
     if (!nblocks) return;
     Launch L = plan(rsi16_sugiyama_kernel, nblocks, c.dev.temp_len + 1);
+    KernelTimer kt_timer("rsi16_sugiyama_kernel", st);
     rsi16_sugiyama_kernel<<<L.grid, L.threads, L.smem, st>>>(c.dev, synds, nblocks, locator, evaluator, status,
                                                              L.gscratch, L.ws_words);
     check_launch("rsi16_sugiyama_kernel");
