@@ -274,6 +274,26 @@ struct CrtHolder {
 
 // ---------------------------------------------------------------- device helpers
 
+// three-input logic in one LOP3 (PTX lop3.b32; the immediate is the truth
+// table over the operand masks 0xF0, 0xCC, 0xAA)
+__device__ __forceinline__ uint32_t xor3(uint32_t a, uint32_t b, uint32_t c) {
+    uint32_t d;
+    asm("lop3.b32 %0, %1, %2, %3, 0x96;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
+// (a & b) ^ c
+__device__ __forceinline__ uint32_t andxor(uint32_t a, uint32_t b, uint32_t c) {
+    uint32_t d;
+    asm("lop3.b32 %0, %1, %2, %3, 0x6A;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
+// (m & a) | (~m & b)
+__device__ __forceinline__ uint32_t bitsel(uint32_t m, uint32_t a, uint32_t b) {
+    uint32_t d;
+    asm("lop3.b32 %0, %1, %2, %3, 0xCA;" : "=r"(d) : "r"(m), "r"(a), "r"(b));
+    return d;
+}
+
 // 32x32 bit transpose in registers: afterwards a[c] bit r == old a[r] bit c
 __device__ __forceinline__ void transpose32(uint32_t (&a)[32]) {
 #pragma unroll
@@ -317,6 +337,20 @@ __device__ __forceinline__ void combos(const uint32_t (&f)[8], uint32_t (&lo)[16
     }
 }
 
+// base ^ (the combination selected by S), in one LOP3 when both nibbles are used
+template <uint8_t S>
+__device__ __forceinline__ uint32_t pickx(uint32_t base, const uint32_t (&lo)[16], const uint32_t (&hi)[16]) {
+    constexpr int a = S & 15, h = S >> 4;
+    if constexpr (a && h)
+        return xor3(base, lo[a], hi[h]);
+    else if constexpr (a)
+        return base ^ lo[a];
+    else if constexpr (h)
+        return base ^ hi[h];
+    else
+        return base;
+}
+
 template <uint8_t S>
 __device__ __forceinline__ uint32_t pick(const uint32_t (&lo)[16], const uint32_t (&hi)[16]) {
     constexpr int a = S & 15, h = S >> 4;
@@ -335,8 +369,8 @@ template <int E, int t, int... K>
 __device__ __forceinline__ void lfsr_apply(uint32_t (&R)[Code<E>::D][8], const uint32_t (&lo)[16],
                                            const uint32_t (&hi)[16], std::integer_sequence<int, K...>) {
     constexpr int D = Code<E>::D;
-    ((R[K / 8][K % 8] = ((K / 8 + 1 < D) ? R[(K / 8 + 1 < D) ? K / 8 + 1 : 0][K % 8] : 0u) ^
-                        pick<Code<E>::template lfsr<t>().s[K / 8][K % 8]>(lo, hi)),
+    ((R[K / 8][K % 8] = pickx<Code<E>::template lfsr<t>().s[K / 8][K % 8]>(
+          (K / 8 + 1 < D) ? R[(K / 8 + 1 < D) ? K / 8 + 1 : 0][K % 8] : 0u, lo, hi)),
      ...);
 }
 
@@ -355,7 +389,7 @@ __device__ __forceinline__ void lfsr_step(uint32_t (&R)[Code<E>::D][8], const ui
 template <int E, int t, int M, int... K>
 __device__ __forceinline__ void synd_accum(uint32_t (&S)[Code<E>::D][8], const uint32_t (&lo)[16],
                                            const uint32_t (&hi)[16], std::integer_sequence<int, K...>) {
-    ((S[K / 8][K % 8] ^= pick<Code<E>::template synd<t>().s[M][K / 8][K % 8]>(lo, hi)), ...);
+    ((S[K / 8][K % 8] = pickx<Code<E>::template synd<t>().s[M][K / 8][K % 8]>(S[K / 8][K % 8], lo, hi)), ...);
 }
 
 template <int E, int t, int... M>
@@ -378,7 +412,7 @@ __device__ __forceinline__ void rem_to_synd(const uint32_t *rs, int stride, uint
 template <int T, int M, int P0, int... K>
 __device__ __forceinline__ void crt_accum(uint32_t (&Pp)[16][8], const uint32_t (&lo)[16], const uint32_t (&hi)[16],
                                           std::integer_sequence<int, K...>) {
-    ((Pp[K / 8][K % 8] ^= pick<CrtHolder::crt.s[T][M][P0 + K / 8][K % 8]>(lo, hi)), ...);
+    ((Pp[K / 8][K % 8] = pickx<CrtHolder::crt.s[T][M][P0 + K / 8][K % 8]>(Pp[K / 8][K % 8], lo, hi)), ...);
 }
 
 template <int P0, int... TM>
@@ -412,24 +446,37 @@ __device__ __forceinline__ int swz(int g) { return g & 31; }
 // `total`).  Positions at or beyond seg_len are never consumed.
 __device__ __forceinline__ void load_window(uint32_t *buf, const uint8_t *__restrict__ base, size_t seg_len,
                                             size_t total, size_t first_block, int nblocks_tile, int p0, int G) {
-    for (int b = threadIdx.x; b < G * 32; b += blockDim.x) {
-        const int g = b >> 5, j = b & 31;
-        uint32_t w[9];
-        uint32_t sh = 0;
-        if (b < nblocks_tile) {
-            const size_t start = (first_block + b) * seg_len + p0;
-            const size_t a0 = start & ~(size_t)3;
-            sh = (uint32_t)(start & 3) * 8;
+    // four blocks per round: their 36 loads are issued before any is used
+    constexpr int R = 4;
+    for (int b0 = threadIdx.x; b0 < G * 32; b0 += R * blockDim.x) {
+        uint32_t w[R][9];
+        uint32_t sh[R];
 #pragma unroll
-            for (int i = 0; i < 9; ++i)
-                w[i] = (a0 + 4 * i < total) ? __ldg(reinterpret_cast<const uint32_t *>(base + a0 + 4 * i)) : 0u;
-        } else {
+        for (int r = 0; r < R; ++r) {
+            const int b = b0 + r * blockDim.x;
+            sh[r] = 0;
+            if (b < G * 32 && b < nblocks_tile) {
+                const size_t start = (first_block + b) * seg_len + p0;
+                const size_t a0 = start & ~(size_t)3;
+                sh[r] = (uint32_t)(start & 3) * 8;
 #pragma unroll
-            for (int i = 0; i < 9; ++i) w[i] = 0u;
+                for (int i = 0; i < 9; ++i)
+                    w[r][i] = (a0 + 4 * i < total) ? __ldg(reinterpret_cast<const uint32_t *>(base + a0 + 4 * i)) : 0u;
+            } else {
+#pragma unroll
+                for (int i = 0; i < 9; ++i) w[r][i] = 0u;
+            }
         }
-        uint32_t *dst = buf + g * 256 + (j ^ swz(g));
 #pragma unroll
-        for (int k = 0; k < 8; ++k) dst[k * 32] = __funnelshift_r(w[k], w[k + 1], sh);
+        for (int r = 0; r < R; ++r) {
+            const int b = b0 + r * blockDim.x;
+            if (b < G * 32) {
+                const int g = b >> 5, j = b & 31;
+                uint32_t *dst = buf + g * 256 + (j ^ swz(g));
+#pragma unroll
+                for (int k = 0; k < 8; ++k) dst[k * 32] = __funnelshift_r(w[r][k], w[r][k + 1], sh[r]);
+            }
+        }
     }
 }
 
@@ -676,7 +723,7 @@ __device__ __forceinline__ void vmul(const uint32_t (&a)[8], const uint32_t (&b)
 #pragma unroll
     for (int i = 0; i < 8; ++i)
 #pragma unroll
-        for (int j = 0; j < 8; ++j) p[i + j] ^= a[i] & b[j];
+        for (int j = 0; j < 8; ++j) p[i + j] = andxor(a[i], b[j], p[i + j]);
     reduce15(p, r);
 }
 
@@ -701,18 +748,34 @@ __device__ __forceinline__ void vinv(const uint32_t (&x)[8], uint32_t (&r)[8]) {
     vmul(y, x14, r);
 }
 
+constexpr int next_bit(int s, int from) {
+    while (from < 8 && !((s >> from) & 1)) ++from;
+    return from;
+}
+
+// acc ^ XOR of in[b] over the set bits b >= B of S, two inputs per LOP3
+template <uint8_t S, int B>
+__device__ __forceinline__ uint32_t xsel_acc(uint32_t acc, const uint32_t (&in)[8]) {
+    constexpr int f = next_bit(S, B);
+    if constexpr (f >= 8) {
+        return acc;
+    } else {
+        constexpr int g = next_bit(S, f + 1);
+        if constexpr (g >= 8)
+            return acc ^ in[f];
+        else
+            return xsel_acc<S, g + 1>(xor3(acc, in[f], in[g]), in);
+    }
+}
+
+// XOR of in[b] over the set bits b of S
 template <uint8_t S>
 __device__ __forceinline__ uint32_t xsel(const uint32_t (&in)[8]) {
-    uint32_t r = 0u;
-    if constexpr ((S & 1) != 0) r ^= in[0];
-    if constexpr ((S & 2) != 0) r ^= in[1];
-    if constexpr ((S & 4) != 0) r ^= in[2];
-    if constexpr ((S & 8) != 0) r ^= in[3];
-    if constexpr ((S & 16) != 0) r ^= in[4];
-    if constexpr ((S & 32) != 0) r ^= in[5];
-    if constexpr ((S & 64) != 0) r ^= in[6];
-    if constexpr ((S & 128) != 0) r ^= in[7];
-    return r;
+    constexpr int f = next_bit(S, 0);
+    if constexpr (f >= 8)
+        return 0u;
+    else
+        return xsel_acc<S, f + 1>(in[f], in);
 }
 
 template <uint8_t C, int... O>
@@ -750,7 +813,7 @@ __device__ __forceinline__ void l_update(uint32_t (&L)[6], int a, uint32_t cond)
         const uint32_t x = ~L[b];
         const uint32_t s = ab ^ x ^ carry;
         carry = (ab & x) | (carry & (ab ^ x));
-        L[b] = (cond & s) | (~cond & L[b]);
+        L[b] = bitsel(cond, s, L[b]);
     }
 }
 
@@ -762,7 +825,7 @@ struct SolveGeom {
     static constexpr int kC = t * 8 * 32;    // words: C_1..C_t planes of 32 groups (also the BM exchange)
     static constexpr int kX = 2 * 2 * 2 * 24 * 32;  // words: Chien exchange (2 buffers x 2 positions x 2 warps)
     static constexpr int kSX = kS > kX ? kS : kX;
-    static constexpr size_t smem = (size_t)(kSX + kC) * 4 + 2 * 32 * 32 + 768;
+    static constexpr size_t smem = (size_t)(kSX + kC) * 4 + 768;
 };
 
 // C_i <- C_i a^{-i}, Omega_k <- Omega_k a^{-k}
@@ -820,11 +883,13 @@ __global__ void __launch_bounds__(64) bs_solve_kernel(uint8_t *__restrict__ data
     using G = SolveGeom<E>;
     constexpr int t = G::t, K = G::K;
     extern __shared__ __align__(16) uint32_t sm[];
-    uint32_t *Ssm = sm;                    // [E*8][32] syndrome planes; later the Chien exchange
-    uint32_t *Csm = sm + G::kSX;           // [t*8][32] C planes; earlier the BM exchange
-    uint8_t *cnt = reinterpret_cast<uint8_t *>(Csm + G::kC);  // [2][32 blocks][32 groups]
-    uint8_t *ex = cnt + 2 * 32 * 32;       // exp[512], log[256]
+    uint32_t *Ssm = sm;           // [E*8][32] syndrome planes; later the Chien exchange
+    uint32_t *Csm = sm + G::kSX;  // [t*8][32] C planes; before them the BM exchange, after them
+                                  // the root counters [2 warps][32 blocks][32 groups]
+    uint32_t *cnt = Csm;
+    uint8_t *ex = reinterpret_cast<uint8_t *>(Csm + G::kC);  // exp[512], log[256]
     uint8_t *lg = ex + 512;
+    static_assert(G::kC >= 2 * 32 * 32, "root counters must fit in the C planes region");
 
     const int lane = threadIdx.x & 31, h = threadIdx.x >> 5;
     const size_t ngroups = (nblocks + 31) / 32;
@@ -833,11 +898,20 @@ __global__ void __launch_bounds__(64) bs_solve_kernel(uint8_t *__restrict__ data
     const bool valid = grp < ngroups;
     uint32_t *tplanes = planes + tile * (size_t)G::kS;
 
+    // phase 0: syndrome planes of the 32 groups, one contiguous region of
+    // E * 1024 bytes, copied asynchronously 16 bytes per thread and round
+    // (groups past the end hold stale words; their blocks are never touched)
+    {
+        const char *src = reinterpret_cast<const char *>(tplanes);
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(Ssm);
+#pragma unroll 4
+        for (int off = threadIdx.x * 16; off < E * 1024; off += 64 * 16)
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst + off), "l"(src + off) : "memory");
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    }
     for (int i = threadIdx.x; i < 512; i += 64) ex[i] = exp512[i];
     for (int i = threadIdx.x; i < 256; i += 64) lg[i] = log256[i];
-    for (int i = threadIdx.x; i < 2 * 32 * 32; i += 64) cnt[i] = 0;
-    // phase 0: syndrome planes of the 32 groups
-    for (int k = h; k < E * 8; k += 2) Ssm[k * 32 + lane] = valid ? tplanes[k * 32 + lane] : 0u;
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
     __syncthreads();
     uint32_t anyS = 0u;
     for (int k = 0; k < E * 8; ++k) anyS |= Ssm[k * 32 + lane];
@@ -915,11 +989,11 @@ __global__ void __launch_bounds__(64) bs_solve_kernel(uint8_t *__restrict__ data
                     lb = X[(24 + b) * 32 + lane];
                 }
                 C[u][b] ^= pr[b];
-                Bs[u][b] = (cond & lc) | (~cond & lb);
+                Bs[u][b] = bitsel(cond, lc, lb);
             }
         }
 #pragma unroll
-        for (int b = 0; b < 8; ++b) binv[b] = (cond & dinv[b]) | (~cond & binv[b]);
+        for (int b = 0; b < 8; ++b) binv[b] = bitsel(cond, dinv[b], binv[b]);
         l_update(L, n + 1, cond);
     }
     __syncthreads();  // BM exchange reads done before Csm is rewritten
@@ -948,12 +1022,14 @@ __global__ void __launch_bounds__(64) bs_solve_kernel(uint8_t *__restrict__ data
             for (int b = 0; b < 8; ++b) Ot[v][b] ^= pr[b];
         }
     }
-    __syncthreads();  // Ssm becomes the Chien exchange
+    __syncthreads();  // Ssm becomes the Chien exchange, Csm the root counters
+    for (int i = threadIdx.x; i < 2 * 32 * 32; i += 64) cnt[i] = 0u;
+    __syncthreads();
 
     // phase 3: Chien search and Forney, two positions per exchange
     const int size = msg_len + E;
     uint8_t *corr = reinterpret_cast<uint8_t *>(tplanes) + (size_t)lane * (E * 32);  // [32 blocks][t][2]
-    uint8_t *mycnt = cnt + h * 1024;
+    uint32_t *mycnt = cnt + h * 1024;
     const uint32_t live = anyS & vmask;
 #pragma unroll 1
     for (int base = 0, it = 0; base < size; base += 2, ++it) {
@@ -990,8 +1066,8 @@ __global__ void __launch_bounds__(64) bs_solve_kernel(uint8_t *__restrict__ data
                     lb |= ((lo[b] >> j) & 1u) << b;
                 }
                 const uint32_t e = (ob && lb) ? ex[lg[ob] + 255 - lg[lb]] : 0u;
-                const int c = mycnt[j * 32 + lane];
-                mycnt[j * 32 + lane] = (uint8_t)(c + 1);
+                const int c = (int)mycnt[j * 32 + lane];
+                mycnt[j * 32 + lane] = (uint32_t)(c + 1);
                 const int slot = h == 0 ? c : t - 1 - c;
                 if (slot >= 0 && slot < t) {
                     corr[(j * t + slot) * 2] = (uint8_t)pos;
@@ -1013,19 +1089,20 @@ __global__ void __launch_bounds__(64) bs_solve_kernel(uint8_t *__restrict__ data
         int l = 0;
 #pragma unroll
         for (int b = 0; b < 6; ++b) l |= (int)((L[b] >> j) & 1u) << b;
-        const int c0 = cnt[j * 32 + lane], c1 = cnt[1024 + j * 32 + lane];
+        const int c0 = (int)cnt[j * 32 + lane], c1 = (int)cnt[1024 + j * 32 + lane];
         if (l > t || c0 + c1 != l) {
             status[blk] = 0;
             continue;
         }
+        // the corrections go out as fire-and-forget word XORs (both buffers
+        // are 4-byte aligned on this path; neighbouring blocks share words)
         for (int s = 0; s < t; ++s) {
             if (s >= c0 && s < t - c1) continue;
             const int p = corr[(j * t + s) * 2];
-            const uint8_t e = corr[(j * t + s) * 2 + 1];
-            if (p < msg_len)
-                data[blk * (size_t)msg_len + p] ^= e;
-            else
-                parity[blk * (size_t)E + (p - msg_len)] ^= e;
+            const uint32_t e = corr[(j * t + s) * 2 + 1];
+            uint8_t *a = p < msg_len ? data + blk * (size_t)msg_len + p : parity + blk * (size_t)E + (p - msg_len);
+            const uintptr_t w = reinterpret_cast<uintptr_t>(a);
+            atomicXor(reinterpret_cast<unsigned int *>(w & ~(uintptr_t)3), e << (8 * (w & 3)));
         }
         status[blk] = 1;
     }
