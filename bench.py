@@ -52,8 +52,14 @@ def load_traffic(workload):
 
 
 class ClockSampler:
-    """nvidia-smi sampling during the timed region."""
+    """SM clock and clock-event reasons sampled during the timed region.
 
+    Uses NVML through ctypes (libnvidia-ml ships with the driver) every
+    millisecond, so that even a region of a few milliseconds gets samples;
+    falls back to `nvidia-smi -lms 100` when NVML cannot be opened."""
+
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
     Q = (
         "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -64,8 +70,59 @@ class ClockSampler:
         self.index = index
         self.proc = None
         self.lines = []
+        self.samples = []  # (sm_mhz, reasons bitmask)
+        self.max_mhz = None
+        self.nvml = None
+        self.stop = threading.Event()
+
+    def _open_nvml(self):
+        import ctypes
+
+        try:
+            L = ctypes.CDLL("libnvidia-ml.so.1")
+        except OSError:
+            return False
+        if L.nvmlInit_v2() != 0:
+            return False
+        h = ctypes.c_void_p()
+        bus = None
+        try:
+            import torch
+
+            pr = torch.cuda.get_device_properties(self.index)
+            bus = "%08x:%02x:%02x.0" % (getattr(pr, "pci_domain_id", 0), pr.pci_bus_id, pr.pci_device_id)
+        except Exception:
+            bus = None
+        ok = bus is not None and L.nvmlDeviceGetHandleByPciBusId_v2(bus.encode(), ctypes.byref(h)) == 0
+        if not ok and L.nvmlDeviceGetHandleByIndex_v2(self.index, ctypes.byref(h)) != 0:
+            return False
+        mx = ctypes.c_uint()
+        if L.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) == 0:
+            self.max_mhz = float(mx.value)
+        self.reason_fn = getattr(L, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            getattr(L, "nvmlDeviceGetCurrentClocksThrottleReasons")
+        self.nvml, self.handle = L, h
+        return True
+
+    def _poll_nvml(self):
+        import ctypes
+
+        clk = ctypes.c_uint()
+        rs = ctypes.c_ulonglong()
+        while not self.stop.is_set():
+            if self.nvml.nvmlDeviceGetClockInfo(self.handle, 1, ctypes.byref(clk)) == 0:
+                r = rs.value if self.reason_fn(self.handle, ctypes.byref(rs)) == 0 else 0
+                self.samples.append((float(clk.value), r))
+            time.sleep(0.001)
 
     def __enter__(self):
+        try:
+            if self._open_nvml():
+                self.t = threading.Thread(target=self._poll_nvml, daemon=True)
+                self.t.start()
+                return self
+        except Exception:
+            self.nvml = None
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
@@ -82,6 +139,9 @@ class ClockSampler:
             self.lines.append(line.strip())
 
     def __exit__(self, *a):
+        self.stop.set()
+        if self.nvml is not None:
+            self.t.join(timeout=2)
         if self.proc:
             self.proc.terminate()
             try:
@@ -90,6 +150,15 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
+        if self.nvml is not None:
+            sm = [c for c, _ in self.samples]
+            reasons = set()
+            for _, r in self.samples:
+                for bit, name in self.REASONS.items():
+                    if r & bit:
+                        reasons.add(name)
+            return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": self.max_mhz,
+                    "reasons": sorted(reasons), "samples": len(sm), "source": "nvml"}
         sm, mx, reasons = [], 0.0, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
@@ -105,7 +174,7 @@ class ClockSampler:
                 if v.lower() == "active":
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "source": "nvidia-smi"}
 
 
 # ---------------------------------------------------------------- workloads

@@ -1078,33 +1078,51 @@ __global__ void __launch_bounds__(64) bs_solve_kernel(uint8_t *__restrict__ data
     }
     __syncthreads();
 
-    // phase 4: status and corrections, warp h takes blocks 16h .. 16h+15
-    for (int j = h * 16; j < h * 16 + 16; ++j) {
-        if (!((vmask >> j) & 1u)) continue;
-        const size_t blk = blk0 + j;
-        if (!((anyS >> j) & 1u)) {
-            status[blk] = 1;
-            continue;
-        }
-        int l = 0;
+    // phase 4: status and corrections, warp h takes blocks 16h .. 16h+15.
+    // Each block's list is 2t bytes (16-byte aligned); four blocks' lists are
+    // fetched together so that their L2 round trips overlap.
+    constexpr int NV = (2 * t) / 16;  // uint4 per block list
+#pragma unroll 1
+    for (int j0 = h * 16; j0 < h * 16 + 16; j0 += 4) {
+        uint4 cv[4][NV];
 #pragma unroll
-        for (int b = 0; b < 6; ++b) l |= (int)((L[b] >> j) & 1u) << b;
-        const int c0 = (int)cnt[j * 32 + lane], c1 = (int)cnt[1024 + j * 32 + lane];
-        if (l > t || c0 + c1 != l) {
-            status[blk] = 0;
-            continue;
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int v = 0; v < NV; ++v)
+                cv[r][v] = reinterpret_cast<const uint4 *>(corr + (size_t)(j0 + r) * t * 2)[v];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int j = j0 + r;
+            if (!((vmask >> j) & 1u)) continue;
+            const size_t blk = blk0 + j;
+            if (!((anyS >> j) & 1u)) {
+                status[blk] = 1;
+                continue;
+            }
+            int l = 0;
+#pragma unroll
+            for (int b = 0; b < 6; ++b) l |= (int)((L[b] >> j) & 1u) << b;
+            const int c0 = (int)cnt[j * 32 + lane], c1 = (int)cnt[1024 + j * 32 + lane];
+            if (l > t || c0 + c1 != l) {
+                status[blk] = 0;
+                continue;
+            }
+            // the corrections go out as fire-and-forget word XORs (both buffers
+            // are 4-byte aligned on this path; neighbouring blocks share words)
+#pragma unroll
+            for (int sl = 0; sl < t; ++sl) {
+                if (sl >= c0 && sl < t - c1) continue;
+                const uint4 q = cv[r][sl / 8];
+                const uint32_t wv = (sl % 8) < 2 ? q.x : (sl % 8) < 4 ? q.y : (sl % 8) < 6 ? q.z : q.w;
+                const uint32_t pe = wv >> (16 * (sl & 1));
+                const int p = (int)(pe & 0xffu);
+                const uint32_t e = (pe >> 8) & 0xffu;
+                uint8_t *a = p < msg_len ? data + blk * (size_t)msg_len + p : parity + blk * (size_t)E + (p - msg_len);
+                const uintptr_t w = reinterpret_cast<uintptr_t>(a);
+                atomicXor(reinterpret_cast<unsigned int *>(w & ~(uintptr_t)3), e << (8 * (w & 3)));
+            }
+            status[blk] = 1;
         }
-        // the corrections go out as fire-and-forget word XORs (both buffers
-        // are 4-byte aligned on this path; neighbouring blocks share words)
-        for (int s = 0; s < t; ++s) {
-            if (s >= c0 && s < t - c1) continue;
-            const int p = corr[(j * t + s) * 2];
-            const uint32_t e = corr[(j * t + s) * 2 + 1];
-            uint8_t *a = p < msg_len ? data + blk * (size_t)msg_len + p : parity + blk * (size_t)E + (p - msg_len);
-            const uintptr_t w = reinterpret_cast<uintptr_t>(a);
-            atomicXor(reinterpret_cast<unsigned int *>(w & ~(uintptr_t)3), e << (8 * (w & 3)));
-        }
-        status[blk] = 1;
     }
 }
 
