@@ -727,6 +727,15 @@ __device__ __forceinline__ void vmul(const uint32_t (&a)[8], const uint32_t (&b)
     reduce15(p, r);
 }
 
+// p += a * b without the reduction (15 planes); several products can share
+// one reduce15
+__device__ __forceinline__ void vmul_acc15(const uint32_t (&a)[8], const uint32_t (&b)[8], uint32_t (&p)[15]) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) p[i + j] = andxor(a[i], b[j], p[i + j]);
+}
+
 __device__ __forceinline__ void vsqr(const uint32_t (&a)[8], uint32_t (&r)[8]) {
     uint32_t p[15];
 #pragma unroll
@@ -822,7 +831,9 @@ struct SolveGeom {
     static constexpr int t = E / 2;
     static constexpr int K = t / 2;          // coefficients per warp
     static constexpr int kS = E * 8 * 32;    // words: syndrome planes of 32 groups
-    static constexpr int kC = t * 8 * 32;    // words: C_1..C_t planes of 32 groups (also the BM exchange)
+    // words: C_1..C_t planes of 32 groups; before them the BM exchange
+    // (2 buffers x 40 rows x 32), after them the root counters (2 x 32 x 32)
+    static constexpr int kC = t * 8 * 32 > 2 * 40 * 32 ? t * 8 * 32 : 2 * 40 * 32;
     static constexpr int kX = 2 * 2 * 2 * 24 * 32;  // words: Chien exchange (2 buffers x 2 positions x 2 warps)
     static constexpr int kSX = kS > kX ? kS : kX;
     static constexpr size_t smem = (size_t)(kSX + kC) * 4 + 768;
@@ -843,33 +854,33 @@ template <int E, int H>
 __device__ __forceinline__ void chien_step(uint32_t (&Ct)[SolveGeom<E>::K][8], uint32_t (&Ot)[SolveGeom<E>::K][8],
                                            uint32_t *out, int stride) {
     constexpr int K = SolveGeom<E>::K;
-    uint32_t pe[8], po[8], pw[8];
+    // with K even, C_i (i = HK+1+u) has odd degree exactly for even u
+    static_assert(K % 2 == 0, "K must be even");
 #pragma unroll
     for (int b = 0; b < 8; ++b) {
-        pe[b] = (H == 0 && b == 0) ? ~0u : 0u;  // C_0 = 1
-        po[b] = 0u;
-        pw[b] = 0u;
-    }
+        uint32_t po = Ct[0][b], pe = Ct[1][b];
 #pragma unroll
-    for (int u = 0; u < K; ++u) {
-        const int i = H * K + 1 + u;
-#pragma unroll
-        for (int b = 0; b < 8; ++b) {
-            if (i & 1)
-                po[b] ^= Ct[u][b];
-            else
-                pe[b] ^= Ct[u][b];
+        for (int u = 2; u < K; u += 4) {
+            if (u + 2 < K) {
+                po = xor3(po, Ct[u][b], Ct[u + 2][b]);
+                pe = xor3(pe, Ct[u + 1][b], Ct[u + 3][b]);
+            } else {
+                po ^= Ct[u][b];
+                pe ^= Ct[u + 1][b];
+            }
         }
-    }
+        if (H == 0 && b == 0) pe = ~pe;  // C_0 = 1
+        uint32_t pw = Ot[0][b];
 #pragma unroll
-    for (int v = 0; v < K; ++v)
-#pragma unroll
-        for (int b = 0; b < 8; ++b) pw[b] ^= Ot[v][b];
-#pragma unroll
-    for (int b = 0; b < 8; ++b) {
-        out[b * stride] = pe[b];
-        out[(8 + b) * stride] = po[b];
-        out[(16 + b) * stride] = pw[b];
+        for (int v = 1; v < K; v += 2) {
+            if (v + 1 < K)
+                pw = xor3(pw, Ot[v][b], Ot[v + 1][b]);
+            else
+                pw ^= Ot[v][b];
+        }
+        out[b * stride] = pe;
+        out[(8 + b) * stride] = po;
+        out[(16 + b) * stride] = pw;
     }
     chien_advance<E, H>(Ct, Ot, std::make_integer_sequence<int, K>{});
 }
@@ -931,25 +942,26 @@ __global__ void __launch_bounds__(64) bs_solve_kernel(uint8_t *__restrict__ data
     for (int b = 0; b < 8; ++b) binv[b] = b == 0 ? ~0u : 0u;
 #pragma unroll
     for (int b = 0; b < 6; ++b) L[b] = 0u;
-    uint32_t *Xb = Csm;  // [2 buffers][4 x 8 words][32]
+    uint32_t *Xb = Csm;  // [2 buffers][40 rows][32]: d partials of both warps, warp 0's top C and Bs, 1/b
 #pragma unroll 1
     for (int n = 0; n < E; ++n) {
-        uint32_t dp[8];
+        // partial discrepancy, one reduction for all products
+        uint32_t p15[15];
 #pragma unroll
-        for (int b = 0; b < 8; ++b) dp[b] = h == 0 ? Ssm[(n * 8 + b) * 32 + lane] : 0u;
+        for (int k = 0; k < 15; ++k) p15[k] = (h == 0 && k < 8) ? Ssm[(n * 8 + k) * 32 + lane] : 0u;
 #pragma unroll
         for (int u = 0; u < K; ++u) {
             const int j = n - (h * K + 1 + u);
             if (j >= 0) {
-                uint32_t sj[8], pr[8];
+                uint32_t sj[8];
 #pragma unroll
                 for (int b = 0; b < 8; ++b) sj[b] = Ssm[(j * 8 + b) * 32 + lane];
-                vmul(C[u], sj, pr);
-#pragma unroll
-                for (int b = 0; b < 8; ++b) dp[b] ^= pr[b];
+                vmul_acc15(C[u], sj, p15);
             }
         }
-        uint32_t *X = Xb + (n & 1) * (32 * 32);
+        uint32_t dp[8];
+        reduce15(p15, dp);
+        uint32_t *X = Xb + (n & 1) * (40 * 32);
 #pragma unroll
         for (int b = 0; b < 8; ++b) X[(h * 8 + b) * 32 + lane] = dp[b];
         if (h == 0) {
@@ -957,6 +969,7 @@ __global__ void __launch_bounds__(64) bs_solve_kernel(uint8_t *__restrict__ data
             for (int b = 0; b < 8; ++b) {
                 X[(16 + b) * 32 + lane] = C[K - 1][b];
                 X[(24 + b) * 32 + lane] = Bs[K - 1][b];
+                X[(32 + b) * 32 + lane] = binv[b];
             }
         }
         __syncthreads();
@@ -967,9 +980,20 @@ __global__ void __launch_bounds__(64) bs_solve_kernel(uint8_t *__restrict__ data
             nzd |= d[b];
         }
         const uint32_t cond = nzd & le_const(L, n >> 1);
-        uint32_t q[8], dinv[8];
-        vmul(d, binv, q);
-        vinv(d, dinv);
+        uint32_t q[8];
+        if (h == 0) {
+            // warp 0 keeps 1/b (the inverse costs 4 products and 7 squares)
+            vmul(d, binv, q);
+            uint32_t dinv[8];
+            vinv(d, dinv);
+#pragma unroll
+            for (int b = 0; b < 8; ++b) binv[b] = bitsel(cond, dinv[b], binv[b]);
+        } else {
+            uint32_t bi[8];
+#pragma unroll
+            for (int b = 0; b < 8; ++b) bi[b] = X[(32 + b) * 32 + lane];
+            vmul(d, bi, q);
+        }
         // C_i ^= q * Bs_i and Bs_i <- cond ? C_{i-1} : Bs_{i-1}, from the top down
 #pragma unroll
         for (int u = K - 1; u >= 0; --u) {
@@ -992,8 +1016,6 @@ __global__ void __launch_bounds__(64) bs_solve_kernel(uint8_t *__restrict__ data
                 Bs[u][b] = bitsel(cond, lc, lb);
             }
         }
-#pragma unroll
-        for (int b = 0; b < 8; ++b) binv[b] = bitsel(cond, dinv[b], binv[b]);
         l_update(L, n + 1, cond);
     }
     __syncthreads();  // BM exchange reads done before Csm is rewritten
@@ -1008,19 +1030,19 @@ __global__ void __launch_bounds__(64) bs_solve_kernel(uint8_t *__restrict__ data
 #pragma unroll
     for (int v = 0; v < K; ++v) {
         const int k = 2 * v + h;
+        uint32_t p15[15];
 #pragma unroll
-        for (int b = 0; b < 8; ++b) Ot[v][b] = Ssm[(k * 8 + b) * 32 + lane];
+        for (int q = 0; q < 15; ++q) p15[q] = q < 8 ? Ssm[(k * 8 + q) * 32 + lane] : 0u;
         for (int i = 1; i <= k; ++i) {
-            uint32_t ci[8], sj[8], pr[8];
+            uint32_t ci[8], sj[8];
 #pragma unroll
             for (int b = 0; b < 8; ++b) {
                 ci[b] = Csm[((i - 1) * 8 + b) * 32 + lane];
                 sj[b] = Ssm[((k - i) * 8 + b) * 32 + lane];
             }
-            vmul(ci, sj, pr);
-#pragma unroll
-            for (int b = 0; b < 8; ++b) Ot[v][b] ^= pr[b];
+            vmul_acc15(ci, sj, p15);
         }
+        reduce15(p15, Ot[v]);
     }
     __syncthreads();  // Ssm becomes the Chien exchange, Csm the root counters
     for (int i = threadIdx.x; i < 2 * 32 * 32; i += 64) cnt[i] = 0u;
@@ -1050,7 +1072,7 @@ __global__ void __launch_bounds__(64) bs_solve_kernel(uint8_t *__restrict__ data
 #pragma unroll
             for (int b = 0; b < 8; ++b) {
                 const uint32_t o = A[(8 + b) * 32] ^ B[(8 + b) * 32];
-                nz |= A[b * 32] ^ B[b * 32] ^ o;
+                nz |= xor3(A[b * 32], B[b * 32], o);
                 lo[b] = o;
                 om[b] = A[(16 + b) * 32] ^ B[(16 + b) * 32];
             }
