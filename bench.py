@@ -552,7 +552,240 @@ def cpu_baseline_rsi16(threads, nblocks, decode):
     return nblocks * 2052 / dt / 1e9, dt
 
 
+# ---------------------------------------------------------------- mixed batch
+
+def make_mixed(torch, total_bytes, seed):
+    """Seeded mixed workload of uneven requests: half the codeword bytes RS256
+    (ecc_len in {2..64}, block_len uniform in [ecc+1, 255]), a quarter RSi16
+    (ecc_len in {16..128}, block_len in [256, 4096] rounded down to a multiple
+    of ecc_len), a quarter CIRC16(128, 8, 128, 8, 4) codewords.  RS256 and
+    RSi16 requests are half encode, half decode with correctable errors
+    (uniform 0 .. ecc_len/2 per block at distinct positions); CIRC16 requests
+    are encodes.  Blocks per request are log-uniform.  Decode inputs are
+    encoded by the plain GPU path and corrupted on the device.
+
+    Returns (requests, pools): every request holds its code and device tensor
+    views; pools hold the pristine inputs for restoring between runs."""
+    from libffrs_gb300 import capi
+
+    rng = np.random.Generator(np.random.PCG64(seed))
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    st = torch.cuda.current_stream().cuda_stream
+    reqs = []
+    codes = {}
+
+    def code(kind, *key):
+        k = (kind,) + key
+        if k not in codes:
+            codes[k] = {"rs256": capi.RS256Code, "rsi16": capi.RSi16Code, "circ16": capi.CIRC16Code}[kind](*key)
+        return codes[k]
+
+    budget = {"rs256": total_bytes // 2, "rsi16": total_bytes // 4, "circ16": total_bytes // 4}
+    # RS256
+    used = 0
+    while used < budget["rs256"]:
+        ecc = int(rng.choice([2, 4, 8, 16, 32, 64]))
+        bl = int(rng.integers(ecc + 1, 256))
+        ml = bl - ecc
+        nb = int(np.exp(rng.uniform(np.log(16), np.log(16384))))
+        nb = max(1, min(nb, (budget["rs256"] - used) // bl + 1))
+        dec = bool(rng.integers(0, 2))
+        data = torch.randint(0, 256, (nb, ml), dtype=torch.uint8, device="cuda", generator=g)
+        par = torch.zeros((nb, ecc), dtype=torch.uint8, device="cuda")
+        c = code("rs256", ecc)
+        r = {"kind": "rs256", "code": c, "op": "dec" if dec else "enc", "nb": nb, "ml": ml, "ecc": ecc,
+             "data": data, "par": par, "status": torch.zeros(nb, dtype=torch.uint8, device="cuda")}
+        if dec:
+            c.encode(data.data_ptr(), nb, ml, par.data_ptr(), st)
+            cw = torch.cat([data, par], dim=1)
+            k = torch.randint(0, ecc // 2 + 1, (nb,), device="cuda", generator=g)
+            kmax = ecc // 2
+            if kmax:
+                pos = torch.rand((nb, bl), device="cuda", generator=g).argsort(dim=1)[:, :kmax]
+                vals = torch.randint(1, 256, (nb, kmax), dtype=torch.uint8, device="cuda", generator=g)
+                vals *= (torch.arange(kmax, device="cuda")[None, :] < k[:, None]).to(torch.uint8)
+                rows = torch.arange(nb, device="cuda")[:, None].expand(nb, kmax)
+                cw[rows, pos] ^= vals
+            data.copy_(cw[:, :ml])
+            par.copy_(cw[:, ml:])
+        r["data0"], r["par0"] = data.clone(), par.clone()
+        reqs.append(r)
+        used += nb * bl
+    # RSi16
+    used = 0
+    while used < budget["rsi16"]:
+        ecc = int(rng.choice([16, 32, 64, 128]))
+        bl = int(rng.integers(256, 4097)) // ecc * ecc
+        ml = bl - ecc
+        nb = int(np.exp(rng.uniform(np.log(2), np.log(512))))
+        nb = max(1, min(nb, (budget["rsi16"] - used) // (2 * bl) + 1))
+        dec = bool(rng.integers(0, 2))
+        msg = torch.randint(-32768, 32768, (nb, ml), dtype=torch.int16, device="cuda", generator=g)
+        par = torch.zeros((nb, ecc), dtype=torch.int16, device="cuda")
+        c = code("rsi16", bl, ecc)
+        r = {"kind": "rsi16", "code": c, "op": "dec" if dec else "enc", "nb": nb, "ml": ml, "ecc": ecc,
+             "data": msg, "par": par, "status": torch.zeros(nb, dtype=torch.uint8, device="cuda")}
+        if dec:
+            c.encode(msg.data_ptr(), nb, par.data_ptr(), st)
+            cw = torch.cat([msg, par], dim=1)
+            kmax = ecc // 2
+            k = torch.randint(0, kmax + 1, (nb,), device="cuda", generator=g)
+            pos = torch.rand((nb, bl), device="cuda", generator=g).argsort(dim=1)[:, :kmax]
+            rows = torch.arange(nb, device="cuda")[:, None].expand(nb, kmax)
+            v = cw[rows, pos].to(torch.int64) & 0xFFFF
+            d = torch.randint(1, 65537, (nb, kmax), device="cuda", generator=g)
+            nv = (v + d) % 65537
+            nv = torch.where(nv == 65536, (v + d + 1) % 65537, nv)
+            nv = torch.where(torch.arange(kmax, device="cuda")[None, :] < k[:, None], nv, v)
+            cw[rows, pos] = nv.to(torch.int32).to(torch.int16)
+            msg.copy_(cw[:, :ml])
+            par.copy_(cw[:, ml:])
+        r["data0"], r["par0"] = msg.clone(), par.clone()
+        reqs.append(r)
+        used += nb * bl * 2
+    # CIRC16 (encode)
+    used = 0
+    c = code("circ16", 128, 8, 128, 8, 4)
+    cwb = (c.message_len + c.ecc_len) * 2
+    while used < budget["circ16"]:
+        nb = int(np.exp(rng.uniform(np.log(1), np.log(64))))
+        nb = max(1, min(nb, (budget["circ16"] - used) // cwb + 1))
+        msg = torch.randint(-32768, 32768, (nb, c.message_len), dtype=torch.int16, device="cuda", generator=g)
+        ecc = torch.zeros((nb, c.ecc_len), dtype=torch.int16, device="cuda")
+        reqs.append({"kind": "circ16", "code": c, "op": "enc", "nb": nb, "data": msg, "par": ecc,
+                     "data0": msg, "par0": ecc, "status": None})
+        used += nb * cwb
+    order = rng.permutation(len(reqs))
+    reqs = [reqs[i] for i in order]
+    torch.cuda.synchronize()
+    return reqs, codes
+
+
+def mixed_bytes(r):
+    return r["data"].numel() * r["data"].element_size() + r["par"].numel() * r["par"].element_size()
+
+
+def mixed_restore(reqs):
+    for r in reqs:
+        if r["op"] == "dec":
+            r["data"].copy_(r["data0"])
+            r["par"].copy_(r["par0"])
+
+
+def mixed_plain(reqs, stream):
+    """one per-code C-ABI call per request"""
+    for r in reqs:
+        c = r["code"]
+        if r["kind"] == "rs256":
+            if r["op"] == "enc":
+                c.encode(r["data"].data_ptr(), r["nb"], r["ml"], r["par"].data_ptr(), stream)
+            else:
+                c.decode(r["data"].data_ptr(), r["par"].data_ptr(), r["nb"], r["ml"], r["status"].data_ptr(), stream)
+        elif r["kind"] == "rsi16":
+            if r["op"] == "enc":
+                c.encode(r["data"].data_ptr(), r["nb"], r["par"].data_ptr(), stream)
+            else:
+                c.repair(r["data"].data_ptr(), r["par"].data_ptr(), r["nb"], r["status"].data_ptr(), stream)
+        else:
+            c.encode(r["data"].data_ptr(), r["nb"], r["par"].data_ptr(), stream)
+
+
+def mixed_batch(reqs):
+    from libffrs_gb300 import capi
+
+    b = capi.Batch()
+    for r in reqs:
+        c = r["code"]
+        op = capi.ENCODE if r["op"] == "enc" else capi.DECODE
+        st = r["status"].data_ptr() if r["op"] == "dec" else None
+        if r["kind"] == "rs256":
+            b.add_rs256(c, op, r["data"].data_ptr(), r["par"].data_ptr(), r["nb"], r["ml"], st)
+        elif r["kind"] == "rsi16":
+            b.add_rsi16(c, op, r["data"].data_ptr(), r["par"].data_ptr(), r["nb"], st)
+        else:
+            b.add_circ16(c, r["data"].data_ptr(), r["par"].data_ptr(), r["nb"])
+    return b
+
+
+def bench_batch_mixed(args, torch, rank, world):
+    from libffrs_gb300 import capi
+
+    total = (args.blocks or 1024) << 20  # --blocks = MiB of codewords for this workload
+    reqs, _codes = make_mixed(torch, total, 4000 + rank)
+    nbytes = sum(mixed_bytes(r) for r in reqs)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+
+    def outputs():
+        return [(r["data"].clone() if r["op"] == "dec" else None, r["par"].clone(),
+                 r["status"].clone() if r["op"] == "dec" else None) for r in reqs]
+
+    def run_timed(fn, steps):
+        ms = []
+        for _ in range(steps):
+            mixed_restore(reqs)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return ms
+
+    # plain per-request path (the reference's API shape: one call per request)
+    for _ in range(max(1, args.warmup)):
+        mixed_restore(reqs)
+        mixed_plain(reqs, sp)
+    torch.cuda.synchronize()
+    plain_ms = run_timed(lambda: mixed_plain(reqs, sp), max(1, min(args.steps, 3)))
+    ref_out = outputs()
+    # batched: autotuned plan, captured graph, one replay per step
+    b = mixed_batch(reqs)
+    mixed_restore(reqs)
+    b.plan(autotune=True, stream=sp)
+    b.capture(sp)
+    for _ in range(args.warmup):
+        mixed_restore(reqs)
+        b.launch(sp)
+    torch.cuda.synchronize()
+    launches0 = capi.kernel_launches()
+    capi.timing_collect()
+    capi.timing_enable(True)
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        kern_ms = run_timed(lambda: b.launch(sp), args.steps)
+    launches = capi.kernel_launches() - launches0
+    kernels = capi.timing_collect()
+    capi.timing_enable(False)
+    got = outputs()
+    same = all(all((x is None and y is None) or torch.equal(x, y) for x, y in zip(o, p))
+               for o, p in zip(ref_out, got))
+    if not same:
+        raise SystemExit("batched outputs differ from the plain per-request path")
+    plain_gbs = nbytes / (statistics.median(plain_ms) / 1e3) / 1e9
+    batch_gbs = nbytes / (statistics.median(kern_ms) / 1e3) / 1e9
+    nk = {}
+    for r in reqs:
+        nk[r["kind"] + "-" + r["op"]] = nk.get(r["kind"] + "-" + r["op"], 0) + 1
+    return {
+        "workload": "batch-mixed", "total_ms": sum(kern_ms), "kern_ms": kern_ms, "algo_bytes_per_step": nbytes,
+        "launches": launches, "kernels": kernels, "clocks": clk.summary(),
+        "e2e": {"value": None, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
+                "note": "device-resident batch; host-buffer serving is the serving workload"},
+        "config": {"workload": "mixed batch: 1/2 RS256 (ecc 2..64, uneven lengths), 1/4 RSi16 (ecc 16..128, "
+                               "block 256..4096), 1/4 CIRC16(128,8,128,8,4); half encode, half decode",
+                   "bytes": nbytes, "requests": len(reqs), "requests_by_kind": nk, "plan": b.info(),
+                   "l2": "inputs larger than L2 (%d MB)" % (nbytes >> 20)},
+        "dtype": "u8 / u32 mod 65537",
+        "extra": {"plain_per_request_gbs": plain_gbs, "batched_gbs": batch_gbs,
+                  "batched_over_plain": batch_gbs / plain_gbs, "bit_identical_to_plain": same,
+                  "plain_ms": statistics.median(plain_ms)},
+    }
+
+
 WORKLOADS = {
+    "batch-mixed": (bench_batch_mixed, None, 0, "GB/s"),
     "rsi16-encode": (lambda a, t, r, w: bench_rsi16(a, t, r, w, False),
                      lambda th, n: cpu_baseline_rsi16(th, n, False), 65536, "GB/s"),
     "rsi16-decode": (lambda a, t, r, w: bench_rsi16(a, t, r, w, True),
@@ -574,6 +807,9 @@ def run_reference(args, rank, world):
     if rank != 0:
         return
     _, cpu_fn, sample, unit = WORKLOADS[args.workload]
+    if cpu_fn is None:
+        print(json.dumps({"impl": "reference", "unavailable": f"no CPU arm for the {args.workload} workload"}))
+        return
     threads = host_threads()
     vals = []
     for _ in range(args.warmup):
@@ -674,7 +910,9 @@ def main():
     }
     if "status_ok_fraction" in r:
         line["status_ok_fraction"] = r["status_ok_fraction"]
-    if not args.no_cpu_baseline:
+    if "extra" in r:
+        line.update(r["extra"])
+    if not args.no_cpu_baseline and WORKLOADS[args.workload][1] is not None:
         _, cpu_fn, sample, unit = WORKLOADS[args.workload]
         threads = host_threads()
         v, dt = cpu_fn(threads, sample)

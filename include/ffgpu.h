@@ -187,6 +187,42 @@ FFGPU_API int ffgpu_circ16_find_outer_error_locations_host(const ffgpu_circ16 *c
                                                            size_t *count);
 FFGPU_API int ffgpu_circ16_repair_host(const ffgpu_circ16 *code, uint16_t *msg, uint16_t *ecc, size_t nblocks, uint8_t *status);
 
+/* ---------------------------------------------------------------- batch */
+/* No reference counterpart.  A batch collects requests of any mix of codes,
+ * geometries and directions (device buffers, laid out as for the per-code
+ * entry points above) and serves all of them with one persistent kernel
+ * launch; the launch can be captured into a CUDA graph and replayed.  Results
+ * are byte-identical to calling the per-code entry point once per request.
+ * A batch holds pointers: the buffers must stay valid while it is planned,
+ * captured and launched. */
+typedef struct ffgpu_batch ffgpu_batch;
+#define FFGPU_OP_ENCODE 0
+#define FFGPU_OP_DECODE 1
+FFGPU_API int ffgpu_batch_create(ffgpu_batch **out);
+FFGPU_API int ffgpu_batch_destroy(ffgpu_batch *batch);
+FFGPU_API int ffgpu_batch_clear(ffgpu_batch *batch);
+/* RS256: ENCODE writes parity (ffgpu_rs256_encode); DECODE repairs in place
+ * and writes one status byte per block (ffgpu_rs256_decode) */
+FFGPU_API int ffgpu_batch_add_rs256(ffgpu_batch *batch, const ffgpu_rs256 *code, int op, uint8_t *data,
+                                    uint8_t *parity, size_t nblocks, size_t message_len, uint8_t *status);
+/* RSi16: as ffgpu_rsi16_encode / ffgpu_rsi16_repair */
+FFGPU_API int ffgpu_batch_add_rsi16(ffgpu_batch *batch, const ffgpu_rsi16 *code, int op, uint16_t *msg,
+                                    uint16_t *parity, size_t nblocks, uint8_t *status);
+/* CIRC16: ENCODE only, as ffgpu_circ16_encode */
+FFGPU_API int ffgpu_batch_add_circ16(ffgpu_batch *batch, const ffgpu_circ16 *code, int op, uint16_t *msg,
+                                     uint16_t *ecc, size_t nblocks);
+/* cut the requests into work items (longest first) and upload them; with
+ * autotune != 0, candidate schedules (RS256 blocks per item, RSi16 blocks per
+ * item, CTAs per SM) are timed on the batch itself -- decode buffers are saved
+ * and restored around every trial -- and the fastest is kept */
+FFGPU_API int ffgpu_batch_plan(ffgpu_batch *batch, int autotune, void *stream);
+/* capture the launch into a CUDA graph (later launches replay it) */
+FFGPU_API int ffgpu_batch_capture(ffgpu_batch *batch, void *stream);
+/* serve every request with one persistent launch (or one graph replay) */
+FFGPU_API int ffgpu_batch_launch(ffgpu_batch *batch, void *stream);
+FFGPU_API int ffgpu_batch_info(const ffgpu_batch *batch, int *tile_rs256, int *tile_rsi16, int *ctas_per_sm,
+                               size_t *items, unsigned *grid);
+
 #ifdef __cplusplus
 }
 #endif

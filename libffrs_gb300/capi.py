@@ -98,6 +98,17 @@ def _declare(L):
         "ffgpu_circ16_find_outer_error_locations": (_I, [_P, _P, _P, _SZ, _P, _P]),
         "ffgpu_circ16_encode_host": (_I, [_P, _P, _SZ, _P]),
         "ffgpu_circ16_repair_host": (_I, [_P, _P, _P, _SZ, _P]),
+        "ffgpu_batch_create": (_I, [_PP]),
+        "ffgpu_batch_destroy": (_I, [_P]),
+        "ffgpu_batch_clear": (_I, [_P]),
+        "ffgpu_batch_add_rs256": (_I, [_P, _P, _I, _P, _P, _SZ, _SZ, _P]),
+        "ffgpu_batch_add_rsi16": (_I, [_P, _P, _I, _P, _P, _SZ, _P]),
+        "ffgpu_batch_add_circ16": (_I, [_P, _P, _I, _P, _P, _SZ]),
+        "ffgpu_batch_plan": (_I, [_P, _I, _P]),
+        "ffgpu_batch_capture": (_I, [_P, _P]),
+        "ffgpu_batch_launch": (_I, [_P, _P]),
+        "ffgpu_batch_info": (_I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I),
+                                  ctypes.POINTER(_SZ), ctypes.POINTER(ctypes.c_uint)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name, None)
@@ -189,6 +200,55 @@ class CIRC16Code:
 
     def repair(self, msg_ptr, ecc_ptr, nblocks, status_ptr, stream=None):
         call("ffgpu_circ16_repair", self.h, msg_ptr, ecc_ptr, nblocks, status_ptr, stream)
+
+
+ENCODE, DECODE = 0, 1
+
+
+class Batch:
+    """Requests of mixed codes served by one persistent launch (ffgpu_batch).
+
+    Buffers are device pointers and must outlive the batch's use."""
+
+    def __init__(self):
+        h = ctypes.c_void_p()
+        call("ffgpu_batch_create", ctypes.byref(h))
+        self.h = h
+        self._keep = []
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.ffgpu_batch_destroy(self.h)
+            self.h = None
+
+    def add_rs256(self, code, op, data_ptr, parity_ptr, nblocks, message_len, status_ptr=None):
+        self._keep.append(code)
+        call("ffgpu_batch_add_rs256", self.h, code.h, op, data_ptr, parity_ptr, nblocks, message_len, status_ptr)
+
+    def add_rsi16(self, code, op, msg_ptr, parity_ptr, nblocks, status_ptr=None):
+        self._keep.append(code)
+        call("ffgpu_batch_add_rsi16", self.h, code.h, op, msg_ptr, parity_ptr, nblocks, status_ptr)
+
+    def add_circ16(self, code, msg_ptr, ecc_ptr, nblocks):
+        self._keep.append(code)
+        call("ffgpu_batch_add_circ16", self.h, code.h, ENCODE, msg_ptr, ecc_ptr, nblocks)
+
+    def plan(self, autotune=False, stream=None):
+        call("ffgpu_batch_plan", self.h, 1 if autotune else 0, stream)
+
+    def capture(self, stream=None):
+        call("ffgpu_batch_capture", self.h, stream)
+
+    def launch(self, stream=None):
+        call("ffgpu_batch_launch", self.h, stream)
+
+    def info(self):
+        a, b, c = _I(), _I(), _I()
+        n, g = _SZ(), ctypes.c_uint()
+        call("ffgpu_batch_info", self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), ctypes.byref(n),
+             ctypes.byref(g))
+        return {"tile_rs256": a.value, "tile_rsi16": b.value, "ctas_per_sm": c.value, "items": n.value,
+                "grid": g.value}
 
 
 def timing_enable(on=True):

@@ -1,0 +1,595 @@
+// Fused batch path: requests of mixed codes (RS256, RSi16, CIRC16), uneven
+// geometries and both directions are cut into work items and served by ONE
+// persistent launch.  Every CTA (four warps) pulls the next item from a global
+// counter; items are ordered longest first so the tail stays short.  The
+// launch can be captured once in a CUDA graph and replayed.  The schedule --
+// RS256 blocks per item, RSi16 blocks per item and CTAs per SM -- is chosen by
+// timing candidate plans on the batch itself (decode buffers are restored
+// after every trial).
+//
+// Each item runs the same per-block device code as the standalone kernels
+// (rs256_device.cuh, rsi16_device.cuh), so the bytes are identical to the
+// plain per-request path.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "handles.h"
+#include "rs256_device.cuh"
+#include "rsi16_device.cuh"
+
+namespace ffgpu {
+
+enum : uint8_t { BK_RS256_ENC = 0, BK_RS256_DEC = 1, BK_RSI16_ENC = 2, BK_RSI16_DEC = 3, BK_CIRC16_ENC = 4 };
+
+constexpr int kBatchThreads = 128;
+constexpr int kBatchWarps = kBatchThreads / 32;
+
+struct BatchCode {
+    // RS256
+    const uint32_t *lut;
+    const uint8_t *exp512, *log256;
+    int W, ecc;
+    // RSi16, or the inner code of a CIRC16
+    Rsi16Dev rsi;
+    // CIRC16: outer code and geometry (pycirc16.hpp:46-65)
+    Rsi16Dev rso;
+    uint32_t c_message_len, c_ecc_len, c_rso_interleave, c_rso_ieccl, c_rsi_ieccl, c_inner_rows, c_outer_rows;
+};
+
+struct BatchItem {
+    uint8_t kind;
+    uint8_t pad[3];
+    uint32_t code;
+    uint32_t nblocks;
+    int32_t msg_len;
+    void *msg;
+    void *par;
+    uint8_t *status;
+};
+
+struct BatchArgs {
+    const BatchItem *items;
+    uint32_t nitems;
+    const BatchCode *codes;
+    uint32_t *counter;
+    uint8_t *rs_scratch;   // per CTA: kBatchThreads * kDecodeScratchBytes
+    uint32_t *circ_tmp;    // per CTA: circ_tmp_words
+    size_t circ_tmp_words;
+    uint32_t ws_words;     // RSi16 workspace words per warp (shared memory)
+};
+
+// ---------------------------------------------------------------- item bodies
+
+template <int W>
+__device__ void rs256_enc_item(const BatchCode &c, const BatchItem &it, uint32_t *sm) {
+    uint32_t *s_lut = sm;
+    uint8_t *s_data = reinterpret_cast<uint8_t *>(sm + 256 * W);
+    for (int i = threadIdx.x; i < 256 * W; i += kBatchThreads) s_lut[i] = c.lut[i];
+    const int ml = it.msg_len;
+    const uint8_t *data = static_cast<const uint8_t *>(it.msg);
+    uint8_t *par = static_cast<uint8_t *>(it.par);
+    for (uint32_t b0 = 0; b0 < it.nblocks; b0 += kBatchThreads) {
+        const int nb = (int)min((uint32_t)kBatchThreads, it.nblocks - b0);
+        __syncthreads();  // table ready, previous chunk consumed
+        for (int i = threadIdx.x; i < nb * ml; i += kBatchThreads) s_data[i] = data[(size_t)b0 * ml + i];
+        __syncthreads();
+        if ((int)threadIdx.x < nb)
+            rs256_encode_one<W>(s_data + (size_t)threadIdx.x * ml, ml, s_lut,
+                                par + (size_t)(b0 + threadIdx.x) * c.ecc, c.ecc);
+    }
+}
+
+template <int W>
+__device__ void rs256_dec_item(const BatchCode &c, const BatchItem &it, uint32_t *sm, uint8_t *scratch) {
+    uint32_t *s_lut = sm;
+    uint8_t *ex = reinterpret_cast<uint8_t *>(sm + 256 * W);
+    uint8_t *lg = ex + 512;
+    for (int i = threadIdx.x; i < 256 * W; i += kBatchThreads) s_lut[i] = c.lut[i];
+    for (int i = threadIdx.x; i < 512; i += kBatchThreads) ex[i] = c.exp512[i];
+    for (int i = threadIdx.x; i < 256; i += kBatchThreads) lg[i] = c.log256[i];
+    __syncthreads();
+    const DecodeScratchG sc(scratch, threadIdx.x, kBatchThreads);
+    const int ml = it.msg_len;
+    uint8_t *data = static_cast<uint8_t *>(it.msg);
+    uint8_t *par = static_cast<uint8_t *>(it.par);
+    for (uint32_t b = threadIdx.x; b < it.nblocks; b += kBatchThreads)
+        decode_one<W>(data + (size_t)b * ml, par + (size_t)b * c.ecc, ml, c.ecc, s_lut, ex, lg, sc, it.status + b,
+                      nullptr);
+}
+
+#define FFGPU_BATCH_W(W, CALL)                       \
+    switch (W) {                                     \
+        case 1: { constexpr int w_ = 1; CALL; } break;   \
+        case 2: { constexpr int w_ = 2; CALL; } break;   \
+        case 4: { constexpr int w_ = 4; CALL; } break;   \
+        case 8: { constexpr int w_ = 8; CALL; } break;   \
+        case 16: { constexpr int w_ = 16; CALL; } break; \
+        case 32: { constexpr int w_ = 32; CALL; } break; \
+        default: { constexpr int w_ = 64; CALL; } break; \
+    }
+
+__device__ void rsi16_item(const Rsi16Dev &c, const BatchItem &it, uint32_t *ws, bool decode) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const BlockView v = contiguous_view(it.msg, true, c.message_len, it.par, true, c.ecc);
+    for (uint32_t b = warp; b < it.nblocks; b += kBatchWarps) {
+        if (decode)
+            rsi16_repair_block(c, v, b, ws, it.status, lane);
+        else
+            rsi16_encode_block(c, v, b, ws, lane);
+    }
+}
+
+// One CIRC16 codeword (circ16_encode for a single block): the outer code over
+// the interleaved columns into untruncated words, their uint16 copy into the
+// ecc, then the inner code over the message rows and over the outer parity rows.
+__device__ void circ16_enc_item(const BatchCode &c, const BatchItem &it, uint32_t *ws, uint32_t *tmp) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint16_t *ecc = static_cast<uint16_t *>(it.par);
+    const uint32_t I = c.c_rso_interleave;
+    const BlockView vo{it.msg, 0, 1, I, tmp, 0, 1, I, I, true, false};
+    for (uint32_t b = warp; b < I; b += kBatchWarps) rsi16_encode_block(c.rso, vo, b, ws, lane);
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < c.c_rso_ieccl; i += kBatchThreads) ecc[i] = (uint16_t)tmp[i];
+    const BlockView vi{it.msg, 0, c.rsi.message_len, 1, ecc + c.c_rso_ieccl, 0, c.rsi.ecc, 1, c.c_inner_rows,
+                       true, true};
+    for (uint32_t b = warp; b < c.c_inner_rows; b += kBatchWarps) rsi16_encode_block(c.rsi, vi, b, ws, lane);
+    const BlockView vio{tmp, 0, c.rsi.message_len, 1, ecc + c.c_rso_ieccl + c.c_rsi_ieccl, 0, c.rsi.ecc, 1,
+                        c.c_outer_rows, false, true};
+    for (uint32_t b = warp; b < c.c_outer_rows; b += kBatchWarps) rsi16_encode_block(c.rsi, vio, b, ws, lane);
+}
+
+__global__ void __launch_bounds__(kBatchThreads) batch_kernel(BatchArgs a) {
+    extern __shared__ __align__(16) uint32_t sm[];
+    __shared__ uint32_t s_idx;
+    uint8_t *rs_scratch = a.rs_scratch + (size_t)blockIdx.x * kBatchThreads * kDecodeScratchBytes;
+    uint32_t *ctmp = a.circ_tmp + (size_t)blockIdx.x * a.circ_tmp_words;
+    uint32_t *ws = sm + (size_t)(threadIdx.x >> 5) * a.ws_words;
+    for (;;) {
+        __syncthreads();  // every thread has read s_idx and finished the last item
+        if (threadIdx.x == 0) s_idx = atomicAdd(a.counter, 1u);
+        __syncthreads();
+        const uint32_t idx = s_idx;
+        if (idx >= a.nitems) break;
+        const BatchItem it = a.items[idx];
+        const BatchCode &c = a.codes[it.code];
+        switch (it.kind) {
+            case BK_RS256_ENC:
+                FFGPU_BATCH_W(c.W, (rs256_enc_item<w_>(c, it, sm)));
+                break;
+            case BK_RS256_DEC:
+                FFGPU_BATCH_W(c.W, (rs256_dec_item<w_>(c, it, sm, rs_scratch)));
+                break;
+            case BK_RSI16_ENC:
+                rsi16_item(c.rsi, it, ws, false);
+                break;
+            case BK_RSI16_DEC:
+                rsi16_item(c.rsi, it, ws, true);
+                break;
+            case BK_CIRC16_ENC:
+                circ16_enc_item(c, it, ws, ctmp);
+                break;
+            default:
+                break;
+        }
+    }
+}
+
+}  // namespace ffgpu
+
+// ---------------------------------------------------------------- host side
+
+using namespace ffgpu;
+
+struct ffgpu_batch {
+    struct Req {
+        uint8_t kind;
+        const void *handle;
+        void *a, *b;
+        uint8_t *status;
+        size_t nblocks, msg_len;
+    };
+    std::vector<Req> reqs;
+    // plan
+    std::vector<BatchCode> codes;
+    std::vector<const void *> code_keys;
+    std::vector<BatchItem> items;
+    DeviceBuffer d_items, d_codes, d_counter, d_rs_scratch, d_circ_tmp, d_backup;
+    size_t smem = 0, circ_tmp_words = 0;
+    uint32_t ws_words = 0;
+    unsigned grid = 0;
+    int tile_rs = 512, tile_rsi = 8, ctas_per_sm = 0;
+    bool planned = false;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::mutex mu;
+
+    ~ffgpu_batch() { drop_graph(); }
+    void drop_graph() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+    }
+};
+
+namespace {
+
+int sm_count_b() {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 132;
+}
+
+uint32_t code_index(ffgpu_batch &B, const void *key, const BatchCode &bc) {
+    for (size_t i = 0; i < B.code_keys.size(); ++i)
+        if (B.code_keys[i] == key) return (uint32_t)i;
+    B.code_keys.push_back(key);
+    B.codes.push_back(bc);
+    return (uint32_t)(B.codes.size() - 1);
+}
+
+// relative cost of one item, for the longest-first order
+double item_cost(const ffgpu_batch &B, const BatchItem &it) {
+    const BatchCode &c = B.codes[it.code];
+    switch (it.kind) {
+        case BK_RS256_ENC: return (double)it.nblocks * it.msg_len * (1 + c.ecc / 8.0);
+        case BK_RS256_DEC: return (double)it.nblocks * (it.msg_len + c.ecc) * (4 + c.ecc);
+        case BK_RSI16_ENC: return (double)it.nblocks * c.rsi.block_len * 8;
+        case BK_RSI16_DEC: return (double)it.nblocks * c.rsi.block_len * (40 + c.rsi.ecc);
+        default:
+            return ((double)c.c_rso_interleave * c.rso.block_len +
+                    (double)(c.c_inner_rows + c.c_outer_rows) * c.rsi.block_len) * 8;
+    }
+}
+
+void build_plan(ffgpu_batch &B, int tile_rs, int tile_rsi, int ctas_per_sm) {
+    B.drop_graph();
+    B.codes.clear();
+    B.code_keys.clear();
+    B.items.clear();
+    size_t smem = 0;
+    uint32_t ws_words = 0;
+    size_t circ_words = 0;
+    bool any_rs_dec = false;
+    for (const auto &r : B.reqs) {
+        BatchCode bc{};
+        if (r.kind == BK_RS256_ENC || r.kind == BK_RS256_DEC) {
+            const Rs256Code &c = *static_cast<const ffgpu_rs256 *>(r.handle)->code;
+            bc.lut = c.d_lut;
+            bc.exp512 = c.d_exp512;
+            bc.log256 = c.d_log256;
+            bc.W = c.W;
+            bc.ecc = c.ecc;
+            const uint32_t ci = code_index(B, r.handle, bc);
+            for (size_t b0 = 0; b0 < r.nblocks; b0 += (size_t)tile_rs) {
+                BatchItem it{};
+                it.kind = r.kind;
+                it.code = ci;
+                it.nblocks = (uint32_t)std::min<size_t>((size_t)tile_rs, r.nblocks - b0);
+                it.msg_len = (int32_t)r.msg_len;
+                it.msg = static_cast<uint8_t *>(r.a) + b0 * r.msg_len;
+                it.par = static_cast<uint8_t *>(r.b) + b0 * (size_t)c.ecc;
+                it.status = r.status ? r.status + b0 : nullptr;
+                B.items.push_back(it);
+            }
+            if (r.kind == BK_RS256_ENC)
+                smem = std::max(smem, (size_t)256 * c.W * 4 + (size_t)kBatchThreads * r.msg_len);
+            else {
+                smem = std::max(smem, (size_t)256 * c.W * 4 + 768);
+                any_rs_dec = true;
+            }
+        } else if (r.kind == BK_RSI16_ENC || r.kind == BK_RSI16_DEC) {
+            const Rsi16Code &c = *static_cast<const ffgpu_rsi16 *>(r.handle)->code;
+            bc.rsi = c.dev;
+            const uint32_t ci = code_index(B, r.handle, bc);
+            for (size_t b0 = 0; b0 < r.nblocks; b0 += (size_t)tile_rsi) {
+                BatchItem it{};
+                it.kind = r.kind;
+                it.code = ci;
+                it.nblocks = (uint32_t)std::min<size_t>((size_t)tile_rsi, r.nblocks - b0);
+                it.msg = static_cast<uint16_t *>(r.a) + b0 * c.message_len;
+                it.par = static_cast<uint16_t *>(r.b) + b0 * c.ecc;
+                it.status = r.status ? r.status + b0 : nullptr;
+                B.items.push_back(it);
+            }
+            ws_words = std::max(ws_words, r.kind == BK_RSI16_DEC ? c.dev.temp_len + 1 : (uint32_t)c.block_len);
+        } else {
+            const Circ16Code &c = *static_cast<const ffgpu_circ16 *>(r.handle)->code;
+            bc.rsi = c.rsi->dev;
+            bc.rso = c.rso->dev;
+            bc.c_message_len = (uint32_t)c.message_len;
+            bc.c_ecc_len = (uint32_t)c.ecc_len;
+            bc.c_rso_interleave = (uint32_t)c.rso_interleave;
+            bc.c_rso_ieccl = (uint32_t)c.rso_ieccl;
+            bc.c_rsi_ieccl = (uint32_t)c.rsi_ieccl;
+            bc.c_inner_rows = (uint32_t)c.inner_rows;
+            bc.c_outer_rows = (uint32_t)c.outer_rows;
+            const uint32_t ci = code_index(B, r.handle, bc);
+            for (size_t b = 0; b < r.nblocks; ++b) {
+                BatchItem it{};
+                it.kind = r.kind;
+                it.code = ci;
+                it.nblocks = 1;
+                it.msg = static_cast<uint16_t *>(r.a) + b * c.message_len;
+                it.par = static_cast<uint16_t *>(r.b) + b * c.ecc_len;
+                B.items.push_back(it);
+            }
+            ws_words = std::max(ws_words, (uint32_t)std::max(c.rsi->block_len, c.rso->block_len));
+            circ_words = std::max(circ_words, c.rso_ieccl);
+        }
+    }
+    // longest first
+    std::vector<std::pair<double, size_t>> order(B.items.size());
+    for (size_t i = 0; i < B.items.size(); ++i) order[i] = {-item_cost(B, B.items[i]), i};
+    std::stable_sort(order.begin(), order.end());
+    std::vector<BatchItem> sorted(B.items.size());
+    for (size_t i = 0; i < order.size(); ++i) sorted[i] = B.items[order[i].second];
+    B.items.swap(sorted);
+
+    ws_words = (ws_words + 3) & ~3u;
+    B.ws_words = ws_words;
+    B.smem = std::max(smem, (size_t)kBatchWarps * ws_words * 4);
+    FFGPU_REQUIRE(B.smem <= 220 * 1024, "batch needs more shared memory per CTA than the device has");
+    FFGPU_CHECK_CUDA(cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)B.smem));
+    int occ = 0;
+    FFGPU_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel, kBatchThreads, B.smem));
+    occ = std::max(occ, 1);
+    const int per_sm = ctas_per_sm > 0 ? std::min(ctas_per_sm, occ) : occ;
+    B.grid = (unsigned)std::max<size_t>(1, std::min<size_t>((size_t)sm_count_b() * per_sm, B.items.size()));
+    B.tile_rs = tile_rs;
+    B.tile_rsi = tile_rsi;
+    B.ctas_per_sm = per_sm;
+    B.circ_tmp_words = (circ_words + 63) & ~(size_t)63;
+
+    B.d_items.get(std::max<size_t>(1, B.items.size()) * sizeof(BatchItem));
+    B.d_codes.get(std::max<size_t>(1, B.codes.size()) * sizeof(BatchCode));
+    B.d_counter.get(256);
+    if (any_rs_dec) B.d_rs_scratch.get((size_t)B.grid * kBatchThreads * kDecodeScratchBytes);
+    if (B.circ_tmp_words) B.d_circ_tmp.get((size_t)B.grid * B.circ_tmp_words * 4);
+    if (!B.items.empty())
+        FFGPU_CHECK_CUDA(cudaMemcpy(B.d_items.ptr, B.items.data(), B.items.size() * sizeof(BatchItem),
+                                    cudaMemcpyHostToDevice));
+    if (!B.codes.empty())
+        FFGPU_CHECK_CUDA(cudaMemcpy(B.d_codes.ptr, B.codes.data(), B.codes.size() * sizeof(BatchCode),
+                                    cudaMemcpyHostToDevice));
+    B.planned = true;
+}
+
+void launch_plan(ffgpu_batch &B, cudaStream_t st, bool timed) {
+    FFGPU_CHECK_CUDA(cudaMemsetAsync(B.d_counter.ptr, 0, 4, st));
+    BatchArgs a;
+    a.items = static_cast<const BatchItem *>(B.d_items.ptr);
+    a.nitems = (uint32_t)B.items.size();
+    a.codes = static_cast<const BatchCode *>(B.d_codes.ptr);
+    a.counter = static_cast<uint32_t *>(B.d_counter.ptr);
+    a.rs_scratch = static_cast<uint8_t *>(B.d_rs_scratch.ptr);
+    a.circ_tmp = static_cast<uint32_t *>(B.d_circ_tmp.ptr);
+    a.circ_tmp_words = B.circ_tmp_words;
+    a.ws_words = B.ws_words;
+    if (timed) {
+        KernelTimer kt_timer("batch_kernel", st);
+        batch_kernel<<<B.grid, kBatchThreads, B.smem, st>>>(a);
+        check_launch("batch_kernel");
+    } else {
+        batch_kernel<<<B.grid, kBatchThreads, B.smem, st>>>(a);
+        check_launch("batch_kernel");
+    }
+}
+
+// decode requests are repaired in place: save / restore them around trials
+struct Region {
+    void *p;
+    size_t n;
+};
+
+std::vector<Region> decode_regions(const ffgpu_batch &B) {
+    std::vector<Region> v;
+    for (const auto &r : B.reqs) {
+        if (r.kind == BK_RS256_DEC) {
+            const Rs256Code &c = *static_cast<const ffgpu_rs256 *>(r.handle)->code;
+            v.push_back({r.a, r.nblocks * r.msg_len});
+            v.push_back({r.b, r.nblocks * (size_t)c.ecc});
+        } else if (r.kind == BK_RSI16_DEC) {
+            const Rsi16Code &c = *static_cast<const ffgpu_rsi16 *>(r.handle)->code;
+            v.push_back({r.a, r.nblocks * c.message_len * 2});
+            v.push_back({r.b, r.nblocks * c.ecc * 2});
+        }
+    }
+    return v;
+}
+
+void copy_regions(ffgpu_batch &B, const std::vector<Region> &rs, bool save, cudaStream_t st) {
+    uint8_t *bk = static_cast<uint8_t *>(B.d_backup.ptr);
+    size_t off = 0;
+    for (const auto &r : rs) {
+        if (save)
+            FFGPU_CHECK_CUDA(cudaMemcpyAsync(bk + off, r.p, r.n, cudaMemcpyDeviceToDevice, st));
+        else
+            FFGPU_CHECK_CUDA(cudaMemcpyAsync(r.p, bk + off, r.n, cudaMemcpyDeviceToDevice, st));
+        off += r.n;
+    }
+}
+
+void autotune(ffgpu_batch &B, cudaStream_t st) {
+    const auto regions = decode_regions(B);
+    size_t total = 0;
+    for (const auto &r : regions) total += r.n;
+    if (total) B.d_backup.get(total);
+    copy_regions(B, regions, true, st);
+    cudaEvent_t e0, e1;
+    FFGPU_CHECK_CUDA(cudaEventCreate(&e0));
+    FFGPU_CHECK_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int bt_rs = 512, bt_rsi = 8, bt_cta = 0;
+    const int tiles_rs[] = {128, 512, 2048};
+    const int tiles_rsi[] = {2, 8, 32};
+    const int ctas[] = {1, 2, 0};
+    for (int trs : tiles_rs)
+        for (int tri : tiles_rsi)
+            for (int cps : ctas) {
+                build_plan(B, trs, tri, cps);
+                float ms = 0.f;
+                for (int rep = 0; rep < 2; ++rep) {  // the first run warms up
+                    copy_regions(B, regions, false, st);
+                    FFGPU_CHECK_CUDA(cudaEventRecord(e0, st));
+                    launch_plan(B, st, false);
+                    FFGPU_CHECK_CUDA(cudaEventRecord(e1, st));
+                    FFGPU_CHECK_CUDA(cudaEventSynchronize(e1));
+                    FFGPU_CHECK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                }
+                if (ms < best) {
+                    best = ms;
+                    bt_rs = trs;
+                    bt_rsi = tri;
+                    bt_cta = cps;
+                }
+            }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    copy_regions(B, regions, false, st);
+    FFGPU_CHECK_CUDA(cudaStreamSynchronize(st));
+    build_plan(B, bt_rs, bt_rsi, bt_cta);
+}
+
+}  // namespace
+
+extern "C" {
+
+int ffgpu_batch_create(ffgpu_batch **out) {
+    return guarded([&] {
+        FFGPU_REQUIRE(out, "out is NULL");
+        *out = new ffgpu_batch();
+    });
+}
+
+int ffgpu_batch_destroy(ffgpu_batch *b) {
+    return guarded([&] { delete b; });
+}
+
+int ffgpu_batch_clear(ffgpu_batch *b) {
+    return guarded([&] {
+        FFGPU_REQUIRE(b, "batch is NULL");
+        std::lock_guard<std::mutex> lk(b->mu);
+        b->reqs.clear();
+        b->planned = false;
+        b->drop_graph();
+    });
+}
+
+int ffgpu_batch_add_rs256(ffgpu_batch *b, const ffgpu_rs256 *code, int op, uint8_t *data, uint8_t *parity,
+                          size_t nblocks, size_t message_len, uint8_t *status) {
+    return guarded([&] {
+        FFGPU_REQUIRE(b && code, "batch or code is NULL");
+        FFGPU_REQUIRE(op == FFGPU_OP_ENCODE || op == FFGPU_OP_DECODE, "op must be FFGPU_OP_ENCODE or FFGPU_OP_DECODE");
+        const Rs256Code &c = *code->code;
+        FFGPU_REQUIRE(message_len >= 1 && message_len + (size_t)c.ecc <= 255,
+                      "message_len + ecc_len must be in [ecc_len + 1, 255]");
+        FFGPU_REQUIRE(op == FFGPU_OP_ENCODE || status, "decode needs a status array");
+        std::lock_guard<std::mutex> lk(b->mu);
+        b->reqs.push_back({op == FFGPU_OP_ENCODE ? BK_RS256_ENC : BK_RS256_DEC, code, data, parity, status, nblocks,
+                           message_len});
+        b->planned = false;
+    });
+}
+
+int ffgpu_batch_add_rsi16(ffgpu_batch *b, const ffgpu_rsi16 *code, int op, uint16_t *msg, uint16_t *parity,
+                          size_t nblocks, uint8_t *status) {
+    return guarded([&] {
+        FFGPU_REQUIRE(b && code, "batch or code is NULL");
+        FFGPU_REQUIRE(op == FFGPU_OP_ENCODE || op == FFGPU_OP_DECODE, "op must be FFGPU_OP_ENCODE or FFGPU_OP_DECODE");
+        FFGPU_REQUIRE(op == FFGPU_OP_ENCODE || status, "decode needs a status array");
+        std::lock_guard<std::mutex> lk(b->mu);
+        b->reqs.push_back({op == FFGPU_OP_ENCODE ? BK_RSI16_ENC : BK_RSI16_DEC, code, msg, parity, status, nblocks, 0});
+        b->planned = false;
+    });
+}
+
+int ffgpu_batch_add_circ16(ffgpu_batch *b, const ffgpu_circ16 *code, int op, uint16_t *msg, uint16_t *ecc,
+                           size_t nblocks) {
+    return guarded([&] {
+        FFGPU_REQUIRE(b && code, "batch or code is NULL");
+        FFGPU_REQUIRE(op == FFGPU_OP_ENCODE, "CIRC16 batches take encode requests");
+        std::lock_guard<std::mutex> lk(b->mu);
+        b->reqs.push_back({BK_CIRC16_ENC, code, msg, ecc, nullptr, nblocks, 0});
+        b->planned = false;
+    });
+}
+
+int ffgpu_batch_plan(ffgpu_batch *b, int autotune_on, void *stream) {
+    return guarded([&] {
+        FFGPU_REQUIRE(b, "batch is NULL");
+        std::lock_guard<std::mutex> lk(b->mu);
+        cudaStream_t st = (cudaStream_t)stream;
+        // the work list is rewritten: no launch of this batch may be in flight
+        FFGPU_CHECK_CUDA(cudaStreamSynchronize(st));
+        if (autotune_on)
+            autotune(*b, st);
+        else
+            build_plan(*b, b->tile_rs, b->tile_rsi, b->ctas_per_sm);
+    });
+}
+
+int ffgpu_batch_capture(ffgpu_batch *b, void *stream) {
+    return guarded([&] {
+        FFGPU_REQUIRE(b, "batch is NULL");
+        std::lock_guard<std::mutex> lk(b->mu);
+        if (!b->planned) build_plan(*b, b->tile_rs, b->tile_rsi, b->ctas_per_sm);
+        b->drop_graph();
+        cudaStream_t st = (cudaStream_t)stream;
+        cudaStream_t cap = st;
+        bool own = false;
+        if (!cap) {  // the legacy default stream cannot be captured
+            FFGPU_CHECK_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+            own = true;
+        }
+        FFGPU_CHECK_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+        try {
+            launch_plan(*b, cap, false);
+        } catch (...) {
+            cudaGraph_t g = nullptr;
+            cudaStreamEndCapture(cap, &g);
+            if (g) cudaGraphDestroy(g);
+            if (own) cudaStreamDestroy(cap);
+            throw;
+        }
+        FFGPU_CHECK_CUDA(cudaStreamEndCapture(cap, &b->graph));
+        if (own) cudaStreamDestroy(cap);
+        FFGPU_CHECK_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
+    });
+}
+
+int ffgpu_batch_launch(ffgpu_batch *b, void *stream) {
+    return guarded([&] {
+        FFGPU_REQUIRE(b, "batch is NULL");
+        std::lock_guard<std::mutex> lk(b->mu);
+        cudaStream_t st = (cudaStream_t)stream;
+        if (b->exec) {
+            KernelTimer kt_timer("batch_kernel", st);
+            FFGPU_CHECK_CUDA(cudaGraphLaunch(b->exec, st));
+            launched();
+            return;
+        }
+        if (!b->planned) build_plan(*b, b->tile_rs, b->tile_rsi, b->ctas_per_sm);
+        launch_plan(*b, st, true);
+    });
+}
+
+int ffgpu_batch_info(const ffgpu_batch *b, int *tile_rs256, int *tile_rsi16, int *ctas_per_sm, size_t *items,
+                     unsigned *grid) {
+    return guarded([&] {
+        FFGPU_REQUIRE(b, "batch is NULL");
+        if (tile_rs256) *tile_rs256 = b->tile_rs;
+        if (tile_rsi16) *tile_rsi16 = b->tile_rsi;
+        if (ctas_per_sm) *ctas_per_sm = b->ctas_per_sm;
+        if (items) *items = b->items.size();
+        if (grid) *grid = b->grid;
+    });
+}
+
+}  // extern "C"

@@ -8,14 +8,10 @@
 
 #include "circ16.cuh"
 #include "common.cuh"
+#include "handles.h"
 
 using namespace ffgpu;
 
-struct ffgpu_circ16 {
-    std::unique_ptr<Circ16Code> code;
-    std::mutex mu;
-    DeviceBuffer d_msg, d_ecc;
-};
 
 // NULL is the CUDA default stream, as everywhere in the CUDA runtime
 static cudaStream_t pick(void *stream) { return (cudaStream_t)stream; }

@@ -10,6 +10,7 @@
 #include <algorithm>
 
 #include "common.cuh"
+#include "handles.h"
 #include "rs256.cuh"
 
 namespace ffgpu {
@@ -64,11 +65,6 @@ void timing_push(const char *name, cudaEvent_t start, cudaEvent_t stop) {
 
 using namespace ffgpu;
 
-struct ffgpu_rs256 {
-    std::unique_ptr<Rs256Code> code;
-    std::mutex mu;
-    DeviceBuffer d_data, d_parity, d_status;
-};
 
 extern "C" {
 

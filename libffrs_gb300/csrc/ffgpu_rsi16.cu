@@ -8,15 +8,11 @@
 #include <vector>
 
 #include "common.cuh"
+#include "handles.h"
 #include "rsi16.cuh"
 
 using namespace ffgpu;
 
-struct ffgpu_rsi16 {
-    std::unique_ptr<Rsi16Code> code;
-    std::mutex mu;
-    DeviceBuffer d_msg, d_par, d_status, d_pos;
-};
 
 // NULL is the CUDA default stream, as everywhere in the CUDA runtime
 static cudaStream_t pick(void *stream) { return (cudaStream_t)stream; }

@@ -70,10 +70,10 @@ struct BlockView {
     }
 };
 
-inline BlockView contiguous_view(void *msg, bool msg16, size_t message_len, void *par, bool par16, size_t ecc) {
+__host__ __device__ inline BlockView contiguous_view(void *msg, bool msg16, size_t message_len, void *par, bool par16, size_t ecc) {
     return BlockView{msg, message_len, 0, 1, par, ecc, 0, 1, 1, msg16, par16};
 }
-inline BlockView interleaved_view(void *msg, bool msg16, size_t message_len, void *par, bool par16, size_t ecc,
+__host__ __device__ inline BlockView interleaved_view(void *msg, bool msg16, size_t message_len, void *par, bool par16, size_t ecc,
                                   size_t interleave) {
     return BlockView{msg, message_len * interleave, 1, interleave, par, ecc * interleave, 1, interleave,
                      interleave, msg16, par16};

@@ -1,0 +1,569 @@
+// RSi16 device code shared by the standalone kernels (rsi16.cu), the CIRC16
+// pipeline and the fused batch kernel: GF(65537) arithmetic, warp-wide NTTs
+// and the polynomial steps of the reference's W = 1 code path, block I/O
+// through a BlockView, and the one-block routines a warp runs (encode,
+// syndromes, unknown- and known-location repair).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "../../include/ffgpu.h"
+#include "rsi16.cuh"
+
+namespace ffgpu {
+
+// ---------------------------------------------------------------- field ops
+
+// GF(65537) on canonical values in [0, 65536] (libffrs/galois.hpp:258-346)
+static __device__ __forceinline__ uint32_t fmul(uint32_t a, uint32_t b) {
+    uint32_t r = a * b;
+    if (r == 0 && a && b) return 1u;  // 65536 * 65536 = 2^32 = 1 (mod p)
+    r = (r & 0xffffu) - (r >> 16);
+    return ((int32_t)r < 0) ? r + 0x10001u : r;
+}
+static __device__ __forceinline__ uint32_t fadd(uint32_t a, uint32_t b) {
+    uint32_t r = a + b;
+    return r >= 0x10001u ? r - 0x10001u : r;
+}
+static __device__ __forceinline__ uint32_t fsub(uint32_t a, uint32_t b) {
+    uint32_t r = a - b;
+    return ((int32_t)r < 0) ? r + 0x10001u : r;
+}
+static __device__ __forceinline__ uint32_t fneg(uint32_t a) { return a ? 0x10001u - a : 0u; }
+// Inverse by Fermat (a^65535) with the reference table's inv(0) == 1
+// (galois.hpp:98-101: _exp[65536 - _log[0]] == _exp[65536] == 1).
+static __device__ __forceinline__ uint32_t finv(uint32_t a) {
+    if (a == 0) return 1u;
+    uint32_t t = a;                                // a^1
+    uint32_t u = fmul(fmul(t, t), t);              // a^3
+    uint32_t v = u;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) v = fmul(v, v);
+    v = fmul(v, u);                                // a^15
+    uint32_t w = v;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) w = fmul(w, w);
+    w = fmul(w, v);                                // a^255
+    uint32_t z = w;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) z = fmul(z, z);
+    return fmul(z, w);                             // a^65535
+}
+// div(a, b) == a * inv(b), div(0, b) == 0, div(a, 0) == a (galois.hpp:187-196)
+static __device__ __forceinline__ uint32_t fdiv(uint32_t a, uint32_t b) { return a ? fmul(a, finv(b)) : 0u; }
+
+// ---------------------------------------------------------------- warp NTTs
+
+// ct_butterfly (libffrs/ntt.hpp:225-249): RBO input, normal order output
+static __device__ void w_ct(const uint32_t *__restrict__ roots, uint32_t *x, uint32_t n, int lane) {
+    for (uint32_t stride = 1, ef = n >> 1; stride < n; stride <<= 1, ef >>= 1) {
+        for (uint32_t b = lane; b < (n >> 1); b += 32) {
+            const uint32_t i = b & (stride - 1);
+            const uint32_t j = ((b - i) << 1) + i;
+            const uint32_t a = x[j], bb = x[j + stride];
+            const uint32_t m = i ? fmul(bb, roots[ef * i]) : bb;
+            x[j] = fadd(a, m);
+            x[j + stride] = fsub(a, m);
+        }
+        __syncwarp();
+    }
+}
+
+// gs_butterfly (libffrs/ntt.hpp:280-302): normal order input, RBO output
+static __device__ void w_gs(const uint32_t *__restrict__ roots, uint32_t *x, uint32_t n, int lane) {
+    for (uint32_t stride = n >> 1, ef = 0; stride > 0; stride >>= 1, ++ef) {
+        for (uint32_t b = lane; b < (n >> 1); b += 32) {
+            const uint32_t i = b & (stride - 1);
+            const uint32_t j = ((b - i) << 1) + i;
+            const uint32_t a = x[j], bb = x[j + stride];
+            x[j] = fadd(a, bb);
+            const uint32_t d = fsub(a, bb);
+            x[j + stride] = i ? fmul(d, roots[i << ef]) : d;
+        }
+        __syncwarp();
+    }
+}
+
+static __device__ __forceinline__ void w_nttr(const Rsi16Dev &c, uint32_t *x, int lane) { w_gs(c.roots_ecc, x, c.ecc, lane); }
+static __device__ __forceinline__ void w_inttr(const Rsi16Dev &c, uint32_t *x, int lane) {
+    w_ct(c.roots_i_ecc, x, c.ecc, lane);
+    for (uint32_t k = lane; k < c.ecc; k += 32) x[k] = fmul(x[k], c.ecc_len_i);
+    __syncwarp();
+}
+
+// NTT::pntt (libffrs/ntt.hpp:133-152) over nchunks chunks, in place; the
+// result is x[0 .. ecc).  nchunks == 0 still transforms chunk 0, as the
+// reference's pntt_message does when block_len == ecc_len.
+static __device__ void w_pntt(const Rsi16Dev &c, uint32_t *x, uint32_t nchunks, int lane) {
+    const uint32_t ecc = c.ecc;
+    w_ct(c.roots_ecc, x, ecc, lane);
+    for (uint32_t k = lane; k < ecc; k += 32) x[k] = fmul(x[k], c.pntt_shift[k]);
+    __syncwarp();
+    for (uint32_t ch = 1; ch < nchunks; ++ch) {
+        uint32_t *p = x + (size_t)ch * ecc;
+        w_ct(c.roots_ecc, p, ecc, lane);
+        for (uint32_t k = lane; k < ecc; k += 32) {
+            const uint32_t v = fmul(p[k], c.pntt_shift[(size_t)ch * ecc + k]);
+            p[k] = v;
+            x[k] = fadd(x[k], v);
+        }
+        __syncwarp();
+    }
+}
+
+// RSi16v::_mix_ecc (libffrs/rsi16v_impl.hpp:100-119)
+static __device__ void w_mix(const Rsi16Dev &c, uint32_t *x, int lane) {
+    for (uint32_t k = lane; k < c.ecc; k += 32) x[k] = fmul(x[k], c.ecc_mix[k]);
+    __syncwarp();
+    w_gs(c.roots_i_ecc, x, c.ecc, lane);
+}
+
+// NTT::pintt_ecc (libffrs/ntt.hpp:206-220)
+static __device__ void w_pintt(const Rsi16Dev &c, uint32_t *b, int lane) {
+    const uint32_t ecc = c.ecc, nch = c.block_len / ecc;
+    for (uint32_t i = 1; i < nch; ++i) {
+        uint32_t *p = b + (size_t)i * ecc;
+        for (uint32_t k = lane; k < ecc; k += 32) p[k] = fmul(b[k], c.pintt_shift[(size_t)i * ecc + k]);
+        __syncwarp();
+        w_gs(c.roots_i_ecc, p, ecc, lane);
+    }
+    for (uint32_t k = lane; k < ecc; k += 32) b[k] = fmul(b[k], c.pintt_shift[k]);
+    __syncwarp();
+    w_gs(c.roots_i_ecc, b, ecc, lane);
+}
+
+// vec::poly::len for W = 1 (libffrs/simd.hpp:339-361): index of the last
+// non-zero word in r[0 .. n), plus one
+static __device__ uint32_t w_poly_len(const uint32_t *r, uint32_t n, int lane) {
+    uint32_t best = 0;
+    for (uint32_t k = lane; k < n; k += 32)
+        if (r[k]) best = k + 1;
+    return __reduce_max_sync(0xffffffffu, best);
+}
+
+static __device__ __forceinline__ bool w_all_zero(const uint32_t *r, uint32_t n, int lane) {
+    bool nz = false;
+    for (uint32_t k = lane; k < n; k += 32) nz |= (r[k] != 0);
+    return !__any_sync(0xffffffffu, nz);
+}
+
+static __device__ __forceinline__ void w_copy(uint32_t *dst, const uint32_t *src, uint32_t n, int lane) {
+    for (uint32_t k = lane; k < n; k += 32) dst[k] = src[k];
+    __syncwarp();
+}
+static __device__ __forceinline__ void w_fill(uint32_t *dst, uint32_t v, uint32_t n, int lane) {
+    for (uint32_t k = lane; k < n; k += 32) dst[k] = v;
+    __syncwarp();
+}
+
+// in-scratch guard: a length that would make the reference run past its
+// scratch buffer is reported as an assertion instead of being executed
+struct Scratch {
+    uint32_t *base;
+    uint32_t size;
+    __device__ bool ok(const uint32_t *p, uint32_t n) const {
+        return p >= base && (uint64_t)(p - base) + n <= size;
+    }
+};
+
+enum { ST_OK = 0, ST_ASSERT = -1 };
+
+// NTT::_reverse_ntt_vec (libffrs/ntt.hpp:343-354).  Index i pairs with
+// k = rbo_ecc[ecc - rbo_ecc[i]] (an involution on [1, ecc)); the sequential
+// loop swaps each pair once at the smaller index and then scales every index
+// by its own twiddles, so each pair is handled by one lane here.
+static __device__ __forceinline__ uint32_t rev_scale(const Rsi16Dev &c, uint32_t i, uint32_t shift) {
+    const uint32_t j = c.rbo_ecc[i];
+    return fmul(c.roots_i_ecc[j], c.roots_ecc[(shift * j) & c.ecc_mask]);
+}
+static __device__ void w_reverse_ntt_vec(const Rsi16Dev &c, uint32_t *v, uint32_t shift, int lane) {
+    const uint32_t ecc = c.ecc;
+    for (uint32_t i = 1 + lane; i < ecc; i += 32) {
+        const uint32_t k = c.rbo_ecc[ecc - c.rbo_ecc[i]];
+        if (k < i) continue;
+        if (k == i) {
+            v[i] = fmul(v[i], rev_scale(c, i, shift));
+        } else {
+            const uint32_t vi = v[i], vk = v[k];
+            v[i] = fmul(vk, rev_scale(c, i, shift));
+            v[k] = fmul(vi, rev_scale(c, k, shift));
+        }
+    }
+    __syncwarp();
+}
+
+// NTT::poly_inv_mod_xn_rev (libffrs/ntt.hpp:363-469), W = 1
+static __device__ int w_poly_inv(const Rsi16Dev &c, const Scratch &s, uint32_t *g, uint32_t g_len, uint32_t g0,
+                          uint32_t a_len, uint32_t *a, int lane) {
+    const uint32_t ecc = c.ecc;
+    const uint32_t a0 = finv(g0);
+    w_fill(a, a0, ecc, lane);
+    uint32_t l = 2;
+    const uint32_t a_max = a_len;
+    while (l < a_len) {
+        if (g_len + l - 2 > ecc) return ST_ASSERT;
+        for (uint32_t k = lane; k < ecc; k += 32) {
+            const uint32_t ai = a[k];
+            a[k] = fmul(ai, fsub(2, fmul(ai, g[k])));
+        }
+        __syncwarp();
+        w_inttr(c, a, lane);
+        if (l > ecc) return ST_ASSERT;
+        for (uint32_t k = l + lane; k < ecc; k += 32) a[k] = 0;
+        __syncwarp();
+        w_nttr(c, a, lane);
+        l *= 2;
+    }
+    for (uint32_t k = lane; k < ecc; k += 32) {
+        const uint32_t ai = a[k];
+        g[k] = fmul(ai, fsub(2, fmul(ai, g[k])));
+    }
+    __syncwarp();
+    w_inttr(c, a, lane);
+    w_inttr(c, g, lane);
+    w_copy(a, g, ecc, lane);
+    if (l > ecc) return ST_ASSERT;
+    for (uint32_t k = l + lane; k < ecc; k += 32) a[k] = 0;
+    __syncwarp();
+    if (!s.ok(a, a_max)) return ST_ASSERT;
+    // std::reverse(&a[0], &a[a_max])
+    {
+        const uint32_t half = a_max / 2;
+        for (uint32_t k = lane; k < half; k += 32) {
+            const uint32_t x = a[k], y = a[a_max - 1 - k];
+            a[k] = y;
+            a[a_max - 1 - k] = x;
+        }
+        __syncwarp();
+    }
+    if (a_len > ecc) return ST_ASSERT;
+    for (uint32_t k = a_len + lane; k < ecc; k += 32) a[k] = 0;
+    __syncwarp();
+    w_nttr(c, a, lane);
+    return ST_OK;
+}
+
+// NTT::poly_div_ntt (libffrs/ntt.hpp:471-564), W = 1
+static __device__ int w_poly_div(const Rsi16Dev &c, const Scratch &s, const uint32_t *f, uint32_t f_len, const uint32_t *g,
+                          uint32_t g_len, uint32_t f0, uint32_t g0, uint32_t *t, uint32_t *q, uint32_t *q_len_out,
+                          int lane) {
+    const uint32_t ecc = c.ecc;
+    const uint32_t q_len = f_len - g_len + 1;
+    if (!(g_len > 0)) return ST_ASSERT;
+    if (f_len < g_len) {
+        w_fill(q, 0, ecc, lane);
+        *q_len_out = 0;
+        return ST_OK;
+    }
+    w_copy(t, g, ecc, lane);
+    w_reverse_ntt_vec(c, t, g_len, lane);
+    int st = w_poly_inv(c, s, t, g_len, g0, q_len, q, lane);
+    if (st) return st;
+    for (uint32_t k = lane; k < ecc; k += 32) t[k] = fmul(fsub(f[k], f0), q[k]);
+    __syncwarp();
+    w_inttr(c, t, lane);
+    const uint32_t right_n = min(q_len, ecc - g_len);
+    if (!s.ok(t + g_len, right_n) || !s.ok(q, right_n)) return ST_ASSERT;
+    if (!s.ok(t, q_len - right_n) || !s.ok(q + right_n, q_len - right_n)) return ST_ASSERT;
+    // std::copy_n(&t[g_len], right_n, &q[0]); std::copy_n(&t[0], q_len - right_n, &q[right_n])
+    if (q_len <= ecc) {  // q and t are disjoint ecc-word arrays
+        for (uint32_t k = lane; k < q_len; k += 32) q[k] = (k < right_n) ? t[g_len + k] : t[k - right_n];
+        __syncwarp();
+    } else {  // overlapping copies: keep the reference's sequential order
+        if (lane == 0) {
+            for (uint32_t k = 0; k < right_n; ++k) q[k] = t[g_len + k];
+            for (uint32_t k = 0; k < q_len - right_n; ++k) q[right_n + k] = t[k];
+        }
+        __syncwarp();
+    }
+    if (q_len > ecc && !s.ok(q, q_len)) return ST_ASSERT;
+    for (uint32_t k = q_len + lane; k < ecc; k += 32) q[k] = 0;
+    __syncwarp();
+    w_nttr(c, q, lane);
+    *q_len_out = q_len;
+    return ST_OK;
+}
+
+// RSi16v::_sugiyama (libffrs/rsi16v_impl.hpp:271-440), W = 1.  a1 = ws + ecc,
+// r1 = ws (the syndromes), temp4 = ws + 2 ecc, as in _repair.
+static __device__ int w_sugiyama(const Rsi16Dev &c, const Scratch &s, uint32_t *a1, uint32_t *r1, uint32_t *temp4,
+                          uint32_t *a1_len_out, int lane) {
+    const uint32_t ecc = c.ecc, mask = c.ecc_mask;
+    w_fill(temp4, 0, 4 * ecc, lane);
+    w_fill(a1, 0, ecc, lane);
+    uint32_t a1_len;
+    uint32_t q_len = 0, t_len = 0;
+    uint32_t *q = temp4, *t = temp4 + ecc, *a2 = temp4 + 2 * ecc, *r2 = temp4 + 3 * ecc;
+    uint32_t a2_len = 1;
+    w_fill(a2, 1, ecc, lane);
+    uint32_t r1_len = w_poly_len(r1, ecc, lane);
+    w_copy(r2, r1, ecc, lane);
+    uint32_t r2_len = r1_len;
+    uint32_t r2l = r2[0];
+    const uint32_t lanes = (r1_len != 0) ? 0xffffffffu : 0u;
+    {
+        const uint32_t r1h = r1[(r1_len - 1) & mask];
+        const uint32_t r1h2 = r1[(uint32_t)(r1_len - 2) & mask];
+        const uint32_t a11 = fneg(finv(r1h));
+        const uint32_t a10 = fmul(r1h2, fmul(a11, a11));
+        __syncwarp();
+        if (lane == 0) {
+            a1[1] = a11;
+            a1[0] = a10;
+        }
+        a1_len = 2 & lanes;
+        // r1[i] = a10 * r1[i] (all i), then r1[i] += a11 * r2[i-1] (i >= 1);
+        // r2 still holds the original r1, so both updates fuse
+        for (uint32_t k = lane; k < ecc; k += 32) {
+            uint32_t v = fmul(a10, r1[k]);
+            if (k >= 1) v = fadd(v, fmul(a11, r2[k - 1]));
+            r1[k] = v;
+        }
+        __syncwarp();
+        r1_len = w_poly_len(r1, ecc - 1, lane) & lanes;
+        for (uint32_t k = r1_len + lane; k < ecc; k += 32) r1[k] = 0;
+        __syncwarp();
+        w_nttr(c, a1, lane);
+        w_nttr(c, r2, lane);
+    }
+    uint32_t cond = (r1_len >= ecc / 2) ? 0xffffffffu : 0u;
+    if (cond) {
+        for (uint32_t it = 1; it < ecc / 2; ++it) {
+            const uint32_t r1h = r1[(r1_len - 1) & mask];
+            const uint32_t r1l = r1[0];
+            __syncwarp();
+            w_nttr(c, r1, lane);
+            int st = w_poly_div(c, s, r2, r2_len & cond, r1, r1_len, r2l, r1h, t, q, &q_len, lane);
+            if (st) return st;
+            // t = q * a1; q = q * r1; t = a2 - t; q = r2 - q  (pointwise, fused)
+            for (uint32_t k = lane; k < ecc; k += 32) {
+                const uint32_t qk = q[k];
+                t[k] = fsub(a2[k], fmul(qk, a1[k]));
+                q[k] = fsub(r2[k], fmul(qk, r1[k]));
+            }
+            __syncwarp();
+            t_len = q_len + a1_len - 1;
+            t_len = a2_len > t_len ? a2_len : t_len;
+            uint32_t ql = q_len + r1_len - 1;
+            q_len = r2_len > ql ? r2_len : ql;
+            w_copy(a2, a1, ecc, lane);
+            a2_len = a1_len;
+            w_copy(r2, r1, ecc, lane);
+            r2_len = r1_len;
+            r2l = r1l;
+            cond = (r1_len >= ecc / 2) ? 0xffffffffu : 0u;
+            if (!cond) {
+                w_inttr(c, r1, lane);
+                break;
+            }
+            w_copy(a1, t, ecc, lane);
+            w_copy(r1, q, ecc, lane);
+            a1_len = t_len;
+            r1_len = q_len;
+            w_inttr(c, r1, lane);
+            if (!s.ok(r1, r1_len & cond)) return ST_ASSERT;
+            r1_len = w_poly_len(r1, r1_len & cond, lane);
+        }
+    }
+    w_inttr(c, a1, lane);
+    if (!s.ok(a1, a1_len & lanes)) return ST_ASSERT;
+    a1_len = w_poly_len(a1, a1_len & lanes, lane);
+    const uint32_t a10i = finv(a1[0]);
+    __syncwarp();
+    for (uint32_t k = lane; k < ecc; k += 32) {
+        a1[k] = fmul(a1[k], a10i);
+        r1[k] = fmul(r1[k], a10i);
+    }
+    __syncwarp();
+    *a1_len_out = a1_len & lanes;
+    return ST_OK;
+}
+
+static __device__ __forceinline__ uint32_t eval_poly(const uint32_t *r, uint32_t n, uint32_t x) {
+    uint32_t sum = 0;
+    for (uint32_t i = n; i-- > 0;) sum = fadd(fmul(sum, x), r[i]);
+    return sum;
+}
+
+// ---------------------------------------------------------------- block I/O
+
+static __device__ __forceinline__ uint32_t ld_word(const void *base, bool w16, size_t idx) {
+    return w16 ? (uint32_t)((const uint16_t *)base)[idx] : ((const uint32_t *)base)[idx];
+}
+static __device__ __forceinline__ void st_word(void *base, bool w16, size_t idx, uint32_t v) {
+    if (w16)
+        ((uint16_t *)base)[idx] = (uint16_t)v;
+    else
+        ((uint32_t *)base)[idx] = v;
+}
+
+// block b -> ws[0 .. block_len): message words then parity words (or zeros)
+static __device__ void w_gather(const Rsi16Dev &c, const BlockView &v, size_t b, uint32_t *ws, bool with_parity, int lane) {
+    for (uint32_t k = lane; k < c.message_len; k += 32)
+        ws[k] = ld_word(v.msg, v.msg16, v.moff(b, k));
+    for (uint32_t k = lane; k < c.ecc; k += 32)
+        ws[c.message_len + k] = with_parity ? ld_word(v.par, v.par16, v.poff(b, k)) : 0u;
+    __syncwarp();
+}
+
+static __device__ __forceinline__ void put_pos(const Rsi16Dev &c, const BlockView &v, size_t b, uint32_t pos, uint32_t val) {
+    if (pos < c.message_len)
+        st_word(v.msg, v.msg16, v.moff(b, pos), val);
+    else
+        st_word(v.par, v.par16, v.poff(b, pos - c.message_len), val);
+}
+static __device__ __forceinline__ uint32_t get_pos(const Rsi16Dev &c, const BlockView &v, size_t b, uint32_t pos) {
+    if (pos < c.message_len) return ld_word(v.msg, v.msg16, v.moff(b, pos));
+    return ld_word(v.par, v.par16, v.poff(b, pos - c.message_len));
+}
+
+// ---------------------------------------------------------------- one block per warp
+
+// parity of block b (ws: block_len words)
+static __device__ __forceinline__ void rsi16_encode_block(const Rsi16Dev &c, const BlockView &v, size_t b, uint32_t *ws,
+                                                   int lane) {
+    w_gather(c, v, b, ws, false, lane);
+    w_pntt(c, ws, c.pntt_blocks - 1, lane);
+    w_mix(c, ws, lane);
+    for (uint32_t k = lane; k < c.ecc; k += 32) st_word(v.par, v.par16, v.poff(b, k), ws[k]);
+    __syncwarp();
+}
+
+// RSi16v::_repair, unknown locations (rsi16v_impl.hpp:122-168) with
+// _find_roots_ntt (:443-497) and _forney (:500-512); temp: temp_len + 1 words
+static __device__ __noinline__ void rsi16_repair_block(const Rsi16Dev &c, const BlockView &v, size_t b, uint32_t *temp,
+                                                uint8_t *status, int lane) {
+    const uint32_t ecc = c.ecc;
+    Scratch s{temp, c.temp_len};
+
+    w_gather(c, v, b, temp, true, lane);
+    w_pntt(c, temp, c.pntt_blocks, lane);
+    if (w_all_zero(temp, ecc, lane)) {
+        if (lane == 0) status[b] = FFGPU_NO_ERRORS;
+        return;
+    }
+    uint32_t *evaluator = temp, *locator = temp + ecc;
+    uint32_t loc_len = 0;
+    int st = w_sugiyama(c, s, locator, evaluator, temp + 2 * ecc, &loc_len, lane);
+    if (st || loc_len > ecc) {
+        if (lane == 0) status[b] = FFGPU_STATUS_ASSERT;
+        __syncwarp();
+        return;
+    }
+    const uint32_t ev_len = ecc - loc_len + 1;
+    uint32_t *deriv = temp + 2 * ecc;
+    // _deriv (rsi16v_impl.hpp:608-616)
+    for (uint32_t k = lane; k < ecc; k += 32) deriv[k] = (k + 1 < ecc) ? fmul(locator[k + 1], k + 1) : 0u;
+    __syncwarp();
+    const uint32_t deriv_len = w_poly_len(deriv, ecc, lane);
+    uint32_t *roots = temp + 3 * ecc;
+    for (uint32_t k = lane; k < c.ntt_len; k += 32) roots[k] = (k < ecc) ? locator[k] : 0u;
+    __syncwarp();
+    w_pintt(c, roots, lane);
+    const bool lanes = loc_len != 0;
+    const uint32_t dl = lanes ? deriv_len : 0u, el = lanes ? ev_len : 0u;
+    uint32_t count = 0;
+    for (uint32_t i0 = 0; i0 < c.block_len; i0 += 32) {
+        const uint32_t i = i0 + lane;
+        const bool hit = lanes && i < c.block_len && roots[i] == 0;
+        count += __popc(__ballot_sync(0xffffffffu, hit));
+    }
+    // second pass: apply corrections (kept separate so the count is final first)
+    for (uint32_t i = lane; i < c.block_len; i += 32) {
+        if (!(lanes && roots[i] == 0)) return;
+        uint16_t bb = (uint16_t)i;
+        bb = (uint16_t)(((bb >> 1) & 0x5555) | ((bb & 0x5555) << 1));
+        bb = (uint16_t)(((bb >> 2) & 0x3333) | ((bb & 0x3333) << 2));
+        bb = (uint16_t)(((bb >> 4) & 0x0f0f) | ((bb & 0x0f0f) << 4));
+        bb = (uint16_t)((bb >> 8) | (bb << 8));
+        const uint32_t x = c.roots_ntt[(uint32_t)(bb >> c.rbo_shift)];
+        const uint32_t xi = finv(x);
+        const uint32_t num = eval_poly(evaluator, el, xi);
+        const uint32_t den = eval_poly(deriv, dl, xi);
+        const uint32_t err = fmul(fdiv(num, den), x);
+        put_pos(c, v, b, i, fadd(get_pos(c, v, b, i), err));
+    }
+    __syncwarp();
+    if (lane == 0)
+        status[b] = count > 0 ? FFGPU_REPAIR_OK : (lanes ? FFGPU_ERROR_LOCATION_FAIL : FFGPU_NO_ERRORS);
+}
+
+// RSi16v::_repair with known locations (rsi16v_impl.hpp:171-231),
+// _error_locator (:531-542), _error_evaluator (:545-563); positions bp[0 .. count)
+static __device__ __noinline__ void rsi16_repair_known_block(const Rsi16Dev &c, const BlockView &v, size_t b,
+                                                      const uint32_t *bp, uint32_t count, uint32_t *temp,
+                                                      uint8_t *status, int lane) {
+    const uint32_t ecc = c.ecc;
+
+    w_gather(c, v, b, temp, true, lane);
+    w_pntt(c, temp, c.pntt_blocks, lane);
+    if (w_all_zero(temp, ecc, lane)) {
+        if (lane == 0 && status) status[b] = FFGPU_NO_ERRORS;
+        return;
+    }
+    uint32_t *ev = temp, *loc = temp + 2 * ecc, *tmp = temp + 4 * ecc;
+    w_fill(loc, 0, ecc, lane);
+    for (uint32_t j = 0; j < count; ++j) {
+        const uint32_t p = bp[j];
+        uint16_t bb = (uint16_t)p;
+        bb = (uint16_t)(((bb >> 1) & 0x5555) | ((bb & 0x5555) << 1));
+        bb = (uint16_t)(((bb >> 2) & 0x3333) | ((bb & 0x3333) << 2));
+        bb = (uint16_t)(((bb >> 4) & 0x0f0f) | ((bb & 0x0f0f) << 4));
+        bb = (uint16_t)((bb >> 8) | (bb << 8));
+        const uint32_t x = c.roots_ntt[(uint32_t)(bb >> c.rbo_shift)];
+        // loc[i] -= loc[i-1] * x for i = count-1 .. 1 (old values), loc[0] -= x
+        uint32_t nv[8];
+        int n = 0;
+        for (uint32_t i = lane; i < count && n < 8; i += 32) nv[n++] = (i == 0) ? fsub(loc[0], x) : fsub(loc[i], fmul(loc[i - 1], x));
+        __syncwarp();
+        n = 0;
+        for (uint32_t i = lane; i < count && n < 8; i += 32) loc[i] = nv[n++];
+        __syncwarp();
+    }
+    for (uint32_t k = ecc + lane; k < 2 * ecc; k += 32) ev[k] = 0;
+    __syncwarp();
+    w_gs(c.roots_ecc2, ev, 2 * ecc, lane);
+    for (uint32_t k = lane; k < 2 * ecc + 1; k += 32) tmp[k] = (k == 0) ? 1u : (k <= count ? loc[k - 1] : 0u);
+    __syncwarp();
+    w_gs(c.roots_ecc2, tmp, 2 * ecc, lane);
+    for (uint32_t k = lane; k < 2 * ecc; k += 32) ev[k] = fmul(ev[k], tmp[k]);
+    __syncwarp();
+    w_ct(c.roots_i_ecc2, ev, 2 * ecc, lane);
+    for (uint32_t k = lane; k < 2 * ecc; k += 32) ev[k] = (k < ecc) ? fmul(ev[k], c.ecc2_len_i) : 0u;
+    __syncwarp();
+    uint32_t *deriv = temp + ecc;
+    for (uint32_t k = lane; k < ecc; k += 32) deriv[k] = fmul(loc[k], k + 1);
+    __syncwarp();
+    const uint32_t dl = w_poly_len(deriv, ecc, lane);
+    // positions may repeat; apply sequentially in list order on lane 0
+    __syncwarp();
+    if (lane == 0) {
+        for (uint32_t i = 0; i < count; ++i) {
+            const uint32_t p = bp[i];
+            uint16_t bb = (uint16_t)p;
+            bb = (uint16_t)(((bb >> 1) & 0x5555) | ((bb & 0x5555) << 1));
+            bb = (uint16_t)(((bb >> 2) & 0x3333) | ((bb & 0x3333) << 2));
+            bb = (uint16_t)(((bb >> 4) & 0x0f0f) | ((bb & 0x0f0f) << 4));
+            bb = (uint16_t)((bb >> 8) | (bb << 8));
+            const uint32_t pr = (uint32_t)(bb >> c.rbo_shift);
+            const uint32_t x = c.roots_ntt[pr];
+            const uint32_t xi = finv(x);
+            const uint32_t num = eval_poly(ev, ecc, xi);
+            const uint32_t den = eval_poly(deriv, dl, xi);
+            const uint32_t err = fmul(fdiv(num, den), x);
+            uint16_t cc = (uint16_t)pr;
+            cc = (uint16_t)(((cc >> 1) & 0x5555) | ((cc & 0x5555) << 1));
+            cc = (uint16_t)(((cc >> 2) & 0x3333) | ((cc & 0x3333) << 2));
+            cc = (uint16_t)(((cc >> 4) & 0x0f0f) | ((cc & 0x0f0f) << 4));
+            cc = (uint16_t)((cc >> 8) | (cc << 8));
+            const uint32_t q = (uint32_t)(cc >> c.rbo_shift);
+            put_pos(c, v, b, q, fadd(get_pos(c, v, b, q), err));
+        }
+        if (status) status[b] = FFGPU_REPAIR_OK;
+    }
+    __syncwarp();
+}
+
+}  // namespace ffgpu
