@@ -784,7 +784,216 @@ def bench_batch_mixed(args, torch, rank, world):
     }
 
 
+# ---------------------------------------------------------------- serving
+
+def make_serving_requests(n, seed, load_gbs):
+    """Seeded request stream on page-locked host buffers: Poisson arrivals at
+    `load_gbs` GB/s of offered codeword bytes, log-normal payloads clipped to
+    [4 KiB, 64 MiB]; codes RS256 ecc 8 / 32 (255-byte blocks), RSi16(1024, 64),
+    CIRC16(128, 8, 128, 8, 4); 70% encode, 30% decode with 0..max correctable
+    errors per block (CIRC16 requests are encodes).  Decode inputs are encoded
+    with the host API and corrupted on the host."""
+    import ctypes
+
+    from libffrs_gb300 import capi
+
+    rng = np.random.Generator(np.random.PCG64(seed))
+    codes = {"rs8": capi.RS256Code(8), "rs32": capi.RS256Code(32), "rsi": capi.RSi16Code(1024, 64),
+             "circ": capi.CIRC16Code(128, 8, 128, 8, 4)}
+    L = capi.lib()
+
+    def pinned(nbytes, dtype):
+        p = ctypes.c_void_p()
+        capi.call("ffgpu_host_alloc", max(nbytes, 1), ctypes.byref(p))
+        arr = np.ctypeslib.as_array((ctypes.c_uint8 * max(nbytes, 1)).from_address(p.value))
+        return p, arr.view(dtype)[: nbytes // np.dtype(dtype).itemsize]
+
+    reqs = []
+    t = 0.0
+    for i in range(n):
+        size = int(np.clip(np.exp(rng.normal(np.log(1 << 20), 1.5)), 4096, 64 << 20))
+        kind = rng.choice(["rs8", "rs32", "rsi", "circ"])
+        dec = rng.random() < 0.3 and kind != "circ"
+        c = codes[kind]
+        r = {"kind": kind, "op": "dec" if dec else "enc", "code": c, "bufs": []}
+        if kind in ("rs8", "rs32"):
+            ecc = c.ecc_len
+            ml = 255 - ecc
+            nb = max(1, size // 255)
+            pa, a = pinned(nb * ml, np.uint8)
+            pb, b = pinned(nb * ecc, np.uint8)
+            a[:] = rng.integers(0, 256, a.size, dtype=np.uint8)
+            r.update(nb=nb, ml=ml, ecc=ecc, a=a, b=b, pa=pa, pb=pb, nbytes=nb * 255)
+            if dec:
+                capi.call("ffgpu_rs256_encode_host", c.h, pa, nb * ml, ml, pb)
+                cw = np.concatenate([a.reshape(nb, ml), b.reshape(nb, ecc)], axis=1)
+                kmax = ecc // 2
+                for s0 in range(0, nb, 8192):
+                    s1 = min(nb, s0 + 8192)
+                    m = s1 - s0
+                    k = rng.integers(0, kmax + 1, m)
+                    pos = np.argsort(rng.random((m, 255), dtype=np.float32), axis=1)[:, :kmax]
+                    vals = rng.integers(1, 256, (m, kmax), dtype=np.uint8) * (np.arange(kmax)[None, :] < k[:, None])
+                    rows = np.repeat(np.arange(s0, s1)[:, None], kmax, axis=1)
+                    cw[rows, pos] ^= vals.astype(np.uint8)
+                a[:] = cw[:, :ml].reshape(-1)
+                b[:] = cw[:, ml:].reshape(-1)
+        elif kind == "rsi":
+            nb = max(1, size // 2048)
+            pa, a = pinned(nb * 960 * 2, np.uint16)
+            pb, b = pinned(nb * 64 * 2, np.uint16)
+            a[:] = rng.integers(0, 65536, a.size, dtype=np.uint16)
+            r.update(nb=nb, a=a, b=b, pa=pa, pb=pb, nbytes=nb * 2048)
+            if dec:
+                capi.call("ffgpu_rsi16_encode_host", c.h, pa, nb, 1, pb)
+                cw = np.concatenate([a.reshape(nb, 960), b.reshape(nb, 64)], axis=1).astype(np.int64)
+                for s0 in range(0, nb, 2048):
+                    s1 = min(nb, s0 + 2048)
+                    m = s1 - s0
+                    k = rng.integers(0, 33, m)
+                    pos = np.argsort(rng.random((m, 1024), dtype=np.float32), axis=1)[:, :32]
+                    rows = np.repeat(np.arange(s0, s1)[:, None], 32, axis=1)
+                    v = cw[rows, pos]
+                    d = rng.integers(1, 65537, (m, 32))
+                    nv = (v + d) % 65537
+                    nv = np.where(nv == 65536, (v + d + 1) % 65537, nv)
+                    cw[rows, pos] = np.where(np.arange(32)[None, :] < k[:, None], nv, v)
+                a[:] = cw[:, :960].reshape(-1).astype(np.uint16)
+                b[:] = cw[:, 960:].reshape(-1).astype(np.uint16)
+        else:
+            cwb = (c.message_len + c.ecc_len) * 2
+            nb = max(1, size // cwb)
+            pa, a = pinned(nb * c.message_len * 2, np.uint16)
+            pb, b = pinned(nb * c.ecc_len * 2, np.uint16)
+            a[:] = rng.integers(0, 65536, a.size, dtype=np.uint16)
+            r.update(nb=nb, a=a, b=b, pa=pa, pb=pb, nbytes=nb * cwb)
+        if dec:
+            ps, s = pinned(r["nb"], np.uint8)
+            r.update(ps=ps, s=s)
+        r["a0"], r["b0"] = r["a"].copy(), r["b"].copy()
+        t += rng.exponential(r["nbytes"] / (load_gbs * 1e9))
+        r["arrival"] = t
+        reqs.append(r)
+    return reqs, codes
+
+
+def serving_restore(reqs):
+    for r in reqs:
+        r["a"][:] = r["a0"]
+        r["b"][:] = r["b0"]
+
+
+def serve_plain_one(r):
+    """the per-request host API, as a plain caller would use it"""
+    from libffrs_gb300 import capi
+
+    c = r["code"]
+    if r["kind"] in ("rs8", "rs32"):
+        if r["op"] == "enc":
+            capi.call("ffgpu_rs256_encode_host", c.h, r["pa"], r["nb"] * r["ml"], r["ml"], r["pb"])
+        else:
+            capi.call("ffgpu_rs256_decode_host", c.h, r["pa"], r["pb"], r["nb"], r["ml"], r["ps"])
+    elif r["kind"] == "rsi":
+        if r["op"] == "enc":
+            capi.call("ffgpu_rsi16_encode_host", c.h, r["pa"], r["nb"], 1, r["pb"])
+        else:
+            capi.call("ffgpu_rsi16_repair_host", c.h, r["pa"], r["pb"], r["nb"], 1, None, -1, r["ps"])
+    else:
+        capi.call("ffgpu_circ16_encode_host", c.h, r["pa"], r["nb"], r["pb"])
+
+
+def serve_submit(srv, r):
+    from libffrs_gb300 import capi
+
+    op = capi.ENCODE if r["op"] == "enc" else capi.DECODE
+    c = r["code"]
+    if r["kind"] in ("rs8", "rs32"):
+        return srv.submit_rs256(c, op, r["pa"], r["pb"], r["nb"], r["ml"], r.get("ps"))
+    if r["kind"] == "rsi":
+        return srv.submit_rsi16(c, op, r["pa"], r["pb"], r["nb"], r.get("ps"))
+    return srv.submit_circ16(c, r["pa"], r["pb"], r["nb"])
+
+
+def run_served(reqs, slots=4):
+    from libffrs_gb300 import capi
+
+    srv = capi.Server(slots=slots, max_batch=64)
+    t0 = time.perf_counter()
+    tickets = []
+    for r in reqs:
+        d = r["arrival"] - (time.perf_counter() - t0)
+        if d > 0:
+            time.sleep(d)
+        tickets.append(serve_submit(srv, r))
+    for tk in tickets:
+        srv.wait(tk)
+    info = [srv.poll(tk) for tk in tickets]
+    srv.close()
+    lat = [i["done"] - i["submit"] for i in info]
+    span = max(i["done"] for i in info) - min(i["submit"] for i in info)
+    return lat, span
+
+
+def run_plain_fifo(reqs):
+    t0 = time.perf_counter()
+    lat, done = [], []
+    for r in reqs:
+        d = r["arrival"] - (time.perf_counter() - t0)
+        if d > 0:
+            time.sleep(d)
+        serve_plain_one(r)
+        t = time.perf_counter() - t0
+        lat.append(t - r["arrival"])
+        done.append(t)
+    return lat, max(done) - reqs[0]["arrival"]
+
+
+def bench_serving(args, torch, rank, world):
+    nreq = args.blocks or 400
+    load = 40.0  # offered GB/s of codeword bytes
+    reqs, _codes = make_serving_requests(nreq, 5000 + rank, load)
+    nbytes = sum(r["nbytes"] for r in reqs)
+    # warm up both paths on a prefix
+    serving_restore(reqs)
+    for r in reqs[:8]:
+        serve_plain_one(r)
+    run_served(reqs[:8])
+    serving_restore(reqs)
+    plain_lat, plain_span = run_plain_fifo(reqs)
+    want = [(r["a"].copy(), r["b"].copy(), r["s"].copy() if "s" in r else None) for r in reqs]
+    best = None
+    for _ in range(max(1, args.steps)):
+        serving_restore(reqs)
+        lat, span = run_served(reqs)
+        if best is None or span < best[1]:
+            best = (lat, span)
+    lat, span = best
+    same = all(np.array_equal(r["a"], w[0]) and np.array_equal(r["b"], w[1]) and
+               (w[2] is None or np.array_equal(r["s"], w[2])) for r, w in zip(reqs, want))
+    if not same:
+        raise SystemExit("served results differ from the plain per-request results")
+
+    def pct(v, q):
+        return float(np.percentile(np.array(v) * 1e3, q))
+
+    gbs = nbytes / span / 1e9
+    return {
+        "workload": "serving", "total_ms": span * 1e3, "kern_ms": [span * 1e3], "algo_bytes_per_step": nbytes,
+        "launches": 0, "kernels": {}, "clocks": {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0},
+        "e2e": {"value": gbs, "unit": "GB/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                "api": "ffgpu_server_submit_* on page-locked host buffers"},
+        "config": {"workload": "serving: Poisson arrivals at %.0f GB/s offered, log-normal payloads 4 KiB-64 MiB, "
+                               "RS256 ecc 8/32, RSi16(1024,64), CIRC16(128,8,128,8,4), 70%% encode" % load,
+                   "requests": nreq, "bytes": nbytes, "slots": 4},
+        "dtype": "u8 / u32 mod 65537",
+        "extra": {"served_p50_ms": pct(lat, 50), "served_p99_ms": pct(lat, 99), "served_gbs": gbs,
+                  "plain_p50_ms": pct(plain_lat, 50), "plain_p99_ms": pct(plain_lat, 99),
+                  "plain_gbs": nbytes / plain_span / 1e9, "bit_identical_to_plain": same},
+    }
+
+
 WORKLOADS = {
+    "serving": (bench_serving, None, 0, "GB/s"),
     "batch-mixed": (bench_batch_mixed, None, 0, "GB/s"),
     "rsi16-encode": (lambda a, t, r, w: bench_rsi16(a, t, r, w, False),
                      lambda th, n: cpu_baseline_rsi16(th, n, False), 65536, "GB/s"),

@@ -223,6 +223,36 @@ FFGPU_API int ffgpu_batch_launch(ffgpu_batch *batch, void *stream);
 FFGPU_API int ffgpu_batch_info(const ffgpu_batch *batch, int *tile_rs256, int *tile_rsi16, int *ctas_per_sm,
                                size_t *items, unsigned *grid);
 
+/* ---------------------------------------------------------------- serving */
+/* No reference counterpart.  A server accepts requests on HOST buffers from
+ * any thread (same layouts and in-place semantics as the *_host entry
+ * points; page-locked memory from ffgpu_host_alloc copies fastest) and
+ * completes them asynchronously: a scheduler thread admits queued requests
+ * into one of `slots` CUDA streams while their device buffers fit in the HBM
+ * budget (0: 80% of the free memory), serves every request admitted together
+ * with one fused batch launch between its copies, and retires slots as they
+ * finish, so requests that arrive while others run overlap with them.  Results
+ * are byte-identical to serving each request alone. */
+typedef struct ffgpu_server ffgpu_server;
+FFGPU_API int ffgpu_server_create(size_t hbm_budget, int slots, int max_batch, ffgpu_server **out);
+/* waits for every submitted request, then frees the server */
+FFGPU_API int ffgpu_server_destroy(ffgpu_server *server);
+FFGPU_API int ffgpu_server_submit_rs256(ffgpu_server *server, const ffgpu_rs256 *code, int op, uint8_t *data,
+                                        uint8_t *parity, size_t nblocks, size_t message_len, uint8_t *status,
+                                        uint64_t *ticket);
+FFGPU_API int ffgpu_server_submit_rsi16(ffgpu_server *server, const ffgpu_rsi16 *code, int op, uint16_t *msg,
+                                        uint16_t *parity, size_t nblocks, uint8_t *status, uint64_t *ticket);
+FFGPU_API int ffgpu_server_submit_circ16(ffgpu_server *server, const ffgpu_circ16 *code, int op, uint16_t *msg,
+                                         uint16_t *ecc, size_t nblocks, uint64_t *ticket);
+/* state: 0 queued, 1 running, 2 done, 3 failed; times are seconds since the
+ * server was created (submitted, admitted into a slot, completion seen) */
+FFGPU_API int ffgpu_server_poll(ffgpu_server *server, uint64_t ticket, int *state, double *t_submit,
+                                double *t_start, double *t_done);
+/* block until the request is done; timeout_s < 0 waits without limit */
+FFGPU_API int ffgpu_server_wait(ffgpu_server *server, uint64_t ticket, double timeout_s);
+/* forget a finished request */
+FFGPU_API int ffgpu_server_release(ffgpu_server *server, uint64_t ticket);
+
 #ifdef __cplusplus
 }
 #endif

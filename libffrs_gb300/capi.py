@@ -98,6 +98,14 @@ def _declare(L):
         "ffgpu_circ16_find_outer_error_locations": (_I, [_P, _P, _P, _SZ, _P, _P]),
         "ffgpu_circ16_encode_host": (_I, [_P, _P, _SZ, _P]),
         "ffgpu_circ16_repair_host": (_I, [_P, _P, _P, _SZ, _P]),
+        "ffgpu_server_create": (_I, [_SZ, _I, _I, _PP]),
+        "ffgpu_server_destroy": (_I, [_P]),
+        "ffgpu_server_submit_rs256": (_I, [_P, _P, _I, _P, _P, _SZ, _SZ, _P, ctypes.POINTER(ctypes.c_uint64)]),
+        "ffgpu_server_submit_rsi16": (_I, [_P, _P, _I, _P, _P, _SZ, _P, ctypes.POINTER(ctypes.c_uint64)]),
+        "ffgpu_server_submit_circ16": (_I, [_P, _P, _I, _P, _P, _SZ, ctypes.POINTER(ctypes.c_uint64)]),
+        "ffgpu_server_poll": (_I, [_P, ctypes.c_uint64, ctypes.POINTER(_I)] + [ctypes.POINTER(ctypes.c_double)] * 3),
+        "ffgpu_server_wait": (_I, [_P, ctypes.c_uint64, ctypes.c_double]),
+        "ffgpu_server_release": (_I, [_P, ctypes.c_uint64]),
         "ffgpu_batch_create": (_I, [_PP]),
         "ffgpu_batch_destroy": (_I, [_P]),
         "ffgpu_batch_clear": (_I, [_P]),
@@ -249,6 +257,54 @@ class Batch:
              ctypes.byref(g))
         return {"tile_rs256": a.value, "tile_rsi16": b.value, "ctas_per_sm": c.value, "items": n.value,
                 "grid": g.value}
+
+
+class Server:
+    """Asynchronous serving of host-buffer requests (ffgpu_server)."""
+
+    def __init__(self, hbm_budget=0, slots=4, max_batch=64):
+        h = ctypes.c_void_p()
+        call("ffgpu_server_create", hbm_budget, slots, max_batch, ctypes.byref(h))
+        self.h = h
+        self._keep = {}
+
+    def close(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.ffgpu_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def _t(self, keep, fn, *args):
+        t = ctypes.c_uint64()
+        call(fn, self.h, *args, ctypes.byref(t))
+        self._keep[t.value] = keep
+        return t.value
+
+    def submit_rs256(self, code, op, data_ptr, parity_ptr, nblocks, message_len, status_ptr=None, keep=None):
+        return self._t((code, keep), "ffgpu_server_submit_rs256", code.h, op, data_ptr, parity_ptr, nblocks,
+                       message_len, status_ptr)
+
+    def submit_rsi16(self, code, op, msg_ptr, parity_ptr, nblocks, status_ptr=None, keep=None):
+        return self._t((code, keep), "ffgpu_server_submit_rsi16", code.h, op, msg_ptr, parity_ptr, nblocks,
+                       status_ptr)
+
+    def submit_circ16(self, code, msg_ptr, ecc_ptr, nblocks, keep=None):
+        return self._t((code, keep), "ffgpu_server_submit_circ16", code.h, ENCODE, msg_ptr, ecc_ptr, nblocks)
+
+    def wait(self, ticket, timeout=-1.0):
+        call("ffgpu_server_wait", self.h, ticket, timeout)
+
+    def poll(self, ticket):
+        st = _I()
+        a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        call("ffgpu_server_poll", self.h, ticket, ctypes.byref(st), ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+        return {"state": st.value, "submit": a.value, "start": b.value, "done": c.value}
+
+    def release(self, ticket):
+        call("ffgpu_server_release", self.h, ticket)
+        self._keep.pop(ticket, None)
 
 
 def timing_enable(on=True):

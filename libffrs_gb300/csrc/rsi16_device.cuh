@@ -472,7 +472,7 @@ static __device__ __noinline__ void rsi16_repair_block(const Rsi16Dev &c, const 
     }
     // second pass: apply corrections (kept separate so the count is final first)
     for (uint32_t i = lane; i < c.block_len; i += 32) {
-        if (!(lanes && roots[i] == 0)) return;
+        if (!(lanes && roots[i] == 0)) continue;
         uint16_t bb = (uint16_t)i;
         bb = (uint16_t)(((bb >> 1) & 0x5555) | ((bb & 0x5555) << 1));
         bb = (uint16_t)(((bb >> 2) & 0x3333) | ((bb & 0x3333) << 2));
