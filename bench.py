@@ -978,7 +978,8 @@ def bench_serving(args, torch, rank, world):
 
     gbs = nbytes / span / 1e9
     return {
-        "workload": "serving", "total_ms": span * 1e3, "kern_ms": [span * 1e3], "algo_bytes_per_step": nbytes,
+        "workload": "serving", "total_ms": span * 1e3 * max(1, args.steps), "kern_ms": [span * 1e3],
+        "algo_bytes_per_step": nbytes,
         "launches": 0, "kernels": {}, "clocks": {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0},
         "e2e": {"value": gbs, "unit": "GB/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                 "api": "ffgpu_server_submit_* on page-locked host buffers"},
