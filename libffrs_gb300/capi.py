@@ -77,6 +77,7 @@ def _declare(L):
         "ffgpu_rs256_decode_host": (_I, [_P, _P, _P, _SZ, _SZ, _P]),
         "ffgpu_rs256_synds_host": (_I, [_P, _P, _P, _SZ, _SZ, _P]),
         "ffgpu_rs256_set_table_only": (_I, [_P, _I]),
+        "ffgpu_rs256_decode_noalloc": (_I, [_P, _P, _P, _SZ, _SZ, _P, _P]),
         "ffgpu_rsi16_create": (_I, [_SZ, _SZ, _U32, _PP]),
         "ffgpu_rsi16_destroy": (_I, [_P]),
         "ffgpu_rsi16_info": (_I, [_P, ctypes.POINTER(_U32), ctypes.POINTER(_SZ)]),

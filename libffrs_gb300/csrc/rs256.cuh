@@ -59,5 +59,10 @@ bool rs256_fast_encode(const Rs256Code &c, const uint8_t *data, size_t nblocks, 
                        cudaStream_t st);
 bool rs256_fast_decode(const Rs256Code &c, uint8_t *data, uint8_t *parity, size_t nblocks, int msg_len,
                        uint8_t *status, cudaStream_t st);
+// the bitsliced decode on caller-provided scratch of rs256_fast_scratch_bytes
+// bytes (4-byte aligned); returns false when the request is not covered
+size_t rs256_fast_scratch_bytes(int ecc, size_t nblocks);
+bool rs256_fast_decode_with(const Rs256Code &c, uint8_t *data, uint8_t *parity, size_t nblocks, int msg_len,
+                            uint8_t *status, void *scratch, cudaStream_t st);
 
 }  // namespace ffgpu
