@@ -117,8 +117,9 @@ __device__ void rsi16_item(const Rsi16Dev &c, const BatchItem &it, uint32_t *ws,
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const BlockView v = contiguous_view(it.msg, true, c.message_len, it.par, true, c.ecc);
     for (uint32_t b = warp; b < it.nblocks; b += kBatchWarps) {
-        if (decode)
-            rsi16_repair_block(c, v, b, ws, it.status, lane);
+        if (decode) {
+            if (!rsi16_repair_bm_block(c, v, b, ws, it.status, lane)) rsi16_repair_block(c, v, b, ws, it.status, lane);
+        }
         else
             rsi16_encode_block(c, v, b, ws, lane);
     }

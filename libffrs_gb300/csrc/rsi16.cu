@@ -192,7 +192,7 @@ __global__ void rsi16_repair_warp_kernel(Rsi16Dev c, BlockView v, size_t nblocks
     WarpCtx w = warp_ctx(gscratch, ws_words);
     for (size_t b = w.warp_global; b < nblocks; b += w.nwarps) {
         if (active && !active[b]) continue;
-        rsi16_repair_block(c, v, b, w.ws, status, w.lane);
+        if (!rsi16_repair_bm_block(c, v, b, w.ws, status, w.lane)) rsi16_repair_block(c, v, b, w.ws, status, w.lane);
     }
 }
 

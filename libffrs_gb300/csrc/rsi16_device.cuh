@@ -490,6 +490,110 @@ static __device__ __noinline__ void rsi16_repair_block(const Rsi16Dev &c, const 
         status[b] = count > 0 ? FFGPU_REPAIR_OK : (lanes ? FFGPU_ERROR_LOCATION_FAIL : FFGPU_NO_ERRORS);
 }
 
+// Bounded-distance repair of block b by Berlekamp-Massey, for the blocks whose
+// error pattern has weight at most t = ecc/2.  The syndromes are the
+// reference's (first ecc outputs of the partial NTT: S_j = sum_i r_i X_i^j,
+// X_i = w^rbo(i)).  When BM returns a connection polynomial C of length
+// L <= t that has exactly L roots X_i^-1 among the block positions, there is
+// exactly one error pattern of weight <= t with these syndromes, and every
+// correct bounded-distance decoder -- the reference's NTT-domain Sugiyama
+// included -- returns it: the corrections block[i] += X_i Omega(X_i^-1) /
+// C'(X_i^-1) and RepairOk.  Returns false (block untouched) otherwise; the
+// caller then runs the reference's algorithm step for step.
+// temp: ntt_len + 6 * ecc words.
+static __device__ __noinline__ bool rsi16_repair_bm_block(const Rsi16Dev &c, const BlockView &v, size_t b,
+                                                         uint32_t *temp, uint8_t *status, int lane) {
+    const uint32_t ecc = c.ecc, t = ecc / 2, n1 = ecc + 1;
+    w_gather(c, v, b, temp, true, lane);
+    w_pntt(c, temp, c.pntt_blocks, lane);
+    uint32_t *S = temp;
+    if (w_all_zero(S, ecc, lane)) {
+        if (lane == 0) status[b] = FFGPU_NO_ERRORS;
+        return true;
+    }
+    uint32_t *C = temp + ecc, *B = C + n1, *T = B + n1;
+    for (uint32_t k = lane; k < n1; k += 32) {
+        C[k] = k == 0;
+        B[k] = k == 0;
+    }
+    __syncwarp();
+    uint32_t L = 0, m = 1, binv = 1;
+    for (uint32_t n = 0; n < ecc; ++n) {
+        // discrepancy d = sum_{i <= L} C_i S_{n-i}
+        uint32_t acc = 0;
+        for (uint32_t i = lane; i <= L && i <= n; i += 32) acc += fmul(C[i], S[n - i]);
+        acc = __reduce_add_sync(0xffffffffu, acc) % 0x10001u;
+        const uint32_t d = acc;
+        if (d == 0) {
+            ++m;
+            continue;
+        }
+        const uint32_t coef = fmul(d, binv);
+        const bool grow = 2 * L <= n;
+        if (grow) {
+            for (uint32_t k = lane; k < n1; k += 32) T[k] = C[k];
+            __syncwarp();
+        }
+        for (uint32_t k = lane; k < n1; k += 32)
+            if (k >= m) C[k] = fsub(C[k], fmul(coef, B[k - m]));
+        __syncwarp();
+        if (grow) {
+            uint32_t *x = B;
+            B = T;
+            T = x;
+            L = n + 1 - L;
+            binv = finv(d);
+            m = 1;
+        } else {
+            ++m;
+        }
+    }
+    if (L == 0 || L > t) return false;
+    // C must have degree exactly L (checked through the root count below)
+    for (uint32_t k = lane; k < n1; k += 32)
+        if (k > L && C[k]) L = 0xffffffffu;
+    if (__any_sync(0xffffffffu, L == 0xffffffffu)) return false;
+    // roots: the inverse partial NTT evaluates C at X_i^-1 for every position
+    uint32_t *R = temp + ecc + 3 * n1;  // block_len words, past S, C, B and T
+    for (uint32_t k = lane; k < c.block_len; k += 32) R[k] = k <= L ? C[k] : 0u;
+    __syncwarp();
+    w_pintt(c, R, lane);
+    uint32_t count = 0;
+    for (uint32_t i0 = 0; i0 < c.block_len; i0 += 32) {
+        const uint32_t i = i0 + lane;
+        count += __popc(__ballot_sync(0xffffffffu, i < c.block_len && R[i] == 0));
+    }
+    if (count != L) return false;
+    // evaluator Omega = S * C mod x^L and the derivative C'
+    uint32_t *Om = B, *D = B + t + 1;  // B is free now: t + L <= ecc words
+    for (uint32_t j = lane; j < L; j += 32) {
+        uint32_t s = 0;
+        for (uint32_t k = 0; k <= j; ++k) s = fadd(s, fmul(C[k], S[j - k]));
+        Om[j] = s;
+        D[j] = fmul(C[j + 1], j + 1);
+    }
+    __syncwarp();
+    const uint32_t N = c.ntt_len;
+    for (uint32_t i = lane; i < c.block_len; i += 32) {
+        if (R[i] != 0) continue;
+        uint16_t bb = (uint16_t)i;
+        bb = (uint16_t)(((bb >> 1) & 0x5555) | ((bb & 0x5555) << 1));
+        bb = (uint16_t)(((bb >> 2) & 0x3333) | ((bb & 0x3333) << 2));
+        bb = (uint16_t)(((bb >> 4) & 0x0f0f) | ((bb & 0x0f0f) << 4));
+        bb = (uint16_t)((bb >> 8) | (bb << 8));
+        const uint32_t e = (uint32_t)(bb >> c.rbo_shift);
+        const uint32_t x = c.roots_ntt[e];
+        const uint32_t xi = c.roots_ntt[(N - e) & (N - 1)];
+        const uint32_t num = eval_poly(Om, L, xi);
+        const uint32_t den = eval_poly(D, L, xi);
+        const uint32_t err = fmul(fmul(num, finv(den)), x);
+        put_pos(c, v, b, i, fadd(get_pos(c, v, b, i), err));
+    }
+    __syncwarp();
+    if (lane == 0) status[b] = FFGPU_REPAIR_OK;
+    return true;
+}
+
 // RSi16v::_repair with known locations (rsi16v_impl.hpp:171-231),
 // _error_locator (:531-542), _error_evaluator (:545-563); positions bp[0 .. count)
 static __device__ __noinline__ void rsi16_repair_known_block(const Rsi16Dev &c, const BlockView &v, size_t b,
