@@ -123,6 +123,11 @@ FFGPU_API int ffgpu_rs256_set_table_only(ffgpu_rs256 *code, int table_only);
  * RSi16v ctor (libffrs/rsi16v_impl.hpp:68-86). */
 FFGPU_API int ffgpu_rsi16_create(size_t block_len, size_t ecc_len, uint32_t primitive, ffgpu_rsi16 **out);
 FFGPU_API int ffgpu_rsi16_destroy(ffgpu_rsi16 *code);
+/* No reference counterpart (observability).  Blocks that the unknown-location
+ * repair served with the bounded-distance (Berlekamp-Massey) path and with the
+ * step-for-step mirror of the reference's algorithm, since load or the last
+ * reset; synchronises the device. */
+FFGPU_API int ffgpu_rsi16_repair_counters(uint64_t *fast_blocks, uint64_t *mirror_blocks, int reset);
 /* root, ntt_len */
 FFGPU_API int ffgpu_rsi16_info(const ffgpu_rsi16 *code, uint32_t *root, size_t *ntt_len);
 

@@ -80,6 +80,7 @@ def _declare(L):
         "ffgpu_rs256_decode_noalloc": (_I, [_P, _P, _P, _SZ, _SZ, _P, _P]),
         "ffgpu_rsi16_create": (_I, [_SZ, _SZ, _U32, _PP]),
         "ffgpu_rsi16_destroy": (_I, [_P]),
+        "ffgpu_rsi16_repair_counters": (_I, [ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64), _I]),
         "ffgpu_rsi16_info": (_I, [_P, ctypes.POINTER(_U32), ctypes.POINTER(_SZ)]),
         "ffgpu_rsi16_encode": (_I, [_P, _P, _SZ, _P, _P]),
         "ffgpu_rsi16_encode_interleaved": (_I, [_P, _P, _SZ, _SZ, _P, _P]),
@@ -306,6 +307,13 @@ class Server:
     def release(self, ticket):
         call("ffgpu_server_release", self.h, ticket)
         self._keep.pop(ticket, None)
+
+
+def rsi16_repair_counters(reset=False):
+    """(blocks served by the bounded-distance path, blocks served by the mirror)"""
+    f, m = ctypes.c_uint64(), ctypes.c_uint64()
+    call("ffgpu_rsi16_repair_counters", ctypes.byref(f), ctypes.byref(m), 1 if reset else 0)
+    return f.value, m.value
 
 
 def timing_enable(on=True):

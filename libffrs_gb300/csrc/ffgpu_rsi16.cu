@@ -49,6 +49,10 @@ int ffgpu_rsi16_info(const ffgpu_rsi16 *code, uint32_t *root, size_t *ntt_len) {
     });
 }
 
+int ffgpu_rsi16_repair_counters(uint64_t *fast_blocks, uint64_t *mirror_blocks, int reset) {
+    return guarded([&] { rsi16_repair_counters(fast_blocks, mirror_blocks, reset != 0); });
+}
+
 int ffgpu_rsi16_encode(const ffgpu_rsi16 *code, const uint16_t *msg, size_t nblocks, uint16_t *parity, void *stream) {
     return guarded([&] {
         FFGPU_REQUIRE(code, "code is NULL");

@@ -120,9 +120,11 @@ Rsi16Code::Rsi16Code(size_t block_len_, size_t ecc_len, uint32_t primitive_)
         while (all.size() % 32) all.push_back(0);
         return off;
     };
+    std::vector<uint32_t> inv_tab(65537);
+    for (uint32_t a = 0; a < 65537; ++a) inv_tab[a] = inv(a);
     const size_t o_rn = put(roots_ntt), o_re = put(roots_ecc), o_rie = put(roots_i_ecc), o_re2 = put(roots_ecc2),
                  o_rie2 = put(roots_i_ecc2), o_ps = put(pntt_shift), o_pis = put(pintt_shift), o_rbo = put(rbo_ecc),
-                 o_mix = put(ecc_mix);
+                 o_mix = put(ecc_mix), o_inv = put(inv_tab);
     FFGPU_CHECK_CUDA(cudaMalloc(&d_tables, all.size() * 4));
     FFGPU_CHECK_CUDA(cudaMemcpy(d_tables, all.data(), all.size() * 4, cudaMemcpyHostToDevice));
     dev.roots_ntt = d_tables + o_rn;
@@ -134,6 +136,7 @@ Rsi16Code::Rsi16Code(size_t block_len_, size_t ecc_len, uint32_t primitive_)
     dev.pintt_shift = d_tables + o_pis;
     dev.rbo_ecc = d_tables + o_rbo;
     dev.ecc_mix = d_tables + o_mix;
+    dev.inv_tab = d_tables + o_inv;
     dev.block_len = (uint32_t)block_len;
     dev.message_len = (uint32_t)message_len;
     dev.ecc = (uint32_t)ecc;
@@ -187,12 +190,39 @@ __global__ void rsi16_synd_warp_kernel(Rsi16Dev c, BlockView v, size_t nblocks, 
     }
 }
 
+// blocks repaired by the bounded-distance path / by the step-for-step mirror
+__device__ unsigned long long g_repair_fast_blocks, g_repair_mirror_blocks;
+
 __global__ void rsi16_repair_warp_kernel(Rsi16Dev c, BlockView v, size_t nblocks, uint8_t *status,
                                          const uint8_t *active, uint32_t *gscratch, uint32_t ws_words) {
     WarpCtx w = warp_ctx(gscratch, ws_words);
+    unsigned long long nfast = 0, nmirror = 0;
     for (size_t b = w.warp_global; b < nblocks; b += w.nwarps) {
         if (active && !active[b]) continue;
-        if (!rsi16_repair_bm_block(c, v, b, w.ws, status, w.lane)) rsi16_repair_block(c, v, b, w.ws, status, w.lane);
+        if (rsi16_repair_bm_block(c, v, b, w.ws, status, w.lane)) {
+            ++nfast;
+        } else {
+            rsi16_repair_block(c, v, b, w.ws, status, w.lane);
+            ++nmirror;
+        }
+    }
+    if (w.lane == 0 && (nfast | nmirror)) {
+        atomicAdd(&g_repair_fast_blocks, nfast);
+        atomicAdd(&g_repair_mirror_blocks, nmirror);
+    }
+}
+
+void rsi16_repair_counters(uint64_t *fast, uint64_t *mirror, bool reset) {
+    unsigned long long f = 0, m = 0;
+    FFGPU_CHECK_CUDA(cudaDeviceSynchronize());
+    FFGPU_CHECK_CUDA(cudaMemcpyFromSymbol(&f, g_repair_fast_blocks, sizeof f));
+    FFGPU_CHECK_CUDA(cudaMemcpyFromSymbol(&m, g_repair_mirror_blocks, sizeof m));
+    if (fast) *fast = f;
+    if (mirror) *mirror = m;
+    if (reset) {
+        const unsigned long long z = 0;
+        FFGPU_CHECK_CUDA(cudaMemcpyToSymbol(g_repair_fast_blocks, &z, sizeof z));
+        FFGPU_CHECK_CUDA(cudaMemcpyToSymbol(g_repair_mirror_blocks, &z, sizeof z));
     }
 }
 

@@ -15,6 +15,7 @@ namespace ffgpu {
 struct Rsi16Dev {
     const uint32_t *roots_ntt, *roots_ecc, *roots_i_ecc, *roots_ecc2, *roots_i_ecc2;
     const uint32_t *pntt_shift, *pintt_shift, *rbo_ecc, *ecc_mix;
+    const uint32_t *inv_tab;  // inverse of every field element (inv(0) == 1, as the reference's table)
     uint32_t block_len, message_len, ecc, ntt_len, pntt_blocks, ecc_mask, rbo_shift;
     uint32_t ecc_len_i, ecc2_len_i;
     uint32_t temp_len;  // ntt_len + 6 * ecc: the reference's repair scratch
@@ -101,6 +102,10 @@ void rsi16_sugiyama(const Rsi16Code &c, const uint32_t *synds, size_t nblocks, u
                     uint8_t *status, cudaStream_t st);
 // pintt_ecc zeros of one polynomial (debug surface of the binding).
 void rsi16_roots(const Rsi16Code &c, const uint32_t *poly, uint8_t *is_zero, cudaStream_t st);
+// blocks the unknown-location repair kernel served by the bounded-distance
+// path and by the step-for-step mirror since load (or the last reset);
+// synchronises the device
+void rsi16_repair_counters(uint64_t *fast, uint64_t *mirror, bool reset);
 // mix_ecc on nvec ecc-word vectors in place (used by the CIRC16 heuristics).
 void rsi16_mix_ecc(const Rsi16Code &c, uint32_t *vecs, size_t nvec, cudaStream_t st);
 

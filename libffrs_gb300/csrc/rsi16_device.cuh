@@ -542,7 +542,7 @@ static __device__ __noinline__ bool rsi16_repair_bm_block(const Rsi16Dev &c, con
             B = T;
             T = x;
             L = n + 1 - L;
-            binv = finv(d);
+            binv = c.inv_tab[d];
             m = 1;
         } else {
             ++m;
@@ -558,11 +558,17 @@ static __device__ __noinline__ bool rsi16_repair_bm_block(const Rsi16Dev &c, con
     for (uint32_t k = lane; k < c.block_len; k += 32) R[k] = k <= L ? C[k] : 0u;
     __syncwarp();
     w_pintt(c, R, lane);
+    // root positions, compacted into T (free after BM; at most ecc + 1 kept)
     uint32_t count = 0;
     for (uint32_t i0 = 0; i0 < c.block_len; i0 += 32) {
         const uint32_t i = i0 + lane;
-        count += __popc(__ballot_sync(0xffffffffu, i < c.block_len && R[i] == 0));
+        const bool hit = i < c.block_len && R[i] == 0;
+        const uint32_t msk = __ballot_sync(0xffffffffu, hit);
+        const uint32_t at = count + __popc(msk & ((1u << lane) - 1u));
+        if (hit && at < n1) T[at] = i;
+        count += __popc(msk);
     }
+    __syncwarp();
     if (count != L) return false;
     // evaluator Omega = S * C mod x^L and the derivative C'
     uint32_t *Om = B, *D = B + t + 1;  // B is free now: t + L <= ecc words
@@ -574,8 +580,8 @@ static __device__ __noinline__ bool rsi16_repair_bm_block(const Rsi16Dev &c, con
     }
     __syncwarp();
     const uint32_t N = c.ntt_len;
-    for (uint32_t i = lane; i < c.block_len; i += 32) {
-        if (R[i] != 0) continue;
+    for (uint32_t r = lane; r < L; r += 32) {
+        const uint32_t i = T[r];
         uint16_t bb = (uint16_t)i;
         bb = (uint16_t)(((bb >> 1) & 0x5555) | ((bb & 0x5555) << 1));
         bb = (uint16_t)(((bb >> 2) & 0x3333) | ((bb & 0x3333) << 2));
@@ -586,7 +592,7 @@ static __device__ __noinline__ bool rsi16_repair_bm_block(const Rsi16Dev &c, con
         const uint32_t xi = c.roots_ntt[(N - e) & (N - 1)];
         const uint32_t num = eval_poly(Om, L, xi);
         const uint32_t den = eval_poly(D, L, xi);
-        const uint32_t err = fmul(fmul(num, finv(den)), x);
+        const uint32_t err = fmul(fmul(num, c.inv_tab[den]), x);
         put_pos(c, v, b, i, fadd(get_pos(c, v, b, i), err));
     }
     __syncwarp();

@@ -84,6 +84,40 @@ def test_rsi16_batched_vs_oracle(ffrs_gpu, bl, ecc):
     np.testing.assert_array_equal(np.frombuffer(bytes(eb), np.uint16).reshape(nb, ecc), eo)
 
 
+def test_rsi16_bounded_distance_path(ffrs_gpu):
+    """Blocks with at most ecc/2 errors are all served by the Berlekamp-Massey
+    path; blocks beyond it fall back to the mirror; both agree with the oracle."""
+    from libffrs_gb300 import capi
+
+    bl, ecc = 1024, 64
+    rng = np.random.Generator(np.random.PCG64(99))
+    rs = ffrs_gpu.RSi16(bl, ecc)
+    o = O.RSi16(bl, ecc)
+    ml = bl - ecc
+    for lo, hi, want_mirror in ((1, ecc // 2 + 1, False), (ecc // 2 + 8, ecc // 2 + 12, True)):
+        nb = 200
+        msg = rng.integers(0, 65536, size=(nb, ml), dtype=np.uint16)
+        par = o.encode_blocks(msg, threads=8)
+        cw = np.concatenate([msg, par], axis=1)
+        for i in range(nb):
+            _corrupt_words(rng, cw[i], int(rng.integers(lo, hi)))
+        m, e = np.ascontiguousarray(cw[:, :ml]), np.ascontiguousarray(cw[:, ml:])
+        mb, eb = bytearray(m.tobytes()), bytearray(e.tobytes())
+        capi.rsi16_repair_counters(reset=True)
+        st = np.frombuffer(bytes(rs.repair_blocks(mb, eb)), np.uint8)
+        fast, mirror = capi.rsi16_repair_counters()
+        assert fast + mirror == nb
+        if want_mirror:
+            assert mirror > 0
+        else:
+            assert mirror == 0 and (st == 2).all()
+        mo, eo = m.copy(), e.copy()
+        so = o.repair_blocks(mo, eo, threads=8)
+        np.testing.assert_array_equal(st.astype(np.int16), np.where(so < 0, 255, so.astype(np.int16)))
+        np.testing.assert_array_equal(np.frombuffer(bytes(mb), np.uint16).reshape(nb, ml), mo)
+        np.testing.assert_array_equal(np.frombuffer(bytes(eb), np.uint16).reshape(nb, ecc), eo)
+
+
 @pytest.mark.parametrize("interleave", [2, 3, 16, 33])
 def test_rsi16_interleaved_vs_oracle(ffrs_gpu, interleave):
     bl, ecc = 256, 32
