@@ -47,6 +47,9 @@ inline void check_launch(const char *what) {
 }
 
 cudaStream_t lib_stream();
+// k-th stream (mod kPipeStreams) of the chunked host-buffer pipelines
+constexpr size_t kPipeStreams = 3;
+cudaStream_t pipe_stream(size_t k);
 
 // Optional per-kernel timing (ffgpu_timing_enable): while it is on, a
 // KernelTimer records a CUDA event pair around one launch on the launching

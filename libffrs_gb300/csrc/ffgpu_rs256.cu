@@ -23,6 +23,16 @@ static std::mutex g_stream_mu;
 static cudaStream_t g_stream = nullptr;
 static int g_device = 0;
 
+// streams of the host-buffer pipelines (created on first use)
+cudaStream_t pipe_stream(size_t k) {
+    static std::mutex mu;
+    static cudaStream_t s[kPipeStreams] = {};
+    std::lock_guard<std::mutex> lk(mu);
+    cudaStream_t &x = s[k % kPipeStreams];
+    if (!x) FFGPU_CHECK_CUDA(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+    return x;
+}
+
 cudaStream_t lib_stream() {
     std::lock_guard<std::mutex> lk(g_stream_mu);
     if (!g_stream) {
@@ -240,18 +250,30 @@ int ffgpu_rs256_decode_host(const ffgpu_rs256 *code, uint8_t *data, uint8_t *par
         check_rs_geometry(c, message_len);
         if (nblocks == 0) return;
         std::lock_guard<std::mutex> lk(h->mu);
-        cudaStream_t st = lib_stream();
         const size_t nd = nblocks * message_len, np = nblocks * (size_t)c.ecc;
         uint8_t *d_d = (uint8_t *)h->d_data.get(nd);
         uint8_t *d_p = (uint8_t *)h->d_parity.get(np);
         uint8_t *d_s = (uint8_t *)h->d_status.get(nblocks);
-        FFGPU_CHECK_CUDA(cudaMemcpyAsync(d_d, data, nd, cudaMemcpyHostToDevice, st));
-        FFGPU_CHECK_CUDA(cudaMemcpyAsync(d_p, parity, np, cudaMemcpyHostToDevice, st));
-        rs256_decode(c, d_d, d_p, nblocks, (int)message_len, d_s, st);
-        FFGPU_CHECK_CUDA(cudaMemcpyAsync(data, d_d, nd, cudaMemcpyDeviceToHost, st));
-        FFGPU_CHECK_CUDA(cudaMemcpyAsync(parity, d_p, np, cudaMemcpyDeviceToHost, st));
-        FFGPU_CHECK_CUDA(cudaMemcpyAsync(status, d_s, nblocks, cudaMemcpyDeviceToHost, st));
-        FFGPU_CHECK_CUDA(cudaStreamSynchronize(st));
+        // chunks of blocks on the pipeline streams: the host-to-device copy of
+        // one chunk, the decode of another and the copy back of a third
+        // overlap (page-locked host memory moves at full speed)
+        const size_t chunk = std::max<size_t>(65536, (nblocks + 7) / 8);
+        size_t k = 0;
+        for (size_t b0 = 0; b0 < nblocks; b0 += chunk, ++k) {
+            cudaStream_t st = pipe_stream(k);
+            const size_t n = std::min(chunk, nblocks - b0);
+            uint8_t *dd = d_d + b0 * message_len, *dp = d_p + b0 * (size_t)c.ecc, *ds = d_s + b0;
+            FFGPU_CHECK_CUDA(cudaMemcpyAsync(dd, data + b0 * message_len, n * message_len, cudaMemcpyHostToDevice, st));
+            FFGPU_CHECK_CUDA(
+                cudaMemcpyAsync(dp, parity + b0 * (size_t)c.ecc, n * (size_t)c.ecc, cudaMemcpyHostToDevice, st));
+            rs256_decode(c, dd, dp, n, (int)message_len, ds, st);
+            FFGPU_CHECK_CUDA(cudaMemcpyAsync(data + b0 * message_len, dd, n * message_len, cudaMemcpyDeviceToHost, st));
+            FFGPU_CHECK_CUDA(
+                cudaMemcpyAsync(parity + b0 * (size_t)c.ecc, dp, n * (size_t)c.ecc, cudaMemcpyDeviceToHost, st));
+            FFGPU_CHECK_CUDA(cudaMemcpyAsync(status + b0, ds, n, cudaMemcpyDeviceToHost, st));
+        }
+        for (size_t i = 0; i < std::min<size_t>(k, kPipeStreams); ++i)
+            FFGPU_CHECK_CUDA(cudaStreamSynchronize(pipe_stream(i)));
     });
 }
 

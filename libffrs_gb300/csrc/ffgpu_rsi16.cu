@@ -178,6 +178,33 @@ int ffgpu_rsi16_repair_host(const ffgpu_rsi16 *code, uint16_t *msg, uint16_t *pa
         uint16_t *dm = (uint16_t *)h->d_msg.get(nm * 2);
         uint16_t *dp = (uint16_t *)h->d_par.get(np * 2);
         uint8_t *ds = (uint8_t *)h->d_status.get(ncol);
+        if (interleave == 1 && error_count < 0 && (size_t)(c.dev.temp_len + 1) * 4 * 4 <= 64 * 1024) {
+            // contiguous blocks, unknown locations: every block is written back
+            // whatever its status, so chunks of blocks pipeline their copies and
+            // repairs over the pipeline streams (only when the repair
+            // workspace lives in shared memory: the global fallback workspace
+            // is one per thread and cannot serve concurrent streams)
+            const size_t chunk = std::max<size_t>(8192, (nblocks + 7) / 8);
+            size_t k = 0;
+            for (size_t b0 = 0; b0 < nblocks; b0 += chunk, ++k) {
+                cudaStream_t ps = pipe_stream(k);
+                const size_t n = std::min(chunk, nblocks - b0);
+                uint16_t *cm = dm + b0 * c.message_len, *cp = dp + b0 * c.ecc;
+                FFGPU_CHECK_CUDA(cudaMemcpyAsync(cm, msg + b0 * c.message_len, n * c.message_len * 2,
+                                                 cudaMemcpyHostToDevice, ps));
+                FFGPU_CHECK_CUDA(
+                    cudaMemcpyAsync(cp, parity + b0 * c.ecc, n * c.ecc * 2, cudaMemcpyHostToDevice, ps));
+                rsi16_repair(c, contiguous_view(cm, true, c.message_len, cp, true, c.ecc), n, ds + b0, ps);
+                FFGPU_CHECK_CUDA(cudaMemcpyAsync(msg + b0 * c.message_len, cm, n * c.message_len * 2,
+                                                 cudaMemcpyDeviceToHost, ps));
+                FFGPU_CHECK_CUDA(
+                    cudaMemcpyAsync(parity + b0 * c.ecc, cp, n * c.ecc * 2, cudaMemcpyDeviceToHost, ps));
+                FFGPU_CHECK_CUDA(cudaMemcpyAsync(status + b0, ds + b0, n, cudaMemcpyDeviceToHost, ps));
+            }
+            for (size_t i = 0; i < std::min<size_t>(k, kPipeStreams); ++i)
+                FFGPU_CHECK_CUDA(cudaStreamSynchronize(pipe_stream(i)));
+            return;
+        }
         FFGPU_CHECK_CUDA(cudaMemcpyAsync(dm, msg, nm * 2, cudaMemcpyHostToDevice, st));
         FFGPU_CHECK_CUDA(cudaMemcpyAsync(dp, parity, np * 2, cudaMemcpyHostToDevice, st));
         BlockView v = interleave == 1 ? contiguous_view(dm, true, c.message_len, dp, true, c.ecc)
