@@ -63,6 +63,11 @@ FFGPU_API uint64_t ffgpu_kernel_launches(void);
  * truncated to cap), the full length into *len, and forgets them. */
 FFGPU_API int ffgpu_timing_enable(int on);
 FFGPU_API int ffgpu_timing_collect(char *out, size_t cap, size_t *len);
+/* No reference counterpart (tuning).  The host-buffer decode entry points
+ * copy, decode and copy back in chunks of blocks on three streams so that
+ * transfers overlap decoding; 0 (the default) chooses the chunk from the
+ * request size, any other value fixes the blocks per chunk. */
+FFGPU_API int ffgpu_set_host_chunk_blocks(size_t blocks);
 /* the library's own stream (cudaStream_t) */
 FFGPU_API void *ffgpu_default_stream(void);
 FFGPU_API int ffgpu_synchronize(void *stream);

@@ -64,6 +64,7 @@ def _declare(L):
         "ffgpu_default_stream": (_P, []),
         "ffgpu_synchronize": (_I, [_P]),
         "ffgpu_timing_enable": (_I, [_I]),
+        "ffgpu_set_host_chunk_blocks": (_I, [_SZ]),
         "ffgpu_timing_collect": (_I, [ctypes.c_char_p, _SZ, ctypes.POINTER(_SZ)]),
         "ffgpu_host_alloc": (_I, [_SZ, _PP]),
         "ffgpu_host_free": (_I, [_P]),

@@ -113,15 +113,30 @@ __device__ void rs256_dec_item(const BatchCode &c, const BatchItem &it, uint32_t
         default: { constexpr int w_ = 64; CALL; } break; \
     }
 
-__device__ void rsi16_item(const Rsi16Dev &c, const BatchItem &it, uint32_t *ws, bool decode) {
+template <int EPL>
+__device__ void rsi16_item_t(const Rsi16Dev &c, const BatchItem &it, uint32_t *ws, bool decode) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const BlockView v = contiguous_view(it.msg, true, c.message_len, it.par, true, c.ecc);
+    RegTw<EPL ? EPL : 1> tw;
+    if constexpr (EPL > 0) reg_twiddles<EPL>(c, lane, tw);
     for (uint32_t b = warp; b < it.nblocks; b += kBatchWarps) {
         if (decode) {
-            if (!rsi16_repair_bm_block(c, v, b, ws, it.status, lane)) rsi16_repair_block(c, v, b, ws, it.status, lane);
-        }
-        else
+            if (!rsi16_repair_bm_block_t<EPL>(c, v, b, ws, it.status, tw, lane))
+                rsi16_repair_block(c, v, b, ws, it.status, lane);
+        } else if constexpr (EPL > 0) {
+            rsi16_encode_block_reg<EPL>(c, v, b, tw, lane);
+        } else {
             rsi16_encode_block(c, v, b, ws, lane);
+        }
+    }
+}
+
+__device__ void rsi16_item(const Rsi16Dev &c, const BatchItem &it, uint32_t *ws, bool decode) {
+    switch (c.ecc) {
+        case 32: rsi16_item_t<1>(c, it, ws, decode); break;
+        case 64: rsi16_item_t<2>(c, it, ws, decode); break;
+        case 128: rsi16_item_t<4>(c, it, ws, decode); break;
+        default: rsi16_item_t<0>(c, it, ws, decode); break;
     }
 }
 

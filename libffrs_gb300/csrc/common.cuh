@@ -50,6 +50,9 @@ cudaStream_t lib_stream();
 // k-th stream (mod kPipeStreams) of the chunked host-buffer pipelines
 constexpr size_t kPipeStreams = 3;
 cudaStream_t pipe_stream(size_t k);
+// blocks per chunk of a host-buffer pipeline: ffgpu_set_host_chunk_blocks, or
+// at least min_chunk and at most max_chunks chunks
+size_t host_chunk_blocks(size_t nblocks, size_t min_chunk, size_t max_chunks);
 
 // Optional per-kernel timing (ffgpu_timing_enable): while it is on, a
 // KernelTimer records a CUDA event pair around one launch on the launching

@@ -23,6 +23,14 @@ static std::mutex g_stream_mu;
 static cudaStream_t g_stream = nullptr;
 static int g_device = 0;
 
+static std::atomic<size_t> g_chunk_blocks{0};
+
+size_t host_chunk_blocks(size_t nblocks, size_t min_chunk, size_t max_chunks) {
+    const size_t fixed = g_chunk_blocks.load();
+    if (fixed) return fixed;
+    return std::max<size_t>(min_chunk, (nblocks + max_chunks - 1) / max_chunks);
+}
+
 // streams of the host-buffer pipelines (created on first use)
 cudaStream_t pipe_stream(size_t k) {
     static std::mutex mu;
@@ -81,6 +89,10 @@ extern "C" {
 const char *ffgpu_last_error(void) { return t_last_error.c_str(); }
 const char *ffgpu_version(void) { return "libffrs-gb300 0.1.0 (sm_103a)"; }
 uint64_t ffgpu_kernel_launches(void) { return g_launches.load(); }
+
+int ffgpu_set_host_chunk_blocks(size_t blocks) {
+    return guarded([&] { g_chunk_blocks.store(blocks); });
+}
 
 int ffgpu_timing_enable(int on) {
     return guarded([&] { g_timing.store(on != 0); });
@@ -257,7 +269,7 @@ int ffgpu_rs256_decode_host(const ffgpu_rs256 *code, uint8_t *data, uint8_t *par
         // chunks of blocks on the pipeline streams: the host-to-device copy of
         // one chunk, the decode of another and the copy back of a third
         // overlap (page-locked host memory moves at full speed)
-        const size_t chunk = std::max<size_t>(65536, (nblocks + 7) / 8);
+        const size_t chunk = host_chunk_blocks(nblocks, 524288, 4);
         size_t k = 0;
         for (size_t b0 = 0; b0 < nblocks; b0 += chunk, ++k) {
             cudaStream_t st = pipe_stream(k);

@@ -184,7 +184,7 @@ int ffgpu_rsi16_repair_host(const ffgpu_rsi16 *code, uint16_t *msg, uint16_t *pa
             // repairs over the pipeline streams (only when the repair
             // workspace lives in shared memory: the global fallback workspace
             // is one per thread and cannot serve concurrent streams)
-            const size_t chunk = std::max<size_t>(8192, (nblocks + 7) / 8);
+            const size_t chunk = host_chunk_blocks(nblocks, 32768, 4);
             size_t k = 0;
             for (size_t b0 = 0; b0 < nblocks; b0 += chunk, ++k) {
                 cudaStream_t ps = pipe_stream(k);

@@ -11,6 +11,7 @@
 #include <cstdint>
 #include <cstring>
 #include <stdexcept>
+#include <type_traits>
 #include <vector>
 
 #include "common.cuh"
@@ -171,11 +172,17 @@ __device__ __forceinline__ WarpCtx warp_ctx(uint32_t *gscratch, uint32_t ws_word
     return w;
 }
 
+// EPL > 0: ecc == 32 * EPL, the transforms run on registers
+template <int EPL>
 __global__ void rsi16_encode_warp_kernel(Rsi16Dev c, BlockView v, size_t nblocks, uint32_t *gscratch,
                                          uint32_t ws_words) {
     WarpCtx w = warp_ctx(gscratch, ws_words);
-    for (size_t b = w.warp_global; b < nblocks; b += w.nwarps) {
-        rsi16_encode_block(c, v, b, w.ws, w.lane);
+    if constexpr (EPL > 0) {
+        RegTw<EPL> tw;
+        reg_twiddles<EPL>(c, w.lane, tw);
+        for (size_t b = w.warp_global; b < nblocks; b += w.nwarps) rsi16_encode_block_reg<EPL>(c, v, b, tw, w.lane);
+    } else {
+        for (size_t b = w.warp_global; b < nblocks; b += w.nwarps) rsi16_encode_block(c, v, b, w.ws, w.lane);
     }
 }
 
@@ -193,13 +200,16 @@ __global__ void rsi16_synd_warp_kernel(Rsi16Dev c, BlockView v, size_t nblocks, 
 // blocks repaired by the bounded-distance path / by the step-for-step mirror
 __device__ unsigned long long g_repair_fast_blocks, g_repair_mirror_blocks;
 
+template <int EPL>
 __global__ void rsi16_repair_warp_kernel(Rsi16Dev c, BlockView v, size_t nblocks, uint8_t *status,
                                          const uint8_t *active, uint32_t *gscratch, uint32_t ws_words) {
     WarpCtx w = warp_ctx(gscratch, ws_words);
+    RegTw<EPL ? EPL : 1> tw;
+    if constexpr (EPL > 0) reg_twiddles<EPL>(c, w.lane, tw);
     unsigned long long nfast = 0, nmirror = 0;
     for (size_t b = w.warp_global; b < nblocks; b += w.nwarps) {
         if (active && !active[b]) continue;
-        if (rsi16_repair_bm_block(c, v, b, w.ws, status, w.lane)) {
+        if (rsi16_repair_bm_block_t<EPL>(c, v, b, w.ws, status, tw, w.lane)) {
             ++nfast;
         } else {
             rsi16_repair_block(c, v, b, w.ws, status, w.lane);
@@ -333,12 +343,25 @@ Launch plan(K kernel, size_t nblocks, uint32_t ws_words) {
 
 }  // namespace
 
+// register-NTT width for this code (0: the shared-memory transforms)
+static int reg_epl(const Rsi16Code &c) { return (c.ecc == 32 || c.ecc == 64 || c.ecc == 128) ? (int)(c.ecc / 32) : 0; }
+
+template <int EPL>
+static void launch_encode(const Rsi16Code &c, const BlockView &v, size_t nblocks, cudaStream_t st) {
+    Launch L = plan(rsi16_encode_warp_kernel<EPL>, nblocks, EPL ? 0u : (uint32_t)c.block_len);
+    KernelTimer kt_timer("rsi16_encode_warp_kernel", st);
+    rsi16_encode_warp_kernel<EPL><<<L.grid, L.threads, L.smem, st>>>(c.dev, v, nblocks, L.gscratch, L.ws_words);
+    check_launch("rsi16_encode_warp_kernel");
+}
+
 void rsi16_encode(const Rsi16Code &c, const BlockView &v, size_t nblocks, cudaStream_t st) {
     if (!nblocks) return;
-    Launch L = plan(rsi16_encode_warp_kernel, nblocks, (uint32_t)c.block_len);
-    KernelTimer kt_timer("rsi16_encode_warp_kernel", st);
-    rsi16_encode_warp_kernel<<<L.grid, L.threads, L.smem, st>>>(c.dev, v, nblocks, L.gscratch, L.ws_words);
-    check_launch("rsi16_encode_warp_kernel");
+    switch (reg_epl(c)) {
+        case 1: launch_encode<1>(c, v, nblocks, st); break;
+        case 2: launch_encode<2>(c, v, nblocks, st); break;
+        case 4: launch_encode<4>(c, v, nblocks, st); break;
+        default: launch_encode<0>(c, v, nblocks, st); break;
+    }
 }
 
 void rsi16_synd(const Rsi16Code &c, const BlockView &v, size_t nblocks, uint32_t *synds, cudaStream_t st) {
@@ -352,11 +375,20 @@ void rsi16_synd(const Rsi16Code &c, const BlockView &v, size_t nblocks, uint32_t
 void rsi16_repair(const Rsi16Code &c, const BlockView &v, size_t nblocks, uint8_t *status, cudaStream_t st,
                   const uint8_t *active) {
     if (!nblocks) return;
-    Launch L = plan(rsi16_repair_warp_kernel, nblocks, c.dev.temp_len + 1);
-    KernelTimer kt_timer("rsi16_repair_warp_kernel", st);
-    rsi16_repair_warp_kernel<<<L.grid, L.threads, L.smem, st>>>(c.dev, v, nblocks, status, active, L.gscratch,
-                                                                L.ws_words);
-    check_launch("rsi16_repair_warp_kernel");
+    auto go = [&](auto epl) {
+        constexpr int E = decltype(epl)::value;
+        Launch L = plan(rsi16_repair_warp_kernel<E>, nblocks, c.dev.temp_len + 1);
+        KernelTimer kt_timer("rsi16_repair_warp_kernel", st);
+        rsi16_repair_warp_kernel<E><<<L.grid, L.threads, L.smem, st>>>(c.dev, v, nblocks, status, active,
+                                                                       L.gscratch, L.ws_words);
+        check_launch("rsi16_repair_warp_kernel");
+    };
+    switch (reg_epl(c)) {
+        case 1: go(std::integral_constant<int, 1>{}); break;
+        case 2: go(std::integral_constant<int, 2>{}); break;
+        case 4: go(std::integral_constant<int, 4>{}); break;
+        default: go(std::integral_constant<int, 0>{}); break;
+    }
 }
 
 void rsi16_repair_known(const Rsi16Code &c, const BlockView &v, size_t nblocks, const uint32_t *pos,

@@ -419,6 +419,138 @@ static __device__ __forceinline__ uint32_t get_pos(const Rsi16Dev &c, const Bloc
     return ld_word(v.par, v.par16, v.poff(b, pos - c.message_len));
 }
 
+// ---------------------------------------------------------------- register NTTs
+//
+// For ecc = 32 * EPL (EPL = 1, 2, 4) a warp keeps one ecc-point vector in
+// registers: lane L holds elements e = L * EPL + h.  Butterfly partners closer
+// than EPL are in the same lane, the others in lane L ^ (stride / EPL) (one
+// shuffle).  The butterflies are the reference's ct_butterfly / gs_butterfly
+// (ntt.hpp:225-302) with the twiddle of each element preloaded per stage;
+// the twiddle of index 0 is 1, and fmul(x, 1) == x, so every element takes
+// the same path.
+
+template <int EPL>
+struct RegTw {
+    uint32_t ct[7][EPL];  // roots_ecc[ef * (e & (stride - 1))], stride = 1, 2, ...
+    uint32_t gs[7][EPL];  // roots_i_ecc[(e & (stride - 1)) << ef], stride = n/2, n/4, ...
+};
+
+template <int EPL>
+static __device__ __forceinline__ void reg_twiddles(const Rsi16Dev &c, int lane, RegTw<EPL> &tw) {
+    constexpr uint32_t n = 32 * EPL;
+    int st = 0;
+#pragma unroll
+    for (uint32_t stride = 1, ef = n >> 1; stride < n; stride <<= 1, ef >>= 1, ++st)
+#pragma unroll
+        for (int h = 0; h < EPL; ++h) tw.ct[st][h] = c.roots_ecc[ef * ((lane * EPL + h) & (stride - 1))];
+    st = 0;
+#pragma unroll
+    for (uint32_t stride = n >> 1, ef = 0; stride > 0; stride >>= 1, ++ef, ++st)
+#pragma unroll
+        for (int h = 0; h < EPL; ++h) tw.gs[st][h] = c.roots_i_ecc[((lane * EPL + h) & (stride - 1)) << ef];
+}
+
+// ct_butterfly on registers: RBO input, normal order output
+template <int EPL>
+static __device__ __forceinline__ void reg_ct(uint32_t (&x)[EPL], const RegTw<EPL> &tw, int lane) {
+    constexpr int n = 32 * EPL;
+    int st = 0;
+#pragma unroll
+    for (int stride = 1; stride < n; stride <<= 1, ++st) {
+        if (stride < EPL) {
+#pragma unroll
+            for (int h = 0; h < EPL; ++h) {
+                if (h & stride) continue;
+                const uint32_t a = x[h], m = fmul(x[h + stride], tw.ct[st][h]);
+                x[h] = fadd(a, m);
+                x[h + stride] = fsub(a, m);
+            }
+        } else {
+            const int lm = stride / EPL;
+            const bool upper = (lane & lm) != 0;
+#pragma unroll
+            for (int h = 0; h < EPL; ++h) {
+                const uint32_t p = __shfl_xor_sync(0xffffffffu, x[h], lm);
+                const uint32_t m = fmul(upper ? x[h] : p, tw.ct[st][h]);
+                x[h] = upper ? fsub(p, m) : fadd(x[h], m);
+            }
+        }
+    }
+}
+
+// gs_butterfly on registers: normal order input, RBO output
+template <int EPL>
+static __device__ __forceinline__ void reg_gs(uint32_t (&x)[EPL], const RegTw<EPL> &tw, int lane) {
+    constexpr int n = 32 * EPL;
+    int st = 0;
+#pragma unroll
+    for (int stride = n >> 1; stride > 0; stride >>= 1, ++st) {
+        if (stride < EPL) {
+#pragma unroll
+            for (int h = 0; h < EPL; ++h) {
+                if (h & stride) continue;
+                const uint32_t a = x[h], bb = x[h + stride];
+                x[h] = fadd(a, bb);
+                x[h + stride] = fmul(fsub(a, bb), tw.gs[st][h + stride]);
+            }
+        } else {
+            const int lm = stride / EPL;
+            const bool upper = (lane & lm) != 0;
+#pragma unroll
+            for (int h = 0; h < EPL; ++h) {
+                const uint32_t p = __shfl_xor_sync(0xffffffffu, x[h], lm);
+                x[h] = upper ? fmul(fsub(p, x[h]), tw.gs[st][h]) : fadd(x[h], p);
+            }
+        }
+    }
+}
+
+// NTT::pntt (ntt.hpp:133-152) of block b over nchunks chunks (at least chunk
+// 0): S = sum_ch ct(chunk_ch) * pntt_shift_ch.  Words past the message are the
+// parity (with_parity) or zeros.
+template <int EPL>
+static __device__ __forceinline__ void reg_pntt(const Rsi16Dev &c, const BlockView &v, size_t b, uint32_t nchunks,
+                                                bool with_parity, const RegTw<EPL> &tw, int lane,
+                                                uint32_t (&acc)[EPL]) {
+    constexpr uint32_t n = 32 * EPL;
+    const size_t mb = (b / v.group) * v.msg_gstride + (b % v.group) * v.msg_bstride;
+    const size_t pb = (b / v.group) * v.par_gstride + (b % v.group) * v.par_bstride;
+    const uint32_t nch = nchunks ? nchunks : 1;
+    for (uint32_t ch = 0; ch < nch; ++ch) {
+        uint32_t x[EPL];
+#pragma unroll
+        for (int h = 0; h < EPL; ++h) {
+            const uint32_t k = ch * n + lane * EPL + h;
+            uint32_t w = 0;
+            if (k < c.message_len)
+                w = ld_word(v.msg, v.msg16, mb + (size_t)k * v.msg_estride);
+            else if (with_parity && k < c.block_len)
+                w = ld_word(v.par, v.par16, pb + (size_t)(k - c.message_len) * v.par_estride);
+            x[h] = w;
+        }
+        reg_ct<EPL>(x, tw, lane);
+#pragma unroll
+        for (int h = 0; h < EPL; ++h) {
+            const uint32_t y = fmul(x[h], c.pntt_shift[ch * n + lane * EPL + h]);
+            acc[h] = ch ? fadd(acc[h], y) : y;
+        }
+    }
+}
+
+// parity of block b with the vector in registers
+template <int EPL>
+static __device__ __forceinline__ void rsi16_encode_block_reg(const Rsi16Dev &c, const BlockView &v, size_t b,
+                                                              const RegTw<EPL> &tw, int lane) {
+    uint32_t acc[EPL];
+    reg_pntt<EPL>(c, v, b, c.pntt_blocks - 1, false, tw, lane, acc);
+#pragma unroll
+    for (int h = 0; h < EPL; ++h) acc[h] = fmul(acc[h], c.ecc_mix[lane * EPL + h]);
+    reg_gs<EPL>(acc, tw, lane);
+    const size_t pb = (b / v.group) * v.par_gstride + (b % v.group) * v.par_bstride;
+#pragma unroll
+    for (int h = 0; h < EPL; ++h) st_word(v.par, v.par16, pb + (size_t)(lane * EPL + h) * v.par_estride, acc[h]);
+}
+
 // ---------------------------------------------------------------- one block per warp
 
 // parity of block b (ws: block_len words)
@@ -501,15 +633,33 @@ static __device__ __noinline__ void rsi16_repair_block(const Rsi16Dev &c, const 
 // C'(X_i^-1) and RepairOk.  Returns false (block untouched) otherwise; the
 // caller then runs the reference's algorithm step for step.
 // temp: ntt_len + 6 * ecc words.
-static __device__ __noinline__ bool rsi16_repair_bm_block(const Rsi16Dev &c, const BlockView &v, size_t b,
-                                                         uint32_t *temp, uint8_t *status, int lane) {
+template <int EPL>
+static __device__ __noinline__ bool rsi16_repair_bm_block_t(const Rsi16Dev &c, const BlockView &v, size_t b,
+                                                           uint32_t *temp, uint8_t *status,
+                                                           const RegTw<EPL ? EPL : 1> &tw, int lane) {
     const uint32_t ecc = c.ecc, t = ecc / 2, n1 = ecc + 1;
-    w_gather(c, v, b, temp, true, lane);
-    w_pntt(c, temp, c.pntt_blocks, lane);
     uint32_t *S = temp;
-    if (w_all_zero(S, ecc, lane)) {
-        if (lane == 0) status[b] = FFGPU_NO_ERRORS;
-        return true;
+    if constexpr (EPL > 0) {
+        uint32_t s[EPL];
+        reg_pntt<EPL>(c, v, b, c.pntt_blocks, true, tw, lane, s);
+        bool nz = false;
+#pragma unroll
+        for (int h = 0; h < EPL; ++h) {
+            S[lane * EPL + h] = s[h];
+            nz |= s[h] != 0;
+        }
+        __syncwarp();
+        if (!__any_sync(0xffffffffu, nz)) {
+            if (lane == 0) status[b] = FFGPU_NO_ERRORS;
+            return true;
+        }
+    } else {
+        w_gather(c, v, b, temp, true, lane);
+        w_pntt(c, temp, c.pntt_blocks, lane);
+        if (w_all_zero(S, ecc, lane)) {
+            if (lane == 0) status[b] = FFGPU_NO_ERRORS;
+            return true;
+        }
     }
     uint32_t *C = temp + ecc, *B = C + n1, *T = B + n1;
     for (uint32_t k = lane; k < n1; k += 32) {
@@ -553,20 +703,42 @@ static __device__ __noinline__ bool rsi16_repair_bm_block(const Rsi16Dev &c, con
     for (uint32_t k = lane; k < n1; k += 32)
         if (k > L && C[k]) L = 0xffffffffu;
     if (__any_sync(0xffffffffu, L == 0xffffffffu)) return false;
-    // roots: the inverse partial NTT evaluates C at X_i^-1 for every position
-    uint32_t *R = temp + ecc + 3 * n1;  // block_len words, past S, C, B and T
-    for (uint32_t k = lane; k < c.block_len; k += 32) R[k] = k <= L ? C[k] : 0u;
-    __syncwarp();
-    w_pintt(c, R, lane);
-    // root positions, compacted into T (free after BM; at most ecc + 1 kept)
+    // roots: the inverse partial NTT (pintt_ecc, ntt.hpp:206-220) evaluates C
+    // at X_i^-1 for every position; the positions found are compacted into T
+    // (free after BM; at most ecc + 1 kept)
     uint32_t count = 0;
-    for (uint32_t i0 = 0; i0 < c.block_len; i0 += 32) {
-        const uint32_t i = i0 + lane;
-        const bool hit = i < c.block_len && R[i] == 0;
-        const uint32_t msk = __ballot_sync(0xffffffffu, hit);
-        const uint32_t at = count + __popc(msk & ((1u << lane) - 1u));
-        if (hit && at < n1) T[at] = i;
-        count += __popc(msk);
+    if constexpr (EPL > 0) {
+        uint32_t cr[EPL];
+#pragma unroll
+        for (int h = 0; h < EPL; ++h) cr[h] = (uint32_t)(lane * EPL + h) <= L ? C[lane * EPL + h] : 0u;
+        const uint32_t nch = c.block_len / ecc;
+        for (uint32_t ch = 0; ch < nch; ++ch) {
+            uint32_t x[EPL];
+#pragma unroll
+            for (int h = 0; h < EPL; ++h) x[h] = fmul(cr[h], c.pintt_shift[ch * ecc + lane * EPL + h]);
+            reg_gs<EPL>(x, tw, lane);
+#pragma unroll
+            for (int h = 0; h < EPL; ++h) {
+                const bool hit = x[h] == 0;
+                const uint32_t msk = __ballot_sync(0xffffffffu, hit);
+                const uint32_t at = count + __popc(msk & ((1u << lane) - 1u));
+                if (hit && at < n1) T[at] = ch * ecc + lane * EPL + h;
+                count += __popc(msk);
+            }
+        }
+    } else {
+        uint32_t *R = temp + ecc + 3 * n1;  // block_len words, past S, C, B and T
+        for (uint32_t k = lane; k < c.block_len; k += 32) R[k] = k <= L ? C[k] : 0u;
+        __syncwarp();
+        w_pintt(c, R, lane);
+        for (uint32_t i0 = 0; i0 < c.block_len; i0 += 32) {
+            const uint32_t i = i0 + lane;
+            const bool hit = i < c.block_len && R[i] == 0;
+            const uint32_t msk = __ballot_sync(0xffffffffu, hit);
+            const uint32_t at = count + __popc(msk & ((1u << lane) - 1u));
+            if (hit && at < n1) T[at] = i;
+            count += __popc(msk);
+        }
     }
     __syncwarp();
     if (count != L) return false;
@@ -598,6 +770,12 @@ static __device__ __noinline__ bool rsi16_repair_bm_block(const Rsi16Dev &c, con
     __syncwarp();
     if (lane == 0) status[b] = FFGPU_REPAIR_OK;
     return true;
+}
+
+static __device__ __forceinline__ bool rsi16_repair_bm_block(const Rsi16Dev &c, const BlockView &v, size_t b,
+                                                            uint32_t *temp, uint8_t *status, int lane) {
+    const RegTw<1> none{};
+    return rsi16_repair_bm_block_t<0>(c, v, b, temp, status, none, lane);
 }
 
 // RSi16v::_repair with known locations (rsi16v_impl.hpp:171-231),
