@@ -46,6 +46,13 @@ cudaStream_t lib_stream() {
     if (!g_stream) {
         FFGPU_CHECK_CUDA(cudaSetDevice(g_device));
         FFGPU_CHECK_CUDA(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking));
+        // the per-call scratch comes from the stream-ordered pool; keep freed
+        // blocks in the pool across synchronisations instead of unmapping them
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, g_device) == cudaSuccess) {
+            uint64_t keep = ~0ull;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
     }
     return g_stream;
 }

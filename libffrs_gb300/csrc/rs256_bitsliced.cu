@@ -682,6 +682,189 @@ __global__ void __launch_bounds__(kGroups * 2) bs_encode32_kernel(const uint8_t 
 }
 
 
+// ---------------------------------------------------------------- segmented encode
+//
+// For batches too small to fill the GPU at one thread per (group, factor), the
+// message is also cut into kSegs segments of kSegLen bytes counted from its
+// end: with seg_s the bytes of segment s (s = 0 last),
+//   data * x^16 mod g_t = sum_s (seg_s * x^16 mod g_t) * x^(kSegLen * s) mod g_t,
+// so every (group, factor, segment) runs its own LFSR from zero and the
+// results meet through the fixed linear maps x^(kSegLen * s) mod g_t (compile
+// time, one four-Russians pass like the syndrome map), then the Chinese
+// remainder map of the unsegmented kernel.
+
+constexpr int kSegs = 4, kSegLen = 56;  // 4 * 56 >= 223, the largest ecc-32 message
+
+// SegSel: [t][s][m][p][o] input-bit mask of output bit o of R'[p] for input byte m
+struct SegSel {
+    uint8_t s[2][kSegs][16][16][8];
+};
+
+constexpr SegSel make_seg_sel() {
+    SegSel S{};
+    for (int t = 0; t < 2; ++t) {
+        const Poly<16> g = factor_poly<16>(16 * t);
+        // r = x^k mod g_t, highest degree first (r[p]: coefficient of x^(15-p))
+        uint8_t r[16] = {};
+        r[15] = 1;
+        for (int k = 0; k <= 15 + kSegLen * (kSegs - 1); ++k) {
+            // record x^k for every (s, m) with 15 - m + kSegLen * s == k
+            for (int s = 0; s < kSegs; ++s) {
+                const int m = 15 + kSegLen * s - k;
+                if (m >= 0 && m < 16)
+                    for (int p = 0; p < 16; ++p)
+                        for (int o = 0; o < 8; ++o) S.s[t][s][m][p][o] = sel_of(r[p], o);
+            }
+            // r <- r * x mod g_t
+            const uint8_t top = r[0];
+            for (int p = 0; p < 15; ++p) r[p] = r[p + 1];
+            r[15] = 0;
+            for (int p = 0; p < 16; ++p) r[p] ^= gm(top, g.c[p + 1]);
+        }
+    }
+    return S;
+}
+
+struct SegHolder {
+    static constexpr SegSel seg = make_seg_sel();
+};
+
+// out[p][o] (p = 8h .. 8h+7) ^= (x^(kSegLen s) mod g_t applied to input byte M)
+template <int T, int S, int M, int H, int... K>
+__device__ __forceinline__ void seg_accum(uint32_t (&out)[8][8], const uint32_t (&lo)[16], const uint32_t (&hi)[16],
+                                          std::integer_sequence<int, K...>) {
+    ((out[K / 8][K % 8] = pickx<SegHolder::seg.s[T][S][M][H * 8 + K / 8][K % 8]>(out[K / 8][K % 8], lo, hi)), ...);
+}
+
+// half H of R' = R * x^(kSegLen S) mod g_T, R read from the stash (16 bytes x 8 planes)
+template <int T, int S, int H, int... M>
+__device__ __forceinline__ void seg_map_half(const uint32_t *rs, int stride, uint32_t (&out)[8][8],
+                                             std::integer_sequence<int, M...>) {
+    auto one = [&](auto mc) {
+        constexpr int m = decltype(mc)::value;
+        uint32_t r[8];
+#pragma unroll
+        for (int b = 0; b < 8; ++b) r[b] = rs[(m * 8 + b) * stride];
+        uint32_t lo[16], hi[16];
+        combos(r, lo, hi);
+        seg_accum<T, S, m, H>(out, lo, hi, std::make_integer_sequence<int, 64>{});
+    };
+    (one(std::integral_constant<int, M>{}), ...);
+}
+
+// maps this thread's stashed remainder in place (both halves)
+template <int T, int S>
+__device__ __forceinline__ void seg_map(uint32_t *rs, int stride) {
+    uint32_t o0[8][8], o1[8][8];
+#pragma unroll
+    for (int p = 0; p < 8; ++p)
+#pragma unroll
+        for (int o = 0; o < 8; ++o) {
+            o0[p][o] = 0u;
+            o1[p][o] = 0u;
+        }
+    seg_map_half<T, S, 0>(rs, stride, o0, std::make_integer_sequence<int, 16>{});
+    seg_map_half<T, S, 1>(rs, stride, o1, std::make_integer_sequence<int, 16>{});
+#pragma unroll
+    for (int p = 0; p < 8; ++p)
+#pragma unroll
+        for (int o = 0; o < 8; ++o) {
+            rs[(p * 8 + o) * stride] = o0[p][o];
+            rs[((8 + p) * 8 + o) * stride] = o1[p][o];
+        }
+}
+
+// CTA: 32 groups (1024 blocks), warp w = (factor t = w & 1, segment s = w >> 1)
+__global__ void __launch_bounds__(64 * kSegs) bs_encode32_seg_kernel(const uint8_t *__restrict__ data,
+                                                                     size_t nblocks, int msg_len,
+                                                                     uint8_t *__restrict__ parity) {
+    constexpr int E = 32, D = 16, G = 32;
+    extern __shared__ __align__(16) uint32_t sm[];  // kSegs window buffers of G * 256 words
+    const int warp = threadIdx.x >> 5, g = threadIdx.x & 31;
+    const int t = warp & 1, s = warp >> 1;
+    const size_t first = (size_t)blockIdx.x * G * 32;
+    const int nb_tile = (int)min((size_t)G * 32, nblocks - first);
+    const int end_s = msg_len - kSegLen * s;
+    const int start_s = max(0, msg_len - kSegLen * (s + 1));
+    uint32_t *mybuf = sm + s * (G * 256);
+    uint32_t R[D][8];
+#pragma unroll
+    for (int m = 0; m < D; ++m)
+#pragma unroll
+        for (int b = 0; b < 8; ++b) R[m][b] = 0u;
+    const size_t total = nblocks * (size_t)msg_len;
+    for (int w0 = 0; w0 < kSegLen; w0 += 32) {
+        __syncthreads();
+        for (int ss = 0; ss < kSegs; ++ss) {
+            const int p0 = max(0, msg_len - kSegLen * (ss + 1)) + w0;
+            if (p0 < msg_len - kSegLen * ss) load_window(sm + ss * (G * 256), data, (size_t)msg_len, total, first,
+                                                         nb_tile, p0, G);
+        }
+        __syncthreads();
+        const int npos = min(32, end_s - (start_s + w0));
+        if (npos > 0) transpose_window<2>(mybuf, g, t);
+        __syncthreads();
+        if (npos > 0) {
+            if (t == 0)
+                run_lfsr_window<E, 0>(mybuf, g, npos, R);
+            else
+                run_lfsr_window<E, 1>(mybuf, g, npos, R);
+        }
+    }
+    __syncthreads();
+    // stash: [warp][m*8+b][g], stride G
+    uint32_t *rs = sm + warp * (128 * G) + g;
+#pragma unroll
+    for (int m = 0; m < D; ++m)
+#pragma unroll
+        for (int b = 0; b < 8; ++b) rs[(m * 8 + b) * G] = R[m][b];
+    // segment maps (each thread rewrites only its own stash)
+    switch (warp) {
+        case 2: seg_map<0, 1>(rs, G); break;
+        case 3: seg_map<1, 1>(rs, G); break;
+        case 4: seg_map<0, 2>(rs, G); break;
+        case 5: seg_map<1, 2>(rs, G); break;
+        case 6: seg_map<0, 3>(rs, G); break;
+        case 7: seg_map<1, 3>(rs, G); break;
+        default: break;
+    }
+    __syncthreads();
+    // sum the segments of each factor into the CRT layout [(t*16+m)*8+b][g]
+    uint32_t *crt = sm + 2 * kSegs * 128 * G;  // past the stashes
+    if (s == 0) {
+#pragma unroll 4
+        for (int k = 0; k < 128; ++k) {
+            uint32_t v = 0u;
+#pragma unroll
+            for (int ss = 0; ss < kSegs; ++ss) v ^= sm[(ss * 2 + t) * (128 * G) + k * G + g];
+            crt[(t * 128 + k) * G + g] = v;
+        }
+    }
+    __syncthreads();
+    if (s != 0) return;
+    uint32_t Pp[16][8];
+#pragma unroll
+    for (int p = 0; p < 16; ++p)
+#pragma unroll
+        for (int o = 0; o < 8; ++o) Pp[p][o] = 0u;
+    if (t == 0)
+        crt_map<0>(crt + g, G, Pp, std::make_integer_sequence<int, 32>{});
+    else
+        crt_map<16>(crt + g, G, Pp, std::make_integer_sequence<int, 32>{});
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        uint32_t a[32];
+#pragma unroll
+        for (int k = 0; k < 32; ++k) a[k] = Pp[q * 4 + k / 8][k % 8];
+        transpose32(a);
+        const int pb = t * 16 + q * 4;
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+            if ((int)(g * 32 + j) < nb_tile)
+                *reinterpret_cast<uint32_t *>(parity + (first + (size_t)g * 32 + j) * E + pb) = a[j];
+    }
+}
+
 // ---------------------------------------------------------------- bitsliced solve
 //
 // Decoding from the bitsliced syndromes, 32 blocks per plane word, following
@@ -1190,6 +1373,17 @@ bool rs256_fast_encode(const Rs256Code &c, const uint8_t *data, size_t nblocks, 
                        cudaStream_t st) {
     if (!c.fast || c.table_only || c.ecc != 32 || !aligned4(data) || !aligned4(parity)) return false;
     if (!nblocks) return true;
+    const size_t seg_ctas = (nblocks + 1023) / 1024;
+    if (msg_len <= bs::kSegs * bs::kSegLen && seg_ctas <= (size_t)sm_count() * 4) {
+        // too few groups to fill the GPU: split the messages into segments too
+        constexpr size_t smem = (size_t)(4 * 32 * 256 + 2 * 128 * 32) * 4;
+        FFGPU_CHECK_CUDA(
+            cudaFuncSetAttribute(bs::bs_encode32_seg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        KernelTimer kt_timer("bs_encode32_seg_kernel", st);
+        bs::bs_encode32_seg_kernel<<<(unsigned)seg_ctas, 64 * bs::kSegs, smem, st>>>(data, nblocks, msg_len, parity);
+        check_launch("bs_encode32_seg_kernel");
+        return true;
+    }
     KernelTimer kt_timer("bs_encode32_kernel", st);
     bs::bs_encode32_kernel<<<tiles_grid(nblocks), bs::kGroups * 2, 0, st>>>(data, nblocks, msg_len, parity);
     check_launch("bs_encode32_kernel");
