@@ -644,17 +644,29 @@ def make_mixed(torch, total_bytes, seed):
         r["data0"], r["par0"] = msg.clone(), par.clone()
         reqs.append(r)
         used += nb * bl * 2
-    # CIRC16 (encode)
+    # CIRC16: half encode, half decode with one burst of 1..64 consecutive
+    # message words changed per codeword
     used = 0
     c = code("circ16", 128, 8, 128, 8, 4)
     cwb = (c.message_len + c.ecc_len) * 2
     while used < budget["circ16"]:
         nb = int(np.exp(rng.uniform(np.log(1), np.log(64))))
         nb = max(1, min(nb, (budget["circ16"] - used) // cwb + 1))
+        dec = bool(rng.integers(0, 2))
         msg = torch.randint(-32768, 32768, (nb, c.message_len), dtype=torch.int16, device="cuda", generator=g)
         ecc = torch.zeros((nb, c.ecc_len), dtype=torch.int16, device="cuda")
-        reqs.append({"kind": "circ16", "code": c, "op": "enc", "nb": nb, "data": msg, "par": ecc,
-                     "data0": msg, "par0": ecc, "status": None})
+        r = {"kind": "circ16", "code": c, "op": "dec" if dec else "enc", "nb": nb, "data": msg, "par": ecc,
+             "status": torch.zeros(nb, dtype=torch.uint8, device="cuda") if dec else None}
+        if dec:
+            c.encode(msg.data_ptr(), nb, ecc.data_ptr(), st)
+            for i in range(nb):
+                blen = int(rng.integers(1, 65))
+                s0 = int(rng.integers(0, c.message_len - blen + 1))
+                d = torch.from_numpy(rng.integers(1, 65536, blen).astype(np.int32)).cuda()
+                v = msg[i, s0:s0 + blen].to(torch.int32) & 0xFFFF
+                msg[i, s0:s0 + blen] = ((v + d) & 0xFFFF).to(torch.int16)
+        r["data0"], r["par0"] = msg.clone(), ecc.clone()
+        reqs.append(r)
         used += nb * cwb
     order = rng.permutation(len(reqs))
     reqs = [reqs[i] for i in order]
@@ -687,8 +699,10 @@ def mixed_plain(reqs, stream):
                 c.encode(r["data"].data_ptr(), r["nb"], r["par"].data_ptr(), stream)
             else:
                 c.repair(r["data"].data_ptr(), r["par"].data_ptr(), r["nb"], r["status"].data_ptr(), stream)
-        else:
+        elif r["op"] == "enc":
             c.encode(r["data"].data_ptr(), r["nb"], r["par"].data_ptr(), stream)
+        else:
+            c.repair(r["data"].data_ptr(), r["par"].data_ptr(), r["nb"], r["status"].data_ptr(), stream)
 
 
 def mixed_batch(reqs):
@@ -704,7 +718,7 @@ def mixed_batch(reqs):
         elif r["kind"] == "rsi16":
             b.add_rsi16(c, op, r["data"].data_ptr(), r["par"].data_ptr(), r["nb"], st)
         else:
-            b.add_circ16(c, r["data"].data_ptr(), r["par"].data_ptr(), r["nb"])
+            b.add_circ16(c, r["data"].data_ptr(), r["par"].data_ptr(), r["nb"], op, st)
     return b
 
 
@@ -774,7 +788,8 @@ def bench_batch_mixed(args, torch, rank, world):
         "e2e": {"value": None, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
                 "note": "device-resident batch; host-buffer serving is the serving workload"},
         "config": {"workload": "mixed batch: 1/2 RS256 (ecc 2..64, uneven lengths), 1/4 RSi16 (ecc 16..128, "
-                               "block 256..4096), 1/4 CIRC16(128,8,128,8,4); half encode, half decode",
+                               "block 256..4096), 1/4 CIRC16(128,8,128,8,4) with 1-64 word bursts; "
+                               "half encode, half decode",
                    "bytes": nbytes, "requests": len(reqs), "requests_by_kind": nk, "plan": b.info(),
                    "l2": "inputs larger than L2 (%d MB)" % (nbytes >> 20)},
         "dtype": "u8 / u32 mod 65537",
@@ -791,7 +806,7 @@ def make_serving_requests(n, seed, load_gbs):
     `load_gbs` GB/s of offered codeword bytes, log-normal payloads clipped to
     [4 KiB, 64 MiB]; codes RS256 ecc 8 / 32 (255-byte blocks), RSi16(1024, 64),
     CIRC16(128, 8, 128, 8, 4); 70% encode, 30% decode with 0..max correctable
-    errors per block (CIRC16 requests are encodes).  Decode inputs are encoded
+    errors per block (CIRC16: one burst of 1..64 message words).  Decode inputs are encoded
     with the host API and corrupted on the host."""
     import ctypes
 
@@ -813,7 +828,7 @@ def make_serving_requests(n, seed, load_gbs):
     for i in range(n):
         size = int(np.clip(np.exp(rng.normal(np.log(1 << 20), 1.5)), 4096, 64 << 20))
         kind = rng.choice(["rs8", "rs32", "rsi", "circ"])
-        dec = rng.random() < 0.3 and kind != "circ"
+        dec = rng.random() < 0.3
         c = codes[kind]
         r = {"kind": kind, "op": "dec" if dec else "enc", "code": c, "bufs": []}
         if kind in ("rs8", "rs32"):
@@ -867,6 +882,13 @@ def make_serving_requests(n, seed, load_gbs):
             pb, b = pinned(nb * c.ecc_len * 2, np.uint16)
             a[:] = rng.integers(0, 65536, a.size, dtype=np.uint16)
             r.update(nb=nb, a=a, b=b, pa=pa, pb=pb, nbytes=nb * cwb)
+            if dec:
+                capi.call("ffgpu_circ16_encode_host", c.h, pa, nb, pb)
+                m = a.reshape(nb, c.message_len)
+                for j in range(nb):  # one burst of 1..64 words per codeword
+                    blen = int(rng.integers(1, 65))
+                    s0 = int(rng.integers(0, c.message_len - blen + 1))
+                    m[j, s0:s0 + blen] += rng.integers(1, 65536, blen).astype(np.uint16)
         if dec:
             ps, s = pinned(r["nb"], np.uint8)
             r.update(ps=ps, s=s)
@@ -898,8 +920,10 @@ def serve_plain_one(r):
             capi.call("ffgpu_rsi16_encode_host", c.h, r["pa"], r["nb"], 1, r["pb"])
         else:
             capi.call("ffgpu_rsi16_repair_host", c.h, r["pa"], r["pb"], r["nb"], 1, None, -1, r["ps"])
-    else:
+    elif r["op"] == "enc":
         capi.call("ffgpu_circ16_encode_host", c.h, r["pa"], r["nb"], r["pb"])
+    else:
+        capi.call("ffgpu_circ16_repair_host", c.h, r["pa"], r["pb"], r["nb"], r["ps"])
 
 
 def serve_submit(srv, r):
@@ -911,7 +935,7 @@ def serve_submit(srv, r):
         return srv.submit_rs256(c, op, r["pa"], r["pb"], r["nb"], r["ml"], r.get("ps"))
     if r["kind"] == "rsi":
         return srv.submit_rsi16(c, op, r["pa"], r["pb"], r["nb"], r.get("ps"))
-    return srv.submit_circ16(c, r["pa"], r["pb"], r["nb"])
+    return srv.submit_circ16(c, r["pa"], r["pb"], r["nb"], op, r.get("ps"))
 
 
 def run_served(reqs, slots=4):
@@ -984,7 +1008,8 @@ def bench_serving(args, torch, rank, world):
         "e2e": {"value": gbs, "unit": "GB/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                 "api": "ffgpu_server_submit_* on page-locked host buffers"},
         "config": {"workload": "serving: Poisson arrivals at %.0f GB/s offered, log-normal payloads 4 KiB-64 MiB, "
-                               "RS256 ecc 8/32, RSi16(1024,64), CIRC16(128,8,128,8,4), 70%% encode" % load,
+                               "RS256 ecc 8/32, RSi16(1024,64), CIRC16(128,8,128,8,4), 70%% encode, decodes with "
+                               "0..max correctable errors (CIRC16: one 1-64 word burst)" % load,
                    "requests": nreq, "bytes": nbytes, "slots": 4},
         "dtype": "u8 / u32 mod 65537",
         "extra": {"served_p50_ms": pct(lat, 50), "served_p99_ms": pct(lat, 99), "served_gbs": gbs,

@@ -228,9 +228,10 @@ FFGPU_API int ffgpu_batch_add_rs256(ffgpu_batch *batch, const ffgpu_rs256 *code,
 /* RSi16: as ffgpu_rsi16_encode / ffgpu_rsi16_repair */
 FFGPU_API int ffgpu_batch_add_rsi16(ffgpu_batch *batch, const ffgpu_rsi16 *code, int op, uint16_t *msg,
                                     uint16_t *parity, size_t nblocks, uint8_t *status);
-/* CIRC16: ENCODE only, as ffgpu_circ16_encode */
+/* CIRC16: as ffgpu_circ16_encode / ffgpu_circ16_repair (one codeword per
+ * work item, its whole CircRepair inside one CTA; status 0 or 0xFF) */
 FFGPU_API int ffgpu_batch_add_circ16(ffgpu_batch *batch, const ffgpu_circ16 *code, int op, uint16_t *msg,
-                                     uint16_t *ecc, size_t nblocks);
+                                     uint16_t *ecc, size_t nblocks, uint8_t *status);
 /* cut the requests into work items (longest first) and upload them; with
  * autotune != 0, candidate schedules (RS256 blocks per item, RSi16 blocks per
  * item, CTAs per SM) are timed on the batch itself -- decode buffers are saved
@@ -263,7 +264,7 @@ FFGPU_API int ffgpu_server_submit_rs256(ffgpu_server *server, const ffgpu_rs256 
 FFGPU_API int ffgpu_server_submit_rsi16(ffgpu_server *server, const ffgpu_rsi16 *code, int op, uint16_t *msg,
                                         uint16_t *parity, size_t nblocks, uint8_t *status, uint64_t *ticket);
 FFGPU_API int ffgpu_server_submit_circ16(ffgpu_server *server, const ffgpu_circ16 *code, int op, uint16_t *msg,
-                                         uint16_t *ecc, size_t nblocks, uint64_t *ticket);
+                                         uint16_t *ecc, size_t nblocks, uint8_t *status, uint64_t *ticket);
 /* state: 0 queued, 1 running, 2 done, 3 failed; times are seconds since the
  * server was created (submitted, admitted into a slot, completion seen) */
 FFGPU_API int ffgpu_server_poll(ffgpu_server *server, uint64_t ticket, int *state, double *t_submit,

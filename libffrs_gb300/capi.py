@@ -105,7 +105,7 @@ def _declare(L):
         "ffgpu_server_destroy": (_I, [_P]),
         "ffgpu_server_submit_rs256": (_I, [_P, _P, _I, _P, _P, _SZ, _SZ, _P, ctypes.POINTER(ctypes.c_uint64)]),
         "ffgpu_server_submit_rsi16": (_I, [_P, _P, _I, _P, _P, _SZ, _P, ctypes.POINTER(ctypes.c_uint64)]),
-        "ffgpu_server_submit_circ16": (_I, [_P, _P, _I, _P, _P, _SZ, ctypes.POINTER(ctypes.c_uint64)]),
+        "ffgpu_server_submit_circ16": (_I, [_P, _P, _I, _P, _P, _SZ, _P, ctypes.POINTER(ctypes.c_uint64)]),
         "ffgpu_server_poll": (_I, [_P, ctypes.c_uint64, ctypes.POINTER(_I)] + [ctypes.POINTER(ctypes.c_double)] * 3),
         "ffgpu_server_wait": (_I, [_P, ctypes.c_uint64, ctypes.c_double]),
         "ffgpu_server_release": (_I, [_P, ctypes.c_uint64]),
@@ -114,7 +114,7 @@ def _declare(L):
         "ffgpu_batch_clear": (_I, [_P]),
         "ffgpu_batch_add_rs256": (_I, [_P, _P, _I, _P, _P, _SZ, _SZ, _P]),
         "ffgpu_batch_add_rsi16": (_I, [_P, _P, _I, _P, _P, _SZ, _P]),
-        "ffgpu_batch_add_circ16": (_I, [_P, _P, _I, _P, _P, _SZ]),
+        "ffgpu_batch_add_circ16": (_I, [_P, _P, _I, _P, _P, _SZ, _P]),
         "ffgpu_batch_plan": (_I, [_P, _I, _P]),
         "ffgpu_batch_capture": (_I, [_P, _P]),
         "ffgpu_batch_launch": (_I, [_P, _P]),
@@ -240,9 +240,9 @@ class Batch:
         self._keep.append(code)
         call("ffgpu_batch_add_rsi16", self.h, code.h, op, msg_ptr, parity_ptr, nblocks, status_ptr)
 
-    def add_circ16(self, code, msg_ptr, ecc_ptr, nblocks):
+    def add_circ16(self, code, msg_ptr, ecc_ptr, nblocks, op=ENCODE, status_ptr=None):
         self._keep.append(code)
-        call("ffgpu_batch_add_circ16", self.h, code.h, ENCODE, msg_ptr, ecc_ptr, nblocks)
+        call("ffgpu_batch_add_circ16", self.h, code.h, op, msg_ptr, ecc_ptr, nblocks, status_ptr)
 
     def plan(self, autotune=False, stream=None):
         call("ffgpu_batch_plan", self.h, 1 if autotune else 0, stream)
@@ -293,8 +293,8 @@ class Server:
         return self._t((code, keep), "ffgpu_server_submit_rsi16", code.h, op, msg_ptr, parity_ptr, nblocks,
                        status_ptr)
 
-    def submit_circ16(self, code, msg_ptr, ecc_ptr, nblocks, keep=None):
-        return self._t((code, keep), "ffgpu_server_submit_circ16", code.h, ENCODE, msg_ptr, ecc_ptr, nblocks)
+    def submit_circ16(self, code, msg_ptr, ecc_ptr, nblocks, op=ENCODE, status_ptr=None, keep=None):
+        return self._t((code, keep), "ffgpu_server_submit_circ16", code.h, op, msg_ptr, ecc_ptr, nblocks, status_ptr)
 
     def wait(self, ticket, timeout=-1.0):
         call("ffgpu_server_wait", self.h, ticket, timeout)

@@ -17,6 +17,7 @@
 #include <string>
 #include <vector>
 
+#include "circ16_device.cuh"
 #include "common.cuh"
 #include "handles.h"
 #include "rs256_device.cuh"
@@ -24,7 +25,14 @@
 
 namespace ffgpu {
 
-enum : uint8_t { BK_RS256_ENC = 0, BK_RS256_DEC = 1, BK_RSI16_ENC = 2, BK_RSI16_DEC = 3, BK_CIRC16_ENC = 4 };
+enum : uint8_t {
+    BK_RS256_ENC = 0,
+    BK_RS256_DEC = 1,
+    BK_RSI16_ENC = 2,
+    BK_RSI16_DEC = 3,
+    BK_CIRC16_ENC = 4,
+    BK_CIRC16_DEC = 5
+};
 
 constexpr int kBatchThreads = 128;
 constexpr int kBatchWarps = kBatchThreads / 32;
@@ -39,6 +47,11 @@ struct BatchCode {
     // CIRC16: outer code and geometry (pycirc16.hpp:46-65)
     Rsi16Dev rso;
     uint32_t c_message_len, c_ecc_len, c_rso_interleave, c_rso_ieccl, c_rsi_ieccl, c_inner_rows, c_outer_rows;
+    uint32_t c_rsi_total;
+    CircDims cd;
+    // CircRepair workspace (word offsets) and the saved message after it
+    uint32_t o_rso, o_rsi, o_syn, o_blk, o_bsyn, o_zpos, o_zoff, o_zcnt, o_zact, o_vec, o_flag, o_locs, o_lcnt, o_poff,
+        o_pcnt, o_kn, o_un, o_st, o_save;
 };
 
 struct BatchItem {
@@ -159,9 +172,105 @@ __device__ void circ16_enc_item(const BatchCode &c, const BatchItem &it, uint32_
     for (uint32_t b = warp; b < c.c_outer_rows; b += kBatchWarps) rsi16_encode_block(c.rsi, vio, b, ws, lane);
 }
 
+// One CIRC16 codeword repaired inside the CTA: CircRepair (pycirc16.hpp:135-335)
+// stage by stage, each stage spread over the four warps with a barrier after
+// it, exactly as the per-request pipeline of stage kernels.  A column whose
+// outer repair raises (status 0xFF) ends the reference's column loop there:
+// the columns from it on get their saved words back and the ecc is not
+// written; the block's status is 0 or 0xFF.
+__device__ void circ16_dec_item(const BatchCode &c, const BatchItem &it, uint32_t *ws, uint32_t *W,
+                                uint32_t *s_first) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, tid = threadIdx.x;
+    const Rsi16Dev &ri = c.rsi, &ro = c.rso;
+    const CircDims d = c.cd;
+    uint16_t *msg = static_cast<uint16_t *>(it.msg), *ecc = static_cast<uint16_t *>(it.par);
+    uint32_t *rso_ecc = W + c.o_rso, *rsi_ecc = W + c.o_rsi, *synd = W + c.o_syn, *blocks = W + c.o_blk,
+             *bsyn = W + c.o_bsyn, *zpos = W + c.o_zpos, *zoff = W + c.o_zoff, *zcnt = W + c.o_zcnt,
+             *vecs = W + c.o_vec, *locs = W + c.o_locs, *lcnt = W + c.o_lcnt, *poff = W + c.o_poff,
+             *pcnt = W + c.o_pcnt;
+    uint8_t *zact = reinterpret_cast<uint8_t *>(W + c.o_zact), *flag = reinterpret_cast<uint8_t *>(W + c.o_flag),
+            *kn = reinterpret_cast<uint8_t *>(W + c.o_kn), *un = reinterpret_cast<uint8_t *>(W + c.o_un),
+            *cst = reinterpret_cast<uint8_t *>(W + c.o_st);
+    uint16_t *save = reinterpret_cast<uint16_t *>(W + c.o_save);
+    const uint32_t I = c.c_rso_interleave, n_oz = d.interleave * ro.ecc, n_iz = d.interleave * ro.block_len;
+    // load_ecc (pycirc16.hpp:159-163), and a copy of the message
+    for (uint32_t i = tid; i < c.c_message_len; i += kBatchThreads) save[i] = msg[i];
+    for (uint32_t i = tid; i < c.c_rso_ieccl; i += kBatchThreads) rso_ecc[i] = ecc[i];
+    for (uint32_t i = tid; i < c.c_rsi_total; i += kBatchThreads) rsi_ecc[i] = ecc[c.c_rso_ieccl + i];
+    __syncthreads();
+    // compute_rsi_synd (pycirc16.hpp:165-181)
+    const BlockView vmsg{msg, 0, ri.message_len, 1, rsi_ecc, 0, ri.ecc, 1, c.c_inner_rows, true, false};
+    for (uint32_t b = warp; b < c.c_inner_rows; b += kBatchWarps)
+        rsi16_synd_block(ri, vmsg, b, ws, synd + (size_t)b * ri.ecc, lane);
+    const BlockView vrso{rso_ecc, 0, ri.message_len, 1, rsi_ecc + c.c_rsi_ieccl, 0, ri.ecc, 1, c.c_outer_rows,
+                         false, false};
+    for (uint32_t b = warp; b < c.c_outer_rows; b += kBatchWarps)
+        rsi16_synd_block(ri, vrso, b, ws, synd + c.c_rsi_ieccl + (size_t)b * ri.ecc, lane);
+    __syncthreads();
+    // repair_outer_zeros
+    for (uint32_t k = warp; k < n_oz; k += kBatchWarps)
+        outer_zeros_prepare_item(d, rso_ecc, rsi_ecc, synd, blocks, zpos, zoff, zcnt, zact, k, lane);
+    __syncthreads();
+    const BlockView vblk{blocks, 0, ri.block_len, 1, blocks + ri.message_len, 0, ri.block_len, 1, n_oz, false, false};
+    for (uint32_t b = warp; b < n_oz; b += kBatchWarps)
+        if (zact[b]) rsi16_repair_known_block(ri, vblk, b, zpos + zoff[b], zcnt[b], ws, nullptr, lane);
+    __syncthreads();
+    for (uint32_t b = warp; b < n_oz; b += kBatchWarps) rsi16_synd_block(ri, vblk, b, ws, bsyn + (size_t)b * ri.ecc, lane);
+    __syncthreads();
+    for (uint32_t k = warp; k < n_oz; k += kBatchWarps)
+        outer_zeros_commit_item(d, rso_ecc, rsi_ecc, synd, blocks, bsyn, zpos, zcnt, zact, k, lane);
+    __syncthreads();
+    // repair_inner_zeros
+    for (uint32_t k = warp; k < n_iz; k += kBatchWarps) inner_zeros_prepare_item(d, rsi_ecc, synd, vecs, flag, k, lane);
+    __syncthreads();
+    for (uint32_t k = warp; k < n_iz; k += kBatchWarps) w_mix(ri, vecs + (size_t)k * ri.ecc, lane);
+    __syncthreads();
+    for (uint32_t k = warp; k < n_iz; k += kBatchWarps) inner_zeros_commit_item(d, rsi_ecc, synd, vecs, flag, k, lane);
+    __syncthreads();
+    // find_error_locations, then the outer repairs
+    for (uint32_t k = warp; k < d.interleave; k += kBatchWarps) find_locations_item(d, synd, locs, lcnt, k, lane);
+    if (tid == 0) *s_first = 0xffffffffu;
+    __syncthreads();
+    for (uint32_t col = tid; col < I; col += kBatchThreads) {
+        outer_modes_col(d, lcnt, poff, pcnt, kn, un, col, 0);
+        cst[col] = 0;
+    }
+    __syncthreads();
+    const BlockView vcol = interleaved_view(msg, true, ro.message_len, rso_ecc, false, ro.ecc, I);
+    for (uint32_t col = warp; col < I; col += kBatchWarps) {
+        if (kn[col])
+            rsi16_repair_known_block(ro, vcol, col, locs + poff[col], pcnt[col], ws, cst, lane);
+        else if (un[col] && !rsi16_repair_bm_block(ro, vcol, col, ws, cst, lane))
+            rsi16_repair_block(ro, vcol, col, ws, cst, lane);
+    }
+    __syncthreads();
+    for (uint32_t col = tid; col < I; col += kBatchThreads)
+        if (cst[col] == FFGPU_STATUS_ASSERT) atomicMin(s_first, col);
+    // recompute_inner_ecc (pycirc16.hpp:320-324)
+    const BlockView vre{msg, 0, ri.message_len, 1, rsi_ecc, 0, ri.ecc, 1, c.c_inner_rows, true, false};
+    for (uint32_t b = warp; b < c.c_inner_rows; b += kBatchWarps) rsi16_encode_block(ri, vre, b, ws, lane);
+    const BlockView vreo{rso_ecc, 0, ri.message_len, 1, rsi_ecc + c.c_rsi_ieccl, 0, ri.ecc, 1, c.c_outer_rows,
+                         false, false};
+    for (uint32_t b = warp; b < c.c_outer_rows; b += kBatchWarps) rsi16_encode_block(ri, vreo, b, ws, lane);
+    __syncthreads();
+    const uint32_t first = *s_first;
+    if (first == 0xffffffffu) {
+        // dump_ecc (pycirc16.hpp:326-330)
+        for (uint32_t i = tid; i < c.c_rso_ieccl; i += kBatchThreads) ecc[i] = (uint16_t)rso_ecc[i];
+        for (uint32_t i = tid; i < c.c_rsi_total; i += kBatchThreads) ecc[c.c_rso_ieccl + i] = (uint16_t)rsi_ecc[i];
+    } else {
+        const uint32_t ncol = I - first;
+        for (uint32_t i = tid; i < ro.message_len * ncol; i += kBatchThreads) {
+            const uint32_t r = i / ncol, col = first + i % ncol;
+            msg[(size_t)r * I + col] = save[(size_t)r * I + col];
+        }
+    }
+    if (tid == 0 && it.status) *it.status = first == 0xffffffffu ? 0 : FFGPU_STATUS_ASSERT;
+}
+
 __global__ void __launch_bounds__(kBatchThreads) batch_kernel(BatchArgs a) {
     extern __shared__ __align__(16) uint32_t sm[];
-    __shared__ uint32_t s_idx;
+    __shared__ uint32_t s_idx, s_first;
     uint8_t *rs_scratch = a.rs_scratch + (size_t)blockIdx.x * kBatchThreads * kDecodeScratchBytes;
     uint32_t *ctmp = a.circ_tmp + (size_t)blockIdx.x * a.circ_tmp_words;
     uint32_t *ws = sm + (size_t)(threadIdx.x >> 5) * a.ws_words;
@@ -188,6 +297,9 @@ __global__ void __launch_bounds__(kBatchThreads) batch_kernel(BatchArgs a) {
                 break;
             case BK_CIRC16_ENC:
                 circ16_enc_item(c, it, ws, ctmp);
+                break;
+            case BK_CIRC16_DEC:
+                circ16_dec_item(c, it, ws, ctmp, &s_first);
                 break;
             default:
                 break;
@@ -258,6 +370,9 @@ double item_cost(const ffgpu_batch &B, const BatchItem &it) {
         case BK_RS256_DEC: return (double)it.nblocks * (it.msg_len + c.ecc) * (4 + c.ecc);
         case BK_RSI16_ENC: return (double)it.nblocks * c.rsi.block_len * 8;
         case BK_RSI16_DEC: return (double)it.nblocks * c.rsi.block_len * (40 + c.rsi.ecc);
+        case BK_CIRC16_DEC:
+            return ((double)c.c_rso_interleave * c.rso.block_len +
+                    (double)(c.c_inner_rows + c.c_outer_rows) * c.rsi.block_len) * 40;
         default:
             return ((double)c.c_rso_interleave * c.rso.block_len +
                     (double)(c.c_inner_rows + c.c_outer_rows) * c.rsi.block_len) * 8;
@@ -326,6 +441,28 @@ void build_plan(ffgpu_batch &B, int tile_rs, int tile_rsi, int ctas_per_sm) {
             bc.c_rsi_ieccl = (uint32_t)c.rsi_ieccl;
             bc.c_inner_rows = (uint32_t)c.inner_rows;
             bc.c_outer_rows = (uint32_t)c.outer_rows;
+            bc.c_rsi_total = (uint32_t)c.rsi_total;
+            bc.cd = circ16_dims(c);
+            const CircLayout lay = circ16_layout(c);
+            bc.o_rso = (uint32_t)lay.o_rso;
+            bc.o_rsi = (uint32_t)lay.o_rsi;
+            bc.o_syn = (uint32_t)lay.o_syn;
+            bc.o_blk = (uint32_t)lay.o_blk;
+            bc.o_bsyn = (uint32_t)lay.o_bsyn;
+            bc.o_zpos = (uint32_t)lay.o_zpos;
+            bc.o_zoff = (uint32_t)lay.o_zoff;
+            bc.o_zcnt = (uint32_t)lay.o_zcnt;
+            bc.o_zact = (uint32_t)lay.o_zact;
+            bc.o_vec = (uint32_t)lay.o_vec;
+            bc.o_flag = (uint32_t)lay.o_flag;
+            bc.o_locs = (uint32_t)lay.o_locs;
+            bc.o_lcnt = (uint32_t)lay.o_lcnt;
+            bc.o_poff = (uint32_t)lay.o_poff;
+            bc.o_pcnt = (uint32_t)lay.o_pcnt;
+            bc.o_kn = (uint32_t)lay.o_kn;
+            bc.o_un = (uint32_t)lay.o_un;
+            bc.o_st = (uint32_t)lay.o_st;
+            bc.o_save = (uint32_t)lay.words;
             const uint32_t ci = code_index(B, r.handle, bc);
             for (size_t b = 0; b < r.nblocks; ++b) {
                 BatchItem it{};
@@ -334,10 +471,16 @@ void build_plan(ffgpu_batch &B, int tile_rs, int tile_rsi, int ctas_per_sm) {
                 it.nblocks = 1;
                 it.msg = static_cast<uint16_t *>(r.a) + b * c.message_len;
                 it.par = static_cast<uint16_t *>(r.b) + b * c.ecc_len;
+                it.status = r.status ? r.status + b : nullptr;
                 B.items.push_back(it);
             }
-            ws_words = std::max(ws_words, (uint32_t)std::max(c.rsi->block_len, c.rso->block_len));
-            circ_words = std::max(circ_words, c.rso_ieccl);
+            if (r.kind == BK_CIRC16_DEC) {
+                ws_words = std::max(ws_words, std::max(c.rsi->dev.temp_len, c.rso->dev.temp_len) + 1);
+                circ_words = std::max(circ_words, lay.words + (c.message_len + 1) / 2);
+            } else {
+                ws_words = std::max(ws_words, (uint32_t)std::max(c.rsi->block_len, c.rso->block_len));
+                circ_words = std::max(circ_words, c.rso_ieccl);
+            }
         }
     }
     // longest first
@@ -415,6 +558,10 @@ std::vector<Region> decode_regions(const ffgpu_batch &B) {
             const Rsi16Code &c = *static_cast<const ffgpu_rsi16 *>(r.handle)->code;
             v.push_back({r.a, r.nblocks * c.message_len * 2});
             v.push_back({r.b, r.nblocks * c.ecc * 2});
+        } else if (r.kind == BK_CIRC16_DEC) {
+            const Circ16Code &c = *static_cast<const ffgpu_circ16 *>(r.handle)->code;
+            v.push_back({r.a, r.nblocks * c.message_len * 2});
+            v.push_back({r.b, r.nblocks * c.ecc_len * 2});
         }
     }
     return v;
@@ -527,12 +674,14 @@ int ffgpu_batch_add_rsi16(ffgpu_batch *b, const ffgpu_rsi16 *code, int op, uint1
 }
 
 int ffgpu_batch_add_circ16(ffgpu_batch *b, const ffgpu_circ16 *code, int op, uint16_t *msg, uint16_t *ecc,
-                           size_t nblocks) {
+                           size_t nblocks, uint8_t *status) {
     return guarded([&] {
         FFGPU_REQUIRE(b && code, "batch or code is NULL");
-        FFGPU_REQUIRE(op == FFGPU_OP_ENCODE, "CIRC16 batches take encode requests");
+        FFGPU_REQUIRE(op == FFGPU_OP_ENCODE || op == FFGPU_OP_DECODE, "op must be FFGPU_OP_ENCODE or FFGPU_OP_DECODE");
+        FFGPU_REQUIRE(op == FFGPU_OP_ENCODE || status, "decode needs a status array");
         std::lock_guard<std::mutex> lk(b->mu);
-        b->reqs.push_back({BK_CIRC16_ENC, code, msg, ecc, nullptr, nblocks, 0});
+        b->reqs.push_back({op == FFGPU_OP_ENCODE ? BK_CIRC16_ENC : BK_CIRC16_DEC, code, msg, ecc,
+                           op == FFGPU_OP_ENCODE ? nullptr : status, nblocks, 0});
         b->planned = false;
     });
 }

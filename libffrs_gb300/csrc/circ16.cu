@@ -100,7 +100,7 @@ __global__ void k_outer_modes(CircDims d, const uint32_t *lcnt, uint32_t *pos_of
 
 static unsigned g1(size_t n) { return (unsigned)std::min<size_t>((n + 255) / 256, 4096); }
 
-static CircDims dims(const Circ16Code &c) {
+CircDims circ16_dims(const Circ16Code &c) {
     CircDims d;
     d.ri_ml = (uint32_t)c.rsi->message_len;
     d.ri_ecc = (uint32_t)c.rsi->ecc;
@@ -111,6 +111,38 @@ static CircDims dims(const Circ16Code &c) {
     d.interleave = (uint32_t)c.interleave;
     d.rso_interleave = (uint32_t)c.rso_interleave;
     return d;
+}
+
+CircLayout circ16_layout(const Circ16Code &c) {
+    const Rsi16Code &ri = *c.rsi, &ro = *c.rso;
+    const size_t n_oz = c.interleave * ro.ecc, n_iz = c.interleave * ro.block_len;
+    size_t off = 0;
+    auto take = [&](size_t words) {
+        size_t o = off;
+        off += (words + 63) & ~(size_t)63;
+        return o;
+    };
+    CircLayout L;
+    L.o_rso = take(c.rso_ieccl);
+    L.o_rsi = take(c.rsi_total);
+    L.o_syn = take(c.rsi_total);
+    L.o_blk = take(n_oz * ri.block_len);
+    L.o_bsyn = take(n_oz * ri.ecc);
+    L.o_zpos = take(n_oz * ri.ecc);
+    L.o_zoff = take(n_oz);
+    L.o_zcnt = take(n_oz);
+    L.o_zact = take(n_oz / 4 + 1);
+    L.o_vec = take(n_iz * ri.ecc);
+    L.o_flag = take(n_iz / 4 + 1);
+    L.o_locs = take(c.interleave * ro.block_len);
+    L.o_lcnt = take(c.interleave);
+    L.o_poff = take(c.rso_interleave);
+    L.o_pcnt = take(c.rso_interleave);
+    L.o_kn = take(c.rso_interleave / 4 + 1);
+    L.o_un = take(c.rso_interleave / 4 + 1);
+    L.o_st = take(c.rso_interleave / 4 + 1);
+    L.words = off;
+    return L;
 }
 
 void circ16_encode(Circ16Code &c, const uint16_t *msg, size_t nblocks, uint16_t *ecc, cudaStream_t st) {
@@ -139,22 +171,14 @@ void circ16_encode(Circ16Code &c, const uint16_t *msg, size_t nblocks, uint16_t 
 void circ16_repair_one(Circ16Code &c, uint16_t *msg, uint16_t *ecc, cudaStream_t st, bool stop_after_find,
                        size_t find_k, uint32_t *locs_out, uint32_t *lcnt_out, uint8_t *col_status) {
     const Rsi16Code &ri = *c.rsi, &ro = *c.rso;
-    const CircDims d = dims(c);
-    // workspace layout (uint32 words)
+    const CircDims d = circ16_dims(c);
     const size_t n_oz = c.interleave * ro.ecc, n_iz = c.interleave * ro.block_len;
-    size_t off = 0;
-    auto take = [&](size_t words) {
-        size_t o = off;
-        off += (words + 63) & ~(size_t)63;
-        return o;
-    };
-    const size_t o_rso = take(c.rso_ieccl), o_rsi = take(c.rsi_total), o_syn = take(c.rsi_total),
-                 o_blk = take(n_oz * ri.block_len), o_bsyn = take(n_oz * ri.ecc), o_zpos = take(n_oz * ri.ecc),
-                 o_zoff = take(n_oz), o_zcnt = take(n_oz), o_zact = take(n_oz / 4 + 1), o_vec = take(n_iz * ri.ecc),
-                 o_flag = take(n_iz / 4 + 1), o_locs = take(c.interleave * ro.block_len), o_lcnt = take(c.interleave),
-                 o_poff = take(c.rso_interleave), o_pcnt = take(c.rso_interleave), o_kn = take(c.rso_interleave / 4 + 1),
-                 o_un = take(c.rso_interleave / 4 + 1), o_st = take(c.rso_interleave / 4 + 1);
-    uint32_t *W = (uint32_t *)c.rep_ws.get(off * 4);
+    const CircLayout lay = circ16_layout(c);
+    const size_t o_rso = lay.o_rso, o_rsi = lay.o_rsi, o_syn = lay.o_syn, o_blk = lay.o_blk, o_bsyn = lay.o_bsyn,
+                 o_zpos = lay.o_zpos, o_zoff = lay.o_zoff, o_zcnt = lay.o_zcnt, o_zact = lay.o_zact, o_vec = lay.o_vec,
+                 o_flag = lay.o_flag, o_locs = lay.o_locs, o_lcnt = lay.o_lcnt, o_poff = lay.o_poff,
+                 o_pcnt = lay.o_pcnt, o_kn = lay.o_kn, o_un = lay.o_un, o_st = lay.o_st;
+    uint32_t *W = (uint32_t *)c.rep_ws.get(lay.words * 4);
     uint32_t *rso_ecc = W + o_rso, *rsi_ecc = W + o_rsi, *synd = W + o_syn;
     uint32_t *blocks = W + o_blk, *bsyn = W + o_bsyn, *zpos = W + o_zpos, *zoff = W + o_zoff, *zcnt = W + o_zcnt;
     uint8_t *zact = (uint8_t *)(W + o_zact);

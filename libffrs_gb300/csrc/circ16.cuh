@@ -22,6 +22,14 @@ struct Circ16Code {
                size_t interleave, uint32_t primitive);
 };
 
+// Word offsets of the CircRepair workspace of one block (every array 64-word
+// aligned); `words` is the total.
+struct CircLayout {
+    size_t o_rso, o_rsi, o_syn, o_blk, o_bsyn, o_zpos, o_zoff, o_zcnt, o_zact, o_vec, o_flag, o_locs, o_lcnt, o_poff,
+        o_pcnt, o_kn, o_un, o_st, words;
+};
+CircLayout circ16_layout(const Circ16Code &c);
+
 void circ16_encode(Circ16Code &c, const uint16_t *msg, size_t nblocks, uint16_t *ecc, cudaStream_t st);
 // Repair of one block up to (not including) the ecc write-back.  With
 // stop_after_find the pipeline stops after the error-row search and copies

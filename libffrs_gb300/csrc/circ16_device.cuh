@@ -10,6 +10,7 @@
 
 namespace ffgpu {
 
+struct Circ16Code;
 struct CircDims {
     uint32_t ri_ml, ri_ecc, ri_bl;          // inner code
     uint32_t ro_ml, ro_ecc, ro_bl;          // outer code
@@ -17,6 +18,8 @@ struct CircDims {
     __device__ uint32_t rso_off(uint32_t k, uint32_t row) const { return rso_interleave * row + k * ri_ml; }
     __device__ uint32_t rsi_off(uint32_t k, uint32_t row) const { return (row * interleave + k) * ri_ecc; }
 };
+
+CircDims circ16_dims(const Circ16Code &c);
 
 // repair_outer_zeros, part 1 (pycirc16.hpp:183-217): one warp per (k, outer
 // parity row r).  Rows with non-zero inner syndromes collect the positions

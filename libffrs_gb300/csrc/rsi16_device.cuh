@@ -563,6 +563,15 @@ static __device__ __forceinline__ void rsi16_encode_block(const Rsi16Dev &c, con
     __syncwarp();
 }
 
+// syndromes of block b (NTT::pntt over every chunk) into out[0 .. ecc)
+static __device__ __forceinline__ void rsi16_synd_block(const Rsi16Dev &c, const BlockView &v, size_t b, uint32_t *ws,
+                                                        uint32_t *out, int lane) {
+    w_gather(c, v, b, ws, true, lane);
+    w_pntt(c, ws, c.pntt_blocks, lane);
+    for (uint32_t k = lane; k < c.ecc; k += 32) out[k] = ws[k];
+    __syncwarp();
+}
+
 // RSi16v::_repair, unknown locations (rsi16v_impl.hpp:122-168) with
 // _find_roots_ntt (:443-497) and _forney (:500-512); temp: temp_len + 1 words
 static __device__ __noinline__ void rsi16_repair_block(const Rsi16Dev &c, const BlockView &v, size_t b, uint32_t *temp,

@@ -64,7 +64,7 @@ int ffgpu_batch_add_rs256(ffgpu_batch *b, const ffgpu_rs256 *code, int op, uint8
 int ffgpu_batch_add_rsi16(ffgpu_batch *b, const ffgpu_rsi16 *code, int op, uint16_t *msg, uint16_t *parity,
                           size_t nblocks, uint8_t *status);
 int ffgpu_batch_add_circ16(ffgpu_batch *b, const ffgpu_circ16 *code, int op, uint16_t *msg, uint16_t *ecc,
-                           size_t nblocks);
+                           size_t nblocks, uint8_t *status);
 int ffgpu_batch_plan(ffgpu_batch *b, int autotune, void *stream);
 int ffgpu_batch_launch(ffgpu_batch *b, void *stream);
 }
@@ -133,7 +133,7 @@ void issue(ffgpu_server &S, Slot &sl) {
         else
             rc = ffgpu_batch_add_circ16(sl.batch, static_cast<const ffgpu_circ16 *>(r->code), r->op,
                                         reinterpret_cast<uint16_t *>(da), reinterpret_cast<uint16_t *>(db),
-                                        r->nblocks);
+                                        r->nblocks, r->op == FFGPU_OP_DECODE ? ds : nullptr);
         if (rc) throw ffgpu::Error(rc, ffgpu_last_error());
     }
     if (int rc = ffgpu_batch_plan(sl.batch, 0, sl.st)) throw ffgpu::Error(rc, ffgpu_last_error());
@@ -333,11 +333,12 @@ int ffgpu_server_submit_rsi16(ffgpu_server *S, const ffgpu_rsi16 *code, int op, 
 }
 
 int ffgpu_server_submit_circ16(ffgpu_server *S, const ffgpu_circ16 *code, int op, uint16_t *msg, uint16_t *ecc,
-                               size_t nblocks, uint64_t *ticket) {
+                               size_t nblocks, uint8_t *status, uint64_t *ticket) {
     return guarded([&] {
         FFGPU_REQUIRE(S && code && ticket, "server, code or ticket is NULL");
-        FFGPU_REQUIRE(op == FFGPU_OP_ENCODE, "CIRC16 requests are encodes");
+        FFGPU_REQUIRE(op == FFGPU_OP_ENCODE || op == FFGPU_OP_DECODE, "op must be FFGPU_OP_ENCODE or FFGPU_OP_DECODE");
         FFGPU_REQUIRE(nblocks > 0 && msg && ecc, "empty request");
+        FFGPU_REQUIRE(op == FFGPU_OP_ENCODE || status, "decode needs a status array");
         const Circ16Code &c = *code->code;
         auto r = std::make_unique<SrvReq>();
         r->kind = SK_CIRC16;
@@ -348,6 +349,8 @@ int ffgpu_server_submit_circ16(ffgpu_server *S, const ffgpu_circ16 *code, int op
         r->nblocks = nblocks;
         r->a_bytes = nblocks * c.message_len * 2;
         r->b_bytes = nblocks * c.ecc_len * 2;
+        r->status = status;
+        r->s_bytes = op == FFGPU_OP_DECODE ? nblocks : 0;
         enqueue(S, std::move(r), ticket);
     });
 }

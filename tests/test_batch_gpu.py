@@ -42,7 +42,8 @@ def test_batch_equals_plain(mixed):
     torch, bench, reqs, _ = mixed
     sp = torch.cuda.current_stream().cuda_stream
     kinds = {(r["kind"], r["op"]) for r in reqs}
-    assert {("rs256", "enc"), ("rs256", "dec"), ("rsi16", "enc"), ("rsi16", "dec"), ("circ16", "enc")} <= kinds
+    assert {("rs256", "enc"), ("rs256", "dec"), ("rsi16", "enc"), ("rsi16", "dec"), ("circ16", "enc"),
+            ("circ16", "dec")} <= kinds
     bench.mixed_restore(reqs)
     bench.mixed_plain(reqs, sp)
     torch.cuda.synchronize()
@@ -110,6 +111,22 @@ def test_batch_sample_vs_oracle(mixed):
                 np.testing.assert_array_equal(r["par"].cpu().numpy().view(np.uint16), p)
             checked += 1
     assert checked >= 4
+    # a CIRC16 repair request, codeword by codeword against the oracle
+    r = next(r for r in reqs if r["kind"] == "circ16" and r["op"] == "dec")
+    c = r["code"]
+    o = O.CIRC16(128, 8, 128, 8, 4)
+    m0 = r["data0"].cpu().numpy().view(np.uint16)
+    e0 = r["par0"].cpu().numpy().view(np.uint16)
+    got_m = r["data"].cpu().numpy().view(np.uint16)
+    got_e = r["par"].cpu().numpy().view(np.uint16)
+    got_s = r["status"].cpu().numpy()
+    for i in range(min(r["nb"], 3)):
+        m, e = m0[i].copy(), e0[i].copy()
+        rc = o.repair(m, e)
+        assert (got_s[i] == 0) == (rc == 0)
+        np.testing.assert_array_equal(got_m[i], m)
+        if rc == 0:
+            np.testing.assert_array_equal(got_e[i], e)
 
 
 def test_batch_rejects_bad_requests(built):
