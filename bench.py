@@ -652,7 +652,7 @@ def make_mixed(torch, total_bytes, seed):
     while used < budget["circ16"]:
         nb = int(np.exp(rng.uniform(np.log(1), np.log(64))))
         nb = max(1, min(nb, (budget["circ16"] - used) // cwb + 1))
-        dec = bool(rng.integers(0, 2))
+        dec = used == 0 or bool(rng.integers(0, 2))  # the first CIRC16 request is a decode
         msg = torch.randint(-32768, 32768, (nb, c.message_len), dtype=torch.int16, device="cuda", generator=g)
         ecc = torch.zeros((nb, c.ecc_len), dtype=torch.int16, device="cuda")
         r = {"kind": "circ16", "code": c, "op": "dec" if dec else "enc", "nb": nb, "data": msg, "par": ecc,
