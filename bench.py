@@ -561,11 +561,13 @@ def make_mixed(torch, total_bytes, seed):
     of ecc_len), a quarter CIRC16(128, 8, 128, 8, 4) codewords.  RS256 and
     RSi16 requests are half encode, half decode with correctable errors
     (uniform 0 .. ecc_len/2 per block at distinct positions); CIRC16 requests
-    are encodes.  Blocks per request are log-uniform.  Decode inputs are
-    encoded by the plain GPU path and corrupted on the device.
+    are encodes or repairs of one burst of 1..64 changed message words per
+    codeword (at most a quarter of the CIRC16 bytes per request).  Blocks per
+    request are log-uniform.  Decode inputs are encoded by the plain GPU path
+    and corrupted on the device.
 
-    Returns (requests, pools): every request holds its code and device tensor
-    views; pools hold the pristine inputs for restoring between runs."""
+    Returns (requests, codes): every request holds its code, device tensor
+    views and the pristine inputs (data0, par0) for restoring between runs."""
     from libffrs_gb300 import capi
 
     rng = np.random.Generator(np.random.PCG64(seed))
@@ -649,10 +651,13 @@ def make_mixed(torch, total_bytes, seed):
     used = 0
     c = code("circ16", 128, 8, 128, 8, 4)
     cwb = (c.message_len + c.ecc_len) * 2
+    ncirc = 0
     while used < budget["circ16"]:
         nb = int(np.exp(rng.uniform(np.log(1), np.log(64))))
-        nb = max(1, min(nb, (budget["circ16"] - used) // cwb + 1))
-        dec = used == 0 or bool(rng.integers(0, 2))  # the first CIRC16 request is a decode
+        nb = max(1, min(nb, (budget["circ16"] - used) // cwb + 1, budget["circ16"] // (4 * cwb)))
+        # the first CIRC16 request is a decode, the second an encode
+        dec = ncirc == 0 or (ncirc > 1 and bool(rng.integers(0, 2)))
+        ncirc += 1
         msg = torch.randint(-32768, 32768, (nb, c.message_len), dtype=torch.int16, device="cuda", generator=g)
         ecc = torch.zeros((nb, c.ecc_len), dtype=torch.int16, device="cuda")
         r = {"kind": "circ16", "code": c, "op": "dec" if dec else "enc", "nb": nb, "data": msg, "par": ecc,

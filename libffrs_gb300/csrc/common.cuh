@@ -122,6 +122,19 @@ struct PinnedBuffer {
     }
 };
 
+// True when `p` is page-locked host memory.  A device-to-host copy into
+// pageable memory blocks the calling thread until the stream's earlier work
+// is done, which serialises the chunks of a host-buffer pipeline; such
+// outputs go through a PinnedBuffer instead.
+inline bool page_locked(const void *p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
 // Runs `f` and converts exceptions into a status code + last-error message.
 template <typename F>
 int guarded(F &&f) {

@@ -252,11 +252,29 @@ int ffgpu_rs256_encode_host(const ffgpu_rs256 *code, const uint8_t *buf, size_t 
         const size_t nout = (full + (tail ? 1 : 0)) * (size_t)c.ecc;
         uint8_t *d_in = (uint8_t *)h->d_data.get(len);
         uint8_t *d_out = (uint8_t *)h->d_parity.get(nout);
-        FFGPU_CHECK_CUDA(cudaMemcpyAsync(d_in, buf, len, cudaMemcpyHostToDevice, st));
-        rs256_encode(c, d_in, full, (int)message_len, d_out, st);
-        if (tail) rs256_encode(c, d_in + full * message_len, 1, (int)tail, d_out + full * (size_t)c.ecc, st);
-        FFGPU_CHECK_CUDA(cudaMemcpyAsync(out, d_out, nout, cudaMemcpyDeviceToHost, st));
-        FFGPU_CHECK_CUDA(cudaStreamSynchronize(st));
+        uint8_t *h_out = page_locked(out) ? out : (uint8_t *)h->h_parity.get(nout);
+        // chunks of full blocks on the pipeline streams (copy in, encode and
+        // copy out of different chunks overlap); the ragged tail block goes
+        // with the last chunk.  An encode launch of fewer blocks than about a
+        // quarter million is latency-bound, so smaller calls stay whole.
+        const size_t chunk = std::max<size_t>(1, host_chunk_blocks(full, 262144, 4));
+        size_t k = 0;
+        for (size_t b0 = 0; b0 < full || (k == 0 && tail); b0 += chunk, ++k) {
+            st = pipe_stream(k);
+            const size_t n = std::min(chunk, full - b0);
+            const bool last = b0 + n >= full;
+            const size_t in_bytes = n * message_len + (last ? tail : 0);
+            const size_t out_bytes = (n + (last && tail ? 1 : 0)) * (size_t)c.ecc;
+            const size_t i0 = b0 * message_len, o0 = b0 * (size_t)c.ecc;
+            FFGPU_CHECK_CUDA(cudaMemcpyAsync(d_in + i0, buf + i0, in_bytes, cudaMemcpyHostToDevice, st));
+            if (n) rs256_encode(c, d_in + i0, n, (int)message_len, d_out + o0, st);
+            if (last && tail)
+                rs256_encode(c, d_in + full * message_len, 1, (int)tail, d_out + full * (size_t)c.ecc, st);
+            FFGPU_CHECK_CUDA(cudaMemcpyAsync(h_out + o0, d_out + o0, out_bytes, cudaMemcpyDeviceToHost, st));
+        }
+        for (size_t i = 0; i < std::min<size_t>(k, kPipeStreams); ++i)
+            FFGPU_CHECK_CUDA(cudaStreamSynchronize(pipe_stream(i)));
+        if (h_out != out) std::memcpy(out, h_out, nout);
     });
 }
 
@@ -273,10 +291,11 @@ int ffgpu_rs256_decode_host(const ffgpu_rs256 *code, uint8_t *data, uint8_t *par
         uint8_t *d_d = (uint8_t *)h->d_data.get(nd);
         uint8_t *d_p = (uint8_t *)h->d_parity.get(np);
         uint8_t *d_s = (uint8_t *)h->d_status.get(nblocks);
+        uint8_t *h_s = page_locked(status) ? status : (uint8_t *)h->h_status.get(nblocks);
         // chunks of blocks on the pipeline streams: the host-to-device copy of
         // one chunk, the decode of another and the copy back of a third
         // overlap (page-locked host memory moves at full speed)
-        const size_t chunk = host_chunk_blocks(nblocks, 524288, 4);
+        const size_t chunk = host_chunk_blocks(nblocks, 262144, 4);
         size_t k = 0;
         for (size_t b0 = 0; b0 < nblocks; b0 += chunk, ++k) {
             cudaStream_t st = pipe_stream(k);
@@ -289,10 +308,11 @@ int ffgpu_rs256_decode_host(const ffgpu_rs256 *code, uint8_t *data, uint8_t *par
             FFGPU_CHECK_CUDA(cudaMemcpyAsync(data + b0 * message_len, dd, n * message_len, cudaMemcpyDeviceToHost, st));
             FFGPU_CHECK_CUDA(
                 cudaMemcpyAsync(parity + b0 * (size_t)c.ecc, dp, n * (size_t)c.ecc, cudaMemcpyDeviceToHost, st));
-            FFGPU_CHECK_CUDA(cudaMemcpyAsync(status + b0, ds, n, cudaMemcpyDeviceToHost, st));
+            FFGPU_CHECK_CUDA(cudaMemcpyAsync(h_s + b0, ds, n, cudaMemcpyDeviceToHost, st));
         }
         for (size_t i = 0; i < std::min<size_t>(k, kPipeStreams); ++i)
             FFGPU_CHECK_CUDA(cudaStreamSynchronize(pipe_stream(i)));
+        if (h_s != status) std::memcpy(status, h_s, nblocks);
     });
 }
 

@@ -145,6 +145,26 @@ int ffgpu_rsi16_encode_host(const ffgpu_rsi16 *code, const uint16_t *msg, size_t
         const size_t nm = nblocks * interleave * c.message_len, np = nblocks * interleave * c.ecc;
         uint16_t *dm = (uint16_t *)h->d_msg.get(nm * 2);
         uint16_t *dp = (uint16_t *)h->d_par.get(np * 2);
+        if (interleave == 1 && rsi16_encode_stream_safe(c)) {
+            // chunks of blocks on the pipeline streams: copies in, encodes and
+            // copies out of different chunks overlap
+            uint16_t *hp = page_locked(parity) ? parity : (uint16_t *)h->h_par.get(np * 2);
+            const size_t chunk = host_chunk_blocks(nblocks, 8192, 4);
+            size_t k = 0;
+            for (size_t b0 = 0; b0 < nblocks; b0 += chunk, ++k) {
+                cudaStream_t ps = pipe_stream(k);
+                const size_t n = std::min(chunk, nblocks - b0);
+                uint16_t *cm = dm + b0 * c.message_len, *cp = dp + b0 * c.ecc;
+                FFGPU_CHECK_CUDA(cudaMemcpyAsync(cm, msg + b0 * c.message_len, n * c.message_len * 2,
+                                                 cudaMemcpyHostToDevice, ps));
+                rsi16_encode(c, contiguous_view(cm, true, c.message_len, cp, true, c.ecc), n, ps);
+                FFGPU_CHECK_CUDA(cudaMemcpyAsync(hp + b0 * c.ecc, cp, n * c.ecc * 2, cudaMemcpyDeviceToHost, ps));
+            }
+            for (size_t i = 0; i < std::min<size_t>(k, kPipeStreams); ++i)
+                FFGPU_CHECK_CUDA(cudaStreamSynchronize(pipe_stream(i)));
+            if (hp != parity) std::memcpy(parity, hp, np * 2);
+            return;
+        }
         FFGPU_CHECK_CUDA(cudaMemcpyAsync(dm, msg, nm * 2, cudaMemcpyHostToDevice, st));
         if (interleave == 1)
             rsi16_encode(c, contiguous_view(dm, true, c.message_len, dp, true, c.ecc), nblocks, st);
@@ -184,7 +204,8 @@ int ffgpu_rsi16_repair_host(const ffgpu_rsi16 *code, uint16_t *msg, uint16_t *pa
             // repairs over the pipeline streams (only when the repair
             // workspace lives in shared memory: the global fallback workspace
             // is one per thread and cannot serve concurrent streams)
-            const size_t chunk = host_chunk_blocks(nblocks, 32768, 4);
+            const size_t chunk = host_chunk_blocks(nblocks, 32768, 8);
+            uint8_t *h_s = page_locked(status) ? status : (uint8_t *)h->h_status.get(nblocks);
             size_t k = 0;
             for (size_t b0 = 0; b0 < nblocks; b0 += chunk, ++k) {
                 cudaStream_t ps = pipe_stream(k);
@@ -199,10 +220,11 @@ int ffgpu_rsi16_repair_host(const ffgpu_rsi16 *code, uint16_t *msg, uint16_t *pa
                                                  cudaMemcpyDeviceToHost, ps));
                 FFGPU_CHECK_CUDA(
                     cudaMemcpyAsync(parity + b0 * c.ecc, cp, n * c.ecc * 2, cudaMemcpyDeviceToHost, ps));
-                FFGPU_CHECK_CUDA(cudaMemcpyAsync(status + b0, ds + b0, n, cudaMemcpyDeviceToHost, ps));
+                FFGPU_CHECK_CUDA(cudaMemcpyAsync(h_s + b0, ds + b0, n, cudaMemcpyDeviceToHost, ps));
             }
             for (size_t i = 0; i < std::min<size_t>(k, kPipeStreams); ++i)
                 FFGPU_CHECK_CUDA(cudaStreamSynchronize(pipe_stream(i)));
+            if (h_s != status) std::memcpy(status, h_s, nblocks);
             return;
         }
         FFGPU_CHECK_CUDA(cudaMemcpyAsync(dm, msg, nm * 2, cudaMemcpyHostToDevice, st));

@@ -354,6 +354,8 @@ static void launch_encode(const Rsi16Code &c, const BlockView &v, size_t nblocks
     check_launch("rsi16_encode_warp_kernel");
 }
 
+bool rsi16_encode_stream_safe(const Rsi16Code &c) { return reg_epl(c) != 0 || (size_t)c.block_len * 4 * 4 <= 64 * 1024; }
+
 void rsi16_encode(const Rsi16Code &c, const BlockView &v, size_t nblocks, cudaStream_t st) {
     if (!nblocks) return;
     switch (reg_epl(c)) {
