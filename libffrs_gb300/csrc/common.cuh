@@ -10,6 +10,7 @@
 #include <mutex>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 #include "../../include/ffgpu.h"
 
@@ -53,6 +54,39 @@ cudaStream_t pipe_stream(size_t k);
 // blocks per chunk of a host-buffer pipeline: ffgpu_set_host_chunk_blocks, or
 // at least min_chunk and at most max_chunks chunks
 size_t host_chunk_blocks(size_t nblocks, size_t min_chunk, size_t max_chunks);
+// memcpy split over a small pool of host threads for large copies (the pages
+// of a fresh pageable destination are also faulted in in parallel)
+void host_copy(void *dst, const void *src, size_t n);
+
+// Outputs of a host-buffer pipeline that land in pageable memory: each
+// chunk's device-to-host copies go to page-locked staging, chunk() records an
+// event behind them on the chunk's stream, and finish() copies every chunk
+// out as soon as its event has completed, while later chunks are still in
+// flight.  copy() with dst == src (the output was page-locked) is a no-op.
+class OutputDrain {
+  public:
+    OutputDrain() = default;
+    OutputDrain(const OutputDrain &) = delete;
+    OutputDrain &operator=(const OutputDrain &) = delete;
+    ~OutputDrain();
+    void copy(void *dst, const void *src, size_t n);
+    void chunk(cudaStream_t st);
+    void finish();
+
+  private:
+    struct Part {
+        void *dst;
+        const void *src;
+        size_t n;
+    };
+    struct Chunk {
+        cudaEvent_t ev;
+        size_t first, count;
+    };
+    std::vector<Part> parts_;
+    std::vector<Chunk> chunks_;
+    size_t open_ = 0;
+};
 
 // Optional per-kernel timing (ffgpu_timing_enable): while it is on, a
 // KernelTimer records a CUDA event pair around one launch on the launching
@@ -133,6 +167,15 @@ inline bool page_locked(const void *p) {
         return false;
     }
     return a.type == cudaMemoryTypeHost;
+}
+
+// Where a host-buffer pipeline lands one output: the caller's memory when it
+// is page-locked or when the call is a single chunk (nothing to overlap: the
+// one blocking copy at the end costs no more than a staging copy), else the
+// page-locked staging buffer.
+template <typename T>
+T *pipeline_out(T *dst, bool chunked, PinnedBuffer &stage, size_t bytes) {
+    return (!chunked || page_locked(dst)) ? dst : (T *)stage.get(bytes);
 }
 
 // Runs `f` and converts exceptions into a status code + last-error message.

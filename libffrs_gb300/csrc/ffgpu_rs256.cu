@@ -1,13 +1,17 @@
 // C ABI: runtime helpers and the RS256 entry points.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
+#include <condition_variable>
 #include <cstring>
+#include <deque>
+#include <functional>
 #include <memory>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
-#include <algorithm>
 
 #include "common.cuh"
 #include "handles.h"
@@ -29,6 +33,96 @@ size_t host_chunk_blocks(size_t nblocks, size_t min_chunk, size_t max_chunks) {
     const size_t fixed = g_chunk_blocks.load();
     if (fixed) return fixed;
     return std::max<size_t>(min_chunk, (nblocks + max_chunks - 1) / max_chunks);
+}
+
+// ---- parallel host copies
+namespace {
+struct CopyPool {
+    std::mutex mu;
+    std::condition_variable cv;
+    std::deque<std::function<void()>> q;
+    unsigned workers = 0;
+    explicit CopyPool(unsigned n) : workers(n) {
+        for (unsigned i = 0; i < n; ++i)
+            std::thread([this] {
+                for (;;) {
+                    std::function<void()> job;
+                    {
+                        std::unique_lock<std::mutex> lk(mu);
+                        cv.wait(lk, [this] { return !q.empty(); });
+                        job = std::move(q.front());
+                        q.pop_front();
+                    }
+                    job();
+                }
+            }).detach();
+    }
+    void push(std::function<void()> f) {
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            q.push_back(std::move(f));
+        }
+        cv.notify_one();
+    }
+};
+
+CopyPool &copy_pool() {
+    // created on first use and never destroyed: its detached workers sleep
+    // on the queue until the process exits
+    static CopyPool *p = new CopyPool(std::max(1u, std::min(8u, std::thread::hardware_concurrency() / 2)));
+    return *p;
+}
+}  // namespace
+
+void host_copy(void *dst, const void *src, size_t n) {
+    constexpr size_t kPart = 4u << 20;
+    if (n <= 2 * kPart) {
+        std::memcpy(dst, src, n);
+        return;
+    }
+    CopyPool &pool = copy_pool();
+    const size_t parts = std::min<size_t>((n + kPart - 1) / kPart, pool.workers + 1);
+    const size_t each = ((n + parts - 1) / parts + 4095) & ~(size_t)4095;
+    std::mutex m;
+    std::condition_variable done;
+    size_t left = 0;
+    for (size_t p = 1; p < parts && p * each < n; ++p) ++left;
+    const size_t helpers = left;
+    for (size_t p = 1; p <= helpers; ++p) {
+        const size_t off = p * each, len = std::min(each, n - off);
+        pool.push([&, off, len] {
+            std::memcpy((char *)dst + off, (const char *)src + off, len);
+            std::lock_guard<std::mutex> lk(m);
+            if (--left == 0) done.notify_one();
+        });
+    }
+    std::memcpy(dst, src, std::min(each, n));
+    std::unique_lock<std::mutex> lk(m);
+    done.wait(lk, [&] { return left == 0; });
+}
+
+OutputDrain::~OutputDrain() {
+    for (auto &c : chunks_) cudaEventDestroy(c.ev);
+}
+
+void OutputDrain::copy(void *dst, const void *src, size_t n) {
+    if (dst != src && n) parts_.push_back({dst, src, n});
+}
+
+void OutputDrain::chunk(cudaStream_t st) {
+    if (parts_.size() == open_) return;
+    cudaEvent_t ev = nullptr;
+    FFGPU_CHECK_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    chunks_.push_back({ev, open_, parts_.size() - open_});
+    FFGPU_CHECK_CUDA(cudaEventRecord(ev, st));
+    open_ = parts_.size();
+}
+
+void OutputDrain::finish() {
+    for (auto &c : chunks_) {
+        FFGPU_CHECK_CUDA(cudaEventSynchronize(c.ev));
+        for (size_t i = c.first; i < c.first + c.count; ++i) host_copy(parts_[i].dst, parts_[i].src, parts_[i].n);
+    }
 }
 
 // streams of the host-buffer pipelines (created on first use)
@@ -252,12 +346,13 @@ int ffgpu_rs256_encode_host(const ffgpu_rs256 *code, const uint8_t *buf, size_t 
         const size_t nout = (full + (tail ? 1 : 0)) * (size_t)c.ecc;
         uint8_t *d_in = (uint8_t *)h->d_data.get(len);
         uint8_t *d_out = (uint8_t *)h->d_parity.get(nout);
-        uint8_t *h_out = page_locked(out) ? out : (uint8_t *)h->h_parity.get(nout);
         // chunks of full blocks on the pipeline streams (copy in, encode and
         // copy out of different chunks overlap); the ragged tail block goes
         // with the last chunk.  An encode launch of fewer blocks than about a
         // quarter million is latency-bound, so smaller calls stay whole.
         const size_t chunk = std::max<size_t>(1, host_chunk_blocks(full, 262144, 4));
+        uint8_t *h_out = pipeline_out(out, chunk < full, h->h_parity, nout);
+        OutputDrain drain;
         size_t k = 0;
         for (size_t b0 = 0; b0 < full || (k == 0 && tail); b0 += chunk, ++k) {
             st = pipe_stream(k);
@@ -271,10 +366,12 @@ int ffgpu_rs256_encode_host(const ffgpu_rs256 *code, const uint8_t *buf, size_t 
             if (last && tail)
                 rs256_encode(c, d_in + full * message_len, 1, (int)tail, d_out + full * (size_t)c.ecc, st);
             FFGPU_CHECK_CUDA(cudaMemcpyAsync(h_out + o0, d_out + o0, out_bytes, cudaMemcpyDeviceToHost, st));
+            drain.copy(out + o0, h_out + o0, out_bytes);
+            drain.chunk(st);
         }
+        drain.finish();
         for (size_t i = 0; i < std::min<size_t>(k, kPipeStreams); ++i)
             FFGPU_CHECK_CUDA(cudaStreamSynchronize(pipe_stream(i)));
-        if (h_out != out) std::memcpy(out, h_out, nout);
     });
 }
 
@@ -291,28 +388,36 @@ int ffgpu_rs256_decode_host(const ffgpu_rs256 *code, uint8_t *data, uint8_t *par
         uint8_t *d_d = (uint8_t *)h->d_data.get(nd);
         uint8_t *d_p = (uint8_t *)h->d_parity.get(np);
         uint8_t *d_s = (uint8_t *)h->d_status.get(nblocks);
-        uint8_t *h_s = page_locked(status) ? status : (uint8_t *)h->h_status.get(nblocks);
+        // outputs in pageable memory come back through page-locked staging
         // chunks of blocks on the pipeline streams: the host-to-device copy of
         // one chunk, the decode of another and the copy back of a third
         // overlap (page-locked host memory moves at full speed)
         const size_t chunk = host_chunk_blocks(nblocks, 262144, 4);
+        const bool chunked = chunk < nblocks;
+        uint8_t *h_d = pipeline_out(data, chunked, h->h_data, nd);
+        uint8_t *h_p = pipeline_out(parity, chunked, h->h_parity, np);
+        uint8_t *h_s = pipeline_out(status, chunked, h->h_status, nblocks);
+        OutputDrain drain;
         size_t k = 0;
         for (size_t b0 = 0; b0 < nblocks; b0 += chunk, ++k) {
             cudaStream_t st = pipe_stream(k);
             const size_t n = std::min(chunk, nblocks - b0);
-            uint8_t *dd = d_d + b0 * message_len, *dp = d_p + b0 * (size_t)c.ecc, *ds = d_s + b0;
-            FFGPU_CHECK_CUDA(cudaMemcpyAsync(dd, data + b0 * message_len, n * message_len, cudaMemcpyHostToDevice, st));
-            FFGPU_CHECK_CUDA(
-                cudaMemcpyAsync(dp, parity + b0 * (size_t)c.ecc, n * (size_t)c.ecc, cudaMemcpyHostToDevice, st));
+            const size_t od = b0 * message_len, op = b0 * (size_t)c.ecc;
+            uint8_t *dd = d_d + od, *dp = d_p + op, *ds = d_s + b0;
+            FFGPU_CHECK_CUDA(cudaMemcpyAsync(dd, data + od, n * message_len, cudaMemcpyHostToDevice, st));
+            FFGPU_CHECK_CUDA(cudaMemcpyAsync(dp, parity + op, n * (size_t)c.ecc, cudaMemcpyHostToDevice, st));
             rs256_decode(c, dd, dp, n, (int)message_len, ds, st);
-            FFGPU_CHECK_CUDA(cudaMemcpyAsync(data + b0 * message_len, dd, n * message_len, cudaMemcpyDeviceToHost, st));
-            FFGPU_CHECK_CUDA(
-                cudaMemcpyAsync(parity + b0 * (size_t)c.ecc, dp, n * (size_t)c.ecc, cudaMemcpyDeviceToHost, st));
+            FFGPU_CHECK_CUDA(cudaMemcpyAsync(h_d + od, dd, n * message_len, cudaMemcpyDeviceToHost, st));
+            FFGPU_CHECK_CUDA(cudaMemcpyAsync(h_p + op, dp, n * (size_t)c.ecc, cudaMemcpyDeviceToHost, st));
             FFGPU_CHECK_CUDA(cudaMemcpyAsync(h_s + b0, ds, n, cudaMemcpyDeviceToHost, st));
+            drain.copy(data + od, h_d + od, n * message_len);
+            drain.copy(parity + op, h_p + op, n * (size_t)c.ecc);
+            drain.copy(status + b0, h_s + b0, n);
+            drain.chunk(st);
         }
+        drain.finish();
         for (size_t i = 0; i < std::min<size_t>(k, kPipeStreams); ++i)
             FFGPU_CHECK_CUDA(cudaStreamSynchronize(pipe_stream(i)));
-        if (h_s != status) std::memcpy(status, h_s, nblocks);
     });
 }
 

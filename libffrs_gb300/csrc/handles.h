@@ -14,14 +14,14 @@ struct ffgpu_rs256 {
     std::unique_ptr<ffgpu::Rs256Code> code;
     std::mutex mu;
     ffgpu::DeviceBuffer d_data, d_parity, d_status;
-    ffgpu::PinnedBuffer h_status, h_parity;
+    ffgpu::PinnedBuffer h_data, h_parity, h_status;
 };
 
 struct ffgpu_rsi16 {
     std::unique_ptr<ffgpu::Rsi16Code> code;
     std::mutex mu;
     ffgpu::DeviceBuffer d_msg, d_par, d_status, d_pos;
-    ffgpu::PinnedBuffer h_status, h_par;
+    ffgpu::PinnedBuffer h_msg, h_par, h_status;
 };
 
 struct ffgpu_circ16 {
