@@ -870,8 +870,8 @@ __global__ void __launch_bounds__(64 * kSegs) bs_encode32_seg_kernel(const uint8
 // Decoding from the bitsliced syndromes, 32 blocks per plane word, following
 // rs_decode::decode (reed_solomon.hpp:559-595) step by step:
 //   * Berlekamp-Massey (berlekamp_massey, reed_solomon.hpp:655-702) in its
-//     normalised form C <- C - (d / b) x^m B, with x^m B kept pre-shifted and
-//     1 / b kept next to it; the length L is a 6-plane bitsliced counter;
+//     inversion-free form C <- b C - d x^m B, with x^m B kept pre-shifted;
+//     the length L is a 6-plane bitsliced counter;
 //   * error evaluator Omega = S * C mod x^t (its degree is below L whenever
 //     the decoder succeeds, so t coefficients are exact);
 //   * Chien search over the positions 0 .. size-1 with x = a^{-i}, as the
@@ -882,9 +882,7 @@ __global__ void __launch_bounds__(64 * kSegs) bs_encode32_seg_kernel(const uint8
 // number of roots equals L; this is exactly when the reference returns true
 // (with roots == L, C has L distinct roots and Omega != 0).
 //
-// One CTA = 32 groups (1024 blocks) and two warps: warp h keeps the
-// coefficients C_i, i = hK+1 .. hK+K (K = t/2) and the evaluator terms
-// Omega_k, k = 2v+h; the two halves meet through shared memory.
+// One CTA = 32 groups (1024 blocks) and four warps (see bs_solve_kernel).
 
 __device__ __forceinline__ void reduce15(uint32_t (&p)[15], uint32_t (&r)[8]) {
 #pragma unroll
@@ -1011,34 +1009,41 @@ __device__ __forceinline__ void l_update(uint32_t (&L)[6], int a, uint32_t cond)
 
 template <int E>
 struct SolveGeom {
+    static constexpr int P = 4;              // warps per tile
     static constexpr int t = E / 2;
-    static constexpr int K = t / 2;          // coefficients per warp
+    static constexpr int K = t / P;          // C coefficients and Omega terms per warp
     static constexpr int kS = E * 8 * 32;    // words: syndrome planes of 32 groups
-    // words: C_1..C_t planes of 32 groups; before them the BM exchange
-    // (2 buffers x 40 rows x 32), after them the root counters (2 x 32 x 32)
-    static constexpr int kC = t * 8 * 32 > 2 * 40 * 32 ? t * 8 * 32 : 2 * 40 * 32;
-    static constexpr int kX = 2 * 2 * 2 * 24 * 32;  // words: Chien exchange (2 buffers x 2 positions x 2 warps)
-    static constexpr int kSX = kS > kX ? kS : kX;
-    static constexpr size_t smem = (size_t)(kSX + kC) * 4 + 768;
+    // BM exchange rows: the d partials of every warp, then the top C and Bs
+    // of every warp but the last (the next warp's lower neighbours)
+    static constexpr int kXrows = P * 8 + (P - 1) * 16;
+    static constexpr int kX = 2 * kXrows * 32;     // double-buffered
+    static constexpr int kCp = (t + 1) * 8 * 32;   // C_0..C_t planes (Omega)
+    static constexpr int kCnt = 32 * 32;           // root counters [block][group]
+    static constexpr int kCx = P * P * 24 * 32;    // Chien exchange [position][warp][24][32]
+    static constexpr int kA = kS + (kX > kCp ? kX : kCp);
+    // the Chien exchange overlays the syndromes and the C planes, the root
+    // counters take the last kCnt words (both live only after Omega)
+    static constexpr int kWords = kA > kCx + kCnt ? kA : kCx + kCnt;
+    static constexpr size_t smem = (size_t)kWords * 4 + 768;
+    static_assert(K % 2 == 0, "K must be even");
 };
 
-// C_i <- C_i a^{-i}, Omega_k <- Omega_k a^{-k}
+// C_i <- C_i a^{-i}, Omega_k <- Omega_k a^{-k} (i = HK+1+u, k = Pu+H)
 template <int E, int H, int... U>
 __device__ __forceinline__ void chien_advance(uint32_t (&Ct)[SolveGeom<E>::K][8], uint32_t (&Ot)[SolveGeom<E>::K][8],
                                               std::integer_sequence<int, U...>) {
-    constexpr int K = SolveGeom<E>::K;
+    constexpr int K = SolveGeom<E>::K, P = SolveGeom<E>::P;
     (cmul_inplace<apow(-(H * K + 1 + U))>(Ct[U]), ...);
-    (cmul_inplace<apow(-(2 * U + H))>(Ot[U]), ...);
+    (cmul_inplace<apow(-(P * U + H))>(Ot[U]), ...);
 }
 
 // One Chien position for warp H: partial sums of the even / odd C terms and of
 // the Omega terms, then every term advances by its constant a^{-i}.
 template <int E, int H>
 __device__ __forceinline__ void chien_step(uint32_t (&Ct)[SolveGeom<E>::K][8], uint32_t (&Ot)[SolveGeom<E>::K][8],
-                                           uint32_t *out, int stride) {
+                                           const uint32_t (&C0)[8], uint32_t *out) {
     constexpr int K = SolveGeom<E>::K;
     // with K even, C_i (i = HK+1+u) has odd degree exactly for even u
-    static_assert(K % 2 == 0, "K must be even");
 #pragma unroll
     for (int b = 0; b < 8; ++b) {
         uint32_t po = Ct[0][b], pe = Ct[1][b];
@@ -1052,7 +1057,7 @@ __device__ __forceinline__ void chien_step(uint32_t (&Ct)[SolveGeom<E>::K][8], u
                 pe ^= Ct[u + 1][b];
             }
         }
-        if (H == 0 && b == 0) pe = ~pe;  // C_0 = 1
+        if (H == 0) pe ^= C0[b];
         uint32_t pw = Ot[0][b];
 #pragma unroll
         for (int v = 1; v < K; v += 2) {
@@ -1061,29 +1066,50 @@ __device__ __forceinline__ void chien_step(uint32_t (&Ct)[SolveGeom<E>::K][8], u
             else
                 pw ^= Ot[v][b];
         }
-        out[b * stride] = pe;
-        out[(8 + b) * stride] = po;
-        out[(16 + b) * stride] = pw;
+        out[b * 32] = pe;
+        out[(8 + b) * 32] = po;
+        out[(16 + b) * 32] = pw;
     }
     chien_advance<E, H>(Ct, Ot, std::make_integer_sequence<int, K>{});
 }
 
+// Partial sums of warp H for the P positions base .. base+P-1 of one step.
+template <int E, int H>
+__device__ __forceinline__ void chien_steps(uint32_t (&Ct)[SolveGeom<E>::K][8], uint32_t (&Ot)[SolveGeom<E>::K][8],
+                                            const uint32_t (&C0)[8], uint32_t *Xc, int lane) {
+    constexpr int P = SolveGeom<E>::P;
+#pragma unroll 1
+    for (int p = 0; p < P; ++p) chien_step<E, H>(Ct, Ot, C0, Xc + (p * P + H) * 24 * 32 + lane);
+}
+
+// One CTA = 32 groups (1024 blocks) and P = 4 warps: warp h keeps the
+// coefficients C_i, i = hK+1 .. hK+K (K = t/P), and the evaluator terms
+// Omega_k, k = Pv+h; warp 0 also keeps C_0.  The warps meet through shared
+// memory once per BM iteration and once per P Chien positions.
+//
+// Berlekamp-Massey runs inversion-free: C <- b C + d x^m B, B <- C and b <- d
+// on a length change.  Every C it produces is a non-zero multiple (per block)
+// of the normalised algorithm's C <- C - (d / b) x^m B, its discrepancies are
+// the same multiples of the normalised ones (so the same length changes
+// happen), and Omega = S C mod x^t carries the same factor: the roots, the
+// root count, L and the Forney values Omega(x) / Lodd(x) are the normalised
+// algorithm's.
 template <int E>
-__global__ void __launch_bounds__(64) bs_solve_kernel(uint8_t *__restrict__ data, uint8_t *__restrict__ parity,
-                                                      size_t nblocks, int msg_len, uint32_t *__restrict__ planes,
-                                                      uint8_t *__restrict__ status,
-                                                      const uint8_t *__restrict__ exp512,
-                                                      const uint8_t *__restrict__ log256) {
+__global__ void __launch_bounds__(128, 4) bs_solve_kernel(uint8_t *__restrict__ data, uint8_t *__restrict__ parity,
+                                                          size_t nblocks, int msg_len, uint32_t *__restrict__ planes,
+                                                          uint8_t *__restrict__ status,
+                                                          const uint8_t *__restrict__ exp512,
+                                                          const uint8_t *__restrict__ log256) {
     using G = SolveGeom<E>;
-    constexpr int t = G::t, K = G::K;
+    constexpr int t = G::t, K = G::K, P = G::P;
     extern __shared__ __align__(16) uint32_t sm[];
-    uint32_t *Ssm = sm;           // [E*8][32] syndrome planes; later the Chien exchange
-    uint32_t *Csm = sm + G::kSX;  // [t*8][32] C planes; before them the BM exchange, after them
-                                  // the root counters [2 warps][32 blocks][32 groups]
-    uint32_t *cnt = Csm;
-    uint8_t *ex = reinterpret_cast<uint8_t *>(Csm + G::kC);  // exp[512], log[256]
+    uint32_t *Ssm = sm;           // [E*8][32] syndrome planes
+    uint32_t *Xb = sm + G::kS;    // BM exchange, then the C planes
+    uint32_t *Csm = Xb;
+    uint32_t *Xc = sm;            // Chien exchange (after Omega)
+    uint32_t *cnt = sm + G::kWords - G::kCnt;
+    uint8_t *ex = reinterpret_cast<uint8_t *>(sm + G::kWords);  // exp[512], log[256]
     uint8_t *lg = ex + 512;
-    static_assert(G::kC >= 2 * 32 * 32, "root counters must fit in the C planes region");
 
     const int lane = threadIdx.x & 31, h = threadIdx.x >> 5;
     const size_t ngroups = (nblocks + 31) / 32;
@@ -1099,12 +1125,12 @@ __global__ void __launch_bounds__(64) bs_solve_kernel(uint8_t *__restrict__ data
         const char *src = reinterpret_cast<const char *>(tplanes);
         const uint32_t dst = (uint32_t)__cvta_generic_to_shared(Ssm);
 #pragma unroll 4
-        for (int off = threadIdx.x * 16; off < E * 1024; off += 64 * 16)
+        for (int off = threadIdx.x * 16; off < E * 1024; off += 128 * 16)
             asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst + off), "l"(src + off) : "memory");
         asm volatile("cp.async.commit_group;" ::: "memory");
     }
-    for (int i = threadIdx.x; i < 512; i += 64) ex[i] = exp512[i];
-    for (int i = threadIdx.x; i < 256; i += 64) lg[i] = log256[i];
+    for (int i = threadIdx.x; i < 512; i += 128) ex[i] = exp512[i];
+    for (int i = threadIdx.x; i < 256; i += 128) lg[i] = log256[i];
     asm volatile("cp.async.wait_group 0;" ::: "memory");
     __syncthreads();
     uint32_t anyS = 0u;
@@ -1113,7 +1139,7 @@ __global__ void __launch_bounds__(64) bs_solve_kernel(uint8_t *__restrict__ data
     const uint32_t vmask = !valid ? 0u : (nblocks - blk0 >= 32 ? ~0u : ((1u << (nblocks - blk0)) - 1u));
 
     // phase 1: Berlekamp-Massey
-    uint32_t C[K][8], Bs[K][8], binv[8], L[6];
+    uint32_t C[K][8], Bs[K][8], C0[8], bb[8], L[6];
 #pragma unroll
     for (int u = 0; u < K; ++u)
 #pragma unroll
@@ -1122,16 +1148,23 @@ __global__ void __launch_bounds__(64) bs_solve_kernel(uint8_t *__restrict__ data
             Bs[u][b] = (h == 0 && u == 0 && b == 0) ? ~0u : 0u;  // x^1 * B, B = 1
         }
 #pragma unroll
-    for (int b = 0; b < 8; ++b) binv[b] = b == 0 ? ~0u : 0u;
+    for (int b = 0; b < 8; ++b) C0[b] = bb[b] = b == 0 ? ~0u : 0u;  // C_0 = 1, b = 1
 #pragma unroll
     for (int b = 0; b < 6; ++b) L[b] = 0u;
-    uint32_t *Xb = Csm;  // [2 buffers][40 rows][32]: d partials of both warps, warp 0's top C and Bs, 1/b
+    constexpr int kTop = P * 8;  // first exchange row of the warp tops
 #pragma unroll 1
     for (int n = 0; n < E; ++n) {
-        // partial discrepancy, one reduction for all products
+        // partial discrepancy, one reduction for all products; at the start
+        // of iteration n, C_i = 0 for i > n
         uint32_t p15[15];
 #pragma unroll
-        for (int k = 0; k < 15; ++k) p15[k] = (h == 0 && k < 8) ? Ssm[(n * 8 + k) * 32 + lane] : 0u;
+        for (int k = 0; k < 15; ++k) p15[k] = 0u;
+        if (h == 0) {
+            uint32_t sn[8];
+#pragma unroll
+            for (int b = 0; b < 8; ++b) sn[b] = Ssm[(n * 8 + b) * 32 + lane];
+            vmul_acc15(C0, sn, p15);
+        }
 #pragma unroll
         for (int u = 0; u < K; ++u) {
             const int j = n - (h * K + 1 + u);
@@ -1144,121 +1177,134 @@ __global__ void __launch_bounds__(64) bs_solve_kernel(uint8_t *__restrict__ data
         }
         uint32_t dp[8];
         reduce15(p15, dp);
-        uint32_t *X = Xb + (n & 1) * (40 * 32);
+        uint32_t *X = Xb + (n & 1) * (G::kXrows * 32);
 #pragma unroll
         for (int b = 0; b < 8; ++b) X[(h * 8 + b) * 32 + lane] = dp[b];
-        if (h == 0) {
+        if (h < P - 1) {
 #pragma unroll
             for (int b = 0; b < 8; ++b) {
-                X[(16 + b) * 32 + lane] = C[K - 1][b];
-                X[(24 + b) * 32 + lane] = Bs[K - 1][b];
-                X[(32 + b) * 32 + lane] = binv[b];
+                X[(kTop + h * 16 + b) * 32 + lane] = C[K - 1][b];
+                X[(kTop + h * 16 + 8 + b) * 32 + lane] = Bs[K - 1][b];
             }
         }
         __syncthreads();
         uint32_t d[8], nzd = 0u;
 #pragma unroll
         for (int b = 0; b < 8; ++b) {
-            d[b] = X[b * 32 + lane] ^ X[(8 + b) * 32 + lane];
-            nzd |= d[b];
+            uint32_t s = X[b * 32 + lane];
+#pragma unroll
+            for (int w = 1; w < P; ++w) s ^= X[(w * 8 + b) * 32 + lane];
+            d[b] = s;
+            nzd |= s;
         }
         const uint32_t cond = nzd & le_const(L, n >> 1);
-        uint32_t q[8];
-        if (h == 0) {
-            // warp 0 keeps 1/b (the inverse costs 4 products and 7 squares)
-            vmul(d, binv, q);
-            uint32_t dinv[8];
-            vinv(d, dinv);
-#pragma unroll
-            for (int b = 0; b < 8; ++b) binv[b] = bitsel(cond, dinv[b], binv[b]);
-        } else {
-            uint32_t bi[8];
-#pragma unroll
-            for (int b = 0; b < 8; ++b) bi[b] = X[(32 + b) * 32 + lane];
-            vmul(d, bi, q);
-        }
-        // C_i ^= q * Bs_i and Bs_i <- cond ? C_{i-1} : Bs_{i-1}, from the top down
+        // C_i <- b C_i + d Bs_i and Bs_i <- cond ? C_{i-1} : Bs_{i-1}, from
+        // the top down; C_i = Bs_i = 0 for i > n+1, so those products are
+        // skipped
 #pragma unroll
         for (int u = K - 1; u >= 0; --u) {
-            uint32_t pr[8];
-            vmul(q, Bs[u], pr);
+            uint32_t lc[8], lb[8];
 #pragma unroll
             for (int b = 0; b < 8; ++b) {
-                uint32_t lc, lb;
                 if (u > 0) {
-                    lc = C[u - 1][b];
-                    lb = Bs[u - 1][b];
+                    lc[b] = C[u - 1][b];
+                    lb[b] = Bs[u - 1][b];
                 } else if (h == 0) {
-                    lc = b == 0 ? ~0u : 0u;  // C_0 = 1, Bs_0 = 0
-                    lb = 0u;
+                    lc[b] = C0[b];  // Bs_0 = 0
+                    lb[b] = 0u;
                 } else {
-                    lc = X[(16 + b) * 32 + lane];
-                    lb = X[(24 + b) * 32 + lane];
+                    lc[b] = X[(kTop + (h - 1) * 16 + b) * 32 + lane];
+                    lb[b] = X[(kTop + (h - 1) * 16 + 8 + b) * 32 + lane];
                 }
-                C[u][b] ^= pr[b];
-                Bs[u][b] = bitsel(cond, lc, lb);
             }
+            if (h * K + 1 + u <= n + 1) {
+                uint32_t pr[15];
+#pragma unroll
+                for (int k = 0; k < 15; ++k) pr[k] = 0u;
+                vmul_acc15(bb, C[u], pr);
+                vmul_acc15(d, Bs[u], pr);
+                reduce15(pr, C[u]);
+            }
+#pragma unroll
+            for (int b = 0; b < 8; ++b) Bs[u][b] = bitsel(cond, lc[b], lb[b]);
         }
+        if (h == 0) vmul(bb, C0, C0);
+#pragma unroll
+        for (int b = 0; b < 8; ++b) bb[b] = bitsel(cond, d[b], bb[b]);
         l_update(L, n + 1, cond);
     }
-    __syncthreads();  // BM exchange reads done before Csm is rewritten
+    __syncthreads();  // BM exchange reads done before the C planes overwrite it
 
-    // phase 2: Omega_k = S_k + sum_{i=1}^{k} C_i S_{k-i}, k = 2v + h
+    // phase 2: Omega_k = sum_{i=0}^{k} C_i S_{k-i}, k = Pv + h
+    if (h == 0) {
+#pragma unroll
+        for (int b = 0; b < 8; ++b) Csm[b * 32 + lane] = C0[b];
+    }
 #pragma unroll
     for (int u = 0; u < K; ++u)
 #pragma unroll
-        for (int b = 0; b < 8; ++b) Csm[((h * K + u) * 8 + b) * 32 + lane] = C[u][b];
+        for (int b = 0; b < 8; ++b) Csm[((h * K + u + 1) * 8 + b) * 32 + lane] = C[u][b];
     __syncthreads();
     uint32_t Ot[K][8];
 #pragma unroll
     for (int v = 0; v < K; ++v) {
-        const int k = 2 * v + h;
+        const int k = P * v + h;
         uint32_t p15[15];
 #pragma unroll
-        for (int q = 0; q < 15; ++q) p15[q] = q < 8 ? Ssm[(k * 8 + q) * 32 + lane] : 0u;
-        for (int i = 1; i <= k; ++i) {
+        for (int q = 0; q < 15; ++q) p15[q] = 0u;
+        for (int i = 0; i <= k; ++i) {
             uint32_t ci[8], sj[8];
 #pragma unroll
             for (int b = 0; b < 8; ++b) {
-                ci[b] = Csm[((i - 1) * 8 + b) * 32 + lane];
+                ci[b] = Csm[(i * 8 + b) * 32 + lane];
                 sj[b] = Ssm[((k - i) * 8 + b) * 32 + lane];
             }
             vmul_acc15(ci, sj, p15);
         }
         reduce15(p15, Ot[v]);
     }
-    __syncthreads();  // Ssm becomes the Chien exchange, Csm the root counters
-    for (int i = threadIdx.x; i < 2 * 32 * 32; i += 64) cnt[i] = 0u;
+    if (h != 0) {
+#pragma unroll
+        for (int b = 0; b < 8; ++b) C0[b] = 0u;  // only warp 0 adds the C_0 term
+    }
+    __syncthreads();  // the syndromes and C planes become the Chien exchange
+    for (int i = threadIdx.x; i < G::kCnt; i += 128) cnt[i] = 0u;
     __syncthreads();
 
-    // phase 3: Chien search and Forney, two positions per exchange
+    // phase 3: Chien search and Forney, P positions per exchange; warp h
+    // takes position base + h
     const int size = msg_len + E;
     uint8_t *corr = reinterpret_cast<uint8_t *>(tplanes) + (size_t)lane * (E * 32);  // [32 blocks][t][2]
-    uint32_t *mycnt = cnt + h * 1024;
     const uint32_t live = anyS & vmask;
 #pragma unroll 1
-    for (int base = 0, it = 0; base < size; base += 2, ++it) {
-        uint32_t *Xc = Ssm + (it & 1) * (2 * 2 * 24 * 32);  // [2 positions][2 warps][24][32]
-        if (h == 0) {
-            chien_step<E, 0>(C, Ot, Xc + (0 * 2 + 0) * 24 * 32 + lane, 32);
-            chien_step<E, 0>(C, Ot, Xc + (1 * 2 + 0) * 24 * 32 + lane, 32);
-        } else {
-            chien_step<E, 1>(C, Ot, Xc + (0 * 2 + 1) * 24 * 32 + lane, 32);
-            chien_step<E, 1>(C, Ot, Xc + (1 * 2 + 1) * 24 * 32 + lane, 32);
+    for (int base = 0; base < size; base += P) {
+        switch (h) {
+            case 0: chien_steps<E, 0>(C, Ot, C0, Xc, lane); break;
+            case 1: chien_steps<E, 1>(C, Ot, C0, Xc, lane); break;
+            case 2: chien_steps<E, 2>(C, Ot, C0, Xc, lane); break;
+            default: chien_steps<E, 3>(C, Ot, C0, Xc, lane); break;
         }
         __syncthreads();
-        const int i = base + h;  // warp h takes position base + h
-        if (i < size) {
-            const uint32_t *A = Xc + (h * 2 + 0) * 24 * 32 + lane;
-            const uint32_t *B = Xc + (h * 2 + 1) * 24 * 32 + lane;
-            uint32_t lo[8], om[8], nz = 0u;
+        const int i = base + h;
+        uint32_t lo[8], om[8], nz = 0u;
+        {
+            const uint32_t *A = Xc + (h * P) * 24 * 32 + lane;
 #pragma unroll
             for (int b = 0; b < 8; ++b) {
-                const uint32_t o = A[(8 + b) * 32] ^ B[(8 + b) * 32];
-                nz |= xor3(A[b * 32], B[b * 32], o);
-                lo[b] = o;
-                om[b] = A[(16 + b) * 32] ^ B[(16 + b) * 32];
+                uint32_t ce = A[b * 32], co = A[(8 + b) * 32], cw = A[(16 + b) * 32];
+#pragma unroll
+                for (int w = 1; w < P; ++w) {
+                    ce ^= A[(w * 24 + b) * 32];
+                    co ^= A[(w * 24 + 8 + b) * 32];
+                    cw ^= A[(w * 24 + 16 + b) * 32];
+                }
+                nz |= ce ^ co;
+                lo[b] = co;
+                om[b] = cw;
             }
+        }
+        __syncthreads();  // every warp has read its position before the next writes
+        if (i < size) {
             uint32_t roots = ~nz & live;
             const int pos = size - 1 - i;
             while (roots) {
@@ -1271,10 +1317,8 @@ __global__ void __launch_bounds__(64) bs_solve_kernel(uint8_t *__restrict__ data
                     lb |= ((lo[b] >> j) & 1u) << b;
                 }
                 const uint32_t e = (ob && lb) ? ex[lg[ob] + 255 - lg[lb]] : 0u;
-                const int c = (int)mycnt[j * 32 + lane];
-                mycnt[j * 32 + lane] = (uint32_t)(c + 1);
-                const int slot = h == 0 ? c : t - 1 - c;
-                if (slot >= 0 && slot < t) {
+                const int slot = (int)atomicAdd(&cnt[j * 32 + lane], 1u);
+                if (slot < t) {
                     corr[(j * t + slot) * 2] = (uint8_t)pos;
                     corr[(j * t + slot) * 2 + 1] = (uint8_t)e;
                 }
@@ -1283,12 +1327,13 @@ __global__ void __launch_bounds__(64) bs_solve_kernel(uint8_t *__restrict__ data
     }
     __syncthreads();
 
-    // phase 4: status and corrections, warp h takes blocks 16h .. 16h+15.
+    // phase 4: status and corrections, warp h takes blocks 8h .. 8h+7.
     // Each block's list is 2t bytes (16-byte aligned); four blocks' lists are
     // fetched together so that their L2 round trips overlap.
     constexpr int NV = (2 * t) / 16;  // uint4 per block list
+    constexpr int BPW = 32 / P;       // blocks per warp
 #pragma unroll 1
-    for (int j0 = h * 16; j0 < h * 16 + 16; j0 += 4) {
+    for (int j0 = h * BPW; j0 < h * BPW + BPW; j0 += 4) {
         uint4 cv[4][NV];
 #pragma unroll
         for (int r = 0; r < 4; ++r)
@@ -1307,8 +1352,8 @@ __global__ void __launch_bounds__(64) bs_solve_kernel(uint8_t *__restrict__ data
             int l = 0;
 #pragma unroll
             for (int b = 0; b < 6; ++b) l |= (int)((L[b] >> j) & 1u) << b;
-            const int c0 = (int)cnt[j * 32 + lane], c1 = (int)cnt[1024 + j * 32 + lane];
-            if (l > t || c0 + c1 != l) {
+            const int c = (int)cnt[j * 32 + lane];
+            if (l > t || c != l) {
                 status[blk] = 0;
                 continue;
             }
@@ -1316,7 +1361,7 @@ __global__ void __launch_bounds__(64) bs_solve_kernel(uint8_t *__restrict__ data
             // are 4-byte aligned on this path; neighbouring blocks share words)
 #pragma unroll
             for (int sl = 0; sl < t; ++sl) {
-                if (sl >= c0 && sl < t - c1) continue;
+                if (sl >= c) continue;
                 const uint4 q = cv[r][sl / 8];
                 const uint32_t wv = (sl % 8) < 2 ? q.x : (sl % 8) < 4 ? q.y : (sl % 8) < 6 ? q.z : q.w;
                 const uint32_t pe = wv >> (16 * (sl & 1));
@@ -1424,9 +1469,12 @@ static void launch_bs_decode(const Rs256Code &c, uint8_t *data, uint8_t *parity,
     }
     FFGPU_CHECK_CUDA(cudaFuncSetAttribute(bs::bs_solve_kernel<E>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)bs::SolveGeom<E>::smem));
+    // four CTAs of 128 threads per SM need the largest shared-memory carveout
+    FFGPU_CHECK_CUDA(
+        cudaFuncSetAttribute(bs::bs_solve_kernel<E>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     const size_t ntiles = ((nblocks + 31) / 32 + 31) / 32;
     KernelTimer kt_timer("bs_solve_kernel", st);
-    bs::bs_solve_kernel<E><<<(unsigned)ntiles, 64, bs::SolveGeom<E>::smem, st>>>(
+    bs::bs_solve_kernel<E><<<(unsigned)ntiles, 128, bs::SolveGeom<E>::smem, st>>>(
         data, parity, nblocks, msg_len, planes, status, c.d_exp512, c.d_log256);
     check_launch("bs_solve_kernel");
 }
