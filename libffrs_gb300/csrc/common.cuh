@@ -49,7 +49,7 @@ inline void check_launch(const char *what) {
 
 cudaStream_t lib_stream();
 // k-th stream (mod kPipeStreams) of the chunked host-buffer pipelines
-constexpr size_t kPipeStreams = 3;
+constexpr size_t kPipeStreams = 8;
 cudaStream_t pipe_stream(size_t k);
 // blocks per chunk of a host-buffer pipeline: ffgpu_set_host_chunk_blocks, or
 // at least min_chunk and at most max_chunks chunks

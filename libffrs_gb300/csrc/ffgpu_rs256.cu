@@ -392,7 +392,7 @@ int ffgpu_rs256_decode_host(const ffgpu_rs256 *code, uint8_t *data, uint8_t *par
         // chunks of blocks on the pipeline streams: the host-to-device copy of
         // one chunk, the decode of another and the copy back of a third
         // overlap (page-locked host memory moves at full speed)
-        const size_t chunk = host_chunk_blocks(nblocks, 262144, 4);
+        const size_t chunk = host_chunk_blocks(nblocks, 65536, 16);
         const bool chunked = chunk < nblocks;
         uint8_t *h_d = pipeline_out(data, chunked, h->h_data, nd);
         uint8_t *h_p = pipeline_out(parity, chunked, h->h_parity, np);

@@ -208,7 +208,7 @@ int ffgpu_rsi16_repair_host(const ffgpu_rsi16 *code, uint16_t *msg, uint16_t *pa
             // repairs over the pipeline streams (only when the repair
             // workspace lives in shared memory: the global fallback workspace
             // is one per thread and cannot serve concurrent streams)
-            const size_t chunk = host_chunk_blocks(nblocks, 32768, 8);
+            const size_t chunk = host_chunk_blocks(nblocks, 16384, 16);
             // outputs in pageable memory come back through page-locked staging
             const bool chunked = chunk < nblocks;
             uint16_t *h_m = pipeline_out(msg, chunked, h->h_msg, nm * 2);
