@@ -222,6 +222,85 @@ __global__ void rsi16_repair_warp_kernel(Rsi16Dev c, BlockView v, size_t nblocks
     }
 }
 
+// ecc 32 and 64: batches of 32 blocks per warp, syndromes warp-wide,
+// Berlekamp-Massey one block per lane, roots and Forney warp-wide.  A block
+// the bounded-distance path does not accept is marked kMirrorPending and left
+// for rsi16_repair_mirror_kernel, so that this kernel's warp workspace is only
+// the batch's syndrome columns [ecc][33], locator columns [ecc/2 + 1][33] and
+// the finishing scratch (2 ecc + 2 words).
+constexpr uint8_t kMirrorPending = 0xFE;
+
+template <int EPL>
+__global__ void __launch_bounds__(128, 4) rsi16_repair_batch_kernel(Rsi16Dev c, BlockView v, size_t nblocks,
+                                                                 uint8_t *status, const uint8_t *active,
+                                                                 uint32_t ws_words) {
+    constexpr int T = 16 * EPL;
+    WarpCtx w = warp_ctx(nullptr, ws_words);
+    RegTw<EPL> tw;
+    reg_twiddles<EPL>(c, w.lane, tw);
+    uint32_t *Ssm = w.ws;
+    uint32_t *Csm = Ssm + 32 * EPL * kColStride;
+    uint32_t *fin = Csm + (T + 1) * kColStride;
+    unsigned long long nfast = 0;
+    for (size_t base = (size_t)w.warp_global * 32; base < nblocks; base += (size_t)w.nwarps * 32) {
+        const int nb = (int)min((size_t)32, nblocks - base);
+        uint32_t live = 0u, nz = 0u;
+        for (int j = 0; j < nb; ++j) {
+            const size_t b = base + j;
+            if (active && !active[b]) continue;
+            live |= 1u << j;
+            uint32_t s[EPL];
+            reg_pntt<EPL>(c, v, b, c.pntt_blocks, true, tw, w.lane, s);
+            bool any = false;
+#pragma unroll
+            for (int h = 0; h < EPL; ++h) {
+                Ssm[(w.lane * EPL + h) * kColStride + j] = s[h];
+                any |= s[h] != 0;
+            }
+            if (__any_sync(0xffffffffu, any)) nz |= 1u << j;
+        }
+        __syncwarp();
+        uint32_t L = 0;
+        if ((nz >> w.lane) & 1u) {
+            uint32_t C[T + 1];
+            L = rsi16_bm_lane<T>(Ssm + w.lane, c.inv_tab, c.ecc, C);
+#pragma unroll
+            for (int i = 0; i <= T; ++i) Csm[i * kColStride + w.lane] = C[i];
+        }
+        __syncwarp();
+        for (int j = 0; j < nb; ++j) {
+            if (!((live >> j) & 1u)) continue;
+            const size_t b = base + j;
+            ++nfast;
+            if (!((nz >> j) & 1u)) {
+                if (w.lane == 0) status[b] = FFGPU_NO_ERRORS;
+                continue;
+            }
+            const uint32_t Lj = __shfl_sync(0xffffffffu, L, j);
+            if (!rsi16_repair_finish_t<EPL>(c, v, b, Ssm + j, Csm + j, Lj, fin, status, tw, w.lane)) {
+                if (w.lane == 0) status[b] = kMirrorPending;
+                --nfast;
+            }
+        }
+        __syncwarp();  // the batch's columns are read before the next batch writes them
+    }
+    if (w.lane == 0 && nfast) atomicAdd(&g_repair_fast_blocks, nfast);
+}
+
+// The step-for-step mirror for the blocks rsi16_repair_batch_kernel marked.
+__global__ void rsi16_repair_mirror_kernel(Rsi16Dev c, BlockView v, size_t nblocks, uint8_t *status,
+                                           const uint8_t *active, uint32_t *gscratch, uint32_t ws_words) {
+    WarpCtx w = warp_ctx(gscratch, ws_words);
+    unsigned long long nmirror = 0;
+    for (size_t b = w.warp_global; b < nblocks; b += w.nwarps) {
+        if ((active && !active[b]) || status[b] != kMirrorPending) continue;
+        __syncwarp();
+        rsi16_repair_block(c, v, b, w.ws, status, w.lane);
+        ++nmirror;
+    }
+    if (w.lane == 0 && nmirror) atomicAdd(&g_repair_mirror_blocks, nmirror);
+}
+
 void rsi16_repair_counters(uint64_t *fast, uint64_t *mirror, bool reset) {
     unsigned long long f = 0, m = 0;
     FFGPU_CHECK_CUDA(cudaDeviceSynchronize());
@@ -379,6 +458,27 @@ void rsi16_repair(const Rsi16Code &c, const BlockView &v, size_t nblocks, uint8_
     if (!nblocks) return;
     auto go = [&](auto epl) {
         constexpr int E = decltype(epl)::value;
+        if constexpr (E == 1 || E == 2) {
+            const uint32_t ws = (uint32_t)((c.ecc + c.ecc / 2 + 1) * kColStride + 2 * c.ecc + 2);
+            const size_t smem = 4 * (size_t)ws * 4;  // four warps per CTA
+            const size_t batches = (nblocks + 31) / 32;
+            const int per_sm = std::max(1, (int)((220 * 1024) / (smem + 1024)));
+            const unsigned grid =
+                (unsigned)std::max<size_t>(1, std::min<size_t>((batches + 3) / 4, (size_t)num_sms() * per_sm));
+            FFGPU_CHECK_CUDA(cudaFuncSetAttribute(rsi16_repair_batch_kernel<E>,
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            {
+                KernelTimer kt_timer("rsi16_repair_batch_kernel", st);
+                rsi16_repair_batch_kernel<E><<<grid, 128, smem, st>>>(c.dev, v, nblocks, status, active, ws);
+                check_launch("rsi16_repair_batch_kernel");
+            }
+            Launch L = plan(rsi16_repair_mirror_kernel, nblocks, c.dev.temp_len + 1);
+            KernelTimer kt_timer("rsi16_repair_mirror_kernel", st);
+            rsi16_repair_mirror_kernel<<<L.grid, L.threads, L.smem, st>>>(c.dev, v, nblocks, status, active,
+                                                                         L.gscratch, L.ws_words);
+            check_launch("rsi16_repair_mirror_kernel");
+            return;
+        }
         Launch L = plan(rsi16_repair_warp_kernel<E>, nblocks, c.dev.temp_len + 1);
         KernelTimer kt_timer("rsi16_repair_warp_kernel", st);
         rsi16_repair_warp_kernel<E><<<L.grid, L.threads, L.smem, st>>>(c.dev, v, nblocks, status, active,

@@ -787,6 +787,135 @@ static __device__ __forceinline__ bool rsi16_repair_bm_block(const Rsi16Dev &c, 
     return rsi16_repair_bm_block_t<0>(c, v, b, temp, status, none, lane);
 }
 
+// ---------------------------------------------------------------- batched repair
+//
+// The bounded-distance path above, with Berlekamp-Massey run by one lane per
+// block over a batch of 32 blocks: the syndromes of the batch are computed
+// warp-wide (register transforms) into the columns of a [ecc][32] array, each
+// lane then runs the whole iteration for its block on registers, and the
+// roots and Forney values are found warp-wide again per block.  The warp-wide
+// Berlekamp-Massey spends a shuffle reduction and three passes over the
+// coefficients per iteration on one block; here those become per-lane loops.
+// Columns are padded to 33 words so that both the row writes of the
+// transforms and the column reads of the lanes avoid bank conflicts.
+constexpr uint32_t kColStride = 33;
+
+// Normalised Berlekamp-Massey over GF(65537) for one block (lane): the same
+// iteration as rsi16_repair_bm_block_t, C <- C - (d / b) x^m B, with x^m B kept
+// pre-shifted and T + 1 = ecc/2 + 1 coefficients.  A block that the
+// bounded-distance path accepts ends with L <= T; while L <= T the locator has
+// degree <= L and every shifted B that is used has degree <= L, and once L
+// exceeds T it never comes back below (the block then goes to the mirror), so
+// the dropped terms never change an accepted result.  S points at S_0 of the
+// block's column (stride kColStride).  Returns L; C receives the locator.
+template <int T>
+static __device__ __forceinline__ uint32_t rsi16_bm_lane(const uint32_t *S, const uint32_t *inv_tab, uint32_t ecc,
+                                                         uint32_t (&C)[T + 1]) {
+    uint32_t Bs[T + 1];
+#pragma unroll
+    for (int i = 0; i <= T; ++i) {
+        C[i] = i == 0 ? 1u : 0u;
+        Bs[i] = i == 1 ? 1u : 0u;  // x^1 * B, B = 1
+    }
+    uint32_t L = 0, binv = 1;
+#pragma unroll 1
+    for (uint32_t n = 0; n < ecc; ++n) {
+        // d = sum_i C_i S_{n-i}: products below 2^33, 64-bit sum, one reduction
+        uint64_t acc = 0;
+#pragma unroll
+        for (int i = 0; i <= T; ++i)
+            if ((uint32_t)i <= n) acc += (uint64_t)C[i] * S[(n - i) * kColStride];
+        const uint32_t d = (uint32_t)(acc % 0x10001u);
+        const uint32_t coef = fmul(d, binv);
+        const bool grow = d != 0 && 2 * L <= n;
+        // C_i <- C_i - coef Bs_i and Bs_i <- grow ? C_{i-1} : Bs_{i-1}, top down
+#pragma unroll
+        for (int i = T; i >= 0; --i) {
+            const uint32_t bi = Bs[i];
+            Bs[i] = i == 0 ? 0u : (grow ? C[i - 1] : Bs[i - 1]);
+            C[i] = fsub(C[i], fmul(coef, bi));
+        }
+        if (grow) {
+            L = n + 1 - L;
+            binv = inv_tab[d];
+        }
+    }
+    return L;
+}
+
+// The rest of the bounded-distance path for block b, from its syndromes (column
+// S) and the lane Berlekamp-Massey's locator (column C, T + 1 words) and
+// length L: the degree check, the roots by inverse partial
+// NTT, Omega = S * C mod x^L and Forney, exactly as in rsi16_repair_bm_block_t.
+// temp holds the positions, Omega and C' (ecc + 2 + ecc words).  Returns false
+// when the block must go to the mirror (nothing written).
+template <int EPL>
+static __device__ __forceinline__ bool rsi16_repair_finish_t(const Rsi16Dev &c, const BlockView &v, size_t b,
+                                                         const uint32_t *S, const uint32_t *C, uint32_t L,
+                                                         uint32_t *temp, uint8_t *status, const RegTw<EPL> &tw,
+                                                         int lane) {
+    const uint32_t ecc = c.ecc, t = ecc / 2, n1 = ecc + 1;
+    if (L == 0 || L > t) return false;
+    // C must have degree exactly L (checked through the root count below)
+    bool high = false;
+    for (uint32_t k = L + 1 + lane; k <= t; k += 32) high |= C[k * kColStride] != 0;
+    if (__any_sync(0xffffffffu, high)) return false;
+    uint32_t *Tp = temp, *Om = temp + n1, *D = Om + t + 1;
+    uint32_t count = 0;
+    {
+        uint32_t cr[EPL];
+#pragma unroll
+        for (int h = 0; h < EPL; ++h) {
+            const uint32_t k = (uint32_t)(lane * EPL + h);
+            cr[h] = k <= L ? C[k * kColStride] : 0u;
+        }
+        const uint32_t nch = c.block_len / ecc;
+        for (uint32_t ch = 0; ch < nch; ++ch) {
+            uint32_t x[EPL];
+#pragma unroll
+            for (int h = 0; h < EPL; ++h) x[h] = fmul(cr[h], c.pintt_shift[ch * ecc + lane * EPL + h]);
+            reg_gs<EPL>(x, tw, lane);
+#pragma unroll
+            for (int h = 0; h < EPL; ++h) {
+                const bool hit = x[h] == 0;
+                const uint32_t msk = __ballot_sync(0xffffffffu, hit);
+                const uint32_t at = count + __popc(msk & ((1u << lane) - 1u));
+                if (hit && at < n1) Tp[at] = ch * ecc + lane * EPL + h;
+                count += __popc(msk);
+            }
+        }
+    }
+    __syncwarp();
+    if (count != L) return false;
+    // evaluator Omega = S * C mod x^L and the derivative C'
+    for (uint32_t j = lane; j < L; j += 32) {
+        uint32_t s = 0;
+        for (uint32_t k = 0; k <= j; ++k) s = fadd(s, fmul(C[k * kColStride], S[(j - k) * kColStride]));
+        Om[j] = s;
+        D[j] = fmul(C[(j + 1) * kColStride], j + 1);
+    }
+    __syncwarp();
+    const uint32_t N = c.ntt_len;
+    for (uint32_t r = lane; r < L; r += 32) {
+        const uint32_t i = Tp[r];
+        uint16_t bb = (uint16_t)i;
+        bb = (uint16_t)(((bb >> 1) & 0x5555) | ((bb & 0x5555) << 1));
+        bb = (uint16_t)(((bb >> 2) & 0x3333) | ((bb & 0x3333) << 2));
+        bb = (uint16_t)(((bb >> 4) & 0x0f0f) | ((bb & 0x0f0f) << 4));
+        bb = (uint16_t)((bb >> 8) | (bb << 8));
+        const uint32_t e = (uint32_t)(bb >> c.rbo_shift);
+        const uint32_t x = c.roots_ntt[e];
+        const uint32_t xi = c.roots_ntt[(N - e) & (N - 1)];
+        const uint32_t num = eval_poly(Om, L, xi);
+        const uint32_t den = eval_poly(D, L, xi);
+        const uint32_t err = fmul(fmul(num, c.inv_tab[den]), x);
+        put_pos(c, v, b, i, fadd(get_pos(c, v, b, i), err));
+    }
+    __syncwarp();
+    if (lane == 0) status[b] = FFGPU_REPAIR_OK;
+    return true;
+}
+
 // RSi16v::_repair with known locations (rsi16v_impl.hpp:171-231),
 // _error_locator (:531-542), _error_evaluator (:545-563); positions bp[0 .. count)
 static __device__ __noinline__ void rsi16_repair_known_block(const Rsi16Dev &c, const BlockView &v, size_t b,
