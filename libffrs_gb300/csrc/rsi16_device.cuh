@@ -435,28 +435,39 @@ struct RegTw {
     uint32_t gs[7][EPL];  // roots_i_ecc[(e & (stride - 1)) << ef], stride = n/2, n/4, ...
 };
 
+// log2 of the register-transform length 32 * EPL
+template <int EPL>
+constexpr int reg_log() {
+    return EPL == 1 ? 5 : (EPL == 2 ? 6 : 7);
+}
+
+// (every stage loop below has one constant trip count, so that it unrolls
+// completely and the twiddle arrays stay in registers)
 template <int EPL>
 static __device__ __forceinline__ void reg_twiddles(const Rsi16Dev &c, int lane, RegTw<EPL> &tw) {
+    constexpr int LOG = reg_log<EPL>();
     constexpr uint32_t n = 32 * EPL;
-    int st = 0;
 #pragma unroll
-    for (uint32_t stride = 1, ef = n >> 1; stride < n; stride <<= 1, ef >>= 1, ++st)
+    for (int st = 0; st < LOG; ++st) {
+        const uint32_t stride = 1u << st, ef = (n >> 1) >> st;
 #pragma unroll
         for (int h = 0; h < EPL; ++h) tw.ct[st][h] = c.roots_ecc[ef * ((lane * EPL + h) & (stride - 1))];
-    st = 0;
+    }
 #pragma unroll
-    for (uint32_t stride = n >> 1, ef = 0; stride > 0; stride >>= 1, ++ef, ++st)
+    for (int st = 0; st < LOG; ++st) {
+        const uint32_t stride = (n >> 1) >> st, ef = (uint32_t)st;
 #pragma unroll
         for (int h = 0; h < EPL; ++h) tw.gs[st][h] = c.roots_i_ecc[((lane * EPL + h) & (stride - 1)) << ef];
+    }
 }
 
 // ct_butterfly on registers: RBO input, normal order output
 template <int EPL>
 static __device__ __forceinline__ void reg_ct(uint32_t (&x)[EPL], const RegTw<EPL> &tw, int lane) {
-    constexpr int n = 32 * EPL;
-    int st = 0;
+    constexpr int LOG = reg_log<EPL>();
 #pragma unroll
-    for (int stride = 1; stride < n; stride <<= 1, ++st) {
+    for (int st = 0; st < LOG; ++st) {
+        const int stride = 1 << st;
         if (stride < EPL) {
 #pragma unroll
             for (int h = 0; h < EPL; ++h) {
@@ -481,10 +492,11 @@ static __device__ __forceinline__ void reg_ct(uint32_t (&x)[EPL], const RegTw<EP
 // gs_butterfly on registers: normal order input, RBO output
 template <int EPL>
 static __device__ __forceinline__ void reg_gs(uint32_t (&x)[EPL], const RegTw<EPL> &tw, int lane) {
+    constexpr int LOG = reg_log<EPL>();
     constexpr int n = 32 * EPL;
-    int st = 0;
 #pragma unroll
-    for (int stride = n >> 1; stride > 0; stride >>= 1, ++st) {
+    for (int st = 0; st < LOG; ++st) {
+        const int stride = (n >> 1) >> st;
         if (stride < EPL) {
 #pragma unroll
             for (int h = 0; h < EPL; ++h) {
@@ -870,6 +882,7 @@ static __device__ __forceinline__ bool rsi16_repair_finish_t(const Rsi16Dev &c, 
             cr[h] = k <= L ? C[k * kColStride] : 0u;
         }
         const uint32_t nch = c.block_len / ecc;
+#pragma unroll 2
         for (uint32_t ch = 0; ch < nch; ++ch) {
             uint32_t x[EPL];
 #pragma unroll
