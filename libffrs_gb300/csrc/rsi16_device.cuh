@@ -16,12 +16,16 @@ namespace ffgpu {
 
 // ---------------------------------------------------------------- field ops
 
-// GF(65537) on canonical values in [0, 65536] (libffrs/galois.hpp:258-346)
+// GF(65537) on canonical values in [0, 65536] (libffrs/galois.hpp:258-346).
+// The product x = a b <= 2^32 is taken to 64 bits (one wide multiply-add);
+// with 2^16 = -1 and 2^32 = 1 (mod p), x = x0 + x1 2^16 + x2 2^32 reduces to
+// x0 - x1 + x2 in [-65535, 65536], and one conditional add of p makes it
+// canonical (65536 * 65536 = 2^32 gives x0 = x1 = 0, x2 = 1).
 static __device__ __forceinline__ uint32_t fmul(uint32_t a, uint32_t b) {
-    uint32_t r = a * b;
-    if (r == 0 && a && b) return 1u;  // 65536 * 65536 = 2^32 = 1 (mod p)
-    r = (r & 0xffffu) - (r >> 16);
-    return ((int32_t)r < 0) ? r + 0x10001u : r;
+    const uint64_t x = (uint64_t)a * b;
+    const uint32_t lo = (uint32_t)x;
+    const int32_t r = (int32_t)(lo & 0xffffu) - (int32_t)(lo >> 16) + (int32_t)(x >> 32);
+    return (uint32_t)(r < 0 ? r + 0x10001 : r);
 }
 static __device__ __forceinline__ uint32_t fadd(uint32_t a, uint32_t b) {
     uint32_t r = a + b;
