@@ -244,29 +244,51 @@ constexpr CrtSel make_crt_sel() {
     return C;
 }
 
-template <int E>
+// Selector tables of the T = E / D factors of degree D.
+template <int D, int T>
+struct LfsrSet {
+    LfsrSel<D> f[T];
+};
+template <int D, int T>
+constexpr LfsrSet<D, T> make_lfsr_set() {
+    LfsrSet<D, T> s{};
+    for (int t = 0; t < T; ++t) s.f[t] = make_lfsr_sel<D>(D * t);
+    return s;
+}
+template <int D, int T>
+struct SyndSet {
+    SyndSel<D> f[T];
+};
+template <int D, int T>
+constexpr SyndSet<D, T> make_synd_set() {
+    SyndSet<D, T> s{};
+    for (int t = 0; t < T; ++t) s.f[t] = make_synd_sel<D>(D * t);
+    return s;
+}
+
+// g split into T = E / D factors of degree D, one thread per factor and group.
+// The encoder needs D = 16 (its CRT map is built for two factors).  For the
+// syndromes D = 8 halves the remainder state per thread but doubles the
+// nibble-combination work per byte; measured on GB300 it was slower
+// (0.52 ms against 0.38 ms per 1,048,576 blocks), so both use D = 16.
+template <int E_, int DD = (E_ > 16 ? 16 : E_)>
 struct Code {
-    static constexpr int T = E > 16 ? E / 16 : 1;  // factors (threads per group)
-    static constexpr int D = E > 16 ? 16 : E;       // factor degree
-    static constexpr LfsrSel<D> lfsr0 = make_lfsr_sel<D>(0);
-    static constexpr LfsrSel<D> lfsr1 = make_lfsr_sel<D>(D);
-    static constexpr SyndSel<D> synd0 = make_synd_sel<D>(0);
-    static constexpr SyndSel<D> synd1 = make_synd_sel<D>(D);
+    static constexpr int E = E_;
+    static constexpr int D = DD;      // factor degree
+    static constexpr int T = E / D;   // factors (threads per group)
+    static constexpr LfsrSet<D, T> lfsrs = make_lfsr_set<D, T>();
+    static constexpr SyndSet<D, T> synds = make_synd_set<D, T>();
     template <int t>
     static constexpr const LfsrSel<D> &lfsr() {
-        if constexpr (t == 0)
-            return lfsr0;
-        else
-            return lfsr1;
+        return lfsrs.f[t];
     }
     template <int t>
     static constexpr const SyndSel<D> &synd() {
-        if constexpr (t == 0)
-            return synd0;
-        else
-            return synd1;
+        return synds.f[t];
     }
 };
+template <int E>
+using SyndCode = Code<E>;
 
 struct CrtHolder {
     static constexpr CrtSel crt = make_crt_sel();
@@ -365,37 +387,37 @@ __device__ __forceinline__ uint32_t pick(const uint32_t (&lo)[16], const uint32_
 }
 
 // one LFSR step of factor t: R[m] <- R[m+1] ^ g[m+1] * (R[0] ^ in)
-template <int E, int t, int... K>
-__device__ __forceinline__ void lfsr_apply(uint32_t (&R)[Code<E>::D][8], const uint32_t (&lo)[16],
+template <typename CD, int t, int... K>
+__device__ __forceinline__ void lfsr_apply(uint32_t (&R)[CD::D][8], const uint32_t (&lo)[16],
                                            const uint32_t (&hi)[16], std::integer_sequence<int, K...>) {
-    constexpr int D = Code<E>::D;
-    ((R[K / 8][K % 8] = pickx<Code<E>::template lfsr<t>().s[K / 8][K % 8]>(
+    constexpr int D = CD::D;
+    ((R[K / 8][K % 8] = pickx<CD::template lfsr<t>().s[K / 8][K % 8]>(
           (K / 8 + 1 < D) ? R[(K / 8 + 1 < D) ? K / 8 + 1 : 0][K % 8] : 0u, lo, hi)),
      ...);
 }
 
-template <int E, int t>
-__device__ __forceinline__ void lfsr_step(uint32_t (&R)[Code<E>::D][8], const uint32_t (&in)[8]) {
-    constexpr int D = Code<E>::D;
+template <typename CD, int t>
+__device__ __forceinline__ void lfsr_step(uint32_t (&R)[CD::D][8], const uint32_t (&in)[8]) {
+    constexpr int D = CD::D;
     uint32_t f[8];
 #pragma unroll
     for (int b = 0; b < 8; ++b) f[b] = R[0][b] ^ in[b];
     uint32_t lo[16], hi[16];
     combos(f, lo, hi);
-    lfsr_apply<E, t>(R, lo, hi, std::make_integer_sequence<int, D * 8>{});
+    lfsr_apply<CD, t>(R, lo, hi, std::make_integer_sequence<int, D * 8>{});
 }
 
 // S[j][o] ^= (c_{m,j} * r)[o] for one remainder byte m
-template <int E, int t, int M, int... K>
-__device__ __forceinline__ void synd_accum(uint32_t (&S)[Code<E>::D][8], const uint32_t (&lo)[16],
+template <typename CD, int t, int M, int... K>
+__device__ __forceinline__ void synd_accum(uint32_t (&S)[CD::D][8], const uint32_t (&lo)[16],
                                            const uint32_t (&hi)[16], std::integer_sequence<int, K...>) {
-    ((S[K / 8][K % 8] = pickx<Code<E>::template synd<t>().s[M][K / 8][K % 8]>(S[K / 8][K % 8], lo, hi)), ...);
+    ((S[K / 8][K % 8] = pickx<CD::template synd<t>().s[M][K / 8][K % 8]>(S[K / 8][K % 8], lo, hi)), ...);
 }
 
-template <int E, int t, int... M>
-__device__ __forceinline__ void rem_to_synd(const uint32_t *rs, int stride, uint32_t (&S)[Code<E>::D][8],
+template <typename CD, int t, int... M>
+__device__ __forceinline__ void rem_to_synd(const uint32_t *rs, int stride, uint32_t (&S)[CD::D][8],
                                             std::integer_sequence<int, M...>) {
-    constexpr int D = Code<E>::D;
+    constexpr int D = CD::D;
     auto one = [&](auto mc) {
         constexpr int m = decltype(mc)::value;
         uint32_t r[8];
@@ -403,7 +425,7 @@ __device__ __forceinline__ void rem_to_synd(const uint32_t *rs, int stride, uint
         for (int b = 0; b < 8; ++b) r[b] = rs[(m * 8 + b) * stride];
         uint32_t lo[16], hi[16];
         combos(r, lo, hi);
-        synd_accum<E, t, m>(S, lo, hi, std::make_integer_sequence<int, D * 8>{});
+        synd_accum<CD, t, m>(S, lo, hi, std::make_integer_sequence<int, D * 8>{});
     };
     (one(std::integral_constant<int, M>{}), ...);
 }
@@ -510,14 +532,14 @@ __device__ __forceinline__ void read_planes(const uint32_t *buf, int g, int i, u
 
 constexpr int kGroups = 64;  // groups per CTA tile (2048 blocks)
 
-template <int E, int t>
-__device__ __forceinline__ void run_lfsr_window(const uint32_t *buf, int g, int npos, uint32_t (&R)[Code<E>::D][8]) {
-    constexpr int T = Code<E>::T;
+template <typename CD, int t>
+__device__ __forceinline__ void run_lfsr_window(const uint32_t *buf, int g, int npos, uint32_t (&R)[CD::D][8]) {
+    constexpr int T = CD::T;
 #pragma unroll 2
     for (int i = 0; i < npos; ++i) {
         uint32_t in[8];
         read_planes<T>(buf, g, i, in);
-        lfsr_step<E, t>(R, in);
+        lfsr_step<CD, t>(R, in);
     }
 }
 
@@ -528,14 +550,15 @@ __device__ __forceinline__ size_t total_bytes_e(int seg, size_t nblocks, int msg
     return seg == 0 ? nblocks * (size_t)msg_len : nblocks * (size_t)E;
 }
 
-template <int E, int t>
+template <typename CD, int t>
 __device__ __forceinline__ void factor_remainder(uint32_t *buf, const uint8_t *data, int msg_len,
                                                  const uint8_t *parity, size_t first, int nb_tile, int g,
-                                                 size_t nblocks_total, uint32_t (&R)[Code<E>::D][8]) {
+                                                 size_t nblocks_total, uint32_t (&R)[CD::D][8]) {
+    constexpr int E = CD::E;
     auto total_bytes = [](int seg, size_t nb, int ml) { return total_bytes_e<E>(seg, nb, ml); };
-    constexpr int T = Code<E>::T;
+    constexpr int T = CD::T;
 #pragma unroll
-    for (int m = 0; m < Code<E>::D; ++m)
+    for (int m = 0; m < CD::D; ++m)
 #pragma unroll
         for (int b = 0; b < 8; ++b) R[m][b] = 0u;
     for (int seg = 0; seg < (parity ? 2 : 1); ++seg) {
@@ -548,9 +571,24 @@ __device__ __forceinline__ void factor_remainder(uint32_t *buf, const uint8_t *d
             __syncthreads();
             transpose_window<T>(buf, g, t);
             __syncthreads();
-            run_lfsr_window<E, t>(buf, g, min(32, len - p0), R);
+            run_lfsr_window<CD, t>(buf, g, min(32, len - p0), R);
         }
     }
+}
+
+// factor_remainder / rem_to_synd for the runtime factor index t
+template <typename CD, int... I>
+__device__ __forceinline__ void factor_remainder_t(int t, uint32_t *buf, const uint8_t *data, int msg_len,
+                                                   const uint8_t *parity, size_t first, int nb_tile, int g,
+                                                   size_t nblocks_total, uint32_t (&R)[CD::D][8],
+                                                   std::integer_sequence<int, I...>) {
+    ((t == I ? factor_remainder<CD, I>(buf, data, msg_len, parity, first, nb_tile, g, nblocks_total, R) : void()),
+     ...);
+}
+template <typename CD, int... I>
+__device__ __forceinline__ void rem_to_synd_t(int t, const uint32_t *rs, int stride, uint32_t (&S)[CD::D][8],
+                                              std::integer_sequence<int, I...>) {
+    ((t == I ? rem_to_synd<CD, I>(rs, stride, S, std::make_integer_sequence<int, CD::D>{}) : void()), ...);
 }
 
 // Syndromes of every block.  PLANES = false: E bytes per block, S_0 first.
@@ -559,14 +597,15 @@ __device__ __forceinline__ void factor_remainder(uint32_t *buf, const uint8_t *d
 // planes[(G / 32) * (E * 8 * 32) + k * 32 + G % 32], so that 32 consecutive
 // groups read or write one plane word with one coalesced access.
 template <int E, bool PLANES>
-__global__ void __launch_bounds__(kGroups * Code<E>::T) bs_synd_kernel(const uint8_t *__restrict__ data,
+__global__ void __launch_bounds__(kGroups * SyndCode<E>::T) bs_synd_kernel(const uint8_t *__restrict__ data,
                                                                          const uint8_t *__restrict__ parity,
                                                                          size_t nblocks, int msg_len,
                                                                          uint8_t *__restrict__ synds) {
-    constexpr int T = Code<E>::T, D = Code<E>::D;
+    using CD = SyndCode<E>;
+    constexpr int T = CD::T, D = CD::D;
     __shared__ uint32_t buf[kGroups * 256];
     const int tid = threadIdx.x;
-    // one factor per warp: warps (2w, 2w+1) share the 32 groups 32w .. 32w+31
+    // one factor per warp: warps T w .. T w + T - 1 share the 32 groups 32w .. 32w+31
     const int warp = tid >> 5, lane = tid & 31;
     const int t = warp % T, g = (warp / T) * 32 + lane;
     const size_t ntiles = (nblocks + kGroups * 32 - 1) / (kGroups * 32);
@@ -575,10 +614,8 @@ __global__ void __launch_bounds__(kGroups * Code<E>::T) bs_synd_kernel(const uin
         const int nb_tile = (int)min((size_t)kGroups * 32, nblocks - first);
         uint32_t R[D][8];
         uint32_t S[D][8];
-        if (t == 0)
-            factor_remainder<E, 0>(buf, data, msg_len, parity, first, nb_tile, g, nblocks, R);
-        else if constexpr (T > 1)
-            factor_remainder<E, 1>(buf, data, msg_len, parity, first, nb_tile, g, nblocks, R);
+        factor_remainder_t<CD>(t, buf, data, msg_len, parity, first, nb_tile, g, nblocks, R,
+                               std::make_integer_sequence<int, T>{});
         // stash remainders, interleaved by thread
         __syncthreads();
         const int stride = kGroups * T;
@@ -590,10 +627,7 @@ __global__ void __launch_bounds__(kGroups * Code<E>::T) bs_synd_kernel(const uin
         for (int m = 0; m < D; ++m)
 #pragma unroll
             for (int b = 0; b < 8; ++b) S[m][b] = 0u;
-        if (t == 0)
-            rem_to_synd<E, 0>(buf + tid, stride, S, std::make_integer_sequence<int, D>{});
-        else if constexpr (T > 1)
-            rem_to_synd<E, 1>(buf + tid, stride, S, std::make_integer_sequence<int, D>{});
+        rem_to_synd_t<CD>(t, buf + tid, stride, S, std::make_integer_sequence<int, T>{});
         if constexpr (PLANES) {
             const size_t G = first / 32 + g;
             if ((int)(g * 32) < nb_tile) {
@@ -643,9 +677,9 @@ __global__ void __launch_bounds__(kGroups * 2) bs_encode32_kernel(const uint8_t 
         const int nb_tile = (int)min((size_t)kGroups * 32, nblocks - first);
         uint32_t R[D][8];
         if (t == 0)
-            factor_remainder<E, 0>(buf, data, msg_len, nullptr, first, nb_tile, g, nblocks, R);
+            factor_remainder<Code<E>, 0>(buf, data, msg_len, nullptr, first, nb_tile, g, nblocks, R);
         else
-            factor_remainder<E, 1>(buf, data, msg_len, nullptr, first, nb_tile, g, nblocks, R);
+            factor_remainder<Code<E>, 1>(buf, data, msg_len, nullptr, first, nb_tile, g, nblocks, R);
         __syncthreads();
         // stash: group g's two factor remainders, [(t*16+m)*8+b] * stride + g
         const int stride = kGroups;
@@ -806,9 +840,9 @@ __global__ void __launch_bounds__(64 * kSegs) bs_encode32_seg_kernel(const uint8
         __syncthreads();
         if (npos > 0) {
             if (t == 0)
-                run_lfsr_window<E, 0>(mybuf, g, npos, R);
+                run_lfsr_window<Code<E>, 0>(mybuf, g, npos, R);
             else
-                run_lfsr_window<E, 1>(mybuf, g, npos, R);
+                run_lfsr_window<Code<E>, 1>(mybuf, g, npos, R);
         }
     }
     __syncthreads();
@@ -1443,9 +1477,9 @@ bool rs256_fast_synds(const Rs256Code &c, const uint8_t *data, const uint8_t *pa
     if (!nblocks) return true;
     KernelTimer kt_timer("bs_synd_kernel", st);
     if (c.ecc == 32)
-        bs::bs_synd_kernel<32, false><<<tiles_grid(nblocks), bs::kGroups * 2, 0, st>>>(data, parity, nblocks, msg_len, synds);
+        bs::bs_synd_kernel<32, false><<<tiles_grid(nblocks), bs::kGroups * bs::SyndCode<32>::T, 0, st>>>(data, parity, nblocks, msg_len, synds);
     else
-        bs::bs_synd_kernel<16, false><<<tiles_grid(nblocks), bs::kGroups, 0, st>>>(data, parity, nblocks, msg_len, synds);
+        bs::bs_synd_kernel<16, false><<<tiles_grid(nblocks), bs::kGroups * bs::SyndCode<16>::T, 0, st>>>(data, parity, nblocks, msg_len, synds);
     check_launch("bs_synd_kernel");
     return true;
 }
@@ -1460,7 +1494,7 @@ size_t rs256_fast_scratch_bytes(int ecc, size_t nblocks) {
 template <int E>
 static void launch_bs_decode(const Rs256Code &c, uint8_t *data, uint8_t *parity, size_t nblocks, int msg_len,
                              uint8_t *status, uint32_t *planes, cudaStream_t st) {
-    constexpr int T = bs::Code<E>::T;
+    constexpr int T = bs::SyndCode<E>::T;
     {
         KernelTimer kt_timer("bs_synd_kernel", st);
         bs::bs_synd_kernel<E, true><<<tiles_grid(nblocks), bs::kGroups * T, 0, st>>>(
