@@ -48,9 +48,38 @@ inline void check_launch(const char *what) {
 }
 
 cudaStream_t lib_stream();
-// k-th stream (mod kPipeStreams) of the chunked host-buffer pipelines
-constexpr size_t kPipeStreams = 8;
+// k-th compute stream (mod kPipeStreams) of the chunked host-buffer pipelines
+constexpr size_t kPipeStreams = 4;
 cudaStream_t pipe_stream(size_t k);
+// the pipelines' upload and download streams
+cudaStream_t pipe_up();
+cudaStream_t pipe_down();
+
+// Stream roles of one host-buffer pipeline call.  Every upload goes to
+// pipe_up() and every download to pipe_down(), so the two directions sit on
+// different copy engines and overlap (with the directions mixed over the
+// same streams, uploads queued behind downloads on a shared engine); the
+// kernels of chunk k run on compute stream k mod kPipeStreams.  Events order
+// upload -> kernels -> download per chunk.
+class HostPipeline {
+  public:
+    HostPipeline() = default;
+    HostPipeline(const HostPipeline &) = delete;
+    HostPipeline &operator=(const HostPipeline &) = delete;
+    ~HostPipeline();
+    cudaStream_t up() const { return pipe_up(); }
+    cudaStream_t down() const { return pipe_down(); }
+    // after chunk k's uploads: the compute stream its kernels go on
+    cudaStream_t compute(size_t k);
+    // after chunk k's kernels: the download stream, ordered behind them
+    cudaStream_t to_down(size_t k);
+    // waits for every download issued (and so for everything before them)
+    void sync();
+
+  private:
+    cudaEvent_t record(cudaStream_t s);
+    std::vector<cudaEvent_t> evs_;
+};
 // blocks per chunk of a host-buffer pipeline: ffgpu_set_host_chunk_blocks, or
 // at least min_chunk and at most max_chunks chunks
 size_t host_chunk_blocks(size_t nblocks, size_t min_chunk, size_t max_chunks);

@@ -125,15 +125,44 @@ void OutputDrain::finish() {
     }
 }
 
-// streams of the host-buffer pipelines (created on first use)
-cudaStream_t pipe_stream(size_t k) {
+// streams of the host-buffer pipelines (created on first use): the compute
+// streams, then the upload and the download stream
+static cudaStream_t pipe_slot(size_t i) {
     static std::mutex mu;
-    static cudaStream_t s[kPipeStreams] = {};
+    static cudaStream_t s[kPipeStreams + 2] = {};
     std::lock_guard<std::mutex> lk(mu);
-    cudaStream_t &x = s[k % kPipeStreams];
+    cudaStream_t &x = s[i];
     if (!x) FFGPU_CHECK_CUDA(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
     return x;
 }
+cudaStream_t pipe_stream(size_t k) { return pipe_slot(k % kPipeStreams); }
+cudaStream_t pipe_up() { return pipe_slot(kPipeStreams); }
+cudaStream_t pipe_down() { return pipe_slot(kPipeStreams + 1); }
+
+HostPipeline::~HostPipeline() {
+    for (cudaEvent_t e : evs_) cudaEventDestroy(e);
+}
+
+cudaEvent_t HostPipeline::record(cudaStream_t s) {
+    cudaEvent_t e = nullptr;
+    FFGPU_CHECK_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    evs_.push_back(e);
+    FFGPU_CHECK_CUDA(cudaEventRecord(e, s));
+    return e;
+}
+
+cudaStream_t HostPipeline::compute(size_t k) {
+    cudaStream_t cs = pipe_stream(k);
+    FFGPU_CHECK_CUDA(cudaStreamWaitEvent(cs, record(up()), 0));
+    return cs;
+}
+
+cudaStream_t HostPipeline::to_down(size_t k) {
+    FFGPU_CHECK_CUDA(cudaStreamWaitEvent(down(), record(pipe_stream(k)), 0));
+    return down();
+}
+
+void HostPipeline::sync() { FFGPU_CHECK_CUDA(cudaStreamSynchronize(down())); }
 
 cudaStream_t lib_stream() {
     std::lock_guard<std::mutex> lk(g_stream_mu);
@@ -353,25 +382,26 @@ int ffgpu_rs256_encode_host(const ffgpu_rs256 *code, const uint8_t *buf, size_t 
         const size_t chunk = std::max<size_t>(1, host_chunk_blocks(full, 262144, 4));
         uint8_t *h_out = pipeline_out(out, chunk < full, h->h_parity, nout);
         OutputDrain drain;
+        HostPipeline pl;
         size_t k = 0;
         for (size_t b0 = 0; b0 < full || (k == 0 && tail); b0 += chunk, ++k) {
-            st = pipe_stream(k);
             const size_t n = std::min(chunk, full - b0);
             const bool last = b0 + n >= full;
             const size_t in_bytes = n * message_len + (last ? tail : 0);
             const size_t out_bytes = (n + (last && tail ? 1 : 0)) * (size_t)c.ecc;
             const size_t i0 = b0 * message_len, o0 = b0 * (size_t)c.ecc;
-            FFGPU_CHECK_CUDA(cudaMemcpyAsync(d_in + i0, buf + i0, in_bytes, cudaMemcpyHostToDevice, st));
+            FFGPU_CHECK_CUDA(cudaMemcpyAsync(d_in + i0, buf + i0, in_bytes, cudaMemcpyHostToDevice, pl.up()));
+            st = pl.compute(k);
             if (n) rs256_encode(c, d_in + i0, n, (int)message_len, d_out + o0, st);
             if (last && tail)
                 rs256_encode(c, d_in + full * message_len, 1, (int)tail, d_out + full * (size_t)c.ecc, st);
+            st = pl.to_down(k);
             FFGPU_CHECK_CUDA(cudaMemcpyAsync(h_out + o0, d_out + o0, out_bytes, cudaMemcpyDeviceToHost, st));
             drain.copy(out + o0, h_out + o0, out_bytes);
             drain.chunk(st);
         }
         drain.finish();
-        for (size_t i = 0; i < std::min<size_t>(k, kPipeStreams); ++i)
-            FFGPU_CHECK_CUDA(cudaStreamSynchronize(pipe_stream(i)));
+        pl.sync();
     });
 }
 
@@ -388,25 +418,26 @@ int ffgpu_rs256_decode_host(const ffgpu_rs256 *code, uint8_t *data, uint8_t *par
         uint8_t *d_d = (uint8_t *)h->d_data.get(nd);
         uint8_t *d_p = (uint8_t *)h->d_parity.get(np);
         uint8_t *d_s = (uint8_t *)h->d_status.get(nblocks);
-        // outputs in pageable memory come back through page-locked staging
-        // chunks of blocks on the pipeline streams: the host-to-device copy of
-        // one chunk, the decode of another and the copy back of a third
-        // overlap (page-locked host memory moves at full speed)
-        const size_t chunk = host_chunk_blocks(nblocks, 65536, 16);
+        // chunks of blocks: the upload of one chunk, the decode of another and
+        // the download of a third overlap; outputs in pageable memory come
+        // back through page-locked staging
+        const size_t chunk = host_chunk_blocks(nblocks, 131072, 8);
         const bool chunked = chunk < nblocks;
         uint8_t *h_d = pipeline_out(data, chunked, h->h_data, nd);
         uint8_t *h_p = pipeline_out(parity, chunked, h->h_parity, np);
         uint8_t *h_s = pipeline_out(status, chunked, h->h_status, nblocks);
         OutputDrain drain;
+        HostPipeline pl;
         size_t k = 0;
         for (size_t b0 = 0; b0 < nblocks; b0 += chunk, ++k) {
-            cudaStream_t st = pipe_stream(k);
             const size_t n = std::min(chunk, nblocks - b0);
             const size_t od = b0 * message_len, op = b0 * (size_t)c.ecc;
             uint8_t *dd = d_d + od, *dp = d_p + op, *ds = d_s + b0;
-            FFGPU_CHECK_CUDA(cudaMemcpyAsync(dd, data + od, n * message_len, cudaMemcpyHostToDevice, st));
-            FFGPU_CHECK_CUDA(cudaMemcpyAsync(dp, parity + op, n * (size_t)c.ecc, cudaMemcpyHostToDevice, st));
+            FFGPU_CHECK_CUDA(cudaMemcpyAsync(dd, data + od, n * message_len, cudaMemcpyHostToDevice, pl.up()));
+            FFGPU_CHECK_CUDA(cudaMemcpyAsync(dp, parity + op, n * (size_t)c.ecc, cudaMemcpyHostToDevice, pl.up()));
+            cudaStream_t st = pl.compute(k);
             rs256_decode(c, dd, dp, n, (int)message_len, ds, st);
+            st = pl.to_down(k);
             FFGPU_CHECK_CUDA(cudaMemcpyAsync(h_d + od, dd, n * message_len, cudaMemcpyDeviceToHost, st));
             FFGPU_CHECK_CUDA(cudaMemcpyAsync(h_p + op, dp, n * (size_t)c.ecc, cudaMemcpyDeviceToHost, st));
             FFGPU_CHECK_CUDA(cudaMemcpyAsync(h_s + b0, ds, n, cudaMemcpyDeviceToHost, st));
@@ -416,8 +447,7 @@ int ffgpu_rs256_decode_host(const ffgpu_rs256 *code, uint8_t *data, uint8_t *par
             drain.chunk(st);
         }
         drain.finish();
-        for (size_t i = 0; i < std::min<size_t>(k, kPipeStreams); ++i)
-            FFGPU_CHECK_CUDA(cudaStreamSynchronize(pipe_stream(i)));
+        pl.sync();
     });
 }
 

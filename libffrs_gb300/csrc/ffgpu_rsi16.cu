@@ -151,22 +151,23 @@ int ffgpu_rsi16_encode_host(const ffgpu_rsi16 *code, const uint16_t *msg, size_t
             const size_t chunk = host_chunk_blocks(nblocks, 8192, 4);
             uint16_t *hp = pipeline_out(parity, chunk < nblocks, h->h_par, np * 2);
             OutputDrain drain;
+            HostPipeline pl;
             size_t k = 0;
             for (size_t b0 = 0; b0 < nblocks; b0 += chunk, ++k) {
-                cudaStream_t ps = pipe_stream(k);
                 const size_t n = std::min(chunk, nblocks - b0);
                 uint16_t *cm = dm + b0 * c.message_len, *cp = dp + b0 * c.ecc;
                 const size_t om = b0 * c.message_len;
                 FFGPU_CHECK_CUDA(
-                    cudaMemcpyAsync(cm, msg + om, n * c.message_len * 2, cudaMemcpyHostToDevice, ps));
+                    cudaMemcpyAsync(cm, msg + om, n * c.message_len * 2, cudaMemcpyHostToDevice, pl.up()));
+                cudaStream_t ps = pl.compute(k);
                 rsi16_encode(c, contiguous_view(cm, true, c.message_len, cp, true, c.ecc), n, ps);
+                ps = pl.to_down(k);
                 FFGPU_CHECK_CUDA(cudaMemcpyAsync(hp + b0 * c.ecc, cp, n * c.ecc * 2, cudaMemcpyDeviceToHost, ps));
                 drain.copy(parity + b0 * c.ecc, hp + b0 * c.ecc, n * c.ecc * 2);
                 drain.chunk(ps);
             }
             drain.finish();
-            for (size_t i = 0; i < std::min<size_t>(k, kPipeStreams); ++i)
-                FFGPU_CHECK_CUDA(cudaStreamSynchronize(pipe_stream(i)));
+            pl.sync();
             return;
         }
         FFGPU_CHECK_CUDA(cudaMemcpyAsync(dm, msg, nm * 2, cudaMemcpyHostToDevice, st));
@@ -208,22 +209,25 @@ int ffgpu_rsi16_repair_host(const ffgpu_rsi16 *code, uint16_t *msg, uint16_t *pa
             // repairs over the pipeline streams (only when the repair
             // workspace lives in shared memory: the global fallback workspace
             // is one per thread and cannot serve concurrent streams)
-            const size_t chunk = host_chunk_blocks(nblocks, 16384, 16);
+            const size_t chunk = host_chunk_blocks(nblocks, 32768, 8);
             // outputs in pageable memory come back through page-locked staging
             const bool chunked = chunk < nblocks;
             uint16_t *h_m = pipeline_out(msg, chunked, h->h_msg, nm * 2);
             uint16_t *h_p = pipeline_out(parity, chunked, h->h_par, np * 2);
             uint8_t *h_s = pipeline_out(status, chunked, h->h_status, nblocks);
             OutputDrain drain;
+            HostPipeline pl;
             size_t k = 0;
             for (size_t b0 = 0; b0 < nblocks; b0 += chunk, ++k) {
-                cudaStream_t ps = pipe_stream(k);
                 const size_t n = std::min(chunk, nblocks - b0);
                 const size_t om = b0 * c.message_len, op = b0 * c.ecc;
                 uint16_t *cm = dm + om, *cp = dp + op;
-                FFGPU_CHECK_CUDA(cudaMemcpyAsync(cm, msg + om, n * c.message_len * 2, cudaMemcpyHostToDevice, ps));
-                FFGPU_CHECK_CUDA(cudaMemcpyAsync(cp, parity + op, n * c.ecc * 2, cudaMemcpyHostToDevice, ps));
+                FFGPU_CHECK_CUDA(
+                    cudaMemcpyAsync(cm, msg + om, n * c.message_len * 2, cudaMemcpyHostToDevice, pl.up()));
+                FFGPU_CHECK_CUDA(cudaMemcpyAsync(cp, parity + op, n * c.ecc * 2, cudaMemcpyHostToDevice, pl.up()));
+                cudaStream_t ps = pl.compute(k);
                 rsi16_repair(c, contiguous_view(cm, true, c.message_len, cp, true, c.ecc), n, ds + b0, ps);
+                ps = pl.to_down(k);
                 FFGPU_CHECK_CUDA(cudaMemcpyAsync(h_m + om, cm, n * c.message_len * 2, cudaMemcpyDeviceToHost, ps));
                 FFGPU_CHECK_CUDA(cudaMemcpyAsync(h_p + op, cp, n * c.ecc * 2, cudaMemcpyDeviceToHost, ps));
                 FFGPU_CHECK_CUDA(cudaMemcpyAsync(h_s + b0, ds + b0, n, cudaMemcpyDeviceToHost, ps));
@@ -233,8 +237,7 @@ int ffgpu_rsi16_repair_host(const ffgpu_rsi16 *code, uint16_t *msg, uint16_t *pa
                 drain.chunk(ps);
             }
             drain.finish();
-            for (size_t i = 0; i < std::min<size_t>(k, kPipeStreams); ++i)
-                FFGPU_CHECK_CUDA(cudaStreamSynchronize(pipe_stream(i)));
+            pl.sync();
             return;
         }
         FFGPU_CHECK_CUDA(cudaMemcpyAsync(dm, msg, nm * 2, cudaMemcpyHostToDevice, st));
