@@ -530,7 +530,10 @@ __device__ __forceinline__ void read_planes(const uint32_t *buf, int g, int i, u
 
 // ---------------------------------------------------------------- kernels
 
-constexpr int kGroups = 64;  // groups per CTA tile (2048 blocks)
+constexpr int kGroups = 64;      // groups per CTA tile of the encoder (2048 blocks)
+// groups per CTA tile of the syndrome kernel (2048 blocks; 32-group tiles of
+// two warps measured 0.44 ms against 0.38 ms per 1,048,576 blocks on GB300)
+constexpr int kSyndGroups = 64;
 
 template <typename CD, int t>
 __device__ __forceinline__ void run_lfsr_window(const uint32_t *buf, int g, int npos, uint32_t (&R)[CD::D][8]) {
@@ -550,7 +553,7 @@ __device__ __forceinline__ size_t total_bytes_e(int seg, size_t nblocks, int msg
     return seg == 0 ? nblocks * (size_t)msg_len : nblocks * (size_t)E;
 }
 
-template <typename CD, int t>
+template <typename CD, int t, int G = kGroups>
 __device__ __forceinline__ void factor_remainder(uint32_t *buf, const uint8_t *data, int msg_len,
                                                  const uint8_t *parity, size_t first, int nb_tile, int g,
                                                  size_t nblocks_total, uint32_t (&R)[CD::D][8]) {
@@ -566,8 +569,7 @@ __device__ __forceinline__ void factor_remainder(uint32_t *buf, const uint8_t *d
         const int len = seg == 0 ? msg_len : E;
         for (int p0 = 0; p0 < len; p0 += 32) {
             __syncthreads();
-            load_window(buf, base, (size_t)len, total_bytes(seg, nblocks_total, msg_len), first, nb_tile, p0,
-                        kGroups);
+            load_window(buf, base, (size_t)len, total_bytes(seg, nblocks_total, msg_len), first, nb_tile, p0, G);
             __syncthreads();
             transpose_window<T>(buf, g, t);
             __syncthreads();
@@ -577,12 +579,13 @@ __device__ __forceinline__ void factor_remainder(uint32_t *buf, const uint8_t *d
 }
 
 // factor_remainder / rem_to_synd for the runtime factor index t
-template <typename CD, int... I>
+template <typename CD, int G, int... I>
 __device__ __forceinline__ void factor_remainder_t(int t, uint32_t *buf, const uint8_t *data, int msg_len,
                                                    const uint8_t *parity, size_t first, int nb_tile, int g,
                                                    size_t nblocks_total, uint32_t (&R)[CD::D][8],
                                                    std::integer_sequence<int, I...>) {
-    ((t == I ? factor_remainder<CD, I>(buf, data, msg_len, parity, first, nb_tile, g, nblocks_total, R) : void()),
+    ((t == I ? factor_remainder<CD, I, G>(buf, data, msg_len, parity, first, nb_tile, g, nblocks_total, R)
+             : void()),
      ...);
 }
 template <typename CD, int... I>
@@ -596,29 +599,29 @@ __device__ __forceinline__ void rem_to_synd_t(int t, const uint32_t *rs, int str
 // 32G+31) keeps plane word k = 8j + b (bit b of S_j) at
 // planes[(G / 32) * (E * 8 * 32) + k * 32 + G % 32], so that 32 consecutive
 // groups read or write one plane word with one coalesced access.
-template <int E, bool PLANES>
-__global__ void __launch_bounds__(kGroups * SyndCode<E>::T) bs_synd_kernel(const uint8_t *__restrict__ data,
+template <int E, bool PLANES, int G = kSyndGroups>
+__global__ void __launch_bounds__(G * SyndCode<E>::T) bs_synd_kernel(const uint8_t *__restrict__ data,
                                                                          const uint8_t *__restrict__ parity,
                                                                          size_t nblocks, int msg_len,
                                                                          uint8_t *__restrict__ synds) {
     using CD = SyndCode<E>;
     constexpr int T = CD::T, D = CD::D;
-    __shared__ uint32_t buf[kGroups * 256];
+    __shared__ uint32_t buf[G * 256];
     const int tid = threadIdx.x;
     // one factor per warp: warps T w .. T w + T - 1 share the 32 groups 32w .. 32w+31
     const int warp = tid >> 5, lane = tid & 31;
     const int t = warp % T, g = (warp / T) * 32 + lane;
-    const size_t ntiles = (nblocks + kGroups * 32 - 1) / (kGroups * 32);
+    const size_t ntiles = (nblocks + G * 32 - 1) / (G * 32);
     for (size_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const size_t first = tile * kGroups * 32;
-        const int nb_tile = (int)min((size_t)kGroups * 32, nblocks - first);
+        const size_t first = tile * G * 32;
+        const int nb_tile = (int)min((size_t)G * 32, nblocks - first);
         uint32_t R[D][8];
         uint32_t S[D][8];
-        factor_remainder_t<CD>(t, buf, data, msg_len, parity, first, nb_tile, g, nblocks, R,
+        factor_remainder_t<CD, G>(t, buf, data, msg_len, parity, first, nb_tile, g, nblocks, R,
                                std::make_integer_sequence<int, T>{});
         // stash remainders, interleaved by thread
         __syncthreads();
-        const int stride = kGroups * T;
+        const int stride = G * T;
 #pragma unroll
         for (int m = 0; m < D; ++m)
 #pragma unroll
@@ -1446,6 +1449,13 @@ static unsigned tiles_grid(size_t nblocks) {
     return (unsigned)std::max<size_t>(1, std::min<size_t>(tiles, (size_t)sm_count() * 4));
 }
 
+// CTAs of the syndrome kernel: one per tile, at most twice the resident
+// count (2T warps of 255 registers per CTA)
+static unsigned synd_grid(size_t nblocks, int T) {
+    const size_t tiles = (nblocks + bs::kSyndGroups * 32 - 1) / (bs::kSyndGroups * 32);
+    return (unsigned)std::max<size_t>(1, std::min<size_t>(tiles, (size_t)sm_count() * (8 / T)));
+}
+
 static bool aligned4(const void *p) { return ((uintptr_t)p & 3) == 0; }
 
 bool rs256_fast_encode(const Rs256Code &c, const uint8_t *data, size_t nblocks, int msg_len, uint8_t *parity,
@@ -1477,9 +1487,9 @@ bool rs256_fast_synds(const Rs256Code &c, const uint8_t *data, const uint8_t *pa
     if (!nblocks) return true;
     KernelTimer kt_timer("bs_synd_kernel", st);
     if (c.ecc == 32)
-        bs::bs_synd_kernel<32, false><<<tiles_grid(nblocks), bs::kGroups * bs::SyndCode<32>::T, 0, st>>>(data, parity, nblocks, msg_len, synds);
+        bs::bs_synd_kernel<32, false><<<synd_grid(nblocks, bs::SyndCode<32>::T), bs::kSyndGroups * bs::SyndCode<32>::T, 0, st>>>(data, parity, nblocks, msg_len, synds);
     else
-        bs::bs_synd_kernel<16, false><<<tiles_grid(nblocks), bs::kGroups * bs::SyndCode<16>::T, 0, st>>>(data, parity, nblocks, msg_len, synds);
+        bs::bs_synd_kernel<16, false><<<synd_grid(nblocks, bs::SyndCode<16>::T), bs::kSyndGroups * bs::SyndCode<16>::T, 0, st>>>(data, parity, nblocks, msg_len, synds);
     check_launch("bs_synd_kernel");
     return true;
 }
@@ -1497,7 +1507,7 @@ static void launch_bs_decode(const Rs256Code &c, uint8_t *data, uint8_t *parity,
     constexpr int T = bs::SyndCode<E>::T;
     {
         KernelTimer kt_timer("bs_synd_kernel", st);
-        bs::bs_synd_kernel<E, true><<<tiles_grid(nblocks), bs::kGroups * T, 0, st>>>(
+        bs::bs_synd_kernel<E, true><<<synd_grid(nblocks, T), bs::kSyndGroups * T, 0, st>>>(
             data, parity, nblocks, msg_len, reinterpret_cast<uint8_t *>(planes));
         check_launch("bs_synd_kernel");
     }
