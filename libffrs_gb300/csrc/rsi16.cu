@@ -245,19 +245,26 @@ __global__ void __launch_bounds__(128, 4) rsi16_repair_batch_kernel(Rsi16Dev c, 
     for (size_t base = (size_t)w.warp_global * 32; base < nblocks; base += (size_t)w.nwarps * 32) {
         const int nb = (int)min((size_t)32, nblocks - base);
         uint32_t live = 0u, nz = 0u;
-        for (int j = 0; j < nb; ++j) {
-            const size_t b = base + j;
-            if (active && !active[b]) continue;
-            live |= 1u << j;
-            uint32_t s[EPL];
-            reg_pntt<EPL>(c, v, b, c.pntt_blocks, true, tw, w.lane, s);
-            bool any = false;
+        for (int j = 0; j < nb; ++j)
+            if (!active || active[base + j]) live |= 1u << j;
+        // syndromes two blocks at a time (a lone last block pairs with itself)
+        for (uint32_t todo = live; todo;) {
+            const int j0 = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const int j1 = todo ? __ffs(todo) - 1 : j0;
+            todo &= todo - 1;
+            uint32_t s0[EPL], s1[EPL];
+            reg_pntt2<EPL>(c, v, base + j0, base + j1, c.pntt_blocks, tw, w.lane, s0, s1);
+            bool any0 = false, any1 = false;
 #pragma unroll
             for (int h = 0; h < EPL; ++h) {
-                Ssm[(w.lane * EPL + h) * kColStride + j] = s[h];
-                any |= s[h] != 0;
+                Ssm[(w.lane * EPL + h) * kColStride + j0] = s0[h];
+                Ssm[(w.lane * EPL + h) * kColStride + j1] = s1[h];
+                any0 |= s0[h] != 0;
+                any1 |= s1[h] != 0;
             }
-            if (__any_sync(0xffffffffu, any)) nz |= 1u << j;
+            if (__any_sync(0xffffffffu, any0)) nz |= 1u << j0;
+            if (__any_sync(0xffffffffu, any1)) nz |= 1u << j1;
         }
         __syncwarp();
         uint32_t L = 0;

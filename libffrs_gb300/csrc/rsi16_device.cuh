@@ -553,6 +553,79 @@ static __device__ __forceinline__ void reg_pntt(const Rsi16Dev &c, const BlockVi
     }
 }
 
+// ct_butterfly on two vectors at once (twice the independent work per stage)
+template <int EPL>
+static __device__ __forceinline__ void reg_ct2(uint32_t (&x)[EPL], uint32_t (&y)[EPL], const RegTw<EPL> &tw,
+                                               int lane) {
+    constexpr int LOG = reg_log<EPL>();
+#pragma unroll
+    for (int st = 0; st < LOG; ++st) {
+        const int stride = 1 << st;
+        if (stride < EPL) {
+#pragma unroll
+            for (int h = 0; h < EPL; ++h) {
+                if (h & stride) continue;
+                const uint32_t a = x[h], m = fmul(x[h + stride], tw.ct[st][h]);
+                const uint32_t a2 = y[h], m2 = fmul(y[h + stride], tw.ct[st][h]);
+                x[h] = fadd(a, m);
+                x[h + stride] = fsub(a, m);
+                y[h] = fadd(a2, m2);
+                y[h + stride] = fsub(a2, m2);
+            }
+        } else {
+            const int lm = stride / EPL;
+            const bool upper = (lane & lm) != 0;
+#pragma unroll
+            for (int h = 0; h < EPL; ++h) {
+                const uint32_t p = __shfl_xor_sync(0xffffffffu, x[h], lm);
+                const uint32_t p2 = __shfl_xor_sync(0xffffffffu, y[h], lm);
+                const uint32_t m = fmul(upper ? x[h] : p, tw.ct[st][h]);
+                const uint32_t m2 = fmul(upper ? y[h] : p2, tw.ct[st][h]);
+                x[h] = upper ? fsub(p, m) : fadd(x[h], m);
+                y[h] = upper ? fsub(p2, m2) : fadd(y[h], m2);
+            }
+        }
+    }
+}
+
+// reg_pntt of two blocks b0, b1 of the same view at once, with parity
+template <int EPL>
+static __device__ __forceinline__ void reg_pntt2(const Rsi16Dev &c, const BlockView &v, size_t b0, size_t b1,
+                                                 uint32_t nchunks, const RegTw<EPL> &tw, int lane,
+                                                 uint32_t (&acc0)[EPL], uint32_t (&acc1)[EPL]) {
+    constexpr uint32_t n = 32 * EPL;
+    const size_t mb0 = (b0 / v.group) * v.msg_gstride + (b0 % v.group) * v.msg_bstride;
+    const size_t pb0 = (b0 / v.group) * v.par_gstride + (b0 % v.group) * v.par_bstride;
+    const size_t mb1 = (b1 / v.group) * v.msg_gstride + (b1 % v.group) * v.msg_bstride;
+    const size_t pb1 = (b1 / v.group) * v.par_gstride + (b1 % v.group) * v.par_bstride;
+    const uint32_t nch = nchunks ? nchunks : 1;
+    for (uint32_t ch = 0; ch < nch; ++ch) {
+        uint32_t x[EPL], y[EPL];
+#pragma unroll
+        for (int h = 0; h < EPL; ++h) {
+            const uint32_t k = ch * n + lane * EPL + h;
+            uint32_t w0 = 0, w1 = 0;
+            if (k < c.message_len) {
+                w0 = ld_word(v.msg, v.msg16, mb0 + (size_t)k * v.msg_estride);
+                w1 = ld_word(v.msg, v.msg16, mb1 + (size_t)k * v.msg_estride);
+            } else if (k < c.block_len) {
+                w0 = ld_word(v.par, v.par16, pb0 + (size_t)(k - c.message_len) * v.par_estride);
+                w1 = ld_word(v.par, v.par16, pb1 + (size_t)(k - c.message_len) * v.par_estride);
+            }
+            x[h] = w0;
+            y[h] = w1;
+        }
+        reg_ct2<EPL>(x, y, tw, lane);
+#pragma unroll
+        for (int h = 0; h < EPL; ++h) {
+            const uint32_t sh = c.pntt_shift[ch * n + lane * EPL + h];
+            const uint32_t r0 = fmul(x[h], sh), r1 = fmul(y[h], sh);
+            acc0[h] = ch ? fadd(acc0[h], r0) : r0;
+            acc1[h] = ch ? fadd(acc1[h], r1) : r1;
+        }
+    }
+}
+
 // parity of block b with the vector in registers
 template <int EPL>
 static __device__ __forceinline__ void rsi16_encode_block_reg(const Rsi16Dev &c, const BlockView &v, size_t b,
