@@ -227,7 +227,7 @@ __global__ void rsi16_repair_warp_kernel(Rsi16Dev c, BlockView v, size_t nblocks
 // the bounded-distance path does not accept is marked kMirrorPending and left
 // for rsi16_repair_mirror_kernel, so that this kernel's warp workspace is only
 // the batch's syndrome columns [ecc][33], locator columns [ecc/2 + 1][33] and
-// the finishing scratch (2 ecc + 2 words).
+// the finishing scratch (two root lists of ecc + 1 words, Omega and C').
 constexpr uint8_t kMirrorPending = 0xFE;
 
 template <int EPL>
@@ -275,18 +275,46 @@ __global__ void __launch_bounds__(128, 4) rsi16_repair_batch_kernel(Rsi16Dev c, 
             for (int i = 0; i <= T; ++i) Csm[i * kColStride + w.lane] = C[i];
         }
         __syncwarp();
+        // blocks whose locator passes the checks get their roots searched in
+        // pairs; the others (and those whose root count is not L) go to the
+        // mirror
+        uint32_t cand = 0u;
         for (int j = 0; j < nb; ++j) {
             if (!((live >> j) & 1u)) continue;
             const size_t b = base + j;
-            ++nfast;
             if (!((nz >> j) & 1u)) {
                 if (w.lane == 0) status[b] = FFGPU_NO_ERRORS;
+                ++nfast;
                 continue;
             }
             const uint32_t Lj = __shfl_sync(0xffffffffu, L, j);
-            if (!rsi16_repair_finish_t<EPL>(c, v, b, Ssm + j, Csm + j, Lj, fin, status, tw, w.lane)) {
-                if (w.lane == 0) status[b] = kMirrorPending;
-                --nfast;
+            if (rsi16_locator_ok(c, Csm + j, Lj, w.lane))
+                cand |= 1u << j;
+            else if (w.lane == 0)
+                status[b] = kMirrorPending;
+        }
+        uint32_t *TA = fin, *TB = fin + (c.ecc + 1), *Om = TB + (c.ecc + 1), *D = Om + (T + 1);
+        for (uint32_t todo = cand; todo;) {
+            const int ja = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const int jb = todo ? __ffs(todo) - 1 : ja;
+            todo &= todo - 1;
+            const uint32_t La = __shfl_sync(0xffffffffu, L, ja), Lb = __shfl_sync(0xffffffffu, L, jb);
+            uint32_t na, nbr;
+            rsi16_roots_pair<EPL>(c, Csm + ja, La, Csm + jb, Lb, TA, TB, tw, w.lane, na, nbr);
+            if (na == La) {
+                rsi16_forney_apply(c, v, base + ja, Ssm + ja, Csm + ja, La, TA, Om, D, status, w.lane);
+                ++nfast;
+            } else if (w.lane == 0) {
+                status[base + ja] = kMirrorPending;
+            }
+            if (jb != ja) {
+                if (nbr == Lb) {
+                    rsi16_forney_apply(c, v, base + jb, Ssm + jb, Csm + jb, Lb, TB, Om, D, status, w.lane);
+                    ++nfast;
+                } else if (w.lane == 0) {
+                    status[base + jb] = kMirrorPending;
+                }
             }
         }
         __syncwarp();  // the batch's columns are read before the next batch writes them
@@ -466,7 +494,7 @@ void rsi16_repair(const Rsi16Code &c, const BlockView &v, size_t nblocks, uint8_
     auto go = [&](auto epl) {
         constexpr int E = decltype(epl)::value;
         if constexpr (E == 1 || E == 2) {
-            const uint32_t ws = (uint32_t)((c.ecc + c.ecc / 2 + 1) * kColStride + 2 * c.ecc + 2);
+            const uint32_t ws = (uint32_t)((c.ecc + c.ecc / 2 + 1) * kColStride + 3 * c.ecc + 4);
             const size_t smem = 4 * (size_t)ws * 4;  // four warps per CTA
             const size_t batches = (nblocks + 31) / 32;
             const int per_sm = std::max(1, (int)((220 * 1024) / (smem + 1024)));

@@ -521,6 +521,40 @@ static __device__ __forceinline__ void reg_gs(uint32_t (&x)[EPL], const RegTw<EP
     }
 }
 
+// gs_butterfly on two vectors at once
+template <int EPL>
+static __device__ __forceinline__ void reg_gs2(uint32_t (&x)[EPL], uint32_t (&y)[EPL], const RegTw<EPL> &tw,
+                                               int lane) {
+    constexpr int LOG = reg_log<EPL>();
+    constexpr int n = 32 * EPL;
+#pragma unroll
+    for (int st = 0; st < LOG; ++st) {
+        const int stride = (n >> 1) >> st;
+        if (stride < EPL) {
+#pragma unroll
+            for (int h = 0; h < EPL; ++h) {
+                if (h & stride) continue;
+                const uint32_t a = x[h], bb = x[h + stride];
+                const uint32_t a2 = y[h], bb2 = y[h + stride];
+                x[h] = fadd(a, bb);
+                x[h + stride] = fmul(fsub(a, bb), tw.gs[st][h + stride]);
+                y[h] = fadd(a2, bb2);
+                y[h + stride] = fmul(fsub(a2, bb2), tw.gs[st][h + stride]);
+            }
+        } else {
+            const int lm = stride / EPL;
+            const bool upper = (lane & lm) != 0;
+#pragma unroll
+            for (int h = 0; h < EPL; ++h) {
+                const uint32_t p = __shfl_xor_sync(0xffffffffu, x[h], lm);
+                const uint32_t p2 = __shfl_xor_sync(0xffffffffu, y[h], lm);
+                x[h] = upper ? fmul(fsub(p, x[h]), tw.gs[st][h]) : fadd(x[h], p);
+                y[h] = upper ? fmul(fsub(p2, y[h]), tw.gs[st][h]) : fadd(y[h], p2);
+            }
+        }
+    }
+}
+
 // NTT::pntt (ntt.hpp:133-152) of block b over nchunks chunks (at least chunk
 // 0): S = sum_ch ct(chunk_ch) * pntt_shift_ch.  Words past the message are the
 // parity (with_parity) or zeros.
@@ -932,51 +966,72 @@ static __device__ __forceinline__ uint32_t rsi16_bm_lane(const uint32_t *S, cons
     return L;
 }
 
-// The rest of the bounded-distance path for block b, from its syndromes (column
-// S) and the lane Berlekamp-Massey's locator (column C, T + 1 words) and
-// length L: the degree check, the roots by inverse partial
-// NTT, Omega = S * C mod x^L and Forney, exactly as in rsi16_repair_bm_block_t.
-// temp holds the positions, Omega and C' (ecc + 2 + ecc words).  Returns false
-// when the block must go to the mirror (nothing written).
-template <int EPL>
-static __device__ __forceinline__ bool rsi16_repair_finish_t(const Rsi16Dev &c, const BlockView &v, size_t b,
-                                                         const uint32_t *S, const uint32_t *C, uint32_t L,
-                                                         uint32_t *temp, uint8_t *status, const RegTw<EPL> &tw,
-                                                         int lane) {
-    const uint32_t ecc = c.ecc, t = ecc / 2, n1 = ecc + 1;
+// The rest of the bounded-distance path, from a block's syndromes (column S)
+// and the lane Berlekamp-Massey's locator (column C, T + 1 words) and length
+// L: the degree check, the roots by inverse partial NTT, Omega = S * C mod x^L
+// and Forney, exactly as in rsi16_repair_bm_block_t.  The root search runs on
+// two blocks at once (twice the independent work per transform stage).
+
+// L in range and C of degree at most L (the root count then checks that it is
+// exactly L)
+static __device__ __forceinline__ bool rsi16_locator_ok(const Rsi16Dev &c, const uint32_t *C, uint32_t L, int lane) {
+    const uint32_t t = c.ecc / 2;
     if (L == 0 || L > t) return false;
-    // C must have degree exactly L (checked through the root count below)
     bool high = false;
     for (uint32_t k = L + 1 + lane; k <= t; k += 32) high |= C[k * kColStride] != 0;
-    if (__any_sync(0xffffffffu, high)) return false;
-    uint32_t *Tp = temp, *Om = temp + n1, *D = Om + t + 1;
-    uint32_t count = 0;
-    {
-        uint32_t cr[EPL];
+    return !__any_sync(0xffffffffu, high);
+}
+
+// positions i with C(X_i^-1) = 0 of two locators (columns CA, CB with lengths
+// LA, LB), into TA / TB (at most ecc + 1 kept); returns the two root counts
+template <int EPL>
+static __device__ __forceinline__ void rsi16_roots_pair(const Rsi16Dev &c, const uint32_t *CA, uint32_t LA,
+                                                        const uint32_t *CB, uint32_t LB, uint32_t *TA,
+                                                        uint32_t *TB, const RegTw<EPL> &tw, int lane,
+                                                        uint32_t &countA, uint32_t &countB) {
+    const uint32_t ecc = c.ecc, n1 = ecc + 1;
+    uint32_t ca[EPL], cb[EPL];
+#pragma unroll
+    for (int h = 0; h < EPL; ++h) {
+        const uint32_t k = (uint32_t)(lane * EPL + h);
+        ca[h] = k <= LA ? CA[k * kColStride] : 0u;
+        cb[h] = k <= LB ? CB[k * kColStride] : 0u;
+    }
+    uint32_t na = 0, nb = 0;
+    const uint32_t nch = c.block_len / ecc;
+    for (uint32_t ch = 0; ch < nch; ++ch) {
+        uint32_t x[EPL], y[EPL];
 #pragma unroll
         for (int h = 0; h < EPL; ++h) {
-            const uint32_t k = (uint32_t)(lane * EPL + h);
-            cr[h] = k <= L ? C[k * kColStride] : 0u;
+            const uint32_t sh = c.pintt_shift[ch * ecc + lane * EPL + h];
+            x[h] = fmul(ca[h], sh);
+            y[h] = fmul(cb[h], sh);
         }
-        const uint32_t nch = c.block_len / ecc;
-#pragma unroll 2
-        for (uint32_t ch = 0; ch < nch; ++ch) {
-            uint32_t x[EPL];
+        reg_gs2<EPL>(x, y, tw, lane);
 #pragma unroll
-            for (int h = 0; h < EPL; ++h) x[h] = fmul(cr[h], c.pintt_shift[ch * ecc + lane * EPL + h]);
-            reg_gs<EPL>(x, tw, lane);
-#pragma unroll
-            for (int h = 0; h < EPL; ++h) {
-                const bool hit = x[h] == 0;
-                const uint32_t msk = __ballot_sync(0xffffffffu, hit);
-                const uint32_t at = count + __popc(msk & ((1u << lane) - 1u));
-                if (hit && at < n1) Tp[at] = ch * ecc + lane * EPL + h;
-                count += __popc(msk);
-            }
+        for (int h = 0; h < EPL; ++h) {
+            const uint32_t pos = ch * ecc + lane * EPL + h;
+            const uint32_t below = (1u << lane) - 1u;
+            const bool ha = x[h] == 0, hb = y[h] == 0;
+            const uint32_t ma = __ballot_sync(0xffffffffu, ha), mb = __ballot_sync(0xffffffffu, hb);
+            const uint32_t at = na + __popc(ma & below), bt = nb + __popc(mb & below);
+            if (ha && at < n1) TA[at] = pos;
+            if (hb && bt < n1) TB[bt] = pos;
+            na += __popc(ma);
+            nb += __popc(mb);
         }
     }
     __syncwarp();
-    if (count != L) return false;
+    countA = na;
+    countB = nb;
+}
+
+// Omega, Forney and the corrections of block b whose L roots are in Tp;
+// Om and D are scratch of t + 1 words each
+static __device__ __forceinline__ void rsi16_forney_apply(const Rsi16Dev &c, const BlockView &v, size_t b,
+                                                          const uint32_t *S, const uint32_t *C, uint32_t L,
+                                                          const uint32_t *Tp, uint32_t *Om, uint32_t *D,
+                                                          uint8_t *status, int lane) {
     // evaluator Omega = S * C mod x^L and the derivative C'
     for (uint32_t j = lane; j < L; j += 32) {
         uint32_t s = 0;
@@ -1003,7 +1058,6 @@ static __device__ __forceinline__ bool rsi16_repair_finish_t(const Rsi16Dev &c, 
     }
     __syncwarp();
     if (lane == 0) status[b] = FFGPU_REPAIR_OK;
-    return true;
 }
 
 // RSi16v::_repair with known locations (rsi16v_impl.hpp:171-231),
