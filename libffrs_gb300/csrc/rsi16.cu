@@ -180,7 +180,9 @@ __global__ void rsi16_encode_warp_kernel(Rsi16Dev c, BlockView v, size_t nblocks
     if constexpr (EPL > 0) {
         RegTw<EPL> tw;
         reg_twiddles<EPL>(c, w.lane, tw);
-        for (size_t b = w.warp_global; b < nblocks; b += w.nwarps) rsi16_encode_block_reg<EPL>(c, v, b, tw, w.lane);
+        // two blocks per pass (a lone last block pairs with itself)
+        for (size_t b = 2 * (size_t)w.warp_global; b < nblocks; b += 2 * (size_t)w.nwarps)
+            rsi16_encode_pair_reg<EPL>(c, v, b, b + 1 < nblocks ? b + 1 : b, tw, w.lane);
     } else {
         for (size_t b = w.warp_global; b < nblocks; b += w.nwarps) rsi16_encode_block(c, v, b, w.ws, w.lane);
     }
@@ -254,7 +256,7 @@ __global__ void __launch_bounds__(128, 4) rsi16_repair_batch_kernel(Rsi16Dev c, 
             const int j1 = todo ? __ffs(todo) - 1 : j0;
             todo &= todo - 1;
             uint32_t s0[EPL], s1[EPL];
-            reg_pntt2<EPL>(c, v, base + j0, base + j1, c.pntt_blocks, tw, w.lane, s0, s1);
+            reg_pntt2<EPL>(c, v, base + j0, base + j1, c.pntt_blocks, true, tw, w.lane, s0, s1);
             bool any0 = false, any1 = false;
 #pragma unroll
             for (int h = 0; h < EPL; ++h) {

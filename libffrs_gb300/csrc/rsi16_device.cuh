@@ -622,11 +622,11 @@ static __device__ __forceinline__ void reg_ct2(uint32_t (&x)[EPL], uint32_t (&y)
     }
 }
 
-// reg_pntt of two blocks b0, b1 of the same view at once, with parity
+// reg_pntt of two blocks b0, b1 of the same view at once
 template <int EPL>
 static __device__ __forceinline__ void reg_pntt2(const Rsi16Dev &c, const BlockView &v, size_t b0, size_t b1,
-                                                 uint32_t nchunks, const RegTw<EPL> &tw, int lane,
-                                                 uint32_t (&acc0)[EPL], uint32_t (&acc1)[EPL]) {
+                                                 uint32_t nchunks, bool with_parity, const RegTw<EPL> &tw,
+                                                 int lane, uint32_t (&acc0)[EPL], uint32_t (&acc1)[EPL]) {
     constexpr uint32_t n = 32 * EPL;
     const size_t mb0 = (b0 / v.group) * v.msg_gstride + (b0 % v.group) * v.msg_bstride;
     const size_t pb0 = (b0 / v.group) * v.par_gstride + (b0 % v.group) * v.par_bstride;
@@ -642,7 +642,7 @@ static __device__ __forceinline__ void reg_pntt2(const Rsi16Dev &c, const BlockV
             if (k < c.message_len) {
                 w0 = ld_word(v.msg, v.msg16, mb0 + (size_t)k * v.msg_estride);
                 w1 = ld_word(v.msg, v.msg16, mb1 + (size_t)k * v.msg_estride);
-            } else if (k < c.block_len) {
+            } else if (with_parity && k < c.block_len) {
                 w0 = ld_word(v.par, v.par16, pb0 + (size_t)(k - c.message_len) * v.par_estride);
                 w1 = ld_word(v.par, v.par16, pb1 + (size_t)(k - c.message_len) * v.par_estride);
             }
@@ -657,6 +657,28 @@ static __device__ __forceinline__ void reg_pntt2(const Rsi16Dev &c, const BlockV
             acc0[h] = ch ? fadd(acc0[h], r0) : r0;
             acc1[h] = ch ? fadd(acc1[h], r1) : r1;
         }
+    }
+}
+
+// parity of blocks b0 and b1 at once (b1 == b0 is allowed)
+template <int EPL>
+static __device__ __forceinline__ void rsi16_encode_pair_reg(const Rsi16Dev &c, const BlockView &v, size_t b0,
+                                                             size_t b1, const RegTw<EPL> &tw, int lane) {
+    uint32_t a0[EPL], a1[EPL];
+    reg_pntt2<EPL>(c, v, b0, b1, c.pntt_blocks - 1, false, tw, lane, a0, a1);
+#pragma unroll
+    for (int h = 0; h < EPL; ++h) {
+        const uint32_t m = c.ecc_mix[lane * EPL + h];
+        a0[h] = fmul(a0[h], m);
+        a1[h] = fmul(a1[h], m);
+    }
+    reg_gs2<EPL>(a0, a1, tw, lane);
+    const size_t p0 = (b0 / v.group) * v.par_gstride + (b0 % v.group) * v.par_bstride;
+    const size_t p1 = (b1 / v.group) * v.par_gstride + (b1 % v.group) * v.par_bstride;
+#pragma unroll
+    for (int h = 0; h < EPL; ++h) {
+        st_word(v.par, v.par16, p0 + (size_t)(lane * EPL + h) * v.par_estride, a0[h]);
+        st_word(v.par, v.par16, p1 + (size_t)(lane * EPL + h) * v.par_estride, a1[h]);
     }
 }
 
