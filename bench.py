@@ -990,13 +990,18 @@ def bench_serving(args, torch, rank, world):
     serving_restore(reqs)
     plain_lat, plain_span = run_plain_fifo(reqs)
     want = [(r["a"].copy(), r["b"].copy(), r["s"].copy() if "s" in r else None) for r in reqs]
+    from libffrs_gb300 import capi
+
     best = None
-    for _ in range(max(1, args.steps)):
-        serving_restore(reqs)
-        lat, span = run_served(reqs)
-        if best is None or span < best[1]:
-            best = (lat, span)
-    lat, span = best
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        for _ in range(max(1, args.steps)):
+            serving_restore(reqs)
+            n0 = capi.kernel_launches()
+            lat, span = run_served(reqs)
+            launched = capi.kernel_launches() - n0
+            if best is None or span < best[1]:
+                best = (lat, span, launched)
+    lat, span, launched = best
     same = all(np.array_equal(r["a"], w[0]) and np.array_equal(r["b"], w[1]) and
                (w[2] is None or np.array_equal(r["s"], w[2])) for r, w in zip(reqs, want))
     if not same:
@@ -1009,7 +1014,7 @@ def bench_serving(args, torch, rank, world):
     return {
         "workload": "serving", "total_ms": span * 1e3 * max(1, args.steps), "kern_ms": [span * 1e3],
         "algo_bytes_per_step": nbytes,
-        "launches": 0, "kernels": {}, "clocks": {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0},
+        "launches": launched, "kernels": {}, "clocks": clk.summary(),
         "e2e": {"value": gbs, "unit": "GB/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                 "api": "ffgpu_server_submit_* on page-locked host buffers"},
         "config": {"workload": "serving: Poisson arrivals at %.0f GB/s offered, log-normal payloads 4 KiB-64 MiB, "

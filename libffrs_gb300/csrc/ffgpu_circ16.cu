@@ -29,6 +29,22 @@ static size_t repair_device(Circ16Code &c, uint16_t *dm, uint16_t *de, cudaStrea
     return (size_t)-1;
 }
 
+// Codewords of a multi-codeword call: one fused batch launch repairs them all,
+// one codeword per CTA with the same stage routines as circ16_repair_one,
+// restoring the columns from a raising one on and skipping the ecc write-back
+// for that codeword as repair_device does; status[i] as in
+// ffgpu_circ16_repair.  The caller holds h->mu.
+static void repair_many(ffgpu_circ16 *h, uint16_t *dm, uint16_t *de, size_t nblocks, uint8_t *ds, cudaStream_t st) {
+    auto ok = [](int rc) {
+        if (rc != FFGPU_OK) throw Error(rc, ffgpu_last_error());
+    };
+    if (!h->batch) ok(ffgpu_batch_create(&h->batch));
+    ok(ffgpu_batch_clear(h->batch));
+    ok(ffgpu_batch_add_circ16(h->batch, h, FFGPU_OP_DECODE, dm, de, nblocks, ds));
+    ok(ffgpu_batch_plan(h->batch, 0, st));
+    ok(ffgpu_batch_launch(h->batch, st));
+}
+
 extern "C" {
 
 int ffgpu_circ16_create(size_t inner_block_len, size_t inner_ecc_len, size_t outer_block_len, size_t outer_ecc_len,
@@ -76,6 +92,10 @@ int ffgpu_circ16_repair(const ffgpu_circ16 *code, uint16_t *msg, uint16_t *ecc, 
         std::lock_guard<std::mutex> lk(h->mu);
         Circ16Code &c = *h->code;
         cudaStream_t st = pick(stream);
+        if (nblocks > 1) {
+            repair_many(h, msg, ecc, nblocks, status ? status : (uint8_t *)h->d_status.get(nblocks), st);
+            return;
+        }
         for (size_t b = 0; b < nblocks; ++b) {
             uint16_t *dm = msg + b * c.message_len, *de = ecc + b * c.ecc_len;
             // keep the message of this block in case a column raises
@@ -162,6 +182,20 @@ int ffgpu_circ16_repair_host(const ffgpu_circ16 *code, uint16_t *msg, uint16_t *
         Circ16Code &c = *h->code;
         if (!nblocks) return;
         cudaStream_t st = lib_stream();
+        if (nblocks > 1) {
+            const size_t nm = nblocks * c.message_len * 2, ne = nblocks * c.ecc_len * 2;
+            uint16_t *dm = (uint16_t *)h->d_msg.get(nm);
+            uint16_t *de = (uint16_t *)h->d_ecc.get(ne);
+            uint8_t *ds = (uint8_t *)h->d_status.get(nblocks);
+            FFGPU_CHECK_CUDA(cudaMemcpyAsync(dm, msg, nm, cudaMemcpyHostToDevice, st));
+            FFGPU_CHECK_CUDA(cudaMemcpyAsync(de, ecc, ne, cudaMemcpyHostToDevice, st));
+            repair_many(h, dm, de, nblocks, ds, st);
+            FFGPU_CHECK_CUDA(cudaMemcpyAsync(msg, dm, nm, cudaMemcpyDeviceToHost, st));
+            FFGPU_CHECK_CUDA(cudaMemcpyAsync(ecc, de, ne, cudaMemcpyDeviceToHost, st));
+            if (status) FFGPU_CHECK_CUDA(cudaMemcpyAsync(status, ds, nblocks, cudaMemcpyDeviceToHost, st));
+            FFGPU_CHECK_CUDA(cudaStreamSynchronize(st));
+            return;
+        }
         uint16_t *dm = (uint16_t *)h->d_msg.get(c.message_len * 2 * 2);
         uint16_t *de = (uint16_t *)h->d_ecc.get(c.ecc_len * 2);
         for (size_t b = 0; b < nblocks; ++b) {
