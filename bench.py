@@ -1048,6 +1048,17 @@ def host_threads():
         return os.cpu_count() or 1
 
 
+# the workload each CPU arm samples, described as the GPU arm's line does
+REFERENCE_CONFIG = {
+    "rs256-decode": {"workload": "RS256 decode ecc_len=32, 1048576 blocks x (223+32) B, 0-16 errors/block, "
+                                 "1% 17-20 errors", "blocks": 1048576, "message_len": 223, "ecc_len": 32},
+    "rs256-encode": {"workload": "RS256 encode ecc_len=32, 65536 blocks x 223 B", "blocks": 65536},
+    "rsi16-decode": {"workload": "RSi16(1024, 64) decode, 262144 blocks, 0-32 symbol errors/block",
+                     "blocks": 262144},
+    "rsi16-encode": {"workload": "RSi16(1024, 64) encode, 262144 blocks x 960 uint16 words", "blocks": 262144},
+}
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -1064,10 +1075,11 @@ def run_reference(args, rank, world):
         vals.append(v)
     v = statistics.median(vals)
     line = {
-        "impl": "reference", "metric": METRIC, "value": v, "unit": unit, "n_gpus": world, "steps": args.steps,
+        "impl": "reference", "metric": METRIC if args.workload == "rs256-decode" else f"{args.workload} GB/s bit-exact",
+        "value": v, "unit": unit, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded numpy PCG64)",
-        "config": {"workload": args.workload, "sample_blocks": sample},
+        "config": dict(REFERENCE_CONFIG.get(args.workload, {"workload": args.workload}), sample_blocks=sample),
         "cpu_baseline": {"value": v, "unit": unit, "cores": threads, "kind": "port",
                          "sample": f"{sample} blocks of the {args.workload} workload per step"},
         "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
