@@ -225,17 +225,18 @@ __global__ void rsi16_repair_warp_kernel(Rsi16Dev c, BlockView v, size_t nblocks
 }
 
 // ecc 32 and 64: batches of 32 blocks per warp, syndromes warp-wide,
-// Berlekamp-Massey one block per lane, roots and Forney warp-wide.  A block
-// the bounded-distance path does not accept is marked kMirrorPending and left
-// for rsi16_repair_mirror_kernel, so that this kernel's warp workspace is only
-// the batch's syndrome columns [ecc][33], locator columns [ecc/2 + 1][33] and
-// the finishing scratch (two root lists of ecc + 1 words, Omega and C').
-constexpr uint8_t kMirrorPending = 0xFE;
-
+// Berlekamp-Massey one block per lane, roots and Forney warp-wide.  Warps take
+// batches from a counter, so that a warp busy with a block the
+// bounded-distance path does not accept (the step-for-step mirror, about 10^5
+// instructions on one warp, on its workspace slice of mirror_ws) takes fewer
+// batches.  The warp workspace in shared memory is the batch's syndrome
+// columns [ecc][33], locator columns [ecc/2 + 1][33] and the finishing scratch
+// (two root lists of ecc + 1 words, Omega and C').
 template <int EPL>
 __global__ void __launch_bounds__(128, 4) rsi16_repair_batch_kernel(Rsi16Dev c, BlockView v, size_t nblocks,
                                                                  uint8_t *status, const uint8_t *active,
-                                                                 uint32_t ws_words) {
+                                                                 uint32_t ws_words, unsigned int *next_batch,
+                                                                 uint32_t *mirror_ws, uint32_t mirror_words) {
     constexpr int T = 16 * EPL;
     WarpCtx w = warp_ctx(nullptr, ws_words);
     RegTw<EPL> tw;
@@ -243,8 +244,15 @@ __global__ void __launch_bounds__(128, 4) rsi16_repair_batch_kernel(Rsi16Dev c, 
     uint32_t *Ssm = w.ws;
     uint32_t *Csm = Ssm + 32 * EPL * kColStride;
     uint32_t *fin = Csm + (T + 1) * kColStride;
-    unsigned long long nfast = 0;
-    for (size_t base = (size_t)w.warp_global * 32; base < nblocks; base += (size_t)w.nwarps * 32) {
+    uint32_t *mws = mirror_ws + (size_t)w.warp_global * mirror_words;
+    const size_t nbatches = (nblocks + 31) / 32;
+    unsigned long long nfast = 0, nmirror = 0;
+    for (;;) {
+        unsigned int bi = 0;
+        if (w.lane == 0) bi = atomicAdd(next_batch, 1u);
+        bi = __shfl_sync(0xffffffffu, bi, 0);
+        if (bi >= nbatches) break;
+        const size_t base = (size_t)bi * 32;
         const int nb = (int)min((size_t)32, nblocks - base);
         uint32_t live = 0u, nz = 0u;
         for (int j = 0; j < nb; ++j)
@@ -280,7 +288,7 @@ __global__ void __launch_bounds__(128, 4) rsi16_repair_batch_kernel(Rsi16Dev c, 
         // blocks whose locator passes the checks get their roots searched in
         // pairs; the others (and those whose root count is not L) go to the
         // mirror
-        uint32_t cand = 0u;
+        uint32_t cand = 0u, mirror = 0u;
         for (int j = 0; j < nb; ++j) {
             if (!((live >> j) & 1u)) continue;
             const size_t b = base + j;
@@ -292,8 +300,8 @@ __global__ void __launch_bounds__(128, 4) rsi16_repair_batch_kernel(Rsi16Dev c, 
             const uint32_t Lj = __shfl_sync(0xffffffffu, L, j);
             if (rsi16_locator_ok(c, Csm + j, Lj, w.lane))
                 cand |= 1u << j;
-            else if (w.lane == 0)
-                status[b] = kMirrorPending;
+            else
+                mirror |= 1u << j;
         }
         uint32_t *TA = fin, *TB = fin + (c.ecc + 1), *Om = TB + (c.ecc + 1), *D = Om + (T + 1);
         for (uint32_t todo = cand; todo;) {
@@ -307,35 +315,29 @@ __global__ void __launch_bounds__(128, 4) rsi16_repair_batch_kernel(Rsi16Dev c, 
             if (na == La) {
                 rsi16_forney_apply(c, v, base + ja, Ssm + ja, Csm + ja, La, TA, Om, D, status, w.lane);
                 ++nfast;
-            } else if (w.lane == 0) {
-                status[base + ja] = kMirrorPending;
+            } else {
+                mirror |= 1u << ja;
             }
             if (jb != ja) {
                 if (nbr == Lb) {
                     rsi16_forney_apply(c, v, base + jb, Ssm + jb, Csm + jb, Lb, TB, Om, D, status, w.lane);
                     ++nfast;
-                } else if (w.lane == 0) {
-                    status[base + jb] = kMirrorPending;
+                } else {
+                    mirror |= 1u << jb;
                 }
             }
         }
+        for (uint32_t todo = mirror; todo; todo &= todo - 1) {
+            __syncwarp();
+            rsi16_repair_block(c, v, base + (__ffs(todo) - 1), mws, status, w.lane);
+            ++nmirror;
+        }
         __syncwarp();  // the batch's columns are read before the next batch writes them
     }
-    if (w.lane == 0 && nfast) atomicAdd(&g_repair_fast_blocks, nfast);
-}
-
-// The step-for-step mirror for the blocks rsi16_repair_batch_kernel marked.
-__global__ void rsi16_repair_mirror_kernel(Rsi16Dev c, BlockView v, size_t nblocks, uint8_t *status,
-                                           const uint8_t *active, uint32_t *gscratch, uint32_t ws_words) {
-    WarpCtx w = warp_ctx(gscratch, ws_words);
-    unsigned long long nmirror = 0;
-    for (size_t b = w.warp_global; b < nblocks; b += w.nwarps) {
-        if ((active && !active[b]) || status[b] != kMirrorPending) continue;
-        __syncwarp();
-        rsi16_repair_block(c, v, b, w.ws, status, w.lane);
-        ++nmirror;
+    if (w.lane == 0 && (nfast | nmirror)) {
+        atomicAdd(&g_repair_fast_blocks, nfast);
+        atomicAdd(&g_repair_mirror_blocks, nmirror);
     }
-    if (w.lane == 0 && nmirror) atomicAdd(&g_repair_mirror_blocks, nmirror);
 }
 
 void rsi16_repair_counters(uint64_t *fast, uint64_t *mirror, bool reset) {
@@ -502,18 +504,27 @@ void rsi16_repair(const Rsi16Code &c, const BlockView &v, size_t nblocks, uint8_
             const int per_sm = std::max(1, (int)((220 * 1024) / (smem + 1024)));
             const unsigned grid =
                 (unsigned)std::max<size_t>(1, std::min<size_t>((batches + 3) / 4, (size_t)num_sms() * per_sm));
+            // the batch counter and the mirror workspaces (one per warp),
+            // stream-ordered so that concurrent calls on other streams get
+            // their own
+            const uint32_t mwords = c.dev.temp_len + 1;
+            const size_t mbytes = 256 + (size_t)grid * 4 * mwords * 4;
+            void *scratch = nullptr;
+            FFGPU_CHECK_CUDA(cudaMallocAsync(&scratch, mbytes, st));
+            FFGPU_CHECK_CUDA(cudaMemsetAsync(scratch, 0, 4, st));
             FFGPU_CHECK_CUDA(cudaFuncSetAttribute(rsi16_repair_batch_kernel<E>,
                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             {
                 KernelTimer kt_timer("rsi16_repair_batch_kernel", st);
-                rsi16_repair_batch_kernel<E><<<grid, 128, smem, st>>>(c.dev, v, nblocks, status, active, ws);
-                check_launch("rsi16_repair_batch_kernel");
+                rsi16_repair_batch_kernel<E><<<grid, 128, smem, st>>>(
+                    c.dev, v, nblocks, status, active, ws, (unsigned int *)scratch,
+                    (uint32_t *)((char *)scratch + 256), mwords);
             }
-            Launch L = plan(rsi16_repair_mirror_kernel, nblocks, c.dev.temp_len + 1);
-            KernelTimer kt_timer("rsi16_repair_mirror_kernel", st);
-            rsi16_repair_mirror_kernel<<<L.grid, L.threads, L.smem, st>>>(c.dev, v, nblocks, status, active,
-                                                                         L.gscratch, L.ws_words);
-            check_launch("rsi16_repair_mirror_kernel");
+            cudaError_t e = cudaGetLastError();
+            cudaFreeAsync(scratch, st);
+            if (e != cudaSuccess)
+                throw Error(FFGPU_ECUDA, std::string("rsi16_repair_batch_kernel: ") + cudaGetErrorString(e));
+            launched();
             return;
         }
         Launch L = plan(rsi16_repair_warp_kernel<E>, nblocks, c.dev.temp_len + 1);
