@@ -1048,6 +1048,23 @@ def host_threads():
         return os.cpu_count() or 1
 
 
+def max_over_ranks(value, world, device):
+    """The slowest rank's timed-region length: the whole job ends with it."""
+    if world <= 1:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_gbs(bytes_per_rank_step, steps, world, total_ms):
+    """Whole-job GB/s: every rank processes its own shard of bytes_per_rank_step
+    per step (weak scaling), over the slowest rank's time."""
+    return bytes_per_rank_step * steps * world / (total_ms / 1e3) / 1e9
+
+
 # the workload each CPU arm samples, described as the GPU arm's line does
 REFERENCE_CONFIG = {
     "rs256-decode": {"workload": "RS256 decode ecc_len=32, 1048576 blocks x (223+32) B, 0-16 errors/block, "
@@ -1132,15 +1149,11 @@ def main():
     capi.call("ffgpu_init", local)
     fn = WORKLOADS[args.workload][0]
     r = fn(args, torch, rank, world)
-    total_ms = r["total_ms"]
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(r["total_ms"], world, "cuda")
     if rank != 0:
         return
     steps = args.steps
-    value = r["algo_bytes_per_step"] * steps * world / (total_ms / 1e3) / 1e9
+    value = job_gbs(r["algo_bytes_per_step"], steps, world, total_ms)
     # dominant kernel: the one with the largest share of the timed region's
     # kernel time (CUDA events around each launch, on its stream)
     kernels = r.get("kernels") or {}
