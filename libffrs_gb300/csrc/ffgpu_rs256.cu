@@ -101,8 +101,34 @@ void host_copy(void *dst, const void *src, size_t n) {
     done.wait(lk, [&] { return left == 0; });
 }
 
+// Ordering events of the host pipelines, reused across calls (creating and
+// destroying a few dozen events per call costs more than the reuse)
+namespace {
+std::mutex g_sync_ev_mu;
+std::vector<cudaEvent_t> g_sync_ev;
+}  // namespace
+
+static cudaEvent_t sync_event_get() {
+    {
+        std::lock_guard<std::mutex> lk(g_sync_ev_mu);
+        if (!g_sync_ev.empty()) {
+            cudaEvent_t e = g_sync_ev.back();
+            g_sync_ev.pop_back();
+            return e;
+        }
+    }
+    cudaEvent_t e = nullptr;
+    FFGPU_CHECK_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    return e;
+}
+
+static void sync_event_put(cudaEvent_t e) {
+    std::lock_guard<std::mutex> lk(g_sync_ev_mu);
+    g_sync_ev.push_back(e);
+}
+
 OutputDrain::~OutputDrain() {
-    for (auto &c : chunks_) cudaEventDestroy(c.ev);
+    for (auto &c : chunks_) sync_event_put(c.ev);
 }
 
 void OutputDrain::copy(void *dst, const void *src, size_t n) {
@@ -111,8 +137,7 @@ void OutputDrain::copy(void *dst, const void *src, size_t n) {
 
 void OutputDrain::chunk(cudaStream_t st) {
     if (parts_.size() == open_) return;
-    cudaEvent_t ev = nullptr;
-    FFGPU_CHECK_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    cudaEvent_t ev = sync_event_get();
     chunks_.push_back({ev, open_, parts_.size() - open_});
     FFGPU_CHECK_CUDA(cudaEventRecord(ev, st));
     open_ = parts_.size();
@@ -140,12 +165,11 @@ cudaStream_t pipe_up() { return pipe_slot(kPipeStreams); }
 cudaStream_t pipe_down() { return pipe_slot(kPipeStreams + 1); }
 
 HostPipeline::~HostPipeline() {
-    for (cudaEvent_t e : evs_) cudaEventDestroy(e);
+    for (cudaEvent_t e : evs_) sync_event_put(e);
 }
 
 cudaEvent_t HostPipeline::record(cudaStream_t s) {
-    cudaEvent_t e = nullptr;
-    FFGPU_CHECK_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    cudaEvent_t e = sync_event_get();
     evs_.push_back(e);
     FFGPU_CHECK_CUDA(cudaEventRecord(e, s));
     return e;
