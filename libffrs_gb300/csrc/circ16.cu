@@ -96,6 +96,126 @@ __global__ void k_outer_modes(CircDims d, const uint32_t *lcnt, uint32_t *pos_of
     outer_modes_col(d, lcnt, pos_off, pos_cnt, known, unknown, blockIdx.x * blockDim.x + threadIdx.x, 0);
 }
 
+// ---------------------------------------------------------------- many codewords
+//
+// The stage kernels over ncw codewords at once: item i of codeword cw is the
+// global item cw * nitems + i, and every per-codeword array is a slice of a
+// codeword-major array.  Position offsets (zoff, pos_off) are made global, so
+// that one known-location repair launch serves every codeword.
+
+struct CircMany {
+    size_t rso_n, rsi_n, n_oz, n_iz;  // words per codeword of rso_ecc / rsi_ecc (and synd), item counts
+};
+
+__global__ void km_widen(const uint16_t *__restrict__ ecc, size_t ecc_len, size_t rso_n, size_t rsi_n,
+                         uint32_t *__restrict__ rso, uint32_t *__restrict__ rsi, size_t ncw) {
+    const size_t per = rso_n + rsi_n, total = per * ncw;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t cw = i / per, j = i - cw * per;
+        const uint32_t w = ecc[cw * ecc_len + j];
+        if (j < rso_n)
+            rso[cw * rso_n + j] = w;
+        else
+            rsi[cw * rsi_n + (j - rso_n)] = w;
+    }
+}
+
+__global__ void km_outer_zeros_prepare(CircDims d, CircMany m, size_t ncw, const uint32_t *rso_ecc,
+                                       const uint32_t *rsi_ecc, const uint32_t *synd, uint32_t *blocks,
+                                       uint32_t *zpos, uint32_t *zoff, uint32_t *zcnt, uint8_t *active) {
+    const size_t gi = blockIdx.x * (size_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (gi >= ncw * m.n_oz) return;
+    const size_t cw = gi / m.n_oz;
+    outer_zeros_prepare_item(d, rso_ecc + cw * m.rso_n, rsi_ecc + cw * m.rsi_n, synd + cw * m.rsi_n,
+                             blocks + cw * m.n_oz * d.ri_bl, zpos + cw * m.n_oz * d.ri_ecc, zoff + cw * m.n_oz,
+                             zcnt + cw * m.n_oz, active + cw * m.n_oz, (uint32_t)(gi - cw * m.n_oz), lane);
+    if (lane == 0) zoff[gi] += (uint32_t)(cw * m.n_oz * d.ri_ecc);
+}
+
+__global__ void km_outer_zeros_commit(CircDims d, CircMany m, size_t ncw, uint32_t *rso_ecc, uint32_t *rsi_ecc,
+                                      uint32_t *synd, const uint32_t *blocks, const uint32_t *blk_synd,
+                                      const uint32_t *zpos, const uint32_t *zcnt, const uint8_t *active) {
+    const size_t gi = blockIdx.x * (size_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (gi >= ncw * m.n_oz) return;
+    const size_t cw = gi / m.n_oz;
+    outer_zeros_commit_item(d, rso_ecc + cw * m.rso_n, rsi_ecc + cw * m.rsi_n, synd + cw * m.rsi_n,
+                            blocks + cw * m.n_oz * d.ri_bl, blk_synd + cw * m.n_oz * d.ri_ecc,
+                            zpos + cw * m.n_oz * d.ri_ecc, zcnt + cw * m.n_oz, active + cw * m.n_oz,
+                            (uint32_t)(gi - cw * m.n_oz), threadIdx.x & 31);
+}
+
+__global__ void km_inner_zeros_prepare(CircDims d, CircMany m, size_t ncw, const uint32_t *rsi_ecc,
+                                       const uint32_t *synd, uint32_t *vecs, uint8_t *flag) {
+    const size_t gi = blockIdx.x * (size_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (gi >= ncw * m.n_iz) return;
+    const size_t cw = gi / m.n_iz;
+    inner_zeros_prepare_item(d, rsi_ecc + cw * m.rsi_n, synd + cw * m.rsi_n, vecs + cw * m.n_iz * d.ri_ecc,
+                             flag + cw * m.n_iz, (uint32_t)(gi - cw * m.n_iz), threadIdx.x & 31);
+}
+
+__global__ void km_inner_zeros_commit(CircDims d, CircMany m, size_t ncw, uint32_t *rsi_ecc, uint32_t *synd,
+                                      const uint32_t *vecs, const uint8_t *flag) {
+    const size_t gi = blockIdx.x * (size_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (gi >= ncw * m.n_iz) return;
+    const size_t cw = gi / m.n_iz;
+    inner_zeros_commit_item(d, rsi_ecc + cw * m.rsi_n, synd + cw * m.rsi_n, vecs + cw * m.n_iz * d.ri_ecc,
+                            flag + cw * m.n_iz, (uint32_t)(gi - cw * m.n_iz), threadIdx.x & 31);
+}
+
+__global__ void km_find_locations(CircDims d, CircMany m, size_t ncw, const uint32_t *synd, uint32_t *locs,
+                                  uint32_t *lcnt) {
+    const size_t gi = blockIdx.x * (size_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (gi >= ncw * d.interleave) return;
+    const size_t cw = gi / d.interleave;
+    find_locations_item(d, synd + cw * m.rsi_n, locs + cw * (size_t)d.interleave * d.ro_bl, lcnt + cw * d.interleave,
+                        (uint32_t)(gi - cw * d.interleave), threadIdx.x & 31);
+}
+
+__global__ void km_outer_modes(CircDims d, size_t ncw, const uint32_t *lcnt, uint32_t *pos_off, uint32_t *pos_cnt,
+                               uint8_t *known, uint8_t *unknown) {
+    const size_t gi = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (gi >= ncw * d.rso_interleave) return;
+    const size_t cw = gi / d.rso_interleave, o = cw * d.rso_interleave;
+    outer_modes_col(d, lcnt + cw * d.interleave, pos_off + o, pos_cnt + o, known + o, unknown + o,
+                    (uint32_t)(gi - o), 0);
+    pos_off[gi] += (uint32_t)(cw * (size_t)d.interleave * d.ro_bl);
+}
+
+// Per codeword (one CTA): the first outer column whose repair raised, in the
+// reference's column order.  With one, the columns from it on get their
+// original words back, the ecc is left as it was and the status is
+// FFGPU_STATUS_ASSERT; otherwise the ecc is written back (16-bit truncation,
+// dump_ecc, pycirc16.hpp:326-330) and the status is 0.
+__global__ void km_finish(CircDims d, CircMany m, size_t ncw, const uint8_t *col_status, uint16_t *msg,
+                          const uint16_t *saved, size_t message_len, uint16_t *ecc, size_t ecc_len,
+                          const uint32_t *rso_ecc, const uint32_t *rsi_ecc, uint8_t *status) {
+    const size_t cw = blockIdx.x;
+    if (cw >= ncw) return;
+    __shared__ uint32_t first;
+    if (threadIdx.x == 0) first = d.rso_interleave;
+    __syncthreads();
+    const uint8_t *cs = col_status + cw * d.rso_interleave;
+    for (uint32_t c = threadIdx.x; c < d.rso_interleave; c += blockDim.x)
+        if (cs[c] == FFGPU_STATUS_ASSERT) atomicMin(&first, c);
+    __syncthreads();
+    const uint32_t f = first;
+    if (f < d.rso_interleave) {
+        const size_t ncols = d.rso_interleave - f;
+        for (size_t i = threadIdx.x; i < (size_t)d.ro_ml * ncols; i += blockDim.x) {
+            const size_t r = i / ncols, col = f + (i - r * ncols);
+            const size_t at = cw * message_len + r * d.rso_interleave + col;
+            msg[at] = saved[at];
+        }
+        if (threadIdx.x == 0 && status) status[cw] = FFGPU_STATUS_ASSERT;
+        return;
+    }
+    uint16_t *e = ecc + cw * ecc_len;
+    for (size_t j = threadIdx.x; j < m.rso_n + m.rsi_n; j += blockDim.x)
+        e[j] = (uint16_t)(j < m.rso_n ? rso_ecc[cw * m.rso_n + j] : rsi_ecc[cw * m.rsi_n + (j - m.rso_n)]);
+    if (threadIdx.x == 0 && status) status[cw] = 0;
+}
+
 // ---------------------------------------------------------------- host side
 
 static unsigned g1(size_t n) { return (unsigned)std::min<size_t>((n + 255) / 256, 4096); }
@@ -236,6 +356,94 @@ void circ16_repair_one(Circ16Code &c, uint16_t *msg, uint16_t *ecc, cudaStream_t
     BlockView vreo{rso_ecc, 0, ri.message_len, 1, rsi_ecc + c.rsi_ieccl, 0, ri.ecc, 1, c.outer_rows, false, false};
     rsi16_encode(ri, vreo, c.outer_rows, st);
     if (col_status) FFGPU_CHECK_CUDA(cudaMemcpyAsync(col_status, cst, c.rso_interleave, cudaMemcpyDeviceToHost, st));
+}
+
+// ncw codewords in place (device pointers): the stages of circ16_repair_one,
+// each one launch over every codeword.  status[cw] is 0 or
+// FFGPU_STATUS_ASSERT as in ffgpu_circ16_repair.
+void circ16_repair_many(Circ16Code &c, uint16_t *msg, uint16_t *ecc, size_t ncw, uint8_t *status, cudaStream_t st) {
+    if (!ncw) return;
+    const Rsi16Code &ri = *c.rsi, &ro = *c.rso;
+    const CircDims d = circ16_dims(c);
+    CircMany m;
+    m.rso_n = c.rso_ieccl;
+    m.rsi_n = c.rsi_total;
+    m.n_oz = c.interleave * ro.ecc;
+    m.n_iz = c.interleave * ro.block_len;
+    // codeword-major workspace
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = off;
+        off += (bytes + 255) & ~(size_t)255;
+        return o;
+    };
+    const size_t o_rso = take(ncw * m.rso_n * 4), o_rsi = take(ncw * m.rsi_n * 4), o_syn = take(ncw * m.rsi_n * 4),
+                 o_blk = take(ncw * m.n_oz * ri.block_len * 4), o_bsyn = take(ncw * m.n_oz * ri.ecc * 4),
+                 o_zpos = take(ncw * m.n_oz * ri.ecc * 4), o_zoff = take(ncw * m.n_oz * 4),
+                 o_zcnt = take(ncw * m.n_oz * 4), o_zact = take(ncw * m.n_oz), o_vec = take(ncw * m.n_iz * ri.ecc * 4),
+                 o_flag = take(ncw * m.n_iz), o_locs = take(ncw * c.interleave * ro.block_len * 4),
+                 o_lcnt = take(ncw * c.interleave * 4), o_poff = take(ncw * c.rso_interleave * 4),
+                 o_pcnt = take(ncw * c.rso_interleave * 4), o_kn = take(ncw * c.rso_interleave),
+                 o_un = take(ncw * c.rso_interleave), o_st = take(ncw * c.rso_interleave),
+                 o_save = take(ncw * c.message_len * 2);
+    char *W = (char *)c.rep_ws.get(off);
+    uint32_t *rso_ecc = (uint32_t *)(W + o_rso), *rsi_ecc = (uint32_t *)(W + o_rsi), *synd = (uint32_t *)(W + o_syn);
+    uint32_t *blocks = (uint32_t *)(W + o_blk), *bsyn = (uint32_t *)(W + o_bsyn), *zpos = (uint32_t *)(W + o_zpos);
+    uint32_t *zoff = (uint32_t *)(W + o_zoff), *zcnt = (uint32_t *)(W + o_zcnt);
+    uint8_t *zact = (uint8_t *)(W + o_zact), *flag = (uint8_t *)(W + o_flag);
+    uint32_t *vecs = (uint32_t *)(W + o_vec), *locs = (uint32_t *)(W + o_locs), *lcnt = (uint32_t *)(W + o_lcnt);
+    uint32_t *poff = (uint32_t *)(W + o_poff), *pcnt = (uint32_t *)(W + o_pcnt);
+    uint8_t *kn = (uint8_t *)(W + o_kn), *un = (uint8_t *)(W + o_un), *cst = (uint8_t *)(W + o_st);
+    uint16_t *saved = (uint16_t *)(W + o_save);
+    const unsigned wpb = 4;  // warps per CTA of the per-item kernels
+    auto items = [&](size_t n) { return (unsigned)((n + wpb - 1) / wpb); };
+
+    FFGPU_CHECK_CUDA(cudaMemcpyAsync(saved, msg, ncw * c.message_len * 2, cudaMemcpyDeviceToDevice, st));
+    // load_ecc (pycirc16.hpp:159-163)
+    km_widen<<<g1(ncw * (m.rso_n + m.rsi_n)), 256, 0, st>>>(ecc, c.ecc_len, m.rso_n, m.rsi_n, rso_ecc, rsi_ecc, ncw);
+    check_launch("km_widen");
+    // compute_rsi_synd (pycirc16.hpp:165-181): message rows, then outer parity rows
+    BlockView vmsg{msg, c.message_len, ri.message_len, 1, rsi_ecc, m.rsi_n, ri.ecc, 1, c.inner_rows, true, false};
+    rsi16_synd_grouped(ri, vmsg, ncw * c.inner_rows, synd, c.inner_rows, m.rsi_n, st);
+    BlockView vrso{rso_ecc, m.rso_n, ri.message_len, 1, rsi_ecc + c.rsi_ieccl, m.rsi_n, ri.ecc, 1, c.outer_rows,
+                   false, false};
+    rsi16_synd_grouped(ri, vrso, ncw * c.outer_rows, synd + c.rsi_ieccl, c.outer_rows, m.rsi_n, st);
+    // repair_outer_zeros for every codeword and k
+    km_outer_zeros_prepare<<<items(ncw * m.n_oz), wpb * 32, 0, st>>>(d, m, ncw, rso_ecc, rsi_ecc, synd, blocks, zpos,
+                                                                     zoff, zcnt, zact);
+    check_launch("km_outer_zeros_prepare");
+    BlockView vblk{blocks, m.n_oz * ri.block_len, ri.block_len, 1, blocks + ri.message_len, m.n_oz * ri.block_len,
+                   ri.block_len, 1, m.n_oz, false, false};
+    rsi16_repair_known(ri, vblk, ncw * m.n_oz, zpos, zoff, zcnt, 0, zact, nullptr, st);
+    rsi16_synd(ri, vblk, ncw * m.n_oz, bsyn, st);
+    km_outer_zeros_commit<<<items(ncw * m.n_oz), wpb * 32, 0, st>>>(d, m, ncw, rso_ecc, rsi_ecc, synd, blocks, bsyn,
+                                                                    zpos, zcnt, zact);
+    check_launch("km_outer_zeros_commit");
+    // repair_inner_zeros for every codeword and k
+    km_inner_zeros_prepare<<<items(ncw * m.n_iz), wpb * 32, 0, st>>>(d, m, ncw, rsi_ecc, synd, vecs, flag);
+    check_launch("km_inner_zeros_prepare");
+    rsi16_mix_ecc(ri, vecs, ncw * m.n_iz, st);
+    km_inner_zeros_commit<<<items(ncw * m.n_iz), wpb * 32, 0, st>>>(d, m, ncw, rsi_ecc, synd, vecs, flag);
+    check_launch("km_inner_zeros_commit");
+    // find_error_locations, then repair_outer_errors (pycirc16.hpp:283-305)
+    km_find_locations<<<items(ncw * c.interleave), wpb * 32, 0, st>>>(d, m, ncw, synd, locs, lcnt);
+    check_launch("km_find_locations");
+    km_outer_modes<<<g1(ncw * c.rso_interleave), 256, 0, st>>>(d, ncw, lcnt, poff, pcnt, kn, un);
+    check_launch("km_outer_modes");
+    FFGPU_CHECK_CUDA(cudaMemsetAsync(cst, 0, ncw * c.rso_interleave, st));
+    BlockView vcol = interleaved_view(msg, true, ro.message_len, rso_ecc, false, ro.ecc, c.rso_interleave);
+    rsi16_repair_known(ro, vcol, ncw * c.rso_interleave, locs, poff, pcnt, 0, kn, cst, st);
+    rsi16_repair(ro, vcol, ncw * c.rso_interleave, cst, st, un);
+    // recompute_inner_ecc (pycirc16.hpp:320-324)
+    BlockView vre{msg, c.message_len, ri.message_len, 1, rsi_ecc, m.rsi_n, ri.ecc, 1, c.inner_rows, true, false};
+    rsi16_encode(ri, vre, ncw * c.inner_rows, st);
+    BlockView vreo{rso_ecc, m.rso_n, ri.message_len, 1, rsi_ecc + c.rsi_ieccl, m.rsi_n, ri.ecc, 1, c.outer_rows,
+                   false, false};
+    rsi16_encode(ri, vreo, ncw * c.outer_rows, st);
+    // raising codewords restored, the others' ecc written back
+    km_finish<<<(unsigned)ncw, 256, 0, st>>>(d, m, ncw, cst, msg, saved, c.message_len, ecc, c.ecc_len, rso_ecc,
+                                             rsi_ecc, status);
+    check_launch("km_finish");
 }
 
 // dump_ecc (pycirc16.hpp:326-330), kept separate so that a raising repair can

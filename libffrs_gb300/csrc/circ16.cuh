@@ -37,5 +37,8 @@ void circ16_encode(Circ16Code &c, const uint16_t *msg, size_t nblocks, uint16_t 
 void circ16_repair_one(Circ16Code &c, uint16_t *msg, uint16_t *ecc, cudaStream_t st, bool stop_after_find,
                        size_t find_k, uint32_t *locs_out, uint32_t *lcnt_out, uint8_t *col_status);
 void circ16_dump_ecc(Circ16Code &c, uint16_t *ecc, cudaStream_t st);
+// ncw codewords in place, every repair stage as one launch over all of them;
+// status[cw] 0 or FFGPU_STATUS_ASSERT (NULL: not written).
+void circ16_repair_many(Circ16Code &c, uint16_t *msg, uint16_t *ecc, size_t ncw, uint8_t *status, cudaStream_t st);
 
 }  // namespace ffgpu

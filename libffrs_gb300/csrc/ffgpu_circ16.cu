@@ -16,35 +16,6 @@ using namespace ffgpu;
 // NULL is the CUDA default stream, as everywhere in the CUDA runtime
 static cudaStream_t pick(void *stream) { return (cudaStream_t)stream; }
 
-// Runs the repair of one block already on the device; returns the first
-// raising outer column or SIZE_MAX, and writes the ecc back only when no
-// column raised (the reference's exception skips dump_ecc).
-static size_t repair_device(Circ16Code &c, uint16_t *dm, uint16_t *de, cudaStream_t st) {
-    std::vector<uint8_t> cst(c.rso_interleave);
-    circ16_repair_one(c, dm, de, st, false, 0, nullptr, nullptr, cst.data());
-    FFGPU_CHECK_CUDA(cudaStreamSynchronize(st));
-    for (size_t i = 0; i < cst.size(); ++i)
-        if (cst[i] == FFGPU_STATUS_ASSERT) return i;
-    circ16_dump_ecc(c, de, st);
-    return (size_t)-1;
-}
-
-// Codewords of a multi-codeword call: one fused batch launch repairs them all,
-// one codeword per CTA with the same stage routines as circ16_repair_one,
-// restoring the columns from a raising one on and skipping the ecc write-back
-// for that codeword as repair_device does; status[i] as in
-// ffgpu_circ16_repair.  The caller holds h->mu.
-static void repair_many(ffgpu_circ16 *h, uint16_t *dm, uint16_t *de, size_t nblocks, uint8_t *ds, cudaStream_t st) {
-    auto ok = [](int rc) {
-        if (rc != FFGPU_OK) throw Error(rc, ffgpu_last_error());
-    };
-    if (!h->batch) ok(ffgpu_batch_create(&h->batch));
-    ok(ffgpu_batch_clear(h->batch));
-    ok(ffgpu_batch_add_circ16(h->batch, h, FFGPU_OP_DECODE, dm, de, nblocks, ds));
-    ok(ffgpu_batch_plan(h->batch, 0, st));
-    ok(ffgpu_batch_launch(h->batch, st));
-}
-
 extern "C" {
 
 int ffgpu_circ16_create(size_t inner_block_len, size_t inner_ecc_len, size_t outer_block_len, size_t outer_ecc_len,
@@ -90,29 +61,8 @@ int ffgpu_circ16_repair(const ffgpu_circ16 *code, uint16_t *msg, uint16_t *ecc, 
         FFGPU_REQUIRE(code, "code is NULL");
         ffgpu_circ16 *h = const_cast<ffgpu_circ16 *>(code);
         std::lock_guard<std::mutex> lk(h->mu);
-        Circ16Code &c = *h->code;
-        cudaStream_t st = pick(stream);
-        if (nblocks > 1) {
-            repair_many(h, msg, ecc, nblocks, status ? status : (uint8_t *)h->d_status.get(nblocks), st);
-            return;
-        }
-        for (size_t b = 0; b < nblocks; ++b) {
-            uint16_t *dm = msg + b * c.message_len, *de = ecc + b * c.ecc_len;
-            // keep the message of this block in case a column raises
-            uint16_t *saved = (uint16_t *)h->d_msg.get(c.message_len * 2);
-            FFGPU_CHECK_CUDA(cudaMemcpyAsync(saved, dm, c.message_len * 2, cudaMemcpyDeviceToDevice, st));
-            const size_t fail = repair_device(c, dm, de, st);
-            if (fail != (size_t)-1) {
-                // columns from the raising one on keep their original words
-                const size_t ncols = c.rso_interleave - fail;
-                FFGPU_CHECK_CUDA(cudaMemcpy2DAsync(dm + fail, c.rso_interleave * 2, saved + fail,
-                                                   c.rso_interleave * 2, ncols * 2, c.rso->message_len,
-                                                   cudaMemcpyDeviceToDevice, st));
-            }
-            const uint8_t s = fail == (size_t)-1 ? 0 : FFGPU_STATUS_ASSERT;
-            if (status) FFGPU_CHECK_CUDA(cudaMemcpyAsync(status + b, &s, 1, cudaMemcpyHostToDevice, st));
-            FFGPU_CHECK_CUDA(cudaStreamSynchronize(st));
-        }
+        // every repair stage as one launch over all codewords
+        circ16_repair_many(*h->code, msg, ecc, nblocks, status, pick(stream));
     });
 }
 
@@ -182,42 +132,17 @@ int ffgpu_circ16_repair_host(const ffgpu_circ16 *code, uint16_t *msg, uint16_t *
         Circ16Code &c = *h->code;
         if (!nblocks) return;
         cudaStream_t st = lib_stream();
-        if (nblocks > 1) {
-            const size_t nm = nblocks * c.message_len * 2, ne = nblocks * c.ecc_len * 2;
-            uint16_t *dm = (uint16_t *)h->d_msg.get(nm);
-            uint16_t *de = (uint16_t *)h->d_ecc.get(ne);
-            uint8_t *ds = (uint8_t *)h->d_status.get(nblocks);
-            FFGPU_CHECK_CUDA(cudaMemcpyAsync(dm, msg, nm, cudaMemcpyHostToDevice, st));
-            FFGPU_CHECK_CUDA(cudaMemcpyAsync(de, ecc, ne, cudaMemcpyHostToDevice, st));
-            repair_many(h, dm, de, nblocks, ds, st);
-            FFGPU_CHECK_CUDA(cudaMemcpyAsync(msg, dm, nm, cudaMemcpyDeviceToHost, st));
-            FFGPU_CHECK_CUDA(cudaMemcpyAsync(ecc, de, ne, cudaMemcpyDeviceToHost, st));
-            if (status) FFGPU_CHECK_CUDA(cudaMemcpyAsync(status, ds, nblocks, cudaMemcpyDeviceToHost, st));
-            FFGPU_CHECK_CUDA(cudaStreamSynchronize(st));
-            return;
-        }
-        uint16_t *dm = (uint16_t *)h->d_msg.get(c.message_len * 2 * 2);
-        uint16_t *de = (uint16_t *)h->d_ecc.get(c.ecc_len * 2);
-        for (size_t b = 0; b < nblocks; ++b) {
-            uint16_t *hm = msg + b * c.message_len, *he = ecc + b * c.ecc_len;
-            FFGPU_CHECK_CUDA(cudaMemcpyAsync(dm, hm, c.message_len * 2, cudaMemcpyHostToDevice, st));
-            FFGPU_CHECK_CUDA(cudaMemcpyAsync(de, he, c.ecc_len * 2, cudaMemcpyHostToDevice, st));
-            const size_t fail = repair_device(c, dm, de, st);
-            if (fail == (size_t)-1) {
-                FFGPU_CHECK_CUDA(cudaMemcpyAsync(hm, dm, c.message_len * 2, cudaMemcpyDeviceToHost, st));
-                FFGPU_CHECK_CUDA(cudaMemcpyAsync(he, de, c.ecc_len * 2, cudaMemcpyDeviceToHost, st));
-                FFGPU_CHECK_CUDA(cudaStreamSynchronize(st));
-                if (status) status[b] = 0;
-            } else {
-                std::vector<uint16_t> tmp(c.message_len);
-                FFGPU_CHECK_CUDA(cudaMemcpyAsync(tmp.data(), dm, c.message_len * 2, cudaMemcpyDeviceToHost, st));
-                FFGPU_CHECK_CUDA(cudaStreamSynchronize(st));
-                for (size_t r = 0; r < c.rso->message_len; ++r)
-                    for (size_t col = 0; col < fail; ++col)
-                        hm[r * c.rso_interleave + col] = tmp[r * c.rso_interleave + col];
-                if (status) status[b] = FFGPU_STATUS_ASSERT;
-            }
-        }
+        const size_t nm = nblocks * c.message_len * 2, ne = nblocks * c.ecc_len * 2;
+        uint16_t *dm = (uint16_t *)h->d_msg.get(nm);
+        uint16_t *de = (uint16_t *)h->d_ecc.get(ne);
+        uint8_t *ds = (uint8_t *)h->d_status.get(nblocks);
+        FFGPU_CHECK_CUDA(cudaMemcpyAsync(dm, msg, nm, cudaMemcpyHostToDevice, st));
+        FFGPU_CHECK_CUDA(cudaMemcpyAsync(de, ecc, ne, cudaMemcpyHostToDevice, st));
+        circ16_repair_many(c, dm, de, nblocks, ds, st);
+        FFGPU_CHECK_CUDA(cudaMemcpyAsync(msg, dm, nm, cudaMemcpyDeviceToHost, st));
+        FFGPU_CHECK_CUDA(cudaMemcpyAsync(ecc, de, ne, cudaMemcpyDeviceToHost, st));
+        if (status) FFGPU_CHECK_CUDA(cudaMemcpyAsync(status, ds, nblocks, cudaMemcpyDeviceToHost, st));
+        FFGPU_CHECK_CUDA(cudaStreamSynchronize(st));
     });
 }
 

@@ -28,10 +28,4 @@ struct ffgpu_circ16 {
     std::unique_ptr<ffgpu::Circ16Code> code;
     std::mutex mu;
     ffgpu::DeviceBuffer d_msg, d_ecc, d_status;
-    // fused batch that repairs the codewords of a multi-codeword call in one
-    // launch (created on first use)
-    ffgpu_batch *batch = nullptr;
-    ~ffgpu_circ16() {
-        if (batch) ffgpu_batch_destroy(batch);
-    }
 };

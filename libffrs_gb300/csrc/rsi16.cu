@@ -188,13 +188,15 @@ __global__ void rsi16_encode_warp_kernel(Rsi16Dev c, BlockView v, size_t nblocks
     }
 }
 
-__global__ void rsi16_synd_warp_kernel(Rsi16Dev c, BlockView v, size_t nblocks, uint32_t *synds, uint32_t *gscratch,
-                                       uint32_t ws_words) {
+// syndromes of block b go to synds[(b / out_group) * out_gstride + (b % out_group) * ecc]
+__global__ void rsi16_synd_warp_kernel(Rsi16Dev c, BlockView v, size_t nblocks, uint32_t *synds, size_t out_group,
+                                       size_t out_gstride, uint32_t *gscratch, uint32_t ws_words) {
     WarpCtx w = warp_ctx(gscratch, ws_words);
     for (size_t b = w.warp_global; b < nblocks; b += w.nwarps) {
         w_gather(c, v, b, w.ws, true, w.lane);
         w_pntt(c, w.ws, c.pntt_blocks, w.lane);
-        for (uint32_t k = w.lane; k < c.ecc; k += 32) synds[b * c.ecc + k] = w.ws[k];
+        uint32_t *o = synds + (b / out_group) * out_gstride + (b % out_group) * c.ecc;
+        for (uint32_t k = w.lane; k < c.ecc; k += 32) o[k] = w.ws[k];
         __syncwarp();
     }
 }
@@ -485,10 +487,16 @@ void rsi16_encode(const Rsi16Code &c, const BlockView &v, size_t nblocks, cudaSt
 }
 
 void rsi16_synd(const Rsi16Code &c, const BlockView &v, size_t nblocks, uint32_t *synds, cudaStream_t st) {
+    rsi16_synd_grouped(c, v, nblocks, synds, nblocks ? nblocks : 1, 0, st);
+}
+
+void rsi16_synd_grouped(const Rsi16Code &c, const BlockView &v, size_t nblocks, uint32_t *synds, size_t out_group,
+                        size_t out_gstride, cudaStream_t st) {
     if (!nblocks) return;
     Launch L = plan(rsi16_synd_warp_kernel, nblocks, (uint32_t)c.block_len);
     KernelTimer kt_timer("rsi16_synd_warp_kernel", st);
-    rsi16_synd_warp_kernel<<<L.grid, L.threads, L.smem, st>>>(c.dev, v, nblocks, synds, L.gscratch, L.ws_words);
+    rsi16_synd_warp_kernel<<<L.grid, L.threads, L.smem, st>>>(c.dev, v, nblocks, synds, out_group, out_gstride,
+                                                              L.gscratch, L.ws_words);
     check_launch("rsi16_synd_warp_kernel");
 }
 

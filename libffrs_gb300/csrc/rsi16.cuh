@@ -87,6 +87,10 @@ void rsi16_encode(const Rsi16Code &c, const BlockView &v, size_t nblocks, cudaSt
 bool rsi16_encode_stream_safe(const Rsi16Code &c);
 // Syndromes (ecc uint32 per block) of nblocks blocks of the view.
 void rsi16_synd(const Rsi16Code &c, const BlockView &v, size_t nblocks, uint32_t *synds, cudaStream_t st);
+// The same with the syndromes of block b at
+// synds + (b / out_group) * out_gstride + (b % out_group) * ecc_len.
+void rsi16_synd_grouped(const Rsi16Code &c, const BlockView &v, size_t nblocks, uint32_t *synds, size_t out_group,
+                        size_t out_gstride, cudaStream_t st);
 // Unknown-location repair in place; status per block (RepairStatus or 0xFF).
 // A non-NULL active array restricts the repair to blocks with active[b] != 0.
 void rsi16_repair(const Rsi16Code &c, const BlockView &v, size_t nblocks, uint8_t *status, cudaStream_t st,
