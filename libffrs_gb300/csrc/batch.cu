@@ -10,6 +10,13 @@
 // Each item runs the same per-block device code as the standalone kernels
 // (rs256_device.cuh, rsi16_device.cuh), so the bytes are identical to the
 // plain per-request path.
+//
+// CIRC16 repairs are not items: one codeword's CircRepair is a chain of
+// stages that each spread over hundreds of rows, which one CTA would walk
+// alone.  Their codewords are gathered (one copy kernel) into contiguous
+// arrays per code, repaired by circ16_repair_many (every stage one launch over
+// all of them) on a second stream beside the persistent kernel, and
+// scattered back.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -17,7 +24,7 @@
 #include <string>
 #include <vector>
 
-#include "circ16_device.cuh"
+#include "circ16.cuh"
 #include "common.cuh"
 #include "handles.h"
 #include "rs256_device.cuh"
@@ -48,10 +55,6 @@ struct BatchCode {
     Rsi16Dev rso;
     uint32_t c_message_len, c_ecc_len, c_rso_interleave, c_rso_ieccl, c_rsi_ieccl, c_inner_rows, c_outer_rows;
     uint32_t c_rsi_total;
-    CircDims cd;
-    // CircRepair workspace (word offsets) and the saved message after it
-    uint32_t o_rso, o_rsi, o_syn, o_blk, o_bsyn, o_zpos, o_zoff, o_zcnt, o_zact, o_vec, o_flag, o_locs, o_lcnt, o_poff,
-        o_pcnt, o_kn, o_un, o_st, o_save;
 };
 
 struct BatchItem {
@@ -172,105 +175,29 @@ __device__ void circ16_enc_item(const BatchCode &c, const BatchItem &it, uint32_
     for (uint32_t b = warp; b < c.c_outer_rows; b += kBatchWarps) rsi16_encode_block(c.rsi, vio, b, ws, lane);
 }
 
-// One CIRC16 codeword repaired inside the CTA: CircRepair (pycirc16.hpp:135-335)
-// stage by stage, each stage spread over the four warps with a barrier after
-// it, exactly as the per-request pipeline of stage kernels.  A column whose
-// outer repair raises (status 0xFF) ends the reference's column loop there:
-// the columns from it on get their saved words back and the ecc is not
-// written; the block's status is 0 or 0xFF.
-__device__ void circ16_dec_item(const BatchCode &c, const BatchItem &it, uint32_t *ws, uint32_t *W,
-                                uint32_t *s_first) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, tid = threadIdx.x;
-    const Rsi16Dev &ri = c.rsi, &ro = c.rso;
-    const CircDims d = c.cd;
-    uint16_t *msg = static_cast<uint16_t *>(it.msg), *ecc = static_cast<uint16_t *>(it.par);
-    uint32_t *rso_ecc = W + c.o_rso, *rsi_ecc = W + c.o_rsi, *synd = W + c.o_syn, *blocks = W + c.o_blk,
-             *bsyn = W + c.o_bsyn, *zpos = W + c.o_zpos, *zoff = W + c.o_zoff, *zcnt = W + c.o_zcnt,
-             *vecs = W + c.o_vec, *locs = W + c.o_locs, *lcnt = W + c.o_lcnt, *poff = W + c.o_poff,
-             *pcnt = W + c.o_pcnt;
-    uint8_t *zact = reinterpret_cast<uint8_t *>(W + c.o_zact), *flag = reinterpret_cast<uint8_t *>(W + c.o_flag),
-            *kn = reinterpret_cast<uint8_t *>(W + c.o_kn), *un = reinterpret_cast<uint8_t *>(W + c.o_un),
-            *cst = reinterpret_cast<uint8_t *>(W + c.o_st);
-    uint16_t *save = reinterpret_cast<uint16_t *>(W + c.o_save);
-    const uint32_t I = c.c_rso_interleave, n_oz = d.interleave * ro.ecc, n_iz = d.interleave * ro.block_len;
-    // load_ecc (pycirc16.hpp:159-163), and a copy of the message
-    for (uint32_t i = tid; i < c.c_message_len; i += kBatchThreads) save[i] = msg[i];
-    for (uint32_t i = tid; i < c.c_rso_ieccl; i += kBatchThreads) rso_ecc[i] = ecc[i];
-    for (uint32_t i = tid; i < c.c_rsi_total; i += kBatchThreads) rsi_ecc[i] = ecc[c.c_rso_ieccl + i];
-    __syncthreads();
-    // compute_rsi_synd (pycirc16.hpp:165-181)
-    const BlockView vmsg{msg, 0, ri.message_len, 1, rsi_ecc, 0, ri.ecc, 1, c.c_inner_rows, true, false};
-    for (uint32_t b = warp; b < c.c_inner_rows; b += kBatchWarps)
-        rsi16_synd_block(ri, vmsg, b, ws, synd + (size_t)b * ri.ecc, lane);
-    const BlockView vrso{rso_ecc, 0, ri.message_len, 1, rsi_ecc + c.c_rsi_ieccl, 0, ri.ecc, 1, c.c_outer_rows,
-                         false, false};
-    for (uint32_t b = warp; b < c.c_outer_rows; b += kBatchWarps)
-        rsi16_synd_block(ri, vrso, b, ws, synd + c.c_rsi_ieccl + (size_t)b * ri.ecc, lane);
-    __syncthreads();
-    // repair_outer_zeros
-    for (uint32_t k = warp; k < n_oz; k += kBatchWarps)
-        outer_zeros_prepare_item(d, rso_ecc, rsi_ecc, synd, blocks, zpos, zoff, zcnt, zact, k, lane);
-    __syncthreads();
-    const BlockView vblk{blocks, 0, ri.block_len, 1, blocks + ri.message_len, 0, ri.block_len, 1, n_oz, false, false};
-    for (uint32_t b = warp; b < n_oz; b += kBatchWarps)
-        if (zact[b]) rsi16_repair_known_block(ri, vblk, b, zpos + zoff[b], zcnt[b], ws, nullptr, lane);
-    __syncthreads();
-    for (uint32_t b = warp; b < n_oz; b += kBatchWarps) rsi16_synd_block(ri, vblk, b, ws, bsyn + (size_t)b * ri.ecc, lane);
-    __syncthreads();
-    for (uint32_t k = warp; k < n_oz; k += kBatchWarps)
-        outer_zeros_commit_item(d, rso_ecc, rsi_ecc, synd, blocks, bsyn, zpos, zcnt, zact, k, lane);
-    __syncthreads();
-    // repair_inner_zeros
-    for (uint32_t k = warp; k < n_iz; k += kBatchWarps) inner_zeros_prepare_item(d, rsi_ecc, synd, vecs, flag, k, lane);
-    __syncthreads();
-    for (uint32_t k = warp; k < n_iz; k += kBatchWarps) w_mix(ri, vecs + (size_t)k * ri.ecc, lane);
-    __syncthreads();
-    for (uint32_t k = warp; k < n_iz; k += kBatchWarps) inner_zeros_commit_item(d, rsi_ecc, synd, vecs, flag, k, lane);
-    __syncthreads();
-    // find_error_locations, then the outer repairs
-    for (uint32_t k = warp; k < d.interleave; k += kBatchWarps) find_locations_item(d, synd, locs, lcnt, k, lane);
-    if (tid == 0) *s_first = 0xffffffffu;
-    __syncthreads();
-    for (uint32_t col = tid; col < I; col += kBatchThreads) {
-        outer_modes_col(d, lcnt, poff, pcnt, kn, un, col, 0);
-        cst[col] = 0;
-    }
-    __syncthreads();
-    const BlockView vcol = interleaved_view(msg, true, ro.message_len, rso_ecc, false, ro.ecc, I);
-    for (uint32_t col = warp; col < I; col += kBatchWarps) {
-        if (kn[col])
-            rsi16_repair_known_block(ro, vcol, col, locs + poff[col], pcnt[col], ws, cst, lane);
-        else if (un[col] && !rsi16_repair_bm_block(ro, vcol, col, ws, cst, lane))
-            rsi16_repair_block(ro, vcol, col, ws, cst, lane);
-    }
-    __syncthreads();
-    for (uint32_t col = tid; col < I; col += kBatchThreads)
-        if (cst[col] == FFGPU_STATUS_ASSERT) atomicMin(s_first, col);
-    // recompute_inner_ecc (pycirc16.hpp:320-324)
-    const BlockView vre{msg, 0, ri.message_len, 1, rsi_ecc, 0, ri.ecc, 1, c.c_inner_rows, true, false};
-    for (uint32_t b = warp; b < c.c_inner_rows; b += kBatchWarps) rsi16_encode_block(ri, vre, b, ws, lane);
-    const BlockView vreo{rso_ecc, 0, ri.message_len, 1, rsi_ecc + c.c_rsi_ieccl, 0, ri.ecc, 1, c.c_outer_rows,
-                         false, false};
-    for (uint32_t b = warp; b < c.c_outer_rows; b += kBatchWarps) rsi16_encode_block(ri, vreo, b, ws, lane);
-    __syncthreads();
-    const uint32_t first = *s_first;
-    if (first == 0xffffffffu) {
-        // dump_ecc (pycirc16.hpp:326-330)
-        for (uint32_t i = tid; i < c.c_rso_ieccl; i += kBatchThreads) ecc[i] = (uint16_t)rso_ecc[i];
-        for (uint32_t i = tid; i < c.c_rsi_total; i += kBatchThreads) ecc[c.c_rso_ieccl + i] = (uint16_t)rsi_ecc[i];
+// Byte ranges copied one CTA per range (ranges of at most kSegBytes): the
+// gather of CIRC16 codewords into the repair arrays and their scatter back.
+struct CopySeg {
+    const uint8_t *src;
+    uint8_t *dst;
+    uint64_t bytes;
+};
+constexpr size_t kSegBytes = 64 * 1024;
+
+__global__ void __launch_bounds__(256) seg_copy_kernel(const CopySeg *segs) {
+    const CopySeg sg = segs[blockIdx.x];
+    if ((((uintptr_t)sg.src | (uintptr_t)sg.dst | sg.bytes) & 15) == 0) {
+        const uint4 *s4 = reinterpret_cast<const uint4 *>(sg.src);
+        uint4 *d4 = reinterpret_cast<uint4 *>(sg.dst);
+        for (size_t i = threadIdx.x; i < sg.bytes / 16; i += blockDim.x) d4[i] = s4[i];
     } else {
-        const uint32_t ncol = I - first;
-        for (uint32_t i = tid; i < ro.message_len * ncol; i += kBatchThreads) {
-            const uint32_t r = i / ncol, col = first + i % ncol;
-            msg[(size_t)r * I + col] = save[(size_t)r * I + col];
-        }
+        for (size_t i = threadIdx.x; i < sg.bytes; i += blockDim.x) sg.dst[i] = sg.src[i];
     }
-    if (tid == 0 && it.status) *it.status = first == 0xffffffffu ? 0 : FFGPU_STATUS_ASSERT;
 }
 
 __global__ void __launch_bounds__(kBatchThreads) batch_kernel(BatchArgs a) {
     extern __shared__ __align__(16) uint32_t sm[];
-    __shared__ uint32_t s_idx, s_first;
+    __shared__ uint32_t s_idx;
     uint8_t *rs_scratch = a.rs_scratch + (size_t)blockIdx.x * kBatchThreads * kDecodeScratchBytes;
     uint32_t *ctmp = a.circ_tmp + (size_t)blockIdx.x * a.circ_tmp_words;
     uint32_t *ws = sm + (size_t)(threadIdx.x >> 5) * a.ws_words;
@@ -297,9 +224,6 @@ __global__ void __launch_bounds__(kBatchThreads) batch_kernel(BatchArgs a) {
                 break;
             case BK_CIRC16_ENC:
                 circ16_enc_item(c, it, ws, ctmp);
-                break;
-            case BK_CIRC16_DEC:
-                circ16_dec_item(c, it, ws, ctmp, &s_first);
                 break;
             default:
                 break;
@@ -332,11 +256,28 @@ struct ffgpu_batch {
     unsigned grid = 0;
     int tile_rs = 512, tile_rsi = 8, ctas_per_sm = 0;
     bool planned = false;
+    // CIRC16 repairs: per code, its codewords' offsets in the gathered arrays
+    struct CircGroup {
+        ffgpu_circ16 *handle;
+        size_t ncw, cw0, ws_off;
+    };
+    std::vector<CircGroup> circ;
+    std::vector<size_t> circ_moff, circ_eoff;  // word offsets in d_cmsg / d_cecc
+    size_t n_gather = 0, n_scatter = 0;
+    DeviceBuffer d_cmsg, d_cecc, d_cst, d_cws, d_segs;
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    int graph_kernels = 1;
     std::mutex mu;
 
-    ~ffgpu_batch() { drop_graph(); }
+    ~ffgpu_batch() {
+        drop_graph();
+        if (side) cudaStreamDestroy(side);
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_join) cudaEventDestroy(ev_join);
+    }
     void drop_graph() {
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
@@ -370,13 +311,93 @@ double item_cost(const ffgpu_batch &B, const BatchItem &it) {
         case BK_RS256_DEC: return (double)it.nblocks * (it.msg_len + c.ecc) * (4 + c.ecc);
         case BK_RSI16_ENC: return (double)it.nblocks * c.rsi.block_len * 8;
         case BK_RSI16_DEC: return (double)it.nblocks * c.rsi.block_len * (40 + c.rsi.ecc);
-        case BK_CIRC16_DEC:
-            return ((double)c.c_rso_interleave * c.rso.block_len +
-                    (double)(c.c_inner_rows + c.c_outer_rows) * c.rsi.block_len) * 40;
         default:
             return ((double)c.c_rso_interleave * c.rso.block_len +
                     (double)(c.c_inner_rows + c.c_outer_rows) * c.rsi.block_len) * 8;
     }
+}
+
+void add_segs(std::vector<CopySeg> &v, const void *src, void *dst, size_t bytes) {
+    for (size_t o = 0; o < bytes; o += kSegBytes)
+        v.push_back({static_cast<const uint8_t *>(src) + o, static_cast<uint8_t *>(dst) + o,
+                     (uint64_t)std::min(kSegBytes, bytes - o)});
+}
+
+// Gathered arrays, workspaces and copy ranges of the CIRC16 repairs.
+void plan_circ(ffgpu_batch &B) {
+    B.n_gather = B.n_scatter = 0;
+    if (B.circ.empty()) return;
+    size_t cw = 0, ws = 0, mwords = 0, ewords = 0;
+    for (auto &g : B.circ) {
+        const Circ16Code &c = *g.handle->code;
+        g.cw0 = cw;
+        g.ws_off = ws;
+        cw += g.ncw;
+        ws += (circ16_repair_many_ws_bytes(c, g.ncw) + 255) & ~(size_t)255;
+        mwords += g.ncw * c.message_len;
+        ewords += g.ncw * c.ecc_len;
+    }
+    uint16_t *cm = static_cast<uint16_t *>(B.d_cmsg.get(mwords * 2));
+    uint16_t *ce = static_cast<uint16_t *>(B.d_cecc.get(ewords * 2));
+    uint8_t *cs = static_cast<uint8_t *>(B.d_cst.get(cw));
+    B.d_cws.get(ws);
+    // a code's codewords sit in request order: message words of all its
+    // codewords, then their ecc words
+    std::vector<CopySeg> gat, sca;
+    std::vector<size_t> next(B.circ.size(), 0);
+    std::vector<size_t> moff(B.circ.size()), eoff(B.circ.size());
+    size_t mo = 0, eo = 0;
+    for (size_t g = 0; g < B.circ.size(); ++g) {
+        const Circ16Code &c = *B.circ[g].handle->code;
+        moff[g] = mo;
+        eoff[g] = eo;
+        mo += B.circ[g].ncw * c.message_len;
+        eo += B.circ[g].ncw * c.ecc_len;
+    }
+    for (const auto &r : B.reqs) {
+        if (r.kind != BK_CIRC16_DEC) continue;
+        size_t g = 0;
+        while (B.circ[g].handle != r.handle) ++g;
+        const Circ16Code &c = *B.circ[g].handle->code;
+        uint16_t *dm = cm + moff[g] + next[g] * c.message_len;
+        uint16_t *de = ce + eoff[g] + next[g] * c.ecc_len;
+        uint8_t *ds = cs + B.circ[g].cw0 + next[g];
+        next[g] += r.nblocks;
+        add_segs(gat, r.a, dm, r.nblocks * c.message_len * 2);
+        add_segs(gat, r.b, de, r.nblocks * c.ecc_len * 2);
+        add_segs(sca, dm, r.a, r.nblocks * c.message_len * 2);
+        add_segs(sca, de, r.b, r.nblocks * c.ecc_len * 2);
+        if (r.status) add_segs(sca, ds, r.status, r.nblocks);
+    }
+    B.n_gather = gat.size();
+    B.n_scatter = sca.size();
+    gat.insert(gat.end(), sca.begin(), sca.end());
+    B.d_segs.get(gat.size() * sizeof(CopySeg));
+    FFGPU_CHECK_CUDA(cudaMemcpy(B.d_segs.ptr, gat.data(), gat.size() * sizeof(CopySeg), cudaMemcpyHostToDevice));
+    // per code: gathered message and ecc base pointers, kept in the group
+    B.circ_moff = moff;
+    B.circ_eoff = eoff;
+    if (!B.side) {
+        FFGPU_CHECK_CUDA(cudaStreamCreateWithFlags(&B.side, cudaStreamNonBlocking));
+        FFGPU_CHECK_CUDA(cudaEventCreateWithFlags(&B.ev_fork, cudaEventDisableTiming));
+        FFGPU_CHECK_CUDA(cudaEventCreateWithFlags(&B.ev_join, cudaEventDisableTiming));
+    }
+}
+
+// The CIRC16 chain on the side stream: gather, repair per code, scatter.
+void launch_circ(ffgpu_batch &B) {
+    const CopySeg *segs = static_cast<const CopySeg *>(B.d_segs.ptr);
+    seg_copy_kernel<<<(unsigned)B.n_gather, 256, 0, B.side>>>(segs);
+    check_launch("seg_copy_kernel");
+    for (size_t g = 0; g < B.circ.size(); ++g) {
+        const auto &cg = B.circ[g];
+        circ16_repair_many(*cg.handle->code, static_cast<uint16_t *>(B.d_cmsg.ptr) + B.circ_moff[g],
+                           static_cast<uint16_t *>(B.d_cecc.ptr) + B.circ_eoff[g], cg.ncw,
+                           static_cast<uint8_t *>(B.d_cst.ptr) + cg.cw0, B.side,
+                           static_cast<char *>(B.d_cws.ptr) + cg.ws_off);
+    }
+    seg_copy_kernel<<<(unsigned)B.n_scatter, 256, 0, B.side>>>(segs + B.n_gather);
+    check_launch("seg_copy_kernel");
 }
 
 void build_plan(ffgpu_batch &B, int tile_rs, int tile_rsi, int ctas_per_sm) {
@@ -384,6 +405,7 @@ void build_plan(ffgpu_batch &B, int tile_rs, int tile_rsi, int ctas_per_sm) {
     B.codes.clear();
     B.code_keys.clear();
     B.items.clear();
+    B.circ.clear();
     size_t smem = 0;
     uint32_t ws_words = 0;
     size_t circ_words = 0;
@@ -430,6 +452,12 @@ void build_plan(ffgpu_batch &B, int tile_rs, int tile_rsi, int ctas_per_sm) {
                 B.items.push_back(it);
             }
             ws_words = std::max(ws_words, r.kind == BK_RSI16_DEC ? c.dev.temp_len + 1 : (uint32_t)c.block_len);
+        } else if (r.kind == BK_CIRC16_DEC) {
+            ffgpu_circ16 *h = const_cast<ffgpu_circ16 *>(static_cast<const ffgpu_circ16 *>(r.handle));
+            size_t g = 0;
+            while (g < B.circ.size() && B.circ[g].handle != h) ++g;
+            if (g == B.circ.size()) B.circ.push_back({h, 0, 0, 0});
+            B.circ[g].ncw += r.nblocks;
         } else {
             const Circ16Code &c = *static_cast<const ffgpu_circ16 *>(r.handle)->code;
             bc.rsi = c.rsi->dev;
@@ -442,27 +470,6 @@ void build_plan(ffgpu_batch &B, int tile_rs, int tile_rsi, int ctas_per_sm) {
             bc.c_inner_rows = (uint32_t)c.inner_rows;
             bc.c_outer_rows = (uint32_t)c.outer_rows;
             bc.c_rsi_total = (uint32_t)c.rsi_total;
-            bc.cd = circ16_dims(c);
-            const CircLayout lay = circ16_layout(c);
-            bc.o_rso = (uint32_t)lay.o_rso;
-            bc.o_rsi = (uint32_t)lay.o_rsi;
-            bc.o_syn = (uint32_t)lay.o_syn;
-            bc.o_blk = (uint32_t)lay.o_blk;
-            bc.o_bsyn = (uint32_t)lay.o_bsyn;
-            bc.o_zpos = (uint32_t)lay.o_zpos;
-            bc.o_zoff = (uint32_t)lay.o_zoff;
-            bc.o_zcnt = (uint32_t)lay.o_zcnt;
-            bc.o_zact = (uint32_t)lay.o_zact;
-            bc.o_vec = (uint32_t)lay.o_vec;
-            bc.o_flag = (uint32_t)lay.o_flag;
-            bc.o_locs = (uint32_t)lay.o_locs;
-            bc.o_lcnt = (uint32_t)lay.o_lcnt;
-            bc.o_poff = (uint32_t)lay.o_poff;
-            bc.o_pcnt = (uint32_t)lay.o_pcnt;
-            bc.o_kn = (uint32_t)lay.o_kn;
-            bc.o_un = (uint32_t)lay.o_un;
-            bc.o_st = (uint32_t)lay.o_st;
-            bc.o_save = (uint32_t)lay.words;
             const uint32_t ci = code_index(B, r.handle, bc);
             for (size_t b = 0; b < r.nblocks; ++b) {
                 BatchItem it{};
@@ -471,18 +478,14 @@ void build_plan(ffgpu_batch &B, int tile_rs, int tile_rsi, int ctas_per_sm) {
                 it.nblocks = 1;
                 it.msg = static_cast<uint16_t *>(r.a) + b * c.message_len;
                 it.par = static_cast<uint16_t *>(r.b) + b * c.ecc_len;
-                it.status = r.status ? r.status + b : nullptr;
+                it.status = nullptr;
                 B.items.push_back(it);
             }
-            if (r.kind == BK_CIRC16_DEC) {
-                ws_words = std::max(ws_words, std::max(c.rsi->dev.temp_len, c.rso->dev.temp_len) + 1);
-                circ_words = std::max(circ_words, lay.words + (c.message_len + 1) / 2);
-            } else {
-                ws_words = std::max(ws_words, (uint32_t)std::max(c.rsi->block_len, c.rso->block_len));
-                circ_words = std::max(circ_words, c.rso_ieccl);
-            }
+            ws_words = std::max(ws_words, (uint32_t)std::max(c.rsi->block_len, c.rso->block_len));
+            circ_words = std::max(circ_words, c.rso_ieccl);
         }
     }
+    plan_circ(B);
     // longest first
     std::vector<std::pair<double, size_t>> order(B.items.size());
     for (size_t i = 0; i < B.items.size(); ++i) order[i] = {-item_cost(B, B.items[i]), i};
@@ -520,7 +523,22 @@ void build_plan(ffgpu_batch &B, int tile_rs, int tile_rsi, int ctas_per_sm) {
     B.planned = true;
 }
 
-void launch_plan(ffgpu_batch &B, cudaStream_t st, bool timed) {
+void launch_items(ffgpu_batch &B, cudaStream_t st, bool timed);
+
+// with_circ: also the CIRC16 repairs, on the side stream joined back into st
+void launch_plan(ffgpu_batch &B, cudaStream_t st, bool timed, bool with_circ = true) {
+    const bool circ = with_circ && !B.circ.empty();
+    if (circ) {
+        FFGPU_CHECK_CUDA(cudaEventRecord(B.ev_fork, st));
+        FFGPU_CHECK_CUDA(cudaStreamWaitEvent(B.side, B.ev_fork, 0));
+        launch_circ(B);
+        FFGPU_CHECK_CUDA(cudaEventRecord(B.ev_join, B.side));
+    }
+    if (!B.items.empty()) launch_items(B, st, timed);
+    if (circ) FFGPU_CHECK_CUDA(cudaStreamWaitEvent(st, B.ev_join, 0));
+}
+
+void launch_items(ffgpu_batch &B, cudaStream_t st, bool timed) {
     FFGPU_CHECK_CUDA(cudaMemsetAsync(B.d_counter.ptr, 0, 4, st));
     BatchArgs a;
     a.items = static_cast<const BatchItem *>(B.d_items.ptr);
@@ -601,7 +619,7 @@ void autotune(ffgpu_batch &B, cudaStream_t st) {
                 for (int rep = 0; rep < 2; ++rep) {  // the first run warms up
                     copy_regions(B, regions, false, st);
                     FFGPU_CHECK_CUDA(cudaEventRecord(e0, st));
-                    launch_plan(B, st, false);
+                    launch_plan(B, st, false, false);
                     FFGPU_CHECK_CUDA(cudaEventRecord(e1, st));
                     FFGPU_CHECK_CUDA(cudaEventSynchronize(e1));
                     FFGPU_CHECK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
@@ -725,6 +743,15 @@ int ffgpu_batch_capture(ffgpu_batch *b, void *stream) {
         }
         FFGPU_CHECK_CUDA(cudaStreamEndCapture(cap, &b->graph));
         if (own) cudaStreamDestroy(cap);
+        size_t nn = 0;
+        FFGPU_CHECK_CUDA(cudaGraphGetNodes(b->graph, nullptr, &nn));
+        std::vector<cudaGraphNode_t> nodes(nn);
+        if (nn) FFGPU_CHECK_CUDA(cudaGraphGetNodes(b->graph, nodes.data(), &nn));
+        b->graph_kernels = 0;
+        for (auto n : nodes) {
+            cudaGraphNodeType t;
+            if (cudaGraphNodeGetType(n, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++b->graph_kernels;
+        }
         FFGPU_CHECK_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
     });
 }
@@ -737,7 +764,7 @@ int ffgpu_batch_launch(ffgpu_batch *b, void *stream) {
         if (b->exec) {
             KernelTimer kt_timer("batch_kernel", st);
             FFGPU_CHECK_CUDA(cudaGraphLaunch(b->exec, st));
-            launched();
+            launched(b->graph_kernels);
             return;
         }
         if (!b->planned) build_plan(*b, b->tile_rs, b->tile_rsi, b->ctas_per_sm);

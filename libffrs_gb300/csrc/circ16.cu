@@ -358,10 +358,55 @@ void circ16_repair_one(Circ16Code &c, uint16_t *msg, uint16_t *ecc, cudaStream_t
     if (col_status) FFGPU_CHECK_CUDA(cudaMemcpyAsync(col_status, cst, c.rso_interleave, cudaMemcpyDeviceToHost, st));
 }
 
+// Codeword-major workspace of circ16_repair_many: byte offsets of every
+// stage array for ncw codewords.
+struct ManyLayout {
+    size_t o_rso, o_rsi, o_syn, o_blk, o_bsyn, o_zpos, o_zoff, o_zcnt, o_zact, o_vec, o_flag, o_locs, o_lcnt, o_poff,
+        o_pcnt, o_kn, o_un, o_st, o_save, bytes;
+};
+
+static ManyLayout many_layout(const Circ16Code &c, size_t ncw) {
+    const Rsi16Code &ri = *c.rsi, &ro = *c.rso;
+    const size_t rso_n = c.rso_ieccl, rsi_n = c.rsi_total, n_oz = c.interleave * ro.ecc,
+                 n_iz = c.interleave * ro.block_len;
+    ManyLayout L;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = off;
+        off += (bytes + 255) & ~(size_t)255;
+        return o;
+    };
+    L.o_rso = take(ncw * rso_n * 4);
+    L.o_rsi = take(ncw * rsi_n * 4);
+    L.o_syn = take(ncw * rsi_n * 4);
+    L.o_blk = take(ncw * n_oz * ri.block_len * 4);
+    L.o_bsyn = take(ncw * n_oz * ri.ecc * 4);
+    L.o_zpos = take(ncw * n_oz * ri.ecc * 4);
+    L.o_zoff = take(ncw * n_oz * 4);
+    L.o_zcnt = take(ncw * n_oz * 4);
+    L.o_zact = take(ncw * n_oz);
+    L.o_vec = take(ncw * n_iz * ri.ecc * 4);
+    L.o_flag = take(ncw * n_iz);
+    L.o_locs = take(ncw * c.interleave * ro.block_len * 4);
+    L.o_lcnt = take(ncw * c.interleave * 4);
+    L.o_poff = take(ncw * c.rso_interleave * 4);
+    L.o_pcnt = take(ncw * c.rso_interleave * 4);
+    L.o_kn = take(ncw * c.rso_interleave);
+    L.o_un = take(ncw * c.rso_interleave);
+    L.o_st = take(ncw * c.rso_interleave);
+    L.o_save = take(ncw * c.message_len * 2);
+    L.bytes = off;
+    return L;
+}
+
+size_t circ16_repair_many_ws_bytes(const Circ16Code &c, size_t ncw) { return many_layout(c, ncw).bytes; }
+
 // ncw codewords in place (device pointers): the stages of circ16_repair_one,
 // each one launch over every codeword.  status[cw] is 0 or
-// FFGPU_STATUS_ASSERT as in ffgpu_circ16_repair.
-void circ16_repair_many(Circ16Code &c, uint16_t *msg, uint16_t *ecc, size_t ncw, uint8_t *status, cudaStream_t st) {
+// FFGPU_STATUS_ASSERT as in ffgpu_circ16_repair.  ws: a workspace of
+// circ16_repair_many_ws_bytes(c, ncw) bytes, or NULL for the code's own.
+void circ16_repair_many(Circ16Code &c, uint16_t *msg, uint16_t *ecc, size_t ncw, uint8_t *status, cudaStream_t st,
+                        void *ws) {
     if (!ncw) return;
     const Rsi16Code &ri = *c.rsi, &ro = *c.rso;
     const CircDims d = circ16_dims(c);
@@ -370,23 +415,12 @@ void circ16_repair_many(Circ16Code &c, uint16_t *msg, uint16_t *ecc, size_t ncw,
     m.rsi_n = c.rsi_total;
     m.n_oz = c.interleave * ro.ecc;
     m.n_iz = c.interleave * ro.block_len;
-    // codeword-major workspace
-    size_t off = 0;
-    auto take = [&](size_t bytes) {
-        const size_t o = off;
-        off += (bytes + 255) & ~(size_t)255;
-        return o;
-    };
-    const size_t o_rso = take(ncw * m.rso_n * 4), o_rsi = take(ncw * m.rsi_n * 4), o_syn = take(ncw * m.rsi_n * 4),
-                 o_blk = take(ncw * m.n_oz * ri.block_len * 4), o_bsyn = take(ncw * m.n_oz * ri.ecc * 4),
-                 o_zpos = take(ncw * m.n_oz * ri.ecc * 4), o_zoff = take(ncw * m.n_oz * 4),
-                 o_zcnt = take(ncw * m.n_oz * 4), o_zact = take(ncw * m.n_oz), o_vec = take(ncw * m.n_iz * ri.ecc * 4),
-                 o_flag = take(ncw * m.n_iz), o_locs = take(ncw * c.interleave * ro.block_len * 4),
-                 o_lcnt = take(ncw * c.interleave * 4), o_poff = take(ncw * c.rso_interleave * 4),
-                 o_pcnt = take(ncw * c.rso_interleave * 4), o_kn = take(ncw * c.rso_interleave),
-                 o_un = take(ncw * c.rso_interleave), o_st = take(ncw * c.rso_interleave),
-                 o_save = take(ncw * c.message_len * 2);
-    char *W = (char *)c.rep_ws.get(off);
+    const ManyLayout L = many_layout(c, ncw);
+    char *W = (char *)(ws ? ws : c.rep_ws.get(L.bytes));
+    const size_t o_rso = L.o_rso, o_rsi = L.o_rsi, o_syn = L.o_syn, o_blk = L.o_blk, o_bsyn = L.o_bsyn,
+                 o_zpos = L.o_zpos, o_zoff = L.o_zoff, o_zcnt = L.o_zcnt, o_zact = L.o_zact, o_vec = L.o_vec,
+                 o_flag = L.o_flag, o_locs = L.o_locs, o_lcnt = L.o_lcnt, o_poff = L.o_poff, o_pcnt = L.o_pcnt,
+                 o_kn = L.o_kn, o_un = L.o_un, o_st = L.o_st, o_save = L.o_save;
     uint32_t *rso_ecc = (uint32_t *)(W + o_rso), *rsi_ecc = (uint32_t *)(W + o_rsi), *synd = (uint32_t *)(W + o_syn);
     uint32_t *blocks = (uint32_t *)(W + o_blk), *bsyn = (uint32_t *)(W + o_bsyn), *zpos = (uint32_t *)(W + o_zpos);
     uint32_t *zoff = (uint32_t *)(W + o_zoff), *zcnt = (uint32_t *)(W + o_zcnt);

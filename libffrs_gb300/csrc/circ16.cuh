@@ -39,6 +39,8 @@ void circ16_repair_one(Circ16Code &c, uint16_t *msg, uint16_t *ecc, cudaStream_t
 void circ16_dump_ecc(Circ16Code &c, uint16_t *ecc, cudaStream_t st);
 // ncw codewords in place, every repair stage as one launch over all of them;
 // status[cw] 0 or FFGPU_STATUS_ASSERT (NULL: not written).
-void circ16_repair_many(Circ16Code &c, uint16_t *msg, uint16_t *ecc, size_t ncw, uint8_t *status, cudaStream_t st);
+void circ16_repair_many(Circ16Code &c, uint16_t *msg, uint16_t *ecc, size_t ncw, uint8_t *status, cudaStream_t st,
+                        void *ws = nullptr);
+size_t circ16_repair_many_ws_bytes(const Circ16Code &c, size_t ncw);
 
 }  // namespace ffgpu

@@ -145,7 +145,7 @@ int ffgpu_rsi16_encode_host(const ffgpu_rsi16 *code, const uint16_t *msg, size_t
         const size_t nm = nblocks * interleave * c.message_len, np = nblocks * interleave * c.ecc;
         uint16_t *dm = (uint16_t *)h->d_msg.get(nm * 2);
         uint16_t *dp = (uint16_t *)h->d_par.get(np * 2);
-        if (interleave == 1 && rsi16_encode_stream_safe(c)) {
+        if (interleave == 1) {
             // chunks of blocks on the pipeline streams: copies in, encodes and
             // copies out of different chunks overlap
             const size_t chunk = host_chunk_blocks(nblocks, 8192, 4);
@@ -203,12 +203,10 @@ int ffgpu_rsi16_repair_host(const ffgpu_rsi16 *code, uint16_t *msg, uint16_t *pa
         uint16_t *dm = (uint16_t *)h->d_msg.get(nm * 2);
         uint16_t *dp = (uint16_t *)h->d_par.get(np * 2);
         uint8_t *ds = (uint8_t *)h->d_status.get(ncol);
-        if (interleave == 1 && error_count < 0 && (size_t)(c.dev.temp_len + 1) * 4 * 4 <= 64 * 1024) {
+        if (interleave == 1 && error_count < 0) {
             // contiguous blocks, unknown locations: every block is written back
             // whatever its status, so chunks of blocks pipeline their copies and
-            // repairs over the pipeline streams (only when the repair
-            // workspace lives in shared memory: the global fallback workspace
-            // is one per thread and cannot serve concurrent streams)
+            // repairs over the pipeline streams
             const size_t chunk = host_chunk_blocks(nblocks, 32768, 8);
             // outputs in pageable memory come back through page-locked staging
             const bool chunked = chunk < nblocks;

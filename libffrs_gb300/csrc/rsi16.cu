@@ -411,19 +411,23 @@ __global__ void rsi16_mix_kernel(Rsi16Dev c, uint32_t *vecs, size_t nvec) {
 
 namespace {
 
+// A launch shape.  Workspaces that do not fit in shared memory come from a
+// stream-ordered allocation, freed on the same stream after the launch, so
+// that launches on concurrent streams (or inside a captured graph) each get
+// their own.
 struct Launch {
-    unsigned grid, threads;
-    size_t smem;
-    uint32_t *gscratch;
-    uint32_t ws_words;
+    unsigned grid = 0, threads = 0;
+    size_t smem = 0;
+    uint32_t *gscratch = nullptr;
+    uint32_t ws_words = 0;
+    cudaStream_t st;
+    explicit Launch(cudaStream_t s) : st(s) {}
+    ~Launch() {
+        if (gscratch) cudaFreeAsync(gscratch, st);
+    }
+    Launch(const Launch &) = delete;
+    Launch &operator=(const Launch &) = delete;
 };
-
-// Per-code global scratch for workspaces that do not fit in shared memory.
-struct ScratchPool {
-    DeviceBuffer buf;
-};
-
-thread_local ScratchPool t_pool;
 
 int num_sms() {
     static int n = 0;
@@ -437,8 +441,7 @@ int num_sms() {
 }
 
 template <typename K>
-Launch plan(K kernel, size_t nblocks, uint32_t ws_words) {
-    Launch L;
+void plan(Launch &L, K kernel, size_t nblocks, uint32_t ws_words) {
     L.threads = 128;
     const unsigned warps_per_cta = L.threads / 32;
     const size_t want_warps = nblocks ? nblocks : 1;
@@ -450,15 +453,11 @@ Launch plan(K kernel, size_t nblocks, uint32_t ws_words) {
     const size_t smem = (size_t)warps_per_cta * ws_words * 4;
     if (smem <= 64 * 1024) {
         L.smem = smem;
-        L.gscratch = nullptr;
-        static thread_local bool set = false;
-        (void)set;
         FFGPU_CHECK_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024));
     } else {
         L.smem = 0;
-        L.gscratch = (uint32_t *)t_pool.buf.get((size_t)ctas * warps_per_cta * ws_words * 4);
+        FFGPU_CHECK_CUDA(cudaMallocAsync((void **)&L.gscratch, (size_t)ctas * warps_per_cta * ws_words * 4, L.st));
     }
-    return L;
 }
 
 }  // namespace
@@ -468,13 +467,12 @@ static int reg_epl(const Rsi16Code &c) { return (c.ecc == 32 || c.ecc == 64 || c
 
 template <int EPL>
 static void launch_encode(const Rsi16Code &c, const BlockView &v, size_t nblocks, cudaStream_t st) {
-    Launch L = plan(rsi16_encode_warp_kernel<EPL>, nblocks, EPL ? 0u : (uint32_t)c.block_len);
+    Launch L(st);
+    plan(L, rsi16_encode_warp_kernel<EPL>, nblocks, EPL ? 0u : (uint32_t)c.block_len);
     KernelTimer kt_timer("rsi16_encode_warp_kernel", st);
     rsi16_encode_warp_kernel<EPL><<<L.grid, L.threads, L.smem, st>>>(c.dev, v, nblocks, L.gscratch, L.ws_words);
     check_launch("rsi16_encode_warp_kernel");
 }
-
-bool rsi16_encode_stream_safe(const Rsi16Code &c) { return reg_epl(c) != 0 || (size_t)c.block_len * 4 * 4 <= 64 * 1024; }
 
 void rsi16_encode(const Rsi16Code &c, const BlockView &v, size_t nblocks, cudaStream_t st) {
     if (!nblocks) return;
@@ -493,7 +491,8 @@ void rsi16_synd(const Rsi16Code &c, const BlockView &v, size_t nblocks, uint32_t
 void rsi16_synd_grouped(const Rsi16Code &c, const BlockView &v, size_t nblocks, uint32_t *synds, size_t out_group,
                         size_t out_gstride, cudaStream_t st) {
     if (!nblocks) return;
-    Launch L = plan(rsi16_synd_warp_kernel, nblocks, (uint32_t)c.block_len);
+    Launch L(st);
+    plan(L, rsi16_synd_warp_kernel, nblocks, (uint32_t)c.block_len);
     KernelTimer kt_timer("rsi16_synd_warp_kernel", st);
     rsi16_synd_warp_kernel<<<L.grid, L.threads, L.smem, st>>>(c.dev, v, nblocks, synds, out_group, out_gstride,
                                                               L.gscratch, L.ws_words);
@@ -535,7 +534,8 @@ void rsi16_repair(const Rsi16Code &c, const BlockView &v, size_t nblocks, uint8_
             launched();
             return;
         }
-        Launch L = plan(rsi16_repair_warp_kernel<E>, nblocks, c.dev.temp_len + 1);
+        Launch L(st);
+        plan(L, rsi16_repair_warp_kernel<E>, nblocks, c.dev.temp_len + 1);
         KernelTimer kt_timer("rsi16_repair_warp_kernel", st);
         rsi16_repair_warp_kernel<E><<<L.grid, L.threads, L.smem, st>>>(c.dev, v, nblocks, status, active,
                                                                        L.gscratch, L.ws_words);
@@ -553,7 +553,8 @@ void rsi16_repair_known(const Rsi16Code &c, const BlockView &v, size_t nblocks, 
                         const uint32_t *pos_off, const uint32_t *pos_cnt, uint32_t count_all, const uint8_t *active,
                         uint8_t *status, cudaStream_t st) {
     if (!nblocks) return;
-    Launch L = plan(rsi16_repair_known_warp_kernel, nblocks, c.dev.temp_len + 1);
+    Launch L(st);
+    plan(L, rsi16_repair_known_warp_kernel, nblocks, c.dev.temp_len + 1);
     KernelTimer kt_timer("rsi16_repair_known_warp_kernel", st);
     rsi16_repair_known_warp_kernel<<<L.grid, L.threads, L.smem, st>>>(c.dev, v, nblocks, pos, pos_off, pos_cnt,
                                                                          count_all, active, status, L.gscratch,
@@ -564,7 +565,8 @@ void rsi16_repair_known(const Rsi16Code &c, const BlockView &v, size_t nblocks, 
 void rsi16_sugiyama(const Rsi16Code &c, const uint32_t *synds, size_t nblocks, uint32_t *locator, uint32_t *evaluator,
                     uint8_t *status, cudaStream_t st) {
     if (!nblocks) return;
-    Launch L = plan(rsi16_sugiyama_kernel, nblocks, c.dev.temp_len + 1);
+    Launch L(st);
+    plan(L, rsi16_sugiyama_kernel, nblocks, c.dev.temp_len + 1);
     KernelTimer kt_timer("rsi16_sugiyama_kernel", st);
     rsi16_sugiyama_kernel<<<L.grid, L.threads, L.smem, st>>>(c.dev, synds, nblocks, locator, evaluator, status,
                                                              L.gscratch, L.ws_words);
@@ -572,8 +574,10 @@ void rsi16_sugiyama(const Rsi16Code &c, const uint32_t *synds, size_t nblocks, u
 }
 
 void rsi16_roots(const Rsi16Code &c, const uint32_t *poly, uint8_t *is_zero, cudaStream_t st) {
-    uint32_t *scratch = (uint32_t *)t_pool.buf.get(c.ntt_len * 4 + 128);
+    uint32_t *scratch = nullptr;
+    FFGPU_CHECK_CUDA(cudaMallocAsync((void **)&scratch, c.ntt_len * 4 + 128, st));
     rsi16_roots_kernel<<<1, 32, 0, st>>>(c.dev, poly, is_zero, scratch);
+    cudaFreeAsync(scratch, st);
     check_launch("rsi16_roots_kernel");
 }
 

@@ -82,9 +82,6 @@ __host__ __device__ inline BlockView interleaved_view(void *msg, bool msg16, siz
 
 // Encode nblocks blocks of the view (parity written into the view's parity).
 void rsi16_encode(const Rsi16Code &c, const BlockView &v, size_t nblocks, cudaStream_t st);
-// True when rsi16_encode keeps its workspace in registers or shared memory,
-// so that launches on several streams may run at the same time.
-bool rsi16_encode_stream_safe(const Rsi16Code &c);
 // Syndromes (ecc uint32 per block) of nblocks blocks of the view.
 void rsi16_synd(const Rsi16Code &c, const BlockView &v, size_t nblocks, uint32_t *synds, cudaStream_t st);
 // The same with the syndromes of block b at

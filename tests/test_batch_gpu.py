@@ -52,8 +52,13 @@ def test_batch_equals_plain(mixed):
     # hand-set plan (defaults), then the autotuned plan, then graph replays
     bench.mixed_restore(reqs)
     b.plan(autotune=False, stream=sp)
+    n0 = capi.kernel_launches()
     b.launch(sp)
     torch.cuda.synchronize()
+    # the persistent kernel, plus the CIRC16 chain: gather, the repair
+    # stages over all codewords, scatter
+    n_direct = capi.kernel_launches() - n0
+    assert n_direct > 1
     assert _same(torch, ref, _outputs(torch, reqs))
     bench.mixed_restore(reqs)
     b.plan(autotune=True, stream=sp)
@@ -69,7 +74,8 @@ def test_batch_equals_plain(mixed):
         n0 = capi.kernel_launches()
         b.launch(sp)
         torch.cuda.synchronize()
-        assert capi.kernel_launches() - n0 == 1
+        # one graph replay runs the same kernels as the direct launch
+        assert capi.kernel_launches() - n0 == n_direct
         assert _same(torch, ref, _outputs(torch, reqs))
 
 
