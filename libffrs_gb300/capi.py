@@ -189,6 +189,10 @@ class RSi16Code:
     def repair(self, msg_ptr, parity_ptr, nblocks, status_ptr, stream=None):
         call("ffgpu_rsi16_repair", self.h, msg_ptr, parity_ptr, nblocks, status_ptr, stream)
 
+    def synd(self, msg_ptr, parity_ptr, nblocks, synds_ptr, stream=None):
+        """ecc_len uint32 syndromes per block (NTT::pntt over the whole block)."""
+        call("ffgpu_rsi16_synd", self.h, msg_ptr, parity_ptr, nblocks, synds_ptr, stream)
+
 
 class CIRC16Code:
     """Device-resident CIRC16 code handle (ffgpu_circ16)."""

@@ -11,12 +11,12 @@
 // (rs256_device.cuh, rsi16_device.cuh), so the bytes are identical to the
 // plain per-request path.
 //
-// CIRC16 repairs are not items: one codeword's CircRepair is a chain of
-// stages that each spread over hundreds of rows, which one CTA would walk
-// alone.  Their codewords are gathered (one copy kernel) into contiguous
-// arrays per code, repaired by circ16_repair_many (every stage one launch over
-// all of them) on a second stream beside the persistent kernel, and
-// scattered back.
+// CIRC16 requests are not items: one codeword's encode or CircRepair is a
+// chain of stages that each spread over hundreds of rows, which one CTA would
+// walk alone.  Their codewords are gathered (one copy kernel) into contiguous
+// arrays per code and direction, run through circ16_encode /
+// circ16_repair_many (every stage one launch over all of them) and scattered
+// back, ahead of the persistent kernel on the same stream.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -49,12 +49,8 @@ struct BatchCode {
     const uint32_t *lut;
     const uint8_t *exp512, *log256;
     int W, ecc;
-    // RSi16, or the inner code of a CIRC16
+    // RSi16
     Rsi16Dev rsi;
-    // CIRC16: outer code and geometry (pycirc16.hpp:46-65)
-    Rsi16Dev rso;
-    uint32_t c_message_len, c_ecc_len, c_rso_interleave, c_rso_ieccl, c_rsi_ieccl, c_inner_rows, c_outer_rows;
-    uint32_t c_rsi_total;
 };
 
 struct BatchItem {
@@ -74,8 +70,6 @@ struct BatchArgs {
     const BatchCode *codes;
     uint32_t *counter;
     uint8_t *rs_scratch;   // per CTA: kBatchThreads * kDecodeScratchBytes
-    uint32_t *circ_tmp;    // per CTA: circ_tmp_words
-    size_t circ_tmp_words;
     uint32_t ws_words;     // RSi16 workspace words per warp (shared memory)
 };
 
@@ -156,25 +150,6 @@ __device__ void rsi16_item(const Rsi16Dev &c, const BatchItem &it, uint32_t *ws,
     }
 }
 
-// One CIRC16 codeword (circ16_encode for a single block): the outer code over
-// the interleaved columns into untruncated words, their uint16 copy into the
-// ecc, then the inner code over the message rows and over the outer parity rows.
-__device__ void circ16_enc_item(const BatchCode &c, const BatchItem &it, uint32_t *ws, uint32_t *tmp) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint16_t *ecc = static_cast<uint16_t *>(it.par);
-    const uint32_t I = c.c_rso_interleave;
-    const BlockView vo{it.msg, 0, 1, I, tmp, 0, 1, I, I, true, false};
-    for (uint32_t b = warp; b < I; b += kBatchWarps) rsi16_encode_block(c.rso, vo, b, ws, lane);
-    __syncthreads();
-    for (uint32_t i = threadIdx.x; i < c.c_rso_ieccl; i += kBatchThreads) ecc[i] = (uint16_t)tmp[i];
-    const BlockView vi{it.msg, 0, c.rsi.message_len, 1, ecc + c.c_rso_ieccl, 0, c.rsi.ecc, 1, c.c_inner_rows,
-                       true, true};
-    for (uint32_t b = warp; b < c.c_inner_rows; b += kBatchWarps) rsi16_encode_block(c.rsi, vi, b, ws, lane);
-    const BlockView vio{tmp, 0, c.rsi.message_len, 1, ecc + c.c_rso_ieccl + c.c_rsi_ieccl, 0, c.rsi.ecc, 1,
-                        c.c_outer_rows, false, true};
-    for (uint32_t b = warp; b < c.c_outer_rows; b += kBatchWarps) rsi16_encode_block(c.rsi, vio, b, ws, lane);
-}
-
 // Byte ranges copied one CTA per range (ranges of at most kSegBytes): the
 // gather of CIRC16 codewords into the repair arrays and their scatter back.
 struct CopySeg {
@@ -199,7 +174,6 @@ __global__ void __launch_bounds__(kBatchThreads) batch_kernel(BatchArgs a) {
     extern __shared__ __align__(16) uint32_t sm[];
     __shared__ uint32_t s_idx;
     uint8_t *rs_scratch = a.rs_scratch + (size_t)blockIdx.x * kBatchThreads * kDecodeScratchBytes;
-    uint32_t *ctmp = a.circ_tmp + (size_t)blockIdx.x * a.circ_tmp_words;
     uint32_t *ws = sm + (size_t)(threadIdx.x >> 5) * a.ws_words;
     for (;;) {
         __syncthreads();  // every thread has read s_idx and finished the last item
@@ -221,9 +195,6 @@ __global__ void __launch_bounds__(kBatchThreads) batch_kernel(BatchArgs a) {
                 break;
             case BK_RSI16_DEC:
                 rsi16_item(c.rsi, it, ws, true);
-                break;
-            case BK_CIRC16_ENC:
-                circ16_enc_item(c, it, ws, ctmp);
                 break;
             default:
                 break;
@@ -250,34 +221,29 @@ struct ffgpu_batch {
     std::vector<BatchCode> codes;
     std::vector<const void *> code_keys;
     std::vector<BatchItem> items;
-    DeviceBuffer d_items, d_codes, d_counter, d_rs_scratch, d_circ_tmp, d_backup;
-    size_t smem = 0, circ_tmp_words = 0;
+    DeviceBuffer d_items, d_codes, d_counter, d_rs_scratch, d_backup;
+    size_t smem = 0;
     uint32_t ws_words = 0;
     unsigned grid = 0;
     int tile_rs = 512, tile_rsi = 8, ctas_per_sm = 0;
     bool planned = false;
-    // CIRC16 repairs: per code, its codewords' offsets in the gathered arrays
+    // CIRC16 requests: per code and direction, the codewords' place in the
+    // gathered arrays (words of d_cmsg / d_cecc, entries of d_cst, bytes of
+    // d_cws)
     struct CircGroup {
         ffgpu_circ16 *handle;
-        size_t ncw, cw0, ws_off;
+        bool decode;
+        size_t ncw, moff, eoff, soff, ws_off;
     };
     std::vector<CircGroup> circ;
-    std::vector<size_t> circ_moff, circ_eoff;  // word offsets in d_cmsg / d_cecc
     size_t n_gather = 0, n_scatter = 0;
     DeviceBuffer d_cmsg, d_cecc, d_cst, d_cws, d_segs;
-    cudaStream_t side = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int graph_kernels = 1;
     std::mutex mu;
 
-    ~ffgpu_batch() {
-        drop_graph();
-        if (side) cudaStreamDestroy(side);
-        if (ev_fork) cudaEventDestroy(ev_fork);
-        if (ev_join) cudaEventDestroy(ev_join);
-    }
+    ~ffgpu_batch() { drop_graph(); }
     void drop_graph() {
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
@@ -310,10 +276,7 @@ double item_cost(const ffgpu_batch &B, const BatchItem &it) {
         case BK_RS256_ENC: return (double)it.nblocks * it.msg_len * (1 + c.ecc / 8.0);
         case BK_RS256_DEC: return (double)it.nblocks * (it.msg_len + c.ecc) * (4 + c.ecc);
         case BK_RSI16_ENC: return (double)it.nblocks * c.rsi.block_len * 8;
-        case BK_RSI16_DEC: return (double)it.nblocks * c.rsi.block_len * (40 + c.rsi.ecc);
-        default:
-            return ((double)c.c_rso_interleave * c.rso.block_len +
-                    (double)(c.c_inner_rows + c.c_outer_rows) * c.rsi.block_len) * 8;
+        default: return (double)it.nblocks * c.rsi.block_len * (40 + c.rsi.ecc);
     }
 }
 
@@ -323,80 +286,89 @@ void add_segs(std::vector<CopySeg> &v, const void *src, void *dst, size_t bytes)
                      (uint64_t)std::min(kSegBytes, bytes - o)});
 }
 
-// Gathered arrays, workspaces and copy ranges of the CIRC16 repairs.
+size_t circ_group(ffgpu_batch &B, const ffgpu_batch::Req &r) {
+    const bool dec = r.kind == BK_CIRC16_DEC;
+    for (size_t g = 0; g < B.circ.size(); ++g)
+        if (B.circ[g].handle == r.handle && B.circ[g].decode == dec) return g;
+    B.circ.push_back({const_cast<ffgpu_circ16 *>(static_cast<const ffgpu_circ16 *>(r.handle)), dec, 0, 0, 0, 0, 0});
+    return B.circ.size() - 1;
+}
+
+// Gathered arrays, workspaces and copy ranges of the CIRC16 requests: an
+// encode gathers messages and scatters ecc; a repair gathers and scatters
+// both, and scatters the status.
 void plan_circ(ffgpu_batch &B) {
+    B.circ.clear();
     B.n_gather = B.n_scatter = 0;
+    for (const auto &r : B.reqs)
+        if (r.kind == BK_CIRC16_ENC || r.kind == BK_CIRC16_DEC) B.circ[circ_group(B, r)].ncw += r.nblocks;
     if (B.circ.empty()) return;
-    size_t cw = 0, ws = 0, mwords = 0, ewords = 0;
+    size_t mw = 0, ew = 0, sw = 0, ws = 0;
     for (auto &g : B.circ) {
         const Circ16Code &c = *g.handle->code;
-        g.cw0 = cw;
+        g.moff = mw;
+        g.eoff = ew;
+        g.soff = sw;
         g.ws_off = ws;
-        cw += g.ncw;
-        ws += (circ16_repair_many_ws_bytes(c, g.ncw) + 255) & ~(size_t)255;
-        mwords += g.ncw * c.message_len;
-        ewords += g.ncw * c.ecc_len;
+        mw += (g.ncw * c.message_len + 127) & ~(size_t)127;
+        ew += (g.ncw * c.ecc_len + 127) & ~(size_t)127;
+        sw += g.decode ? (g.ncw + 255) & ~(size_t)255 : 0;
+        const size_t wb = g.decode ? circ16_repair_many_ws_bytes(c, g.ncw) : circ16_encode_ws_bytes(c, g.ncw);
+        ws += (wb + 255) & ~(size_t)255;
     }
-    uint16_t *cm = static_cast<uint16_t *>(B.d_cmsg.get(mwords * 2));
-    uint16_t *ce = static_cast<uint16_t *>(B.d_cecc.get(ewords * 2));
-    uint8_t *cs = static_cast<uint8_t *>(B.d_cst.get(cw));
+    uint16_t *cm = static_cast<uint16_t *>(B.d_cmsg.get(mw * 2));
+    uint16_t *ce = static_cast<uint16_t *>(B.d_cecc.get(ew * 2));
+    uint8_t *cs = static_cast<uint8_t *>(B.d_cst.get(std::max<size_t>(sw, 1)));
     B.d_cws.get(ws);
-    // a code's codewords sit in request order: message words of all its
-    // codewords, then their ecc words
     std::vector<CopySeg> gat, sca;
     std::vector<size_t> next(B.circ.size(), 0);
-    std::vector<size_t> moff(B.circ.size()), eoff(B.circ.size());
-    size_t mo = 0, eo = 0;
-    for (size_t g = 0; g < B.circ.size(); ++g) {
-        const Circ16Code &c = *B.circ[g].handle->code;
-        moff[g] = mo;
-        eoff[g] = eo;
-        mo += B.circ[g].ncw * c.message_len;
-        eo += B.circ[g].ncw * c.ecc_len;
-    }
     for (const auto &r : B.reqs) {
-        if (r.kind != BK_CIRC16_DEC) continue;
-        size_t g = 0;
-        while (B.circ[g].handle != r.handle) ++g;
-        const Circ16Code &c = *B.circ[g].handle->code;
-        uint16_t *dm = cm + moff[g] + next[g] * c.message_len;
-        uint16_t *de = ce + eoff[g] + next[g] * c.ecc_len;
-        uint8_t *ds = cs + B.circ[g].cw0 + next[g];
+        if (r.kind != BK_CIRC16_ENC && r.kind != BK_CIRC16_DEC) continue;
+        const size_t g = circ_group(B, r);
+        const auto &cg = B.circ[g];
+        const Circ16Code &c = *cg.handle->code;
+        uint16_t *dm = cm + cg.moff + next[g] * c.message_len;
+        uint16_t *de = ce + cg.eoff + next[g] * c.ecc_len;
+        uint8_t *ds = cs + cg.soff + next[g];
         next[g] += r.nblocks;
-        add_segs(gat, r.a, dm, r.nblocks * c.message_len * 2);
-        add_segs(gat, r.b, de, r.nblocks * c.ecc_len * 2);
-        add_segs(sca, dm, r.a, r.nblocks * c.message_len * 2);
-        add_segs(sca, de, r.b, r.nblocks * c.ecc_len * 2);
-        if (r.status) add_segs(sca, ds, r.status, r.nblocks);
+        const size_t mb = r.nblocks * c.message_len * 2, eb = r.nblocks * c.ecc_len * 2;
+        add_segs(gat, r.a, dm, mb);
+        if (cg.decode) {
+            add_segs(gat, r.b, de, eb);
+            add_segs(sca, dm, r.a, mb);
+            if (r.status) add_segs(sca, ds, r.status, r.nblocks);
+        }
+        add_segs(sca, de, r.b, eb);
     }
     B.n_gather = gat.size();
     B.n_scatter = sca.size();
     gat.insert(gat.end(), sca.begin(), sca.end());
     B.d_segs.get(gat.size() * sizeof(CopySeg));
     FFGPU_CHECK_CUDA(cudaMemcpy(B.d_segs.ptr, gat.data(), gat.size() * sizeof(CopySeg), cudaMemcpyHostToDevice));
-    // per code: gathered message and ecc base pointers, kept in the group
-    B.circ_moff = moff;
-    B.circ_eoff = eoff;
-    if (!B.side) {
-        FFGPU_CHECK_CUDA(cudaStreamCreateWithFlags(&B.side, cudaStreamNonBlocking));
-        FFGPU_CHECK_CUDA(cudaEventCreateWithFlags(&B.ev_fork, cudaEventDisableTiming));
-        FFGPU_CHECK_CUDA(cudaEventCreateWithFlags(&B.ev_join, cudaEventDisableTiming));
-    }
 }
 
-// The CIRC16 chain on the side stream: gather, repair per code, scatter.
-void launch_circ(ffgpu_batch &B) {
+// The CIRC16 chain: gather, encode / repair per group, scatter.
+void launch_circ(ffgpu_batch &B, cudaStream_t st) {
     const CopySeg *segs = static_cast<const CopySeg *>(B.d_segs.ptr);
-    seg_copy_kernel<<<(unsigned)B.n_gather, 256, 0, B.side>>>(segs);
-    check_launch("seg_copy_kernel");
-    for (size_t g = 0; g < B.circ.size(); ++g) {
-        const auto &cg = B.circ[g];
-        circ16_repair_many(*cg.handle->code, static_cast<uint16_t *>(B.d_cmsg.ptr) + B.circ_moff[g],
-                           static_cast<uint16_t *>(B.d_cecc.ptr) + B.circ_eoff[g], cg.ncw,
-                           static_cast<uint8_t *>(B.d_cst.ptr) + cg.cw0, B.side,
-                           static_cast<char *>(B.d_cws.ptr) + cg.ws_off);
+    {
+        KernelTimer kt_timer("seg_copy_kernel", st);
+        seg_copy_kernel<<<(unsigned)B.n_gather, 256, 0, st>>>(segs);
     }
-    seg_copy_kernel<<<(unsigned)B.n_scatter, 256, 0, B.side>>>(segs + B.n_gather);
+    check_launch("seg_copy_kernel");
+    for (const auto &cg : B.circ) {
+        Circ16Code &c = *cg.handle->code;
+        uint16_t *m = static_cast<uint16_t *>(B.d_cmsg.ptr) + cg.moff;
+        uint16_t *e = static_cast<uint16_t *>(B.d_cecc.ptr) + cg.eoff;
+        void *w = static_cast<char *>(B.d_cws.ptr) + cg.ws_off;
+        if (cg.decode)
+            circ16_repair_many(c, m, e, cg.ncw, static_cast<uint8_t *>(B.d_cst.ptr) + cg.soff, st, w);
+        else
+            circ16_encode(c, m, cg.ncw, e, st, w);
+    }
+    {
+        KernelTimer kt_timer("seg_copy_kernel", st);
+        seg_copy_kernel<<<(unsigned)B.n_scatter, 256, 0, st>>>(segs + B.n_gather);
+    }
     check_launch("seg_copy_kernel");
 }
 
@@ -405,10 +377,8 @@ void build_plan(ffgpu_batch &B, int tile_rs, int tile_rsi, int ctas_per_sm) {
     B.codes.clear();
     B.code_keys.clear();
     B.items.clear();
-    B.circ.clear();
     size_t smem = 0;
     uint32_t ws_words = 0;
-    size_t circ_words = 0;
     bool any_rs_dec = false;
     for (const auto &r : B.reqs) {
         BatchCode bc{};
@@ -452,37 +422,6 @@ void build_plan(ffgpu_batch &B, int tile_rs, int tile_rsi, int ctas_per_sm) {
                 B.items.push_back(it);
             }
             ws_words = std::max(ws_words, r.kind == BK_RSI16_DEC ? c.dev.temp_len + 1 : (uint32_t)c.block_len);
-        } else if (r.kind == BK_CIRC16_DEC) {
-            ffgpu_circ16 *h = const_cast<ffgpu_circ16 *>(static_cast<const ffgpu_circ16 *>(r.handle));
-            size_t g = 0;
-            while (g < B.circ.size() && B.circ[g].handle != h) ++g;
-            if (g == B.circ.size()) B.circ.push_back({h, 0, 0, 0});
-            B.circ[g].ncw += r.nblocks;
-        } else {
-            const Circ16Code &c = *static_cast<const ffgpu_circ16 *>(r.handle)->code;
-            bc.rsi = c.rsi->dev;
-            bc.rso = c.rso->dev;
-            bc.c_message_len = (uint32_t)c.message_len;
-            bc.c_ecc_len = (uint32_t)c.ecc_len;
-            bc.c_rso_interleave = (uint32_t)c.rso_interleave;
-            bc.c_rso_ieccl = (uint32_t)c.rso_ieccl;
-            bc.c_rsi_ieccl = (uint32_t)c.rsi_ieccl;
-            bc.c_inner_rows = (uint32_t)c.inner_rows;
-            bc.c_outer_rows = (uint32_t)c.outer_rows;
-            bc.c_rsi_total = (uint32_t)c.rsi_total;
-            const uint32_t ci = code_index(B, r.handle, bc);
-            for (size_t b = 0; b < r.nblocks; ++b) {
-                BatchItem it{};
-                it.kind = r.kind;
-                it.code = ci;
-                it.nblocks = 1;
-                it.msg = static_cast<uint16_t *>(r.a) + b * c.message_len;
-                it.par = static_cast<uint16_t *>(r.b) + b * c.ecc_len;
-                it.status = nullptr;
-                B.items.push_back(it);
-            }
-            ws_words = std::max(ws_words, (uint32_t)std::max(c.rsi->block_len, c.rso->block_len));
-            circ_words = std::max(circ_words, c.rso_ieccl);
         }
     }
     plan_circ(B);
@@ -507,13 +446,11 @@ void build_plan(ffgpu_batch &B, int tile_rs, int tile_rsi, int ctas_per_sm) {
     B.tile_rs = tile_rs;
     B.tile_rsi = tile_rsi;
     B.ctas_per_sm = per_sm;
-    B.circ_tmp_words = (circ_words + 63) & ~(size_t)63;
 
     B.d_items.get(std::max<size_t>(1, B.items.size()) * sizeof(BatchItem));
     B.d_codes.get(std::max<size_t>(1, B.codes.size()) * sizeof(BatchCode));
     B.d_counter.get(256);
     if (any_rs_dec) B.d_rs_scratch.get((size_t)B.grid * kBatchThreads * kDecodeScratchBytes);
-    if (B.circ_tmp_words) B.d_circ_tmp.get((size_t)B.grid * B.circ_tmp_words * 4);
     if (!B.items.empty())
         FFGPU_CHECK_CUDA(cudaMemcpy(B.d_items.ptr, B.items.data(), B.items.size() * sizeof(BatchItem),
                                     cudaMemcpyHostToDevice));
@@ -525,17 +462,10 @@ void build_plan(ffgpu_batch &B, int tile_rs, int tile_rsi, int ctas_per_sm) {
 
 void launch_items(ffgpu_batch &B, cudaStream_t st, bool timed);
 
-// with_circ: also the CIRC16 repairs, on the side stream joined back into st
+// with_circ: also the CIRC16 chain (the autotuner times the items alone)
 void launch_plan(ffgpu_batch &B, cudaStream_t st, bool timed, bool with_circ = true) {
-    const bool circ = with_circ && !B.circ.empty();
-    if (circ) {
-        FFGPU_CHECK_CUDA(cudaEventRecord(B.ev_fork, st));
-        FFGPU_CHECK_CUDA(cudaStreamWaitEvent(B.side, B.ev_fork, 0));
-        launch_circ(B);
-        FFGPU_CHECK_CUDA(cudaEventRecord(B.ev_join, B.side));
-    }
+    if (with_circ && !B.circ.empty()) launch_circ(B, st);
     if (!B.items.empty()) launch_items(B, st, timed);
-    if (circ) FFGPU_CHECK_CUDA(cudaStreamWaitEvent(st, B.ev_join, 0));
 }
 
 void launch_items(ffgpu_batch &B, cudaStream_t st, bool timed) {
@@ -546,8 +476,6 @@ void launch_items(ffgpu_batch &B, cudaStream_t st, bool timed) {
     a.codes = static_cast<const BatchCode *>(B.d_codes.ptr);
     a.counter = static_cast<uint32_t *>(B.d_counter.ptr);
     a.rs_scratch = static_cast<uint8_t *>(B.d_rs_scratch.ptr);
-    a.circ_tmp = static_cast<uint32_t *>(B.d_circ_tmp.ptr);
-    a.circ_tmp_words = B.circ_tmp_words;
     a.ws_words = B.ws_words;
     if (timed) {
         KernelTimer kt_timer("batch_kernel", st);
@@ -559,7 +487,8 @@ void launch_items(ffgpu_batch &B, cudaStream_t st, bool timed) {
     }
 }
 
-// decode requests are repaired in place: save / restore them around trials
+// RS256 / RSi16 decode requests are repaired in place: save / restore them
+// around the autotuner's trials (which leave the CIRC16 chain out)
 struct Region {
     void *p;
     size_t n;
@@ -576,10 +505,6 @@ std::vector<Region> decode_regions(const ffgpu_batch &B) {
             const Rsi16Code &c = *static_cast<const ffgpu_rsi16 *>(r.handle)->code;
             v.push_back({r.a, r.nblocks * c.message_len * 2});
             v.push_back({r.b, r.nblocks * c.ecc * 2});
-        } else if (r.kind == BK_CIRC16_DEC) {
-            const Circ16Code &c = *static_cast<const ffgpu_circ16 *>(r.handle)->code;
-            v.push_back({r.a, r.nblocks * c.message_len * 2});
-            v.push_back({r.b, r.nblocks * c.ecc_len * 2});
         }
     }
     return v;

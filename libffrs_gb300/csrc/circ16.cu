@@ -265,10 +265,10 @@ CircLayout circ16_layout(const Circ16Code &c) {
     return L;
 }
 
-void circ16_encode(Circ16Code &c, const uint16_t *msg, size_t nblocks, uint16_t *ecc, cudaStream_t st) {
+void circ16_encode(Circ16Code &c, const uint16_t *msg, size_t nblocks, uint16_t *ecc, cudaStream_t st, void *ws) {
     if (!nblocks) return;
     const Rsi16Code &ri = *c.rsi, &ro = *c.rso;
-    uint32_t *tmp = (uint32_t *)c.enc_tmp.get(nblocks * c.rso_ieccl * 4);
+    uint32_t *tmp = (uint32_t *)(ws ? ws : c.enc_tmp.get(circ16_encode_ws_bytes(c, nblocks)));
     // outer code over the interleaved columns -> untruncated uint32 parity
     BlockView vo{(void *)msg, c.message_len, 1, c.rso_interleave, tmp, c.rso_ieccl, 1, c.rso_interleave,
                  c.rso_interleave, true, false};
@@ -285,6 +285,8 @@ void circ16_encode(Circ16Code &c, const uint16_t *msg, size_t nblocks, uint16_t 
                   c.outer_rows, false, true};
     rsi16_encode(ri, vio, nblocks * c.outer_rows, st);
 }
+
+size_t circ16_encode_ws_bytes(const Circ16Code &c, size_t nblocks) { return nblocks * c.rso_ieccl * 4; }
 
 // One CIRC16 block in place.  Returns through *assert_col the first outer
 // column (in the reference's k-major order) whose repair raised, or SIZE_MAX.
@@ -434,7 +436,10 @@ void circ16_repair_many(Circ16Code &c, uint16_t *msg, uint16_t *ecc, size_t ncw,
 
     FFGPU_CHECK_CUDA(cudaMemcpyAsync(saved, msg, ncw * c.message_len * 2, cudaMemcpyDeviceToDevice, st));
     // load_ecc (pycirc16.hpp:159-163)
-    km_widen<<<g1(ncw * (m.rso_n + m.rsi_n)), 256, 0, st>>>(ecc, c.ecc_len, m.rso_n, m.rsi_n, rso_ecc, rsi_ecc, ncw);
+    {
+        KernelTimer kt_timer("km_widen", st);
+        km_widen<<<g1(ncw * (m.rso_n + m.rsi_n)), 256, 0, st>>>(ecc, c.ecc_len, m.rso_n, m.rsi_n, rso_ecc, rsi_ecc, ncw);
+    }
     check_launch("km_widen");
     // compute_rsi_synd (pycirc16.hpp:165-181): message rows, then outer parity rows
     BlockView vmsg{msg, c.message_len, ri.message_len, 1, rsi_ecc, m.rsi_n, ri.ecc, 1, c.inner_rows, true, false};
@@ -443,26 +448,44 @@ void circ16_repair_many(Circ16Code &c, uint16_t *msg, uint16_t *ecc, size_t ncw,
                    false, false};
     rsi16_synd_grouped(ri, vrso, ncw * c.outer_rows, synd + c.rsi_ieccl, c.outer_rows, m.rsi_n, st);
     // repair_outer_zeros for every codeword and k
-    km_outer_zeros_prepare<<<items(ncw * m.n_oz), wpb * 32, 0, st>>>(d, m, ncw, rso_ecc, rsi_ecc, synd, blocks, zpos,
-                                                                     zoff, zcnt, zact);
+    {
+        KernelTimer kt_timer("km_outer_zeros_prepare", st);
+        km_outer_zeros_prepare<<<items(ncw * m.n_oz), wpb * 32, 0, st>>>(d, m, ncw, rso_ecc, rsi_ecc, synd, blocks, zpos,
+                                                                         zoff, zcnt, zact);
+    }
     check_launch("km_outer_zeros_prepare");
     BlockView vblk{blocks, m.n_oz * ri.block_len, ri.block_len, 1, blocks + ri.message_len, m.n_oz * ri.block_len,
                    ri.block_len, 1, m.n_oz, false, false};
     rsi16_repair_known(ri, vblk, ncw * m.n_oz, zpos, zoff, zcnt, 0, zact, nullptr, st);
     rsi16_synd(ri, vblk, ncw * m.n_oz, bsyn, st);
-    km_outer_zeros_commit<<<items(ncw * m.n_oz), wpb * 32, 0, st>>>(d, m, ncw, rso_ecc, rsi_ecc, synd, blocks, bsyn,
-                                                                    zpos, zcnt, zact);
+    {
+        KernelTimer kt_timer("km_outer_zeros_commit", st);
+        km_outer_zeros_commit<<<items(ncw * m.n_oz), wpb * 32, 0, st>>>(d, m, ncw, rso_ecc, rsi_ecc, synd, blocks, bsyn,
+                                                                        zpos, zcnt, zact);
+    }
     check_launch("km_outer_zeros_commit");
     // repair_inner_zeros for every codeword and k
-    km_inner_zeros_prepare<<<items(ncw * m.n_iz), wpb * 32, 0, st>>>(d, m, ncw, rsi_ecc, synd, vecs, flag);
+    {
+        KernelTimer kt_timer("km_inner_zeros_prepare", st);
+        km_inner_zeros_prepare<<<items(ncw * m.n_iz), wpb * 32, 0, st>>>(d, m, ncw, rsi_ecc, synd, vecs, flag);
+    }
     check_launch("km_inner_zeros_prepare");
     rsi16_mix_ecc(ri, vecs, ncw * m.n_iz, st);
-    km_inner_zeros_commit<<<items(ncw * m.n_iz), wpb * 32, 0, st>>>(d, m, ncw, rsi_ecc, synd, vecs, flag);
+    {
+        KernelTimer kt_timer("km_inner_zeros_commit", st);
+        km_inner_zeros_commit<<<items(ncw * m.n_iz), wpb * 32, 0, st>>>(d, m, ncw, rsi_ecc, synd, vecs, flag);
+    }
     check_launch("km_inner_zeros_commit");
     // find_error_locations, then repair_outer_errors (pycirc16.hpp:283-305)
-    km_find_locations<<<items(ncw * c.interleave), wpb * 32, 0, st>>>(d, m, ncw, synd, locs, lcnt);
+    {
+        KernelTimer kt_timer("km_find_locations", st);
+        km_find_locations<<<items(ncw * c.interleave), wpb * 32, 0, st>>>(d, m, ncw, synd, locs, lcnt);
+    }
     check_launch("km_find_locations");
-    km_outer_modes<<<g1(ncw * c.rso_interleave), 256, 0, st>>>(d, ncw, lcnt, poff, pcnt, kn, un);
+    {
+        KernelTimer kt_timer("km_outer_modes", st);
+        km_outer_modes<<<g1(ncw * c.rso_interleave), 256, 0, st>>>(d, ncw, lcnt, poff, pcnt, kn, un);
+    }
     check_launch("km_outer_modes");
     FFGPU_CHECK_CUDA(cudaMemsetAsync(cst, 0, ncw * c.rso_interleave, st));
     BlockView vcol = interleaved_view(msg, true, ro.message_len, rso_ecc, false, ro.ecc, c.rso_interleave);
@@ -475,8 +498,11 @@ void circ16_repair_many(Circ16Code &c, uint16_t *msg, uint16_t *ecc, size_t ncw,
                    false, false};
     rsi16_encode(ri, vreo, ncw * c.outer_rows, st);
     // raising codewords restored, the others' ecc written back
-    km_finish<<<(unsigned)ncw, 256, 0, st>>>(d, m, ncw, cst, msg, saved, c.message_len, ecc, c.ecc_len, rso_ecc,
-                                             rsi_ecc, status);
+    {
+        KernelTimer kt_timer("km_finish", st);
+        km_finish<<<(unsigned)ncw, 256, 0, st>>>(d, m, ncw, cst, msg, saved, c.message_len, ecc, c.ecc_len, rso_ecc,
+                                                 rsi_ecc, status);
+    }
     check_launch("km_finish");
 }
 

@@ -30,7 +30,11 @@ struct CircLayout {
 };
 CircLayout circ16_layout(const Circ16Code &c);
 
-void circ16_encode(Circ16Code &c, const uint16_t *msg, size_t nblocks, uint16_t *ecc, cudaStream_t st);
+// ws: circ16_encode_ws_bytes(c, nblocks) bytes of workspace, or NULL for the
+// code's own.
+void circ16_encode(Circ16Code &c, const uint16_t *msg, size_t nblocks, uint16_t *ecc, cudaStream_t st,
+                   void *ws = nullptr);
+size_t circ16_encode_ws_bytes(const Circ16Code &c, size_t nblocks);
 // Repair of one block up to (not including) the ecc write-back.  With
 // stop_after_find the pipeline stops after the error-row search and copies
 // the rows of group find_k to locs_out / lcnt_out (host pointers).

@@ -201,6 +201,68 @@ __global__ void rsi16_synd_warp_kernel(Rsi16Dev c, BlockView v, size_t nblocks, 
     }
 }
 
+// ecc = N < 32: 32 / N blocks per warp pass, the transforms on registers
+template <int N>
+__global__ void __launch_bounds__(128) rsi16_encode_sub_kernel(Rsi16Dev c, BlockView v, size_t nblocks) {
+    constexpr int G = 32 / N;
+    const int lane = threadIdx.x & 31, e = lane % N, s = lane / N;
+    SubTw<N> tw;
+    sub_twiddles<N>(c, e, tw);
+    const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const size_t nw = ((size_t)gridDim.x * blockDim.x) >> 5;
+    for (size_t b0 = warp * G; b0 < nblocks; b0 += nw * G) {
+        const size_t b = b0 + s;
+        const bool act = b < nblocks;
+        uint32_t a = sub_pntt<N>(c, v, act ? b : b0, act, c.pntt_blocks - 1, false, tw, e);
+        a = sub_gs<N>(fmul(a, c.ecc_mix[e]), tw, e);
+        if (act) {
+            const size_t pb = (b / v.group) * v.par_gstride + (b % v.group) * v.par_bstride;
+            st_word(v.par, v.par16, pb + (size_t)e * v.par_estride, a);
+        }
+    }
+}
+
+// syndromes, ecc = N < 32 (output layout as rsi16_synd_warp_kernel)
+template <int N>
+__global__ void __launch_bounds__(128) rsi16_synd_sub_kernel(Rsi16Dev c, BlockView v, size_t nblocks,
+                                                             uint32_t *synds, size_t out_group, size_t out_gstride) {
+    constexpr int G = 32 / N;
+    const int lane = threadIdx.x & 31, e = lane % N, s = lane / N;
+    SubTw<N> tw;
+    sub_twiddles<N>(c, e, tw);
+    const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const size_t nw = ((size_t)gridDim.x * blockDim.x) >> 5;
+    for (size_t b0 = warp * G; b0 < nblocks; b0 += nw * G) {
+        const size_t b = b0 + s;
+        const bool act = b < nblocks;
+        const uint32_t a = sub_pntt<N>(c, v, act ? b : b0, act, c.pntt_blocks, true, tw, e);
+        if (act) synds[(b / out_group) * out_gstride + (b % out_group) * N + e] = a;
+    }
+}
+
+// syndromes, ecc = 32 * EPL: two blocks per warp pass on registers
+template <int EPL>
+__global__ void __launch_bounds__(128) rsi16_synd_reg_kernel(Rsi16Dev c, BlockView v, size_t nblocks,
+                                                             uint32_t *synds, size_t out_group, size_t out_gstride) {
+    const int lane = threadIdx.x & 31;
+    RegTw<EPL> tw;
+    reg_twiddles<EPL>(c, lane, tw);
+    const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const size_t nw = ((size_t)gridDim.x * blockDim.x) >> 5;
+    for (size_t b = 2 * warp; b < nblocks; b += 2 * nw) {
+        const size_t b1 = b + 1 < nblocks ? b + 1 : b;
+        uint32_t a0[EPL], a1[EPL];
+        reg_pntt2<EPL>(c, v, b, b1, c.pntt_blocks, true, tw, lane, a0, a1);
+        uint32_t *o0 = synds + (b / out_group) * out_gstride + (b % out_group) * c.ecc;
+        uint32_t *o1 = synds + (b1 / out_group) * out_gstride + (b1 % out_group) * c.ecc;
+#pragma unroll
+        for (int h = 0; h < EPL; ++h) {
+            o0[lane * EPL + h] = a0[h];
+            o1[lane * EPL + h] = a1[h];
+        }
+    }
+}
+
 // blocks repaired by the bounded-distance path / by the step-for-step mirror
 __device__ unsigned long long g_repair_fast_blocks, g_repair_mirror_blocks;
 
@@ -474,13 +536,53 @@ static void launch_encode(const Rsi16Code &c, const BlockView &v, size_t nblocks
     check_launch("rsi16_encode_warp_kernel");
 }
 
+// sub-warp transform width for this code (0: none)
+static int sub_n(const Rsi16Code &c) { return (c.ecc == 2 || c.ecc == 4 || c.ecc == 8 || c.ecc == 16) ? (int)c.ecc : 0; }
+
+// CTAs of 128 threads for nwarps warps of work
+static unsigned warp_grid(size_t nwarps) {
+    return (unsigned)std::max<size_t>(1, std::min<size_t>((size_t)num_sms() * 16, (nwarps + 3) / 4));
+}
+
+template <int N>
+static void launch_encode_sub(const Rsi16Code &c, const BlockView &v, size_t nblocks, cudaStream_t st) {
+    KernelTimer kt_timer("rsi16_encode_sub_kernel", st);
+    rsi16_encode_sub_kernel<N><<<warp_grid((nblocks + 32 / N - 1) / (32 / N)), 128, 0, st>>>(c.dev, v, nblocks);
+    check_launch("rsi16_encode_sub_kernel");
+}
+
+template <int N>
+static void launch_synd_sub(const Rsi16Code &c, const BlockView &v, size_t nblocks, uint32_t *synds,
+                            size_t out_group, size_t out_gstride, cudaStream_t st) {
+    KernelTimer kt_timer("rsi16_synd_sub_kernel", st);
+    rsi16_synd_sub_kernel<N><<<warp_grid((nblocks + 32 / N - 1) / (32 / N)), 128, 0, st>>>(
+        c.dev, v, nblocks, synds, out_group, out_gstride);
+    check_launch("rsi16_synd_sub_kernel");
+}
+
+template <int EPL>
+static void launch_synd_reg(const Rsi16Code &c, const BlockView &v, size_t nblocks, uint32_t *synds,
+                            size_t out_group, size_t out_gstride, cudaStream_t st) {
+    KernelTimer kt_timer("rsi16_synd_reg_kernel", st);
+    rsi16_synd_reg_kernel<EPL><<<warp_grid((nblocks + 1) / 2), 128, 0, st>>>(c.dev, v, nblocks, synds, out_group,
+                                                                             out_gstride);
+    check_launch("rsi16_synd_reg_kernel");
+}
+
 void rsi16_encode(const Rsi16Code &c, const BlockView &v, size_t nblocks, cudaStream_t st) {
     if (!nblocks) return;
     switch (reg_epl(c)) {
-        case 1: launch_encode<1>(c, v, nblocks, st); break;
-        case 2: launch_encode<2>(c, v, nblocks, st); break;
-        case 4: launch_encode<4>(c, v, nblocks, st); break;
-        default: launch_encode<0>(c, v, nblocks, st); break;
+        case 1: launch_encode<1>(c, v, nblocks, st); return;
+        case 2: launch_encode<2>(c, v, nblocks, st); return;
+        case 4: launch_encode<4>(c, v, nblocks, st); return;
+        default: break;
+    }
+    switch (sub_n(c)) {
+        case 2: launch_encode_sub<2>(c, v, nblocks, st); return;
+        case 4: launch_encode_sub<4>(c, v, nblocks, st); return;
+        case 8: launch_encode_sub<8>(c, v, nblocks, st); return;
+        case 16: launch_encode_sub<16>(c, v, nblocks, st); return;
+        default: launch_encode<0>(c, v, nblocks, st); return;
     }
 }
 
@@ -491,6 +593,19 @@ void rsi16_synd(const Rsi16Code &c, const BlockView &v, size_t nblocks, uint32_t
 void rsi16_synd_grouped(const Rsi16Code &c, const BlockView &v, size_t nblocks, uint32_t *synds, size_t out_group,
                         size_t out_gstride, cudaStream_t st) {
     if (!nblocks) return;
+    switch (reg_epl(c)) {
+        case 1: launch_synd_reg<1>(c, v, nblocks, synds, out_group, out_gstride, st); return;
+        case 2: launch_synd_reg<2>(c, v, nblocks, synds, out_group, out_gstride, st); return;
+        case 4: launch_synd_reg<4>(c, v, nblocks, synds, out_group, out_gstride, st); return;
+        default: break;
+    }
+    switch (sub_n(c)) {
+        case 2: launch_synd_sub<2>(c, v, nblocks, synds, out_group, out_gstride, st); return;
+        case 4: launch_synd_sub<4>(c, v, nblocks, synds, out_group, out_gstride, st); return;
+        case 8: launch_synd_sub<8>(c, v, nblocks, synds, out_group, out_gstride, st); return;
+        case 16: launch_synd_sub<16>(c, v, nblocks, synds, out_group, out_gstride, st); return;
+        default: break;
+    }
     Launch L(st);
     plan(L, rsi16_synd_warp_kernel, nblocks, (uint32_t)c.block_len);
     KernelTimer kt_timer("rsi16_synd_warp_kernel", st);
@@ -584,6 +699,7 @@ void rsi16_roots(const Rsi16Code &c, const uint32_t *poly, uint8_t *is_zero, cud
 void rsi16_mix_ecc(const Rsi16Code &c, uint32_t *vecs, size_t nvec, cudaStream_t st) {
     if (!nvec) return;
     const unsigned grid = (unsigned)std::min<size_t>((nvec + 3) / 4, (size_t)num_sms() * 8);
+    KernelTimer kt_timer("rsi16_mix_kernel", st);
     rsi16_mix_kernel<<<grid, 128, 0, st>>>(c.dev, vecs, nvec);
     check_launch("rsi16_mix_kernel");
 }

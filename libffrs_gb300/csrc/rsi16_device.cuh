@@ -696,6 +696,96 @@ static __device__ __forceinline__ void rsi16_encode_block_reg(const Rsi16Dev &c,
     for (int h = 0; h < EPL; ++h) st_word(v.par, v.par16, pb + (size_t)(lane * EPL + h) * v.par_estride, acc[h]);
 }
 
+// ---------------------------------------------------------------- sub-warp register NTTs
+//
+// For ecc = N < 32 (N = 2, 4, 8, 16) a warp transforms 32 / N blocks at once:
+// lane L holds element e = L % N of the block in slot L / N.  Every butterfly
+// partner is lane L ^ stride with stride < N, inside the slot's N lanes, so
+// one shuffle per stage serves every slot.  Twiddles as in RegTw with
+// EPL = 1 over an N-point transform.
+
+template <int N>
+constexpr int sub_log() {
+    return N == 2 ? 1 : (N == 4 ? 2 : (N == 8 ? 3 : 4));
+}
+
+template <int N>
+struct SubTw {
+    uint32_t ct[sub_log<N>()];
+    uint32_t gs[sub_log<N>()];
+};
+
+template <int N>
+static __device__ __forceinline__ void sub_twiddles(const Rsi16Dev &c, int e, SubTw<N> &tw) {
+    constexpr int LOG = sub_log<N>();
+#pragma unroll
+    for (int st = 0; st < LOG; ++st) {
+        const uint32_t stride = 1u << st, ef = (uint32_t)(N >> 1) >> st;
+        tw.ct[st] = c.roots_ecc[ef * ((uint32_t)e & (stride - 1))];
+    }
+#pragma unroll
+    for (int st = 0; st < LOG; ++st) {
+        const uint32_t stride = (uint32_t)(N >> 1) >> st;
+        tw.gs[st] = c.roots_i_ecc[((uint32_t)e & (stride - 1)) << st];
+    }
+}
+
+// ct_butterfly of each slot's vector: RBO input, normal order output
+template <int N>
+static __device__ __forceinline__ uint32_t sub_ct(uint32_t x, const SubTw<N> &tw, int e) {
+    constexpr int LOG = sub_log<N>();
+#pragma unroll
+    for (int st = 0; st < LOG; ++st) {
+        const int stride = 1 << st;
+        const bool upper = (e & stride) != 0;
+        const uint32_t p = __shfl_xor_sync(0xffffffffu, x, stride);
+        const uint32_t m = fmul(upper ? x : p, tw.ct[st]);
+        x = upper ? fsub(p, m) : fadd(x, m);
+    }
+    return x;
+}
+
+// gs_butterfly of each slot's vector: normal order input, RBO output
+template <int N>
+static __device__ __forceinline__ uint32_t sub_gs(uint32_t x, const SubTw<N> &tw, int e) {
+    constexpr int LOG = sub_log<N>();
+#pragma unroll
+    for (int st = 0; st < LOG; ++st) {
+        const int stride = (N >> 1) >> st;
+        const bool upper = (e & stride) != 0;
+        const uint32_t p = __shfl_xor_sync(0xffffffffu, x, stride);
+        x = upper ? fmul(fsub(p, x), tw.gs[st]) : fadd(x, p);
+    }
+    return x;
+}
+
+// NTT::pntt (ntt.hpp:133-152) of the block b in this lane's slot over nchunks
+// chunks (at least chunk 0); element e of the result.  act false: the slot
+// has no block (zeros, no loads; its lanes still take part in the shuffles).
+template <int N>
+static __device__ __forceinline__ uint32_t sub_pntt(const Rsi16Dev &c, const BlockView &v, size_t b, bool act,
+                                                    uint32_t nchunks, bool with_parity, const SubTw<N> &tw, int e) {
+    const size_t mb = (b / v.group) * v.msg_gstride + (b % v.group) * v.msg_bstride;
+    const size_t pb = (b / v.group) * v.par_gstride + (b % v.group) * v.par_bstride;
+    const uint32_t nch = nchunks ? nchunks : 1;
+    uint32_t acc = 0;
+#pragma unroll 2
+    for (uint32_t ch = 0; ch < nch; ++ch) {
+        const uint32_t k = ch * N + (uint32_t)e;
+        uint32_t w = 0;
+        if (act) {
+            if (k < c.message_len)
+                w = ld_word(v.msg, v.msg16, mb + (size_t)k * v.msg_estride);
+            else if (with_parity && k < c.block_len)
+                w = ld_word(v.par, v.par16, pb + (size_t)(k - c.message_len) * v.par_estride);
+        }
+        w = sub_ct<N>(w, tw, e);
+        const uint32_t y = fmul(w, c.pntt_shift[k]);
+        acc = ch ? fadd(acc, y) : y;
+    }
+    return acc;
+}
+
 // ---------------------------------------------------------------- one block per warp
 
 // parity of block b (ws: block_len words)

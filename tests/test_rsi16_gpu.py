@@ -60,7 +60,8 @@ def _corrupt_words(rng, cw, k):
         cw[q] = v
 
 
-@pytest.mark.parametrize("bl,ecc", [(1024, 64), (256, 32), (96, 16), (4096, 128), (128, 64), (512, 2)])
+@pytest.mark.parametrize("bl,ecc", [(1024, 64), (256, 32), (96, 16), (4096, 128), (128, 64), (512, 2), (128, 8),
+                                    (60, 4), (130, 2), (48, 16)])
 def test_rsi16_batched_vs_oracle(ffrs_gpu, bl, ecc):
     rng = np.random.Generator(np.random.PCG64(bl * 7 + ecc))
     rs = ffrs_gpu.RSi16(bl, ecc)
@@ -159,3 +160,29 @@ def test_rsi16_errors(ffrs_gpu):
     m, e = bytearray(24), bytearray(8)
     assert rs.repair(m, e, []) == ffrs_gpu.RepairStatus.NoErrors
     assert rs.repair(m, e) == ffrs_gpu.RepairStatus.NoErrors
+
+
+@pytest.mark.parametrize("bl,ecc", [(130, 2), (60, 4), (128, 8), (96, 16), (256, 32), (1024, 64), (4096, 128),
+                                    (2048, 256)])
+def test_rsi16_synd_blocks_vs_oracle(bl, ecc):
+    """Batched syndromes (every ecc: the sub-warp, register and shared-memory
+    transforms) against the oracle's NTT::pntt, block by block."""
+    import torch
+
+    from libffrs_gb300 import capi
+
+    rng = np.random.Generator(np.random.PCG64(bl + 31 * ecc))
+    nb = 333
+    ml = bl - ecc
+    o = O.RSi16(bl, ecc)
+    msg = rng.integers(0, 65536, size=(nb, ml), dtype=np.uint16)
+    par = rng.integers(0, 65536, size=(nb, ecc), dtype=np.uint16)
+    code = capi.RSi16Code(bl, ecc)
+    dm = torch.from_numpy(msg.view(np.int16)).cuda()
+    dp = torch.from_numpy(par.view(np.int16)).cuda()
+    ds = torch.zeros((nb, ecc), dtype=torch.int32, device="cuda")
+    code.synd(dm.data_ptr(), dp.data_ptr(), nb, ds.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    got = ds.cpu().numpy().view(np.uint32)
+    for i in range(nb):
+        blk = np.concatenate([msg[i], par[i]]).astype(np.uint32)
+        np.testing.assert_array_equal(got[i], o.synd(blk), err_msg=f"block {i}")
