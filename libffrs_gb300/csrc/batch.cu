@@ -103,7 +103,10 @@ __device__ void rs256_dec_item(const BatchCode &c, const BatchItem &it, uint32_t
     for (int i = threadIdx.x; i < 512; i += kBatchThreads) ex[i] = c.exp512[i];
     for (int i = threadIdx.x; i < 256; i += kBatchThreads) lg[i] = c.log256[i];
     __syncthreads();
-    const DecodeScratchG sc(scratch, threadIdx.x, kBatchThreads);
+    // scratch in shared memory after the tables for ecc <= 64 (W <= 16),
+    // else this CTA's slice of global memory
+    const DecodeScratchG sc = W <= 16 ? DecodeScratchG(lg + 256, threadIdx.x, kBatchThreads, c.ecc)
+                                      : DecodeScratchG(scratch, threadIdx.x, kBatchThreads);
     const int ml = it.msg_len;
     uint8_t *data = static_cast<uint8_t *>(it.msg);
     uint8_t *par = static_cast<uint8_t *>(it.par);
@@ -112,16 +115,6 @@ __device__ void rs256_dec_item(const BatchCode &c, const BatchItem &it, uint32_t
                       nullptr);
 }
 
-#define FFGPU_BATCH_W(W, CALL)                       \
-    switch (W) {                                     \
-        case 1: { constexpr int w_ = 1; CALL; } break;   \
-        case 2: { constexpr int w_ = 2; CALL; } break;   \
-        case 4: { constexpr int w_ = 4; CALL; } break;   \
-        case 8: { constexpr int w_ = 8; CALL; } break;   \
-        case 16: { constexpr int w_ = 16; CALL; } break; \
-        case 32: { constexpr int w_ = 32; CALL; } break; \
-        default: { constexpr int w_ = 64; CALL; } break; \
-    }
 
 template <int EPL>
 __device__ void rsi16_item_t(const Rsi16Dev &c, const BatchItem &it, uint32_t *ws, bool decode) {
@@ -170,10 +163,39 @@ __global__ void __launch_bounds__(256) seg_copy_kernel(const CopySeg *segs) {
     }
 }
 
+// Item classes, one persistent launch each with its own registers, shared
+// memory and CTAs per SM: RS256 items by the width W of their LFSR remainder
+// (W <= 4: ecc <= 16; W <= 16: ecc <= 64; wider), then the RSi16 items.
+constexpr int kClasses = 4;
+constexpr int kClsRsi16 = 3;
+
+__host__ __device__ constexpr int rs256_class(int W) { return W <= 4 ? 0 : (W <= 16 ? 1 : 2); }
+
+#define FFGPU_BATCH_W_CLS(CLS, W, CALL)                                    \
+    if constexpr (CLS == 0) {                                              \
+        switch (W) {                                                       \
+            case 1: { constexpr int w_ = 1; CALL; } break;                 \
+            case 2: { constexpr int w_ = 2; CALL; } break;                 \
+            default: { constexpr int w_ = 4; CALL; } break;                \
+        }                                                                  \
+    } else if constexpr (CLS == 1) {                                       \
+        switch (W) {                                                       \
+            case 8: { constexpr int w_ = 8; CALL; } break;                 \
+            default: { constexpr int w_ = 16; CALL; } break;               \
+        }                                                                  \
+    } else {                                                               \
+        switch (W) {                                                       \
+            case 32: { constexpr int w_ = 32; CALL; } break;               \
+            default: { constexpr int w_ = 64; CALL; } break;               \
+        }                                                                  \
+    }
+
+template <int CLS>
 __global__ void __launch_bounds__(kBatchThreads) batch_kernel(BatchArgs a) {
     extern __shared__ __align__(16) uint32_t sm[];
     __shared__ uint32_t s_idx;
-    uint8_t *rs_scratch = a.rs_scratch + (size_t)blockIdx.x * kBatchThreads * kDecodeScratchBytes;
+    uint8_t *rs_scratch =
+        CLS < kClsRsi16 ? a.rs_scratch + (size_t)blockIdx.x * kBatchThreads * kDecodeScratchBytes : nullptr;
     uint32_t *ws = sm + (size_t)(threadIdx.x >> 5) * a.ws_words;
     for (;;) {
         __syncthreads();  // every thread has read s_idx and finished the last item
@@ -183,21 +205,14 @@ __global__ void __launch_bounds__(kBatchThreads) batch_kernel(BatchArgs a) {
         if (idx >= a.nitems) break;
         const BatchItem it = a.items[idx];
         const BatchCode &c = a.codes[it.code];
-        switch (it.kind) {
-            case BK_RS256_ENC:
-                FFGPU_BATCH_W(c.W, (rs256_enc_item<w_>(c, it, sm)));
-                break;
-            case BK_RS256_DEC:
-                FFGPU_BATCH_W(c.W, (rs256_dec_item<w_>(c, it, sm, rs_scratch)));
-                break;
-            case BK_RSI16_ENC:
-                rsi16_item(c.rsi, it, ws, false);
-                break;
-            case BK_RSI16_DEC:
-                rsi16_item(c.rsi, it, ws, true);
-                break;
-            default:
-                break;
+        if constexpr (CLS < kClsRsi16) {
+            if (it.kind == BK_RS256_ENC) {
+                FFGPU_BATCH_W_CLS(CLS, c.W, (rs256_enc_item<w_>(c, it, sm)));
+            } else {
+                FFGPU_BATCH_W_CLS(CLS, c.W, (rs256_dec_item<w_>(c, it, sm, rs_scratch)));
+            }
+        } else {
+            rsi16_item(c.rsi, it, ws, it.kind == BK_RSI16_DEC);
         }
     }
 }
@@ -220,12 +235,20 @@ struct ffgpu_batch {
     // plan
     std::vector<BatchCode> codes;
     std::vector<const void *> code_keys;
-    std::vector<BatchItem> items;
-    DeviceBuffer d_items, d_codes, d_counter, d_rs_scratch, d_backup;
-    size_t smem = 0;
-    uint32_t ws_words = 0;
-    unsigned grid = 0;
-    int tile_rs = 512, tile_rsi = 8, ctas_per_sm = 0;
+    // items by class (rs256_class, kClsRsi16), each served by its own
+    // persistent launch
+    struct ItemClass {
+        std::vector<BatchItem> items;
+        DeviceBuffer d_items;
+        size_t smem = 0;
+        uint32_t ws_words = 0;
+        unsigned grid = 0;
+        int per_sm = 0;
+        size_t scratch_cta0 = 0;  // first CTA slice of the RS256 decode scratch
+    };
+    ItemClass cls[kClasses];
+    DeviceBuffer d_codes, d_counter, d_rs_scratch, d_backup;
+    int tile_rs = 512, tile_rsi = 8, ctas_rs = 0, ctas_rsi = 0;
     bool planned = false;
     // CIRC16 requests: per code and direction, the codewords' place in the
     // gathered arrays (words of d_cmsg / d_cecc, entries of d_cst, bytes of
@@ -238,12 +261,22 @@ struct ffgpu_batch {
     std::vector<CircGroup> circ;
     size_t n_gather = 0, n_scatter = 0;
     DeviceBuffer d_cmsg, d_cecc, d_cst, d_cws, d_segs;
+    // side streams of the class launches (index 0 unused: the caller's)
+    cudaStream_t side[kClasses] = {};
+    cudaEvent_t ev_fork = nullptr, ev_join[kClasses] = {};
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int graph_kernels = 1;
     std::mutex mu;
 
-    ~ffgpu_batch() { drop_graph(); }
+    ~ffgpu_batch() {
+        drop_graph();
+        for (int k = 1; k < kClasses; ++k) {
+            if (side[k]) cudaStreamDestroy(side[k]);
+            if (ev_join[k]) cudaEventDestroy(ev_join[k]);
+        }
+        if (ev_fork) cudaEventDestroy(ev_fork);
+    }
     void drop_graph() {
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
@@ -372,12 +405,30 @@ void launch_circ(ffgpu_batch &B, cudaStream_t st) {
     check_launch("seg_copy_kernel");
 }
 
-void build_plan(ffgpu_batch &B, int tile_rs, int tile_rsi, int ctas_per_sm) {
+// Occupancy-limited grid of one class's persistent launch: ctas CTAs per SM
+// (0: as many as fit), at most one CTA per item.
+template <int CLS>
+void size_class(ffgpu_batch::ItemClass &k, int ctas) {
+    FFGPU_REQUIRE(k.smem <= 220 * 1024, "batch needs more shared memory per CTA than the device has");
+    FFGPU_CHECK_CUDA(
+        cudaFuncSetAttribute(batch_kernel<CLS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem));
+    int occ = 0;
+    FFGPU_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel<CLS>, kBatchThreads, k.smem));
+    occ = std::max(occ, 1);
+    k.per_sm = ctas > 0 ? std::min(ctas, occ) : occ;
+    k.grid = (unsigned)std::max<size_t>(1, std::min<size_t>((size_t)sm_count_b() * k.per_sm, k.items.size()));
+}
+
+void build_plan(ffgpu_batch &B, int tile_rs, int tile_rsi, int ctas_rs, int ctas_rsi) {
     B.drop_graph();
     B.codes.clear();
     B.code_keys.clear();
-    B.items.clear();
-    size_t smem = 0;
+    for (auto &K : B.cls) {
+        K.items.clear();
+        K.smem = 0;
+        K.ws_words = 0;
+    }
+    auto &K1 = B.cls[kClsRsi16];
     uint32_t ws_words = 0;
     bool any_rs_dec = false;
     for (const auto &r : B.reqs) {
@@ -390,6 +441,7 @@ void build_plan(ffgpu_batch &B, int tile_rs, int tile_rsi, int ctas_per_sm) {
             bc.W = c.W;
             bc.ecc = c.ecc;
             const uint32_t ci = code_index(B, r.handle, bc);
+            auto &K = B.cls[rs256_class(c.W)];
             for (size_t b0 = 0; b0 < r.nblocks; b0 += (size_t)tile_rs) {
                 BatchItem it{};
                 it.kind = r.kind;
@@ -399,12 +451,13 @@ void build_plan(ffgpu_batch &B, int tile_rs, int tile_rsi, int ctas_per_sm) {
                 it.msg = static_cast<uint8_t *>(r.a) + b0 * r.msg_len;
                 it.par = static_cast<uint8_t *>(r.b) + b0 * (size_t)c.ecc;
                 it.status = r.status ? r.status + b0 : nullptr;
-                B.items.push_back(it);
+                K.items.push_back(it);
             }
             if (r.kind == BK_RS256_ENC)
-                smem = std::max(smem, (size_t)256 * c.W * 4 + (size_t)kBatchThreads * r.msg_len);
+                K.smem = std::max(K.smem, (size_t)256 * c.W * 4 + (size_t)kBatchThreads * r.msg_len);
             else {
-                smem = std::max(smem, (size_t)256 * c.W * 4 + 768);
+                const size_t sc = c.W <= 16 ? (size_t)kDecodeScratchCols * c.ecc * kBatchThreads : 0;
+                K.smem = std::max(K.smem, (size_t)256 * c.W * 4 + 768 + sc);
                 any_rs_dec = true;
             }
         } else if (r.kind == BK_RSI16_ENC || r.kind == BK_RSI16_DEC) {
@@ -419,72 +472,113 @@ void build_plan(ffgpu_batch &B, int tile_rs, int tile_rsi, int ctas_per_sm) {
                 it.msg = static_cast<uint16_t *>(r.a) + b0 * c.message_len;
                 it.par = static_cast<uint16_t *>(r.b) + b0 * c.ecc;
                 it.status = r.status ? r.status + b0 : nullptr;
-                B.items.push_back(it);
+                K1.items.push_back(it);
             }
             ws_words = std::max(ws_words, r.kind == BK_RSI16_DEC ? c.dev.temp_len + 1 : (uint32_t)c.block_len);
         }
     }
     plan_circ(B);
-    // longest first
-    std::vector<std::pair<double, size_t>> order(B.items.size());
-    for (size_t i = 0; i < B.items.size(); ++i) order[i] = {-item_cost(B, B.items[i]), i};
-    std::stable_sort(order.begin(), order.end());
-    std::vector<BatchItem> sorted(B.items.size());
-    for (size_t i = 0; i < order.size(); ++i) sorted[i] = B.items[order[i].second];
-    B.items.swap(sorted);
-
-    ws_words = (ws_words + 3) & ~3u;
-    B.ws_words = ws_words;
-    B.smem = std::max(smem, (size_t)kBatchWarps * ws_words * 4);
-    FFGPU_REQUIRE(B.smem <= 220 * 1024, "batch needs more shared memory per CTA than the device has");
-    FFGPU_CHECK_CUDA(cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)B.smem));
-    int occ = 0;
-    FFGPU_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel, kBatchThreads, B.smem));
-    occ = std::max(occ, 1);
-    const int per_sm = ctas_per_sm > 0 ? std::min(ctas_per_sm, occ) : occ;
-    B.grid = (unsigned)std::max<size_t>(1, std::min<size_t>((size_t)sm_count_b() * per_sm, B.items.size()));
+    // longest first within each class
+    for (auto &K : B.cls) {
+        std::vector<std::pair<double, size_t>> order(K.items.size());
+        for (size_t i = 0; i < K.items.size(); ++i) order[i] = {-item_cost(B, K.items[i]), i};
+        std::stable_sort(order.begin(), order.end());
+        std::vector<BatchItem> sorted(K.items.size());
+        for (size_t i = 0; i < order.size(); ++i) sorted[i] = K.items[order[i].second];
+        K.items.swap(sorted);
+    }
+    K1.ws_words = (ws_words + 3) & ~3u;
+    K1.smem = (size_t)kBatchWarps * K1.ws_words * 4;
+    size_class<0>(B.cls[0], ctas_rs);
+    size_class<1>(B.cls[1], ctas_rs);
+    size_class<2>(B.cls[2], ctas_rs);
+    size_class<kClsRsi16>(K1, ctas_rsi);
     B.tile_rs = tile_rs;
     B.tile_rsi = tile_rsi;
-    B.ctas_per_sm = per_sm;
+    B.ctas_rs = ctas_rs;
+    B.ctas_rsi = ctas_rsi;
 
-    B.d_items.get(std::max<size_t>(1, B.items.size()) * sizeof(BatchItem));
     B.d_codes.get(std::max<size_t>(1, B.codes.size()) * sizeof(BatchCode));
     B.d_counter.get(256);
-    if (any_rs_dec) B.d_rs_scratch.get((size_t)B.grid * kBatchThreads * kDecodeScratchBytes);
-    if (!B.items.empty())
-        FFGPU_CHECK_CUDA(cudaMemcpy(B.d_items.ptr, B.items.data(), B.items.size() * sizeof(BatchItem),
-                                    cudaMemcpyHostToDevice));
+    // decode scratch: one slice per CTA of every RS256 class (the classes
+    // run at the same time)
+    size_t g = 0;
+    for (int k = 0; k < kClsRsi16; ++k) {
+        B.cls[k].scratch_cta0 = g;
+        g += B.cls[k].items.empty() ? 0 : B.cls[k].grid;
+    }
+    if (any_rs_dec) B.d_rs_scratch.get(g * kBatchThreads * kDecodeScratchBytes);
+    for (auto &K : B.cls) {
+        K.d_items.get(std::max<size_t>(1, K.items.size()) * sizeof(BatchItem));
+        if (!K.items.empty())
+            FFGPU_CHECK_CUDA(cudaMemcpy(K.d_items.ptr, K.items.data(), K.items.size() * sizeof(BatchItem),
+                                        cudaMemcpyHostToDevice));
+    }
     if (!B.codes.empty())
         FFGPU_CHECK_CUDA(cudaMemcpy(B.d_codes.ptr, B.codes.data(), B.codes.size() * sizeof(BatchCode),
                                     cudaMemcpyHostToDevice));
     B.planned = true;
 }
 
-void launch_items(ffgpu_batch &B, cudaStream_t st, bool timed);
-
-// with_circ: also the CIRC16 chain (the autotuner times the items alone)
-void launch_plan(ffgpu_batch &B, cudaStream_t st, bool timed, bool with_circ = true) {
-    if (with_circ && !B.circ.empty()) launch_circ(B, st);
-    if (!B.items.empty()) launch_items(B, st, timed);
+template <int CLS>
+void launch_class(ffgpu_batch &B, cudaStream_t st, bool timed) {
+    const auto &K = B.cls[CLS];
+    if (K.items.empty()) return;
+    uint32_t *counter = static_cast<uint32_t *>(B.d_counter.ptr) + CLS * 32;
+    FFGPU_CHECK_CUDA(cudaMemsetAsync(counter, 0, 4, st));
+    BatchArgs a;
+    a.items = static_cast<const BatchItem *>(K.d_items.ptr);
+    a.nitems = (uint32_t)K.items.size();
+    a.codes = static_cast<const BatchCode *>(B.d_codes.ptr);
+    a.counter = counter;
+    a.rs_scratch = B.d_rs_scratch.ptr
+                       ? static_cast<uint8_t *>(B.d_rs_scratch.ptr) + K.scratch_cta0 * kBatchThreads * kDecodeScratchBytes
+                       : nullptr;
+    a.ws_words = K.ws_words;
+    if (timed) {
+        KernelTimer kt_timer(CLS < kClsRsi16 ? "batch_kernel_rs256" : "batch_kernel_rsi16", st);
+        batch_kernel<CLS><<<K.grid, kBatchThreads, K.smem, st>>>(a);
+    } else {
+        batch_kernel<CLS><<<K.grid, kBatchThreads, K.smem, st>>>(a);
+    }
+    check_launch("batch_kernel");
 }
 
-void launch_items(ffgpu_batch &B, cudaStream_t st, bool timed) {
-    FFGPU_CHECK_CUDA(cudaMemsetAsync(B.d_counter.ptr, 0, 4, st));
-    BatchArgs a;
-    a.items = static_cast<const BatchItem *>(B.d_items.ptr);
-    a.nitems = (uint32_t)B.items.size();
-    a.codes = static_cast<const BatchCode *>(B.d_codes.ptr);
-    a.counter = static_cast<uint32_t *>(B.d_counter.ptr);
-    a.rs_scratch = static_cast<uint8_t *>(B.d_rs_scratch.ptr);
-    a.ws_words = B.ws_words;
-    if (timed) {
-        KernelTimer kt_timer("batch_kernel", st);
-        batch_kernel<<<B.grid, kBatchThreads, B.smem, st>>>(a);
-        check_launch("batch_kernel");
-    } else {
-        batch_kernel<<<B.grid, kBatchThreads, B.smem, st>>>(a);
-        check_launch("batch_kernel");
+// which: bit k the items of class k, bit 4 the CIRC16 chain (the autotuner
+// times the RS256 classes and the RSi16 class apart)
+constexpr int kRunRs256 = 7, kRunRsi16 = 8, kRunCirc = 16, kRunAll = 31;
+// The class launches run side by side (class k > 0 on side stream k, forked
+// from and joined back into st), so that one class's tail overlaps the
+// others' work.
+void launch_plan(ffgpu_batch &B, cudaStream_t st, bool timed, int which = kRunAll) {
+    if ((which & kRunCirc) && !B.circ.empty()) launch_circ(B, st);
+    int run[kClasses], n = 0;
+    for (int k = 0; k < kClasses; ++k)
+        if ((which & (1 << k)) && !B.cls[k].items.empty()) run[n++] = k;
+    if (!n) return;
+    if (n > 1) {
+        if (!B.side[1]) {
+            for (int k = 1; k < kClasses; ++k)
+                FFGPU_CHECK_CUDA(cudaStreamCreateWithFlags(&B.side[k], cudaStreamNonBlocking));
+            FFGPU_CHECK_CUDA(cudaEventCreateWithFlags(&B.ev_fork, cudaEventDisableTiming));
+            for (int k = 1; k < kClasses; ++k)
+                FFGPU_CHECK_CUDA(cudaEventCreateWithFlags(&B.ev_join[k], cudaEventDisableTiming));
+        }
+        FFGPU_CHECK_CUDA(cudaEventRecord(B.ev_fork, st));
     }
+    for (int i = 0; i < n; ++i) {
+        const int k = run[i];
+        cudaStream_t s = i == 0 ? st : B.side[i];
+        if (i > 0) FFGPU_CHECK_CUDA(cudaStreamWaitEvent(s, B.ev_fork, 0));
+        switch (k) {
+            case 0: launch_class<0>(B, s, timed); break;
+            case 1: launch_class<1>(B, s, timed); break;
+            case 2: launch_class<2>(B, s, timed); break;
+            default: launch_class<kClsRsi16>(B, s, timed); break;
+        }
+        if (i > 0) FFGPU_CHECK_CUDA(cudaEventRecord(B.ev_join[i], s));
+    }
+    for (int i = 1; i < n; ++i) FFGPU_CHECK_CUDA(cudaStreamWaitEvent(st, B.ev_join[i], 0));
 }
 
 // RS256 / RSi16 decode requests are repaired in place: save / restore them
@@ -522,6 +616,10 @@ void copy_regions(ffgpu_batch &B, const std::vector<Region> &rs, bool save, cuda
     }
 }
 
+// Times candidate schedules of each item class on the batch itself (the
+// decode inputs restored before every run) and keeps the fastest: RS256
+// blocks per item x CTAs per SM for the RS256 launch, RSi16 blocks per item x
+// CTAs per SM for the RSi16 launch.
 void autotune(ffgpu_batch &B, cudaStream_t st) {
     const auto regions = decode_regions(B);
     size_t total = 0;
@@ -531,36 +629,55 @@ void autotune(ffgpu_batch &B, cudaStream_t st) {
     cudaEvent_t e0, e1;
     FFGPU_CHECK_CUDA(cudaEventCreate(&e0));
     FFGPU_CHECK_CUDA(cudaEventCreate(&e1));
-    float best = 1e30f;
-    int bt_rs = 512, bt_rsi = 8, bt_cta = 0;
+    auto trial = [&](int which) {
+        float ms = 0.f;
+        for (int rep = 0; rep < 2; ++rep) {  // the first run warms up
+            copy_regions(B, regions, false, st);
+            FFGPU_CHECK_CUDA(cudaEventRecord(e0, st));
+            launch_plan(B, st, false, which);
+            FFGPU_CHECK_CUDA(cudaEventRecord(e1, st));
+            FFGPU_CHECK_CUDA(cudaEventSynchronize(e1));
+            FFGPU_CHECK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        }
+        return ms;
+    };
     const int tiles_rs[] = {128, 512, 2048};
     const int tiles_rsi[] = {2, 8, 32};
-    const int ctas[] = {1, 2, 0};
-    for (int trs : tiles_rs)
-        for (int tri : tiles_rsi)
+    const int ctas[] = {1, 2, 4, 0};
+    int bt_rs = B.tile_rs, bt_rsi = B.tile_rsi, bc_rs = B.ctas_rs, bc_rsi = B.ctas_rsi;
+    bool any_rs = false;
+    for (int k = 0; k < kClsRsi16; ++k) any_rs |= !B.cls[k].items.empty();
+    if (any_rs) {
+        float best = 1e30f;
+        for (int t : tiles_rs)
             for (int cps : ctas) {
-                build_plan(B, trs, tri, cps);
-                float ms = 0.f;
-                for (int rep = 0; rep < 2; ++rep) {  // the first run warms up
-                    copy_regions(B, regions, false, st);
-                    FFGPU_CHECK_CUDA(cudaEventRecord(e0, st));
-                    launch_plan(B, st, false, false);
-                    FFGPU_CHECK_CUDA(cudaEventRecord(e1, st));
-                    FFGPU_CHECK_CUDA(cudaEventSynchronize(e1));
-                    FFGPU_CHECK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-                }
+                build_plan(B, t, bt_rsi, cps, bc_rsi);
+                const float ms = trial(kRunRs256);
                 if (ms < best) {
                     best = ms;
-                    bt_rs = trs;
-                    bt_rsi = tri;
-                    bt_cta = cps;
+                    bt_rs = t;
+                    bc_rs = cps;
                 }
             }
+    }
+    if (!B.cls[kClsRsi16].items.empty()) {
+        float best = 1e30f;
+        for (int t : tiles_rsi)
+            for (int cps : ctas) {
+                build_plan(B, bt_rs, t, bc_rs, cps);
+                const float ms = trial(kRunRsi16);
+                if (ms < best) {
+                    best = ms;
+                    bt_rsi = t;
+                    bc_rsi = cps;
+                }
+            }
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     copy_regions(B, regions, false, st);
     FFGPU_CHECK_CUDA(cudaStreamSynchronize(st));
-    build_plan(B, bt_rs, bt_rsi, bt_cta);
+    build_plan(B, bt_rs, bt_rsi, bc_rs, bc_rsi);
 }
 
 }  // namespace
@@ -639,7 +756,7 @@ int ffgpu_batch_plan(ffgpu_batch *b, int autotune_on, void *stream) {
         if (autotune_on)
             autotune(*b, st);
         else
-            build_plan(*b, b->tile_rs, b->tile_rsi, b->ctas_per_sm);
+            build_plan(*b, b->tile_rs, b->tile_rsi, b->ctas_rs, b->ctas_rsi);
     });
 }
 
@@ -647,7 +764,7 @@ int ffgpu_batch_capture(ffgpu_batch *b, void *stream) {
     return guarded([&] {
         FFGPU_REQUIRE(b, "batch is NULL");
         std::lock_guard<std::mutex> lk(b->mu);
-        if (!b->planned) build_plan(*b, b->tile_rs, b->tile_rsi, b->ctas_per_sm);
+        if (!b->planned) build_plan(*b, b->tile_rs, b->tile_rsi, b->ctas_rs, b->ctas_rsi);
         b->drop_graph();
         cudaStream_t st = (cudaStream_t)stream;
         cudaStream_t cap = st;
@@ -692,7 +809,7 @@ int ffgpu_batch_launch(ffgpu_batch *b, void *stream) {
             launched(b->graph_kernels);
             return;
         }
-        if (!b->planned) build_plan(*b, b->tile_rs, b->tile_rsi, b->ctas_per_sm);
+        if (!b->planned) build_plan(*b, b->tile_rs, b->tile_rsi, b->ctas_rs, b->ctas_rsi);
         launch_plan(*b, st, true);
     });
 }
@@ -703,9 +820,19 @@ int ffgpu_batch_info(const ffgpu_batch *b, int *tile_rs256, int *tile_rsi16, int
         FFGPU_REQUIRE(b, "batch is NULL");
         if (tile_rs256) *tile_rs256 = b->tile_rs;
         if (tile_rsi16) *tile_rsi16 = b->tile_rsi;
-        if (ctas_per_sm) *ctas_per_sm = b->ctas_per_sm;
-        if (items) *items = b->items.size();
-        if (grid) *grid = b->grid;
+        // the first RS256 launch's CTAs per SM (the RSi16 launch's when there
+        // are no RS256 items); items and grids of all launches together
+        int k = 0;
+        while (k < kClsRsi16 && b->cls[k].items.empty()) ++k;
+        size_t n = 0;
+        unsigned g = 0;
+        for (const auto &K : b->cls) {
+            n += K.items.size();
+            g += K.items.empty() ? 0 : K.grid;
+        }
+        if (ctas_per_sm) *ctas_per_sm = b->cls[k].per_sm;
+        if (items) *items = n;
+        if (grid) *grid = g;
     });
 }
 

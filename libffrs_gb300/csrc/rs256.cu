@@ -42,8 +42,10 @@ __global__ void __launch_bounds__(128) rs256_encode_table_kernel(const uint8_t *
                         parity + (first + threadIdx.x) * (size_t)ecc, ecc);
 }
 
-// Per-thread decode scratch in global memory, interleaved across the threads
-// of the launch so that lock-step accesses of a warp coalesce.
+// Per-thread decode scratch, interleaved across threads so that lock-step
+// accesses of a warp fall on consecutive bytes: in shared memory after the
+// tables (gscratch == NULL, kDecodeScratchCols columns of ecc bytes for the
+// CTA's threads), else in global memory (256-byte columns across the launch).
 template <int W>
 __global__ void __launch_bounds__(128) rs256_decode_table_kernel(uint8_t *__restrict__ data,
                                                                  uint8_t *__restrict__ parity, size_t nblocks,
@@ -63,7 +65,9 @@ __global__ void __launch_bounds__(128) rs256_decode_table_kernel(uint8_t *__rest
     __syncthreads();
     const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const size_t nthreads = (size_t)gridDim.x * blockDim.x;
-    const DecodeScratchG sc(gscratch, tid, nthreads);
+    const DecodeScratchG sc = gscratch ? DecodeScratchG(gscratch, tid, nthreads)
+                                       : DecodeScratchG(reinterpret_cast<uint8_t *>(lg + 256), threadIdx.x,
+                                                        blockDim.x, ecc);
     for (size_t blk = tid; blk < nblocks; blk += nthreads)
         decode_one<W>(data + blk * (size_t)msg_len, parity + blk * (size_t)ecc, msg_len, ecc, s_lut, ex, lg, sc,
                       status ? status + blk : nullptr, synds_out ? synds_out + blk * (size_t)ecc : nullptr);
@@ -191,7 +195,10 @@ template <int W>
 static void launch_decode_table(const Rs256Code &c, uint8_t *data, uint8_t *parity, size_t nblocks, int msg_len,
                                 uint8_t *status, uint8_t *synds, cudaStream_t st) {
     const unsigned threads = 128;
-    const size_t smem = (size_t)256 * W * 4 + 768;
+    const size_t tables = (size_t)256 * W * 4 + 768;
+    const size_t sm_scratch = (size_t)kDecodeScratchCols * c.ecc * threads;
+    const bool in_smem = tables + sm_scratch <= 100 * 1024;  // ecc <= 64
+    const size_t smem = tables + (in_smem ? sm_scratch : 0);
     static bool attr = false;
     if (!attr) {
         FFGPU_CHECK_CUDA(cudaFuncSetAttribute(rs256_decode_table_kernel<W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -203,13 +210,13 @@ static void launch_decode_table(const Rs256Code &c, uint8_t *data, uint8_t *pari
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const size_t grid = std::min<size_t>(grid_for(nblocks, threads), (size_t)(sms > 0 ? sms : 132) * 8);
     void *scratch = nullptr;
-    FFGPU_CHECK_CUDA(cudaMallocAsync(&scratch, grid * threads * kDecodeScratchBytes, st));
+    if (!in_smem) FFGPU_CHECK_CUDA(cudaMallocAsync(&scratch, grid * threads * kDecodeScratchBytes, st));
     KernelTimer kt_timer("rs256_decode_table_kernel", st);
     rs256_decode_table_kernel<W><<<(unsigned)grid, threads, smem, st>>>(data, parity, nblocks, msg_len, c.d_lut,
                                                                         c.d_exp512, c.d_log256, c.ecc, status, synds,
                                                                         (uint8_t *)scratch);
     cudaError_t le = cudaGetLastError();
-    cudaFreeAsync(scratch, st);
+    if (scratch) cudaFreeAsync(scratch, st);
     if (le != cudaSuccess) throw Error(FFGPU_ECUDA, std::string("rs256_decode_table_kernel: ") + cudaGetErrorString(le));
     launched();
 }

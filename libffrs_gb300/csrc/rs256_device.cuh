@@ -64,87 +64,109 @@ struct ScratchBytes {
     __device__ __forceinline__ uint8_t &operator[](int k) const { return base[(size_t)k * stride]; }
     __device__ __forceinline__ ScratchBytes operator+(int k) const { return {base + (size_t)k * stride, stride}; }
 };
+
+// Per-thread decode scratch: five byte columns of `cols` bytes (cols >= ecc).
+// Byte k of column c of thread tid sits at g[(c * cols + k) * nthreads + tid],
+// so that the lock-step accesses of a warp fall on consecutive bytes (global
+// memory: one sector; shared memory: no bank conflict).
+//   S: syndromes; A, B, C: the rotating Berlekamp-Massey polynomials (then
+//   the root positions in a free one); R: remainder logs, Chien exponents,
+//   then the evaluator.
 struct DecodeScratchG {
-    ScratchBytes S, lam, prev, tmp, pos, mag, ev;
-    __device__ DecodeScratchG(uint8_t *g, size_t tid, size_t nthreads) {
+    ScratchBytes S, A, B, C, R;
+    __device__ DecodeScratchG(uint8_t *g, size_t tid, size_t nthreads, int cols = 256) {
         uint8_t *b = g + tid;
+        const size_t cs = (size_t)cols * nthreads;
         S = {b, nthreads};
-        lam = {b + 256 * nthreads, nthreads};
-        prev = {b + 512 * nthreads, nthreads};
-        tmp = {b + 768 * nthreads, nthreads};
-        pos = {b + 1024 * nthreads, nthreads};
-        mag = {b + 1280 * nthreads, nthreads};
-        ev = {b + 1536 * nthreads, nthreads};
+        A = {b + cs, nthreads};
+        B = {b + 2 * cs, nthreads};
+        C = {b + 3 * cs, nthreads};
+        R = {b + 4 * cs, nthreads};
     }
 };
-constexpr size_t kDecodeScratchBytes = 2048;
+constexpr int kDecodeScratchCols = 5;
+constexpr size_t kDecodeScratchBytes = 2048;  // per thread at cols = 256
 
-// Syndromes from the remainder: S_j = sum_m R[m] a^{-j(m+1)}.
-template <int W, typename A>
-static __device__ void synds_from_rem(const uint32_t (&rem)[W], int ecc, const uint8_t *ex, const uint8_t *lg, A S) {
-    for (int j = 0; j < ecc; ++j) S[j] = 0;
+// Syndromes from the remainder: S_j = sum_m R[m] a^{-j(m+1)}, j-outer with
+// the exponent of each term stepped by j (no multiplications), the remainder
+// bytes' logs (mod 255) staged in sc.R (255 marks a zero byte).
+template <int W>
+static __device__ void synds_from_rem(const uint32_t (&rem)[W], int ecc, const uint8_t *ex, const uint8_t *lg,
+                                      const DecodeScratchG &sc) {
     for (int m = 0; m < ecc; ++m) {
         const uint32_t r = rem_byte<W>(rem, m);
-        if (!r) continue;
-        const int step = (m + 1) % 255;
-        int e = lg[r] % 255;
-        for (int j = 0; j < ecc; ++j) {
-            S[j] ^= ex[e];
-            e -= step;
-            if (e < 0) e += 255;
+        sc.R[m] = r ? lg[r] % 255 : 255;  // logs may be stored as 1..255
+    }
+    for (int j = 0; j < ecc; ++j) {
+        uint32_t acc = 0;
+        int sub = 0;  // j * (m + 1) mod 255
+        for (int m = 0; m < ecc; ++m) {
+            sub += j;
+            if (sub >= 255) sub -= 255;
+            const uint32_t lr = sc.R[m];
+            const uint32_t v = ex[lr + 255u - (uint32_t)sub];  // lr + 255 - sub <= 510
+            acc ^= lr != 255u ? v : 0u;
         }
+        sc.S[j] = (uint8_t)acc;
     }
 }
 
-// rs_decode::berlekamp_massey (reed_solomon.hpp:655-702); err_poly is
-// right-aligned and reversed: err_poly[ecc-1-i] holds Lambda_i.
-template <typename A>
-static __device__ int rs_bm(A S, int ecc, const uint8_t *ex, const uint8_t *lg, A err_poly, A prev, A temp) {
-    for (int i = 0; i < ecc; ++i) {
-        prev[i] = 0;
-        err_poly[i] = 0;
-    }
-    prev[ecc - 1] = 1;
-    err_poly[ecc - 1] = 1;
-    int errors = 0, m = 1;
+// rs_decode::berlekamp_massey (reed_solomon.hpp:655-702) on normal-order
+// polynomials (A[k] = Lambda_k, degrees below ecc), with the same updates and
+// truncation as the reference's reversed layout.  Loops run over the live
+// degrees only, and the three buffers rotate instead of being copied.
+// Returns the number of errors L; *lam is left on the buffer holding Lambda
+// and *fr on a free one.
+static __device__ int rs_bm(const DecodeScratchG &sc, int ecc, const uint8_t *ex, const uint8_t *lg,
+                            ScratchBytes *lam, ScratchBytes *fr) {
+    ScratchBytes A = sc.A, P = sc.B, T = sc.C;
+    A[0] = 1;
+    P[0] = 1;
+    int degA = 0, degP = 0, L = 0, m = 1;
     uint32_t b = 1;
     for (int n = 0; n < ecc; ++n) {
-        uint32_t d = S[n];
-        for (int i = 1; i < errors + 1; ++i) d ^= gmul(ex, lg, err_poly[ecc - 1 - i], S[n - i]);
+        uint32_t d = sc.S[n];
+        const int top = L < degA ? L : degA;
+        for (int i = 1; i <= top; ++i) d ^= gmul(ex, lg, A[i], sc.S[n - i]);
         if (d == 0) {
-            m = m + 1;
-        } else if (2 * errors <= n) {
-            for (int i = 0; i < ecc; ++i) temp[i] = err_poly[i];
-            const uint32_t s = gdiv(ex, lg, d, b);
-            for (int i = 0; i < ecc; ++i) {
-                const uint32_t p = (i < ecc - m) ? prev[i + m] : 0u;
-                err_poly[i] ^= gmul(ex, lg, s, p);
+            ++m;
+            continue;
+        }
+        const uint32_t s = gdiv(ex, lg, d, b);
+        const int hi = m + degP < ecc - 1 ? m + degP : ecc - 1;
+        const int nd = degA > hi ? degA : hi;
+        if (2 * L <= n) {
+            // T = A + s x^m P; P <- A; A <- T
+            for (int k = 0; k <= nd; ++k) {
+                uint32_t v = k <= degA ? (uint32_t)A[k] : 0u;
+                if (k >= m && k <= hi) v ^= gmul(ex, lg, s, P[k - m]);
+                T[k] = (uint8_t)v;
             }
-            errors = n + 1 - errors;
-            for (int i = 0; i < ecc; ++i) prev[i] = temp[i];
+            const ScratchBytes oldP = P;
+            P = A;
+            A = T;
+            T = oldP;
+            degP = degA;
+            degA = nd;
+            L = n + 1 - L;
             b = d;
             m = 1;
         } else {
-            const uint32_t s = gdiv(ex, lg, d, b);
-            for (int i = 0; i < ecc; ++i) {
-                const uint32_t p = (i < ecc - m) ? prev[i + m] : 0u;
-                err_poly[i] ^= gmul(ex, lg, s, p);
-            }
-            m = m + 1;
+            for (int k = degA + 1; k <= hi; ++k) A[k] = 0;  // stale bytes above the live degree
+            for (int k = m; k <= hi; ++k) A[k] ^= (uint8_t)gmul(ex, lg, s, P[k - m]);
+            degA = nd;
+            ++m;
         }
     }
-    return errors;
-}
-
-template <typename A>
-static __device__ __forceinline__ uint32_t poly_eval(A p, int n, uint32_t x, const uint8_t *ex, const uint8_t *lg) {
-    uint32_t r = 0;
-    for (int i = 0; i < n; ++i) r = gmul(ex, lg, r, x) ^ p[i];
-    return r;
+    // coefficients up to L are read below: clear those above the live degree
+    for (int k = degA + 1; k <= L; ++k) A[k] = 0;
+    *lam = A;
+    *fr = T;
+    return L;
 }
 
 static __device__ void decode_solve(uint8_t *d, uint8_t *p, int msg_len, int ecc, const uint8_t *ex, const uint8_t *lg,
-                             const DecodeScratchG &sc, uint8_t *status);
+                                    const DecodeScratchG &sc, uint8_t *status);
 
 // One block: rs_decode::decode (reed_solomon.hpp:559-595).  Writes the
 // status (1/0) or, when synds_out is set, only the syndromes.
@@ -160,70 +182,102 @@ static __device__ void decode_one(uint8_t *d, uint8_t *p, int msg_len, int ecc, 
 #pragma unroll
     for (int w = 0; w < W; ++w) any |= rem[w];
     if (synds_out) {
-        if (any)
-            synds_from_rem<W>(rem, ecc, ex, lg, sc.S);
-        else
-            for (int j = 0; j < ecc; ++j) sc.S[j] = 0;
-        for (int j = 0; j < ecc; ++j) synds_out[j] = sc.S[j];
+        if (any) {
+            synds_from_rem<W>(rem, ecc, ex, lg, sc);
+            for (int j = 0; j < ecc; ++j) synds_out[j] = sc.S[j];
+        } else {
+            for (int j = 0; j < ecc; ++j) synds_out[j] = 0;
+        }
         return;
     }
     if (!any) {
         *status = 1;
         return;
     }
-    synds_from_rem<W>(rem, ecc, ex, lg, sc.S);
+    synds_from_rem<W>(rem, ecc, ex, lg, sc);
     decode_solve(d, p, msg_len, ecc, ex, lg, sc, status);
 }
 
 // The part of rs_decode::decode after the syndromes (reed_solomon.hpp:568-594),
-// with sc.S holding non-zero syndromes.
+// with sc.S holding non-zero syndromes.  Every decision and every corrected
+// byte is the reference's; only the evaluation order of the (exact) field
+// sums differs.
 static __device__ void decode_solve(uint8_t *d, uint8_t *p, int msg_len, int ecc, const uint8_t *ex, const uint8_t *lg,
                              const DecodeScratchG &sc, uint8_t *status) {
-    const int errors = rs_bm(sc.S, ecc, ex, lg, sc.lam, sc.prev, sc.tmp);
+    ScratchBytes lam, pos;
+    const int errors = rs_bm(sc, ecc, ex, lg, &lam, &pos);
     if (errors > ecc / 2) {
         *status = 0;
         return;
     }
-    const ScratchBytes loc = sc.lam + (ecc - errors - 1);
     const int size = msg_len + ecc;
+    const int npos = size < 256 ? size : 256;
+    // Chien search (rs_roots_eval_lut_pw2, reed_solomon.hpp:511-552): the
+    // zeros of Lambda at x = a^{-i}, i < size, in increasing i, stopping at
+    // errors + 1 roots.  Term k at position i has exponent
+    // log(Lambda_k) - i k (mod 255); eight positions per pass, each term's
+    // exponent kept in sc.R between passes (255: a zero coefficient).
+    for (int k = 0; k <= errors; ++k) {
+        const uint32_t c = lam[k];
+        sc.R[k] = c ? lg[c] % 255 : 255;
+    }
     int roots = 0;
-    for (int i = 0; i < size && i < 256; ++i) {
-        const uint32_t x = ex[(255 - i) % 255];
-        if (poly_eval(loc, errors + 1, x, ex, lg) == 0) sc.pos[roots++] = (uint8_t)i;
-        if (roots > errors) break;
+    for (int i0 = 0; i0 < npos && roots <= errors; i0 += 8) {
+        uint32_t acc[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[j] = 0;
+        for (int k = 0; k <= errors; ++k) {
+            int e = sc.R[k];
+            if (e == 255) continue;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                acc[j] ^= ex[e];
+                e -= k;
+                if (e < 0) e += 255;
+            }
+            sc.R[k] = (uint8_t)e;
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            if (acc[j] == 0 && i0 + j < npos && roots <= errors) pos[roots++] = (uint8_t)(i0 + j);
     }
     if (roots != errors) {
         *status = 0;
         return;
     }
-    // Forney: omega = (S reversed * Lambda) mod x^ecc, highest degree first
-    const int esize = ecc + errors;
-    for (int i = 0; i < esize; ++i) sc.ev[i] = 0;
-    for (int i = 0; i < ecc; ++i)
-        for (int j = 0; j < errors + 1; ++j) sc.ev[i + j] ^= gmul(ex, lg, sc.S[ecc - 1 - i], loc[j]);
-    int begin = errors;
-    while (begin < esize && sc.ev[begin] == 0) ++begin;
-    if (begin >= esize) {
+    // Forney: Omega = (S * Lambda) mod x^ecc (into sc.R), nonzero
+    uint32_t anyo = 0;
+    for (int k = 0; k < ecc; ++k) {
+        uint32_t v = 0;
+        const int top = k < errors ? k : errors;
+        for (int j = 0; j <= top; ++j) v ^= gmul(ex, lg, lam[j], sc.S[k - j]);
+        sc.R[k] = (uint8_t)v;
+        anyo |= v;
+    }
+    if (!anyo) {
         *status = 0;
         return;
     }
-    // formal derivative in place (gf_poly_deriv_pw2, galois.hpp:725-734)
-    const ScratchBytes lp = loc;
-    const int psize = errors + 1;
-    for (int i = 1; i < psize; ++i) lp[psize - i] = (i & 1) ? lp[psize - i - 1] : 0;
+    // magnitudes X * Omega(X^-1) / Lambda'(X^-1) (gf_poly_deriv_pw2,
+    // galois.hpp:725-734: Lambda'(x) = sum over odd k of Lambda_k x^(k-1)).
+    // They depend on the syndromes and Lambda only, and nothing fails from
+    // here on, so each is applied as soon as it is known.
     for (int i = 0; i < errors; ++i) {
-        const uint32_t xi = ex[sc.pos[i]];
+        const uint32_t xi = ex[pos[i]];
         const uint32_t xinv = ginv(ex, lg, xi);
-        const uint32_t num = poly_eval(sc.ev + begin, esize - begin, xinv, ex, lg);
-        const uint32_t den = poly_eval(lp + 1, errors, xinv, ex, lg);
-        sc.mag[i] = (uint8_t)gmul(ex, lg, xi, gdiv(ex, lg, num, den));
-    }
-    for (int i = 0; i < errors; ++i) {
-        const int pos = size - 1 - sc.pos[i];
-        if (pos < msg_len)
-            d[pos] ^= sc.mag[i];
+        uint32_t num = 0;
+        for (int k = ecc - 1; k >= 0; --k) num = gmul(ex, lg, num, xinv) ^ sc.R[k];
+        uint32_t den = 0;
+        for (int k = errors - ((errors & 1) ? 0 : 1); k >= 1; k -= 2) {
+            den = gmul(ex, lg, den, xinv);
+            den = gmul(ex, lg, den, xinv) ^ lam[k];
+        }
+        const uint8_t mag = (uint8_t)gmul(ex, lg, xi, gdiv(ex, lg, num, den));
+        const int q = size - 1 - pos[i];
+        if (q < msg_len)
+            d[q] ^= mag;
         else
-            p[pos - msg_len] ^= sc.mag[i];
+            p[q - msg_len] ^= mag;
     }
     *status = 1;
 }
