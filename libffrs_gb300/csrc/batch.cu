@@ -55,7 +55,8 @@ struct BatchCode {
 
 struct BatchItem {
     uint8_t kind;
-    uint8_t pad[3];
+    uint8_t lane_bm;  // RSi16 repair by 32-block batches with a Berlekamp-Massey per lane
+    uint8_t pad[2];
     uint32_t code;
     uint32_t nblocks;
     int32_t msg_len;
@@ -116,31 +117,63 @@ __device__ void rs256_dec_item(const BatchCode &c, const BatchItem &it, uint32_t
 }
 
 
+// A whole RSi16 item on the calling warp: repairs by 32-block batches with a
+// Berlekamp-Massey per lane (ecc 32, 64) or block by block, encodes two
+// blocks per pass on registers (ecc 32..128), 32/ecc blocks per pass on the
+// sub-warp transforms (ecc 2..16) or block by block.
 template <int EPL>
 __device__ void rsi16_item_t(const Rsi16Dev &c, const BatchItem &it, uint32_t *ws, bool decode) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
     const BlockView v = contiguous_view(it.msg, true, c.message_len, it.par, true, c.ecc);
+    const size_t nb = it.nblocks;
     RegTw<EPL ? EPL : 1> tw;
     if constexpr (EPL > 0) reg_twiddles<EPL>(c, lane, tw);
-    for (uint32_t b = warp; b < it.nblocks; b += kBatchWarps) {
-        if (decode) {
+    if (decode) {
+        if constexpr (EPL == 1 || EPL == 2) {
+            if (it.lane_bm) {
+                unsigned long long nf = 0, nm = 0;
+                for (size_t base = 0; base < nb; base += 32)
+                    rsi16_repair32<EPL>(c, v, base, (int)min((size_t)32, nb - base), it.status, nullptr, tw, lane, ws,
+                                        ws, nf, nm);
+                return;
+            }
+        }
+        for (size_t b = 0; b < nb; ++b)
             if (!rsi16_repair_bm_block_t<EPL>(c, v, b, ws, it.status, tw, lane))
                 rsi16_repair_block(c, v, b, ws, it.status, lane);
-        } else if constexpr (EPL > 0) {
-            rsi16_encode_block_reg<EPL>(c, v, b, tw, lane);
-        } else {
-            rsi16_encode_block(c, v, b, ws, lane);
-        }
+    } else if constexpr (EPL > 0) {
+        for (size_t b = 0; b < nb; b += 2) rsi16_encode_pair_reg<EPL>(c, v, b, b + 1 < nb ? b + 1 : b, tw, lane);
+    } else {
+        for (size_t b = 0; b < nb; ++b) rsi16_encode_block(c, v, b, ws, lane);
     }
+}
+
+template <int N>
+__device__ void rsi16_encode_item_sub(const Rsi16Dev &c, const BatchItem &it) {
+    const int lane = threadIdx.x & 31;
+    const BlockView v = contiguous_view(it.msg, true, c.message_len, it.par, true, c.ecc);
+    SubTw<N> tw;
+    sub_twiddles<N>(c, lane % N, tw);
+    for (size_t b0 = 0; b0 < it.nblocks; b0 += 32 / N) rsi16_encode_sub_pass<N>(c, v, b0, it.nblocks, tw, lane);
 }
 
 __device__ void rsi16_item(const Rsi16Dev &c, const BatchItem &it, uint32_t *ws, bool decode) {
     switch (c.ecc) {
-        case 32: rsi16_item_t<1>(c, it, ws, decode); break;
-        case 64: rsi16_item_t<2>(c, it, ws, decode); break;
-        case 128: rsi16_item_t<4>(c, it, ws, decode); break;
-        default: rsi16_item_t<0>(c, it, ws, decode); break;
+        case 32: rsi16_item_t<1>(c, it, ws, decode); return;
+        case 64: rsi16_item_t<2>(c, it, ws, decode); return;
+        case 128: rsi16_item_t<4>(c, it, ws, decode); return;
+        default: break;
     }
+    if (!decode) {
+        switch (c.ecc) {
+            case 2: rsi16_encode_item_sub<2>(c, it); return;
+            case 4: rsi16_encode_item_sub<4>(c, it); return;
+            case 8: rsi16_encode_item_sub<8>(c, it); return;
+            case 16: rsi16_encode_item_sub<16>(c, it); return;
+            default: break;
+        }
+    }
+    rsi16_item_t<0>(c, it, ws, decode);
 }
 
 // Byte ranges copied one CTA per range (ranges of at most kSegBytes): the
@@ -193,10 +226,22 @@ __host__ __device__ constexpr int rs256_class(int W) { return W <= 4 ? 0 : (W <=
 template <int CLS>
 __global__ void __launch_bounds__(kBatchThreads) batch_kernel(BatchArgs a) {
     extern __shared__ __align__(16) uint32_t sm[];
+    if constexpr (CLS == kClsRsi16) {
+        // RSi16 items are warp-sized: every warp pulls whole items
+        const int lane = threadIdx.x & 31;
+        uint32_t *wws = sm + (size_t)(threadIdx.x >> 5) * a.ws_words;
+        for (;;) {
+            uint32_t idx = 0;
+            if (lane == 0) idx = atomicAdd(a.counter, 1u);
+            idx = __shfl_sync(0xffffffffu, idx, 0);
+            if (idx >= a.nitems) break;
+            const BatchItem it = a.items[idx];
+            rsi16_item(a.codes[it.code].rsi, it, wws, it.kind == BK_RSI16_DEC);
+        }
+        return;
+    }
     __shared__ uint32_t s_idx;
-    uint8_t *rs_scratch =
-        CLS < kClsRsi16 ? a.rs_scratch + (size_t)blockIdx.x * kBatchThreads * kDecodeScratchBytes : nullptr;
-    uint32_t *ws = sm + (size_t)(threadIdx.x >> 5) * a.ws_words;
+    uint8_t *rs_scratch = a.rs_scratch + (size_t)blockIdx.x * kBatchThreads * kDecodeScratchBytes;
     for (;;) {
         __syncthreads();  // every thread has read s_idx and finished the last item
         if (threadIdx.x == 0) s_idx = atomicAdd(a.counter, 1u);
@@ -205,14 +250,10 @@ __global__ void __launch_bounds__(kBatchThreads) batch_kernel(BatchArgs a) {
         if (idx >= a.nitems) break;
         const BatchItem it = a.items[idx];
         const BatchCode &c = a.codes[it.code];
-        if constexpr (CLS < kClsRsi16) {
-            if (it.kind == BK_RS256_ENC) {
-                FFGPU_BATCH_W_CLS(CLS, c.W, (rs256_enc_item<w_>(c, it, sm)));
-            } else {
-                FFGPU_BATCH_W_CLS(CLS, c.W, (rs256_dec_item<w_>(c, it, sm, rs_scratch)));
-            }
+        if (it.kind == BK_RS256_ENC) {
+            FFGPU_BATCH_W_CLS(CLS, c.W, (rs256_enc_item<w_>(c, it, sm)));
         } else {
-            rsi16_item(c.rsi, it, ws, it.kind == BK_RSI16_DEC);
+            FFGPU_BATCH_W_CLS(CLS, c.W, (rs256_dec_item<w_>(c, it, sm, rs_scratch)));
         }
     }
 }
@@ -464,17 +505,24 @@ void build_plan(ffgpu_batch &B, int tile_rs, int tile_rsi, int ctas_rs, int ctas
             const Rsi16Code &c = *static_cast<const ffgpu_rsi16 *>(r.handle)->code;
             bc.rsi = c.dev;
             const uint32_t ci = code_index(B, r.handle, bc);
-            for (size_t b0 = 0; b0 < r.nblocks; b0 += (size_t)tile_rsi) {
+            // repairs of 16 blocks or more with a Berlekamp-Massey per lane go
+            // by 32-block batches (fewer would leave most lanes idle)
+            const bool lane_bm = r.kind == BK_RSI16_DEC && (c.ecc == 32 || c.ecc == 64) && r.nblocks >= 16;
+            const size_t tile = lane_bm ? 32 : (size_t)tile_rsi;
+            for (size_t b0 = 0; b0 < r.nblocks; b0 += tile) {
                 BatchItem it{};
                 it.kind = r.kind;
                 it.code = ci;
-                it.nblocks = (uint32_t)std::min<size_t>((size_t)tile_rsi, r.nblocks - b0);
+                it.nblocks = (uint32_t)std::min<size_t>(tile, r.nblocks - b0);
+                it.lane_bm = lane_bm && it.nblocks >= 16;
                 it.msg = static_cast<uint16_t *>(r.a) + b0 * c.message_len;
                 it.par = static_cast<uint16_t *>(r.b) + b0 * c.ecc;
                 it.status = r.status ? r.status + b0 : nullptr;
                 K1.items.push_back(it);
             }
             ws_words = std::max(ws_words, r.kind == BK_RSI16_DEC ? c.dev.temp_len + 1 : (uint32_t)c.block_len);
+            if (lane_bm)  // the batch's columns (the mirror overlays them)
+                ws_words = std::max(ws_words, (uint32_t)((c.ecc + c.ecc / 2 + 1) * kColStride + 3 * c.ecc + 4));
         }
     }
     plan_circ(B);

@@ -205,21 +205,12 @@ __global__ void rsi16_synd_warp_kernel(Rsi16Dev c, BlockView v, size_t nblocks, 
 template <int N>
 __global__ void __launch_bounds__(128) rsi16_encode_sub_kernel(Rsi16Dev c, BlockView v, size_t nblocks) {
     constexpr int G = 32 / N;
-    const int lane = threadIdx.x & 31, e = lane % N, s = lane / N;
+    const int lane = threadIdx.x & 31;
     SubTw<N> tw;
-    sub_twiddles<N>(c, e, tw);
+    sub_twiddles<N>(c, lane % N, tw);
     const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const size_t nw = ((size_t)gridDim.x * blockDim.x) >> 5;
-    for (size_t b0 = warp * G; b0 < nblocks; b0 += nw * G) {
-        const size_t b = b0 + s;
-        const bool act = b < nblocks;
-        uint32_t a = sub_pntt<N>(c, v, act ? b : b0, act, c.pntt_blocks - 1, false, tw, e);
-        a = sub_gs<N>(fmul(a, c.ecc_mix[e]), tw, e);
-        if (act) {
-            const size_t pb = (b / v.group) * v.par_gstride + (b % v.group) * v.par_bstride;
-            st_word(v.par, v.par16, pb + (size_t)e * v.par_estride, a);
-        }
-    }
+    for (size_t b0 = warp * G; b0 < nblocks; b0 += nw * G) rsi16_encode_sub_pass<N>(c, v, b0, nblocks, tw, lane);
 }
 
 // syndromes, ecc = N < 32 (output layout as rsi16_synd_warp_kernel)
@@ -296,6 +287,7 @@ __global__ void rsi16_repair_warp_kernel(Rsi16Dev c, BlockView v, size_t nblocks
 // batches.  The warp workspace in shared memory is the batch's syndrome
 // columns [ecc][33], locator columns [ecc/2 + 1][33] and the finishing scratch
 // (two root lists of ecc + 1 words, Omega and C').
+
 template <int EPL>
 __global__ void __launch_bounds__(128, 4) rsi16_repair_batch_kernel(Rsi16Dev c, BlockView v, size_t nblocks,
                                                                  uint8_t *status, const uint8_t *active,
@@ -305,9 +297,6 @@ __global__ void __launch_bounds__(128, 4) rsi16_repair_batch_kernel(Rsi16Dev c, 
     WarpCtx w = warp_ctx(nullptr, ws_words);
     RegTw<EPL> tw;
     reg_twiddles<EPL>(c, w.lane, tw);
-    uint32_t *Ssm = w.ws;
-    uint32_t *Csm = Ssm + 32 * EPL * kColStride;
-    uint32_t *fin = Csm + (T + 1) * kColStride;
     uint32_t *mws = mirror_ws + (size_t)w.warp_global * mirror_words;
     const size_t nbatches = (nblocks + 31) / 32;
     unsigned long long nfast = 0, nmirror = 0;
@@ -317,86 +306,8 @@ __global__ void __launch_bounds__(128, 4) rsi16_repair_batch_kernel(Rsi16Dev c, 
         bi = __shfl_sync(0xffffffffu, bi, 0);
         if (bi >= nbatches) break;
         const size_t base = (size_t)bi * 32;
-        const int nb = (int)min((size_t)32, nblocks - base);
-        uint32_t live = 0u, nz = 0u;
-        for (int j = 0; j < nb; ++j)
-            if (!active || active[base + j]) live |= 1u << j;
-        // syndromes two blocks at a time (a lone last block pairs with itself)
-        for (uint32_t todo = live; todo;) {
-            const int j0 = __ffs(todo) - 1;
-            todo &= todo - 1;
-            const int j1 = todo ? __ffs(todo) - 1 : j0;
-            todo &= todo - 1;
-            uint32_t s0[EPL], s1[EPL];
-            reg_pntt2<EPL>(c, v, base + j0, base + j1, c.pntt_blocks, true, tw, w.lane, s0, s1);
-            bool any0 = false, any1 = false;
-#pragma unroll
-            for (int h = 0; h < EPL; ++h) {
-                Ssm[(w.lane * EPL + h) * kColStride + j0] = s0[h];
-                Ssm[(w.lane * EPL + h) * kColStride + j1] = s1[h];
-                any0 |= s0[h] != 0;
-                any1 |= s1[h] != 0;
-            }
-            if (__any_sync(0xffffffffu, any0)) nz |= 1u << j0;
-            if (__any_sync(0xffffffffu, any1)) nz |= 1u << j1;
-        }
-        __syncwarp();
-        uint32_t L = 0;
-        if ((nz >> w.lane) & 1u) {
-            uint32_t C[T + 1];
-            L = rsi16_bm_lane<T>(Ssm + w.lane, c.inv_tab, c.ecc, C);
-#pragma unroll
-            for (int i = 0; i <= T; ++i) Csm[i * kColStride + w.lane] = C[i];
-        }
-        __syncwarp();
-        // blocks whose locator passes the checks get their roots searched in
-        // pairs; the others (and those whose root count is not L) go to the
-        // mirror
-        uint32_t cand = 0u, mirror = 0u;
-        for (int j = 0; j < nb; ++j) {
-            if (!((live >> j) & 1u)) continue;
-            const size_t b = base + j;
-            if (!((nz >> j) & 1u)) {
-                if (w.lane == 0) status[b] = FFGPU_NO_ERRORS;
-                ++nfast;
-                continue;
-            }
-            const uint32_t Lj = __shfl_sync(0xffffffffu, L, j);
-            if (rsi16_locator_ok(c, Csm + j, Lj, w.lane))
-                cand |= 1u << j;
-            else
-                mirror |= 1u << j;
-        }
-        uint32_t *TA = fin, *TB = fin + (c.ecc + 1), *Om = TB + (c.ecc + 1), *D = Om + (T + 1);
-        for (uint32_t todo = cand; todo;) {
-            const int ja = __ffs(todo) - 1;
-            todo &= todo - 1;
-            const int jb = todo ? __ffs(todo) - 1 : ja;
-            todo &= todo - 1;
-            const uint32_t La = __shfl_sync(0xffffffffu, L, ja), Lb = __shfl_sync(0xffffffffu, L, jb);
-            uint32_t na, nbr;
-            rsi16_roots_pair<EPL>(c, Csm + ja, La, Csm + jb, Lb, TA, TB, tw, w.lane, na, nbr);
-            if (na == La) {
-                rsi16_forney_apply(c, v, base + ja, Ssm + ja, Csm + ja, La, TA, Om, D, status, w.lane);
-                ++nfast;
-            } else {
-                mirror |= 1u << ja;
-            }
-            if (jb != ja) {
-                if (nbr == Lb) {
-                    rsi16_forney_apply(c, v, base + jb, Ssm + jb, Csm + jb, Lb, TB, Om, D, status, w.lane);
-                    ++nfast;
-                } else {
-                    mirror |= 1u << jb;
-                }
-            }
-        }
-        for (uint32_t todo = mirror; todo; todo &= todo - 1) {
-            __syncwarp();
-            rsi16_repair_block(c, v, base + (__ffs(todo) - 1), mws, status, w.lane);
-            ++nmirror;
-        }
-        __syncwarp();  // the batch's columns are read before the next batch writes them
+        rsi16_repair32<EPL>(c, v, base, (int)min((size_t)32, nblocks - base), status, active, tw, w.lane, w.ws, mws,
+                            nfast, nmirror);
     }
     if (w.lane == 0 && (nfast | nmirror)) {
         atomicAdd(&g_repair_fast_blocks, nfast);

@@ -786,6 +786,22 @@ static __device__ __forceinline__ uint32_t sub_pntt(const Rsi16Dev &c, const Blo
     return acc;
 }
 
+// parity of the 32 / N blocks b0 .. b0 + 32/N - 1 (those below nblocks) on
+// the sub-warp transforms
+template <int N>
+static __device__ __forceinline__ void rsi16_encode_sub_pass(const Rsi16Dev &c, const BlockView &v, size_t b0,
+                                                             size_t nblocks, const SubTw<N> &tw, int lane) {
+    const int e = lane % N, s = lane / N;
+    const size_t b = b0 + s;
+    const bool act = b < nblocks;
+    uint32_t a = sub_pntt<N>(c, v, act ? b : b0, act, c.pntt_blocks - 1, false, tw, e);
+    a = sub_gs<N>(fmul(a, c.ecc_mix[e]), tw, e);
+    if (act) {
+        const size_t pb = (b / v.group) * v.par_gstride + (b % v.group) * v.par_bstride;
+        st_word(v.par, v.par16, pb + (size_t)e * v.par_estride, a);
+    }
+}
+
 // ---------------------------------------------------------------- one block per warp
 
 // parity of block b (ws: block_len words)
@@ -1246,6 +1262,100 @@ static __device__ __noinline__ void rsi16_repair_known_block(const Rsi16Dev &c, 
         if (status) status[b] = FFGPU_REPAIR_OK;
     }
     __syncwarp();
+}
+
+// One batch of up to 32 blocks (base .. base+nb-1) on one warp: syndromes two
+// blocks per pass into the columns of ws, a Berlekamp-Massey per lane, roots
+// and Forney per pair; blocks the bounded-distance path does not accept go
+// to the step-for-step mirror on mws (which may overlay ws: the columns are
+// dead by then).
+template <int EPL>
+static __device__ __forceinline__ void rsi16_repair32(const Rsi16Dev &c, const BlockView &v, size_t base, int nb, uint8_t *status,
+                               const uint8_t *active, const RegTw<EPL> &tw, int lane, uint32_t *ws, uint32_t *mws,
+                               unsigned long long &nfast, unsigned long long &nmirror) {
+    constexpr int T = 16 * EPL;
+    uint32_t *Ssm = ws;
+    uint32_t *Csm = Ssm + 32 * EPL * kColStride;
+    uint32_t *fin = Csm + (T + 1) * kColStride;
+    uint32_t live = 0u, nz = 0u;
+    for (int j = 0; j < nb; ++j)
+        if (!active || active[base + j]) live |= 1u << j;
+    // syndromes two blocks at a time (a lone last block pairs with itself)
+    for (uint32_t todo = live; todo;) {
+        const int j0 = __ffs(todo) - 1;
+        todo &= todo - 1;
+        const int j1 = todo ? __ffs(todo) - 1 : j0;
+        todo &= todo - 1;
+        uint32_t s0[EPL], s1[EPL];
+        reg_pntt2<EPL>(c, v, base + j0, base + j1, c.pntt_blocks, true, tw, lane, s0, s1);
+        bool any0 = false, any1 = false;
+#pragma unroll
+        for (int h = 0; h < EPL; ++h) {
+            Ssm[(lane * EPL + h) * kColStride + j0] = s0[h];
+            Ssm[(lane * EPL + h) * kColStride + j1] = s1[h];
+            any0 |= s0[h] != 0;
+            any1 |= s1[h] != 0;
+        }
+        if (__any_sync(0xffffffffu, any0)) nz |= 1u << j0;
+        if (__any_sync(0xffffffffu, any1)) nz |= 1u << j1;
+    }
+    __syncwarp();
+    uint32_t L = 0;
+    if ((nz >> lane) & 1u) {
+        uint32_t C[T + 1];
+        L = rsi16_bm_lane<T>(Ssm + lane, c.inv_tab, c.ecc, C);
+#pragma unroll
+        for (int i = 0; i <= T; ++i) Csm[i * kColStride + lane] = C[i];
+    }
+    __syncwarp();
+    // blocks whose locator passes the checks get their roots searched in
+    // pairs; the others (and those whose root count is not L) go to the
+    // mirror
+    uint32_t cand = 0u, mirror = 0u;
+    for (int j = 0; j < nb; ++j) {
+        if (!((live >> j) & 1u)) continue;
+        const size_t b = base + j;
+        if (!((nz >> j) & 1u)) {
+            if (lane == 0) status[b] = FFGPU_NO_ERRORS;
+            ++nfast;
+            continue;
+        }
+        const uint32_t Lj = __shfl_sync(0xffffffffu, L, j);
+        if (rsi16_locator_ok(c, Csm + j, Lj, lane))
+            cand |= 1u << j;
+        else
+            mirror |= 1u << j;
+    }
+    uint32_t *TA = fin, *TB = fin + (c.ecc + 1), *Om = TB + (c.ecc + 1), *D = Om + (T + 1);
+    for (uint32_t todo = cand; todo;) {
+        const int ja = __ffs(todo) - 1;
+        todo &= todo - 1;
+        const int jb = todo ? __ffs(todo) - 1 : ja;
+        todo &= todo - 1;
+        const uint32_t La = __shfl_sync(0xffffffffu, L, ja), Lb = __shfl_sync(0xffffffffu, L, jb);
+        uint32_t na, nbr;
+        rsi16_roots_pair<EPL>(c, Csm + ja, La, Csm + jb, Lb, TA, TB, tw, lane, na, nbr);
+        if (na == La) {
+            rsi16_forney_apply(c, v, base + ja, Ssm + ja, Csm + ja, La, TA, Om, D, status, lane);
+            ++nfast;
+        } else {
+            mirror |= 1u << ja;
+        }
+        if (jb != ja) {
+            if (nbr == Lb) {
+                rsi16_forney_apply(c, v, base + jb, Ssm + jb, Csm + jb, Lb, TB, Om, D, status, lane);
+                ++nfast;
+            } else {
+                mirror |= 1u << jb;
+            }
+        }
+    }
+    for (uint32_t todo = mirror; todo; todo &= todo - 1) {
+        __syncwarp();
+        rsi16_repair_block(c, v, base + (__ffs(todo) - 1), mws, status, lane);
+        ++nmirror;
+    }
+    __syncwarp();  // the batch's columns are read before the next batch writes them
 }
 
 }  // namespace ffgpu
