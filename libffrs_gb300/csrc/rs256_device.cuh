@@ -28,13 +28,37 @@ static __device__ __forceinline__ void stage_bytes(uint8_t *dst, const uint8_t *
 }
 
 // One LFSR step: rem <- (rem >> 8) ^ lut[(rem & 0xff) ^ in], rem held as W words.
+// Rows of four words or more are read 16 bytes at a time (the table is
+// 16-byte aligned, in shared or global memory).
 template <int W>
 static __device__ __forceinline__ void lfsr_step(uint32_t (&rem)[W], uint32_t in, const uint32_t *s_lut) {
     const uint32_t fb = (rem[0] & 0xffu) ^ in;
     const uint32_t *row = s_lut + fb * W;
+    uint32_t r[W];
+    if constexpr (W >= 4) {
 #pragma unroll
-    for (int w = 0; w < W - 1; ++w) rem[w] = __funnelshift_r(rem[w], rem[w + 1], 8) ^ row[w];
-    rem[W - 1] = (rem[W - 1] >> 8) ^ row[W - 1];
+        for (int q = 0; q < W / 4; ++q) {
+            const uint4 v = reinterpret_cast<const uint4 *>(row)[q];
+            r[4 * q] = v.x;
+            r[4 * q + 1] = v.y;
+            r[4 * q + 2] = v.z;
+            r[4 * q + 3] = v.w;
+        }
+    } else {
+#pragma unroll
+        for (int w = 0; w < W; ++w) r[w] = row[w];
+    }
+#pragma unroll
+    for (int w = 0; w < W - 1; ++w) rem[w] = __funnelshift_r(rem[w], rem[w + 1], 8) ^ r[w];
+    rem[W - 1] = (rem[W - 1] >> 8) ^ r[W - 1];
+}
+
+// Decoders of remainder width W >= 16 (ecc > 32) read the LFSR table from
+// global memory (through L1) instead of staging it in shared memory: the
+// shared memory goes to the scratch, and more blocks are in flight.
+template <int W>
+constexpr bool lut_in_global() {
+    return W >= 16;
 }
 
 template <int W>

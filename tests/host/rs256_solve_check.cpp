@@ -1,7 +1,9 @@
-// The per-thread RS256 decoder of the GPU table path (remainder -> syndromes,
-// Berlekamp-Massey, Chien search, Forney: rs256_device.cuh), compiled for the
-// host and run block by block against the oracle's rs_decode::decode
-// (reed_solomon.hpp:559-595): same status, same bytes.  Usage:
+// The per-thread RS256 decoder of the GPU table path (rs256_device.cuh: the
+// LFSR remainder over the table rows, syndromes, Berlekamp-Massey, Chien
+// search, Forney), compiled for the host and run block by block against the
+// oracle's rs_decode::decode (reed_solomon.hpp:559-595): same status, same
+// bytes, both from the oracle's remainder and through decode_one with the
+// library's own tables (gf256.h).  Usage:
 // rs256_solve_check <seed> <trials per ecc>; prints "bad N", exits 1 if N > 0.
 #include <cstdio>
 #include <cstdlib>
@@ -9,6 +11,7 @@
 #include <random>
 #include <vector>
 
+#include "gf256.h"
 #include "rs256_device.cuh"
 extern "C" {
 #include "ffrs_oracle.h"
@@ -22,6 +25,17 @@ static int run(int ecc, int trials, std::mt19937 &g) {
     orc_rs256_tables(rs, e256, lg);
     for (int i = 0; i < 512; ++i) ex[i] = e256[i % 255];
     std::vector<uint8_t> scratch(kDecodeScratchBytes);
+    // the library's LFSR table (rows of W words) and field tables
+    GF256Host gf(2, 0x1d);
+    std::vector<uint8_t> gen(ecc + 1), roots(ecc), lutb;
+    rs256_generator(gf, ecc, gen.data(), roots.data());
+    rs256_lut(gf, ecc, gen.data(), lutb);
+    std::vector<uint32_t> lut((size_t)256 * W + 4, 0);
+    uint32_t *lut16 = lut.data() + ((16 - ((uintptr_t)lut.data() & 15)) & 15) / 4;  // 16-byte aligned rows
+    for (int v = 0; v < 256; ++v)
+        for (int j = 0; j < ecc; ++j) lut16[(size_t)v * W + j / 4] |= (uint32_t)lutb[(size_t)v * ecc + j] << (8 * (j % 4));
+    uint8_t gex[512];
+    for (int i = 0; i < 512; ++i) gex[i] = gf.exp[i % 255];
     int bad = 0;
     for (int t = 0; t < trials; ++t) {
         const int ml = 1 + (int)(g() % (unsigned)(255 - ecc));
@@ -49,6 +63,19 @@ static int run(int ecc, int trials, std::mt19937 &g) {
             const DecodeScratchG sc(scratch.data(), 0, 1, ecc);
             synds_from_rem<W>(r, ecc, ex, lg, sc);
             decode_solve(d.data(), p.data(), ml, ecc, ex, lg, sc, &st);
+        }
+        // the whole per-thread decoder from the received bytes
+        std::vector<uint8_t> d1(cw.begin(), cw.begin() + ml), p1(cw.begin() + ml, cw.end());
+        uint8_t st1 = 9;
+        {
+            std::memset(scratch.data(), 0x5A, scratch.size());
+            const DecodeScratchG sc(scratch.data(), 0, 1, ecc);
+            decode_one<W>(d1.data(), p1.data(), ml, ecc, lut16, gex, gf.log, sc, &st1, nullptr);
+        }
+        if ((int)st1 != (ok ? 1 : 0) || d1 != dr || p1 != pr) {
+            if (bad < 5)
+                std::printf("decode_one ecc %d msg_len %d corrupted %d: status %d oracle %d\n", ecc, ml, k, st1, ok);
+            ++bad;
         }
         if ((int)st != (ok ? 1 : 0) || d != dr || p != pr) {
             if (bad < 5)

@@ -10,6 +10,10 @@
 static inline unsigned __funnelshift_r(unsigned lo, unsigned hi, unsigned shift) {
     return (unsigned)((((unsigned long long)hi << 32) | lo) >> (shift & 31));
 }
+#define __align__(n) alignas(n)
+struct uint4 {
+    unsigned x, y, z, w;
+};
 struct HostDim3 {
     unsigned x = 0, y = 0, z = 0;
 };
