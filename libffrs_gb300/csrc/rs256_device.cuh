@@ -53,6 +53,13 @@ static __device__ __forceinline__ void lfsr_step(uint32_t (&rem)[W], uint32_t in
     rem[W - 1] = (rem[W - 1] >> 8) ^ r[W - 1];
 }
 
+// Decoders of remainder width W >= 16 (ecc > 32) read the LFSR table from
+// global memory (through L1) instead of staging it in shared memory: the
+// shared memory goes to the scratch, and more blocks are in flight.
+template <int W>
+constexpr bool lut_in_global() {
+    return W >= 16;
+}
 
 template <int W>
 static __device__ __forceinline__ uint32_t rem_byte(const uint32_t (&rem)[W], int j) {
@@ -299,227 +306,5 @@ static __device__ void decode_solve(uint8_t *d, uint8_t *p, int msg_len, int ecc
     *status = 1;
 }
 
-
-// ---------------------------------------------------------------- warp solve
-//
-// For 17 <= ecc <= 64 the part of rs_decode::decode after the syndromes runs
-// on a whole warp, one block at a time: lanes over the locator's
-// coefficients for Berlekamp-Massey, over positions for the Chien search, over
-// the evaluator's coefficients, and over the roots for Forney.  A per-thread
-// solve there walks ecc-long loops with dependent table lookups on a few
-// resident warps; the warp form keeps every lane busy on short ones.  The
-// decisions and bytes are rs_decode::decode's (reed_solomon.hpp:559-595).
-
-constexpr int kWarpSolveMinEcc = 17, kWarpSolveMaxEcc = 64;
-
-struct WarpSolveSmem {
-    uint8_t lam[64];  // log(Lambda_k) mod 255 (255: zero), k <= L
-    uint8_t om[64];   // Omega_k, k < ecc
-    uint8_t pos[64];  // the roots' positions i (Lambda(a^-i) == 0), increasing
-};
-
-static __device__ __forceinline__ uint32_t warp_xor(uint32_t v) {
-#pragma unroll
-    for (int o = 16; o; o >>= 1) v ^= __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
-// One block with non-zero syndromes S[0 .. ecc) (shared memory, stride 1), on
-// the whole warp.  Lane 0 writes the status.
-static __device__ void warp_solve(uint8_t *d, uint8_t *p, int msg_len, int ecc, const uint8_t *S, const uint8_t *ex,
-                                  const uint8_t *lg, WarpSolveSmem &w, int lane, uint8_t *status) {
-    const uint32_t FULL = 0xffffffffu;
-    const int i0 = lane, i1 = lane + 32;
-    // Berlekamp-Massey (reed_solomon.hpp:655-702): lane l keeps Lambda_l,
-    // Lambda_{l+32} and B likewise; degrees stay below ecc as in the
-    // reference's truncated layout
-    uint32_t c0 = lane == 0 ? 1u : 0u, c1 = 0, b0 = c0, b1 = 0, bb = 1;
-    int L = 0, m = 1;
-    for (int n = 0; n < ecc; ++n) {
-        uint32_t t = 0;
-        if (i0 >= 1 && i0 <= L) t = gmul(ex, lg, c0, S[n - i0]);
-        if (i1 <= L) t ^= gmul(ex, lg, c1, S[n - i1]);
-        const uint32_t dsc = warp_xor(t) ^ S[n];
-        if (dsc == 0) {
-            ++m;
-            continue;
-        }
-        const uint32_t s = gdiv(ex, lg, dsc, bb);
-        // x^m B: index i takes B_{i-m}
-        const int src = (lane - m) & 31;
-        const uint32_t v0 = __shfl_sync(FULL, b0, src), v1 = __shfl_sync(FULL, b1, src);
-        const uint32_t sh0 = (m < 32 && lane >= m) ? v0 : 0u;
-        const int q = lane + 32 - m;
-        const uint32_t sh1 = q >= 32 ? v1 : (q >= 0 ? v0 : 0u);
-        const uint32_t n0 = i0 < ecc ? c0 ^ gmul(ex, lg, s, sh0) : 0u;
-        const uint32_t n1 = i1 < ecc ? c1 ^ gmul(ex, lg, s, sh1) : 0u;
-        if (2 * L <= n) {
-            b0 = c0;
-            b1 = c1;
-            L = n + 1 - L;
-            bb = dsc;
-            m = 1;
-        } else {
-            ++m;
-        }
-        c0 = n0;
-        c1 = n1;
-        if (2 * L > ecc) break;  // L never shrinks: errors > ecc/2 is final
-    }
-    if (2 * L > ecc) {
-        if (lane == 0) *status = 0;
-        return;
-    }
-    if (i0 <= L) w.lam[i0] = (uint8_t)(c0 ? lg[c0] % 255 : 255);
-    if (i1 <= L) w.lam[i1] = (uint8_t)(c1 ? lg[c1] % 255 : 255);
-    __syncwarp();
-    // Chien search: lane l evaluates positions i = l + 32 q; term k has
-    // exponent log(Lambda_k) - i k (mod 255)
-    const int size = msg_len + ecc;
-    const int npos = size < 256 ? size : 256;
-    uint32_t acc[8];
-#pragma unroll
-    for (int qq = 0; qq < 8; ++qq) acc[qq] = 0;
-    int koff = 0, k32 = 0;  // lane k and 32 k, mod 255
-    for (int k = 0; k <= L; ++k) {
-        const int lk = w.lam[k];
-        if (lk != 255) {
-            int e = lk - koff;
-            if (e < 0) e += 255;
-#pragma unroll
-            for (int qq = 0; qq < 8; ++qq) {
-                acc[qq] ^= ex[e];
-                e -= k32;
-                if (e < 0) e += 255;
-            }
-        }
-        koff += lane;
-        if (koff >= 255) koff -= 255;
-        k32 += 32;
-        if (k32 >= 255) k32 -= 255;
-    }
-    uint32_t masks[8];
-    int total = 0;
-#pragma unroll
-    for (int qq = 0; qq < 8; ++qq) {
-        masks[qq] = __ballot_sync(FULL, acc[qq] == 0 && lane + 32 * qq < npos);
-        total += __popc(masks[qq]);
-    }
-    // the reference stops at errors + 1 roots: roots != errors <=> total != L
-    if (total != L) {
-        if (lane == 0) *status = 0;
-        return;
-    }
-    int before = 0;
-#pragma unroll
-    for (int qq = 0; qq < 8; ++qq) {
-        if ((masks[qq] >> lane) & 1u) w.pos[before + __popc(masks[qq] & ((1u << lane) - 1u))] = (uint8_t)(lane + 32 * qq);
-        before += __popc(masks[qq]);
-    }
-    // Omega = (S * Lambda) mod x^ecc, non-zero
-    uint32_t o0 = 0, o1 = 0;
-    for (int j = 0; j <= L; ++j) {
-        const int lj = w.lam[j];
-        if (lj == 255) continue;
-        if (i0 < ecc && j <= i0) {
-            const uint32_t sv = S[i0 - j];
-            if (sv) o0 ^= ex[lj + lg[sv]];
-        }
-        if (i1 < ecc && j <= i1) {
-            const uint32_t sv = S[i1 - j];
-            if (sv) o1 ^= ex[lj + lg[sv]];
-        }
-    }
-    if (!__any_sync(FULL, (o0 | o1) != 0)) {
-        if (lane == 0) *status = 0;
-        return;
-    }
-    if (i0 < ecc) w.om[i0] = (uint8_t)o0;
-    if (i1 < ecc) w.om[i1] = (uint8_t)o1;
-    __syncwarp();
-    // Forney, one root per lane: X Omega(X^-1) / Lambda'(X^-1)
-    if (lane < L) {
-        const uint32_t pi = w.pos[lane];
-        const uint32_t xi = ex[pi];
-        const uint32_t xinv = ginv(ex, lg, xi);
-        uint32_t num = 0;
-        for (int k = ecc - 1; k >= 0; --k) num = gmul(ex, lg, num, xinv) ^ w.om[k];
-        uint32_t den = 0;
-        for (int k = L - ((L & 1) ? 0 : 1); k >= 1; k -= 2) {
-            const int lk = w.lam[k];
-            den = gmul(ex, lg, den, xinv);
-            den = gmul(ex, lg, den, xinv) ^ (lk == 255 ? 0u : (uint32_t)ex[lk]);
-        }
-        const uint8_t mag = (uint8_t)gmul(ex, lg, xi, gdiv(ex, lg, num, den));
-        const int qd = size - 1 - (int)pi;
-        if (qd < msg_len)
-            d[qd] ^= mag;
-        else
-            p[qd - msg_len] ^= mag;
-    }
-    if (lane == 0) *status = 1;
-    __syncwarp();  // the warp's shared bytes are free for the next block
-}
-
-// Syndrome rows: one per thread of the CTA, ceil(ecc/4) words rounded up to an
-// odd count so that a warp writing one byte column hits 32 different banks.
-__host__ __device__ constexpr int warp_solve_row_bytes(int ecc) { return (((ecc + 3) / 4) | 1) * 4; }
-
-// Shared memory after the tables for decode_warp_blocks: syndrome rows,
-// remainder-log columns, one WarpSolveSmem per warp.
-__host__ __device__ constexpr size_t warp_solve_smem(int ecc, int cta_threads) {
-    return (size_t)cta_threads * warp_solve_row_bytes(ecc) + (size_t)ecc * cta_threads +
-           (size_t)(cta_threads / 32) * sizeof(WarpSolveSmem);
-}
-
-// Decoders of remainder width W = 8 or 16 (ecc 17..64) solve on the warp.
-template <int W>
-constexpr bool warp_solve_width() {
-    return W == 8 || W == 16;
-}
-
-// Blocks first + lane (those below nblocks) of the calling warp: remainder
-// and syndromes per thread (into its row of srows and its column of rcols,
-// stride cta_threads), then every block with errors solved by the whole warp.
-// tcta: the thread's index in the CTA.
-template <int W>
-static __device__ void decode_warp_blocks(uint8_t *data, uint8_t *parity, size_t first, size_t nblocks, int msg_len,
-                                          int ecc, const uint32_t *s_lut, const uint8_t *ex, const uint8_t *lg,
-                                          uint8_t *srows, uint8_t *rcols, int cta_threads, WarpSolveSmem &wsm,
-                                          uint8_t *status, int lane, int tcta) {
-    const int rb = warp_solve_row_bytes(ecc);
-    const size_t blk = first + lane;
-    bool need = false;
-    if (blk < nblocks) {
-        const uint8_t *dd = data + blk * (size_t)msg_len, *pp = parity + blk * (size_t)ecc;
-        uint32_t rem[W];
-#pragma unroll
-        for (int w = 0; w < W; ++w) rem[w] = 0;
-        for (int i = 0; i < msg_len; ++i) lfsr_step<W>(rem, dd[i], s_lut);
-        for (int i = 0; i < ecc; ++i) lfsr_step<W>(rem, pp[i], s_lut);
-        uint32_t any = 0;
-#pragma unroll
-        for (int w = 0; w < W; ++w) any |= rem[w];
-        if (any) {
-            DecodeScratchG sc(rcols, tcta, cta_threads, ecc);
-            sc.S = {srows + (size_t)tcta * rb, 1};
-            sc.R = {rcols + tcta, (size_t)cta_threads};
-            synds_from_rem<W>(rem, ecc, ex, lg, sc);
-            need = true;
-        } else {
-            status[blk] = 1;
-        }
-    }
-    uint32_t mask = __ballot_sync(0xffffffffu, need);
-    __syncwarp();
-    const uint8_t *wrows = srows + (size_t)(tcta - lane) * rb;
-    while (mask) {
-        const int j = __ffs(mask) - 1;
-        mask &= mask - 1;
-        const size_t b = first + j;
-        warp_solve(data + b * (size_t)msg_len, parity + b * (size_t)ecc, msg_len, ecc, wrows + (size_t)j * rb, ex, lg,
-                   wsm, lane, status + b);
-    }
-}
 
 }  // namespace ffgpu

@@ -11,7 +11,6 @@
 #include <random>
 #include <vector>
 
-#include "warp_emu.h"  // declares the warp intrinsics the header's warp solve uses
 #include "gf256.h"
 #include "rs256_device.cuh"
 extern "C" {

@@ -1,9 +1,8 @@
-"""The GPU table path's RS256 decoders (rs256_device.cuh) compiled for the
-host and checked block by block against the oracle: a CPU parity check of
-the device algorithms themselves (LFSR remainder, syndromes, Berlekamp-Massey,
-Chien search, Forney) over shortened blocks and error counts past the
-capacity.  The per-thread decoder covers ecc 1..254; the warp solve (ecc
-17..64) runs with its warp emulated by 32 host threads in lock step."""
+"""The GPU table path's per-thread RS256 decoder (rs256_device.cuh) compiled
+for the host and checked block by block against the oracle: a CPU parity
+check of the device algorithm itself (syndromes from the LFSR remainder,
+Berlekamp-Massey, Chien search, Forney), over ecc 1..254, shortened blocks
+and error counts past the capacity."""
 
 import os
 import shutil
@@ -25,18 +24,4 @@ def test_rs256_device_decoder_on_host(tmp_path):
                    check=True)
     r = subprocess.run([str(exe), "11", "3000"], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True,
                        timeout=600)
-    assert r.returncode == 0 and r.stdout.strip().endswith("bad 0"), r.stdout[-2000:]
-
-
-@pytest.mark.skipif(shutil.which("g++") is None or shutil.which("gcc") is None, reason="needs gcc/g++")
-def test_rs256_warp_solve_on_host(tmp_path):
-    obj = tmp_path / "ffrs_oracle.o"
-    exe = tmp_path / "rs256_warp_solve_check"
-    subprocess.run(["gcc", "-O2", "-c", os.path.join(REPO, "oracle", "ffrs_oracle.c"), "-o", str(obj)], check=True)
-    subprocess.run(["g++", "-O2", "-std=c++20", "-pthread", "-I", os.path.join(REPO, "tests", "host", "stub"),
-                    "-I", os.path.join(REPO, "libffrs_gb300", "csrc"), "-I", os.path.join(REPO, "oracle"),
-                    os.path.join(REPO, "tests", "host", "rs256_warp_solve_check.cpp"), str(obj), "-o", str(exe)],
-                   check=True)
-    r = subprocess.run([str(exe), "13", "20"], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True,
-                       timeout=900)
     assert r.returncode == 0 and r.stdout.strip().endswith("bad 0"), r.stdout[-2000:]
