@@ -97,12 +97,10 @@ __device__ void rs256_enc_item(const BatchCode &c, const BatchItem &it, uint32_t
 
 template <int W>
 __device__ void rs256_dec_item(const BatchCode &c, const BatchItem &it, uint32_t *sm, uint8_t *scratch) {
-    constexpr bool kGlobalLut = lut_in_global<W>();
     uint32_t *s_lut = sm;
-    uint8_t *ex = reinterpret_cast<uint8_t *>(sm + (kGlobalLut ? 0 : 256 * W));
+    uint8_t *ex = reinterpret_cast<uint8_t *>(sm + 256 * W);
     uint8_t *lg = ex + 512;
-    if (!kGlobalLut)
-        for (int i = threadIdx.x; i < 256 * W; i += kBatchThreads) s_lut[i] = c.lut[i];
+    for (int i = threadIdx.x; i < 256 * W; i += kBatchThreads) s_lut[i] = c.lut[i];
     for (int i = threadIdx.x; i < 512; i += kBatchThreads) ex[i] = c.exp512[i];
     for (int i = threadIdx.x; i < 256; i += kBatchThreads) lg[i] = c.log256[i];
     __syncthreads();
@@ -114,8 +112,7 @@ __device__ void rs256_dec_item(const BatchCode &c, const BatchItem &it, uint32_t
     uint8_t *data = static_cast<uint8_t *>(it.msg);
     uint8_t *par = static_cast<uint8_t *>(it.par);
     for (uint32_t b = threadIdx.x; b < it.nblocks; b += kBatchThreads)
-        decode_one<W>(data + (size_t)b * ml, par + (size_t)b * c.ecc, ml, c.ecc, kGlobalLut ? c.lut : s_lut, ex, lg,
-                      sc, it.status + b,
+        decode_one<W>(data + (size_t)b * ml, par + (size_t)b * c.ecc, ml, c.ecc, s_lut, ex, lg, sc, it.status + b,
                       nullptr);
 }
 
@@ -501,8 +498,7 @@ void build_plan(ffgpu_batch &B, int tile_rs, int tile_rsi, int ctas_rs, int ctas
                 K.smem = std::max(K.smem, (size_t)256 * c.W * 4 + (size_t)kBatchThreads * r.msg_len);
             else {
                 const size_t sc = c.W <= 16 ? (size_t)kDecodeScratchCols * c.ecc * kBatchThreads : 0;
-                const size_t lut = c.W >= 16 ? 0 : (size_t)256 * c.W * 4;  // lut_in_global
-                K.smem = std::max(K.smem, lut + 768 + sc);
+                K.smem = std::max(K.smem, (size_t)256 * c.W * 4 + 768 + sc);
                 any_rs_dec = true;
             }
         } else if (r.kind == BK_RSI16_ENC || r.kind == BK_RSI16_DEC) {

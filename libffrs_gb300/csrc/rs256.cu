@@ -56,23 +56,20 @@ __global__ void __launch_bounds__(128) rs256_decode_table_kernel(uint8_t *__rest
                                                                  uint8_t *__restrict__ synds_out,
                                                                  uint8_t *__restrict__ gscratch) {
     extern __shared__ __align__(16) uint32_t smem[];
-    constexpr bool kGlobalLut = lut_in_global<W>();
     uint32_t *s_lut = smem;
-    uint8_t *ex = reinterpret_cast<uint8_t *>(smem + (kGlobalLut ? 0 : 256 * W));
+    uint8_t *ex = reinterpret_cast<uint8_t *>(smem + 256 * W);
     uint8_t *lg = ex + 512;
-    if (!kGlobalLut)
-        for (int i = threadIdx.x; i < 256 * W; i += blockDim.x) s_lut[i] = lut[i];
+    for (int i = threadIdx.x; i < 256 * W; i += blockDim.x) s_lut[i] = lut[i];
     for (int i = threadIdx.x; i < 512; i += blockDim.x) ex[i] = exp512[i];
     for (int i = threadIdx.x; i < 256; i += blockDim.x) lg[i] = log256[i];
     __syncthreads();
-    const uint32_t *tab = kGlobalLut ? lut : s_lut;
     const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const size_t nthreads = (size_t)gridDim.x * blockDim.x;
     const DecodeScratchG sc = gscratch ? DecodeScratchG(gscratch, tid, nthreads)
                                        : DecodeScratchG(reinterpret_cast<uint8_t *>(lg + 256), threadIdx.x,
                                                         blockDim.x, ecc);
     for (size_t blk = tid; blk < nblocks; blk += nthreads)
-        decode_one<W>(data + blk * (size_t)msg_len, parity + blk * (size_t)ecc, msg_len, ecc, tab, ex, lg, sc,
+        decode_one<W>(data + blk * (size_t)msg_len, parity + blk * (size_t)ecc, msg_len, ecc, s_lut, ex, lg, sc,
                       status ? status + blk : nullptr, synds_out ? synds_out + blk * (size_t)ecc : nullptr);
 }
 
@@ -198,7 +195,7 @@ template <int W>
 static void launch_decode_table(const Rs256Code &c, uint8_t *data, uint8_t *parity, size_t nblocks, int msg_len,
                                 uint8_t *status, uint8_t *synds, cudaStream_t st) {
     const unsigned threads = 128;
-    const size_t tables = (lut_in_global<W>() ? 0 : (size_t)256 * W * 4) + 768;
+    const size_t tables = (size_t)256 * W * 4 + 768;
     const size_t sm_scratch = (size_t)kDecodeScratchCols * c.ecc * threads;
     const bool in_smem = tables + sm_scratch <= 100 * 1024;  // ecc <= 64
     const size_t smem = tables + (in_smem ? sm_scratch : 0);

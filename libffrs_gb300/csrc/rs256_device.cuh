@@ -53,13 +53,6 @@ static __device__ __forceinline__ void lfsr_step(uint32_t (&rem)[W], uint32_t in
     rem[W - 1] = (rem[W - 1] >> 8) ^ r[W - 1];
 }
 
-// Decoders of remainder width W >= 16 (ecc > 32) read the LFSR table from
-// global memory (through L1) instead of staging it in shared memory: the
-// shared memory goes to the scratch, and more blocks are in flight.
-template <int W>
-constexpr bool lut_in_global() {
-    return W >= 16;
-}
 
 template <int W>
 static __device__ __forceinline__ uint32_t rem_byte(const uint32_t (&rem)[W], int j) {
