@@ -285,7 +285,6 @@ struct ffgpu_batch {
         uint32_t ws_words = 0;
         unsigned grid = 0;
         int per_sm = 0;
-        size_t scratch_cta0 = 0;  // first CTA slice of the RS256 decode scratch
     };
     ItemClass cls[kClasses];
     DeviceBuffer d_codes, d_counter, d_rs_scratch, d_backup;
@@ -499,7 +498,7 @@ void build_plan(ffgpu_batch &B, int tile_rs, int tile_rsi, int ctas_rs, int ctas
             else {
                 const size_t sc = c.W <= 16 ? (size_t)kDecodeScratchCols * c.ecc * kBatchThreads : 0;
                 K.smem = std::max(K.smem, (size_t)256 * c.W * 4 + 768 + sc);
-                any_rs_dec = true;
+                any_rs_dec |= c.W > 16;  // only the widest class keeps its scratch in global memory
             }
         } else if (r.kind == BK_RSI16_ENC || r.kind == BK_RSI16_DEC) {
             const Rsi16Code &c = *static_cast<const ffgpu_rsi16 *>(r.handle)->code;
@@ -548,14 +547,9 @@ void build_plan(ffgpu_batch &B, int tile_rs, int tile_rsi, int ctas_rs, int ctas
 
     B.d_codes.get(std::max<size_t>(1, B.codes.size()) * sizeof(BatchCode));
     B.d_counter.get(256);
-    // decode scratch: one slice per CTA of every RS256 class (the classes
-    // run at the same time)
-    size_t g = 0;
-    for (int k = 0; k < kClsRsi16; ++k) {
-        B.cls[k].scratch_cta0 = g;
-        g += B.cls[k].items.empty() ? 0 : B.cls[k].grid;
-    }
-    if (any_rs_dec) B.d_rs_scratch.get(g * kBatchThreads * kDecodeScratchBytes);
+    // global decode scratch: one slice per CTA of the widest RS256 class
+    // (the narrower ones keep theirs in shared memory)
+    if (any_rs_dec) B.d_rs_scratch.get((size_t)B.cls[2].grid * kBatchThreads * kDecodeScratchBytes);
     for (auto &K : B.cls) {
         K.d_items.get(std::max<size_t>(1, K.items.size()) * sizeof(BatchItem));
         if (!K.items.empty())
@@ -579,9 +573,7 @@ void launch_class(ffgpu_batch &B, cudaStream_t st, bool timed) {
     a.nitems = (uint32_t)K.items.size();
     a.codes = static_cast<const BatchCode *>(B.d_codes.ptr);
     a.counter = counter;
-    a.rs_scratch = B.d_rs_scratch.ptr
-                       ? static_cast<uint8_t *>(B.d_rs_scratch.ptr) + K.scratch_cta0 * kBatchThreads * kDecodeScratchBytes
-                       : nullptr;
+    a.rs_scratch = static_cast<uint8_t *>(B.d_rs_scratch.ptr);
     a.ws_words = K.ws_words;
     if (timed) {
         KernelTimer kt_timer(CLS < kClsRsi16 ? "batch_kernel_rs256" : "batch_kernel_rsi16", st);
