@@ -210,11 +210,13 @@ FFGPU_API int ffgpu_circ16_repair_host(const ffgpu_circ16 *code, uint16_t *msg, 
 /* ---------------------------------------------------------------- batch */
 /* No reference counterpart.  A batch collects requests of any mix of codes,
  * geometries and directions (device buffers, laid out as for the per-code
- * entry points above) and serves all of them with one persistent kernel
- * launch; the launch can be captured into a CUDA graph and replayed.  Results
- * are byte-identical to calling the per-code entry point once per request.
- * A batch holds pointers: the buffers must stay valid while it is planned,
- * captured and launched. */
+ * entry points above) and serves all of them in one launch sequence: the
+ * CIRC16 requests gathered per code and direction through the staged
+ * encode / repair, then one persistent kernel per item class (RS256 by
+ * remainder width, RSi16) side by side on forked streams.  The sequence can
+ * be captured into a CUDA graph and replayed.  Results are byte-identical to
+ * calling the per-code entry point once per request.  A batch holds pointers:
+ * the buffers must stay valid while it is planned, captured and launched. */
 typedef struct ffgpu_batch ffgpu_batch;
 #define FFGPU_OP_ENCODE 0
 #define FFGPU_OP_DECODE 1
@@ -228,8 +230,8 @@ FFGPU_API int ffgpu_batch_add_rs256(ffgpu_batch *batch, const ffgpu_rs256 *code,
 /* RSi16: as ffgpu_rsi16_encode / ffgpu_rsi16_repair */
 FFGPU_API int ffgpu_batch_add_rsi16(ffgpu_batch *batch, const ffgpu_rsi16 *code, int op, uint16_t *msg,
                                     uint16_t *parity, size_t nblocks, uint8_t *status);
-/* CIRC16: as ffgpu_circ16_encode / ffgpu_circ16_repair (one codeword per
- * work item, its whole CircRepair inside one CTA; status 0 or 0xFF) */
+/* CIRC16: as ffgpu_circ16_encode / ffgpu_circ16_repair (status 0 or 0xFF
+ * per codeword) */
 FFGPU_API int ffgpu_batch_add_circ16(ffgpu_batch *batch, const ffgpu_circ16 *code, int op, uint16_t *msg,
                                      uint16_t *ecc, size_t nblocks, uint8_t *status);
 /* cut the requests into work items (longest first) and upload them; with
@@ -237,9 +239,9 @@ FFGPU_API int ffgpu_batch_add_circ16(ffgpu_batch *batch, const ffgpu_circ16 *cod
  * item, CTAs per SM) are timed on the batch itself -- decode buffers are saved
  * and restored around every trial -- and the fastest is kept */
 FFGPU_API int ffgpu_batch_plan(ffgpu_batch *batch, int autotune, void *stream);
-/* capture the launch into a CUDA graph (later launches replay it) */
+/* capture the launch sequence into a CUDA graph (later launches replay it) */
 FFGPU_API int ffgpu_batch_capture(ffgpu_batch *batch, void *stream);
-/* serve every request with one persistent launch (or one graph replay) */
+/* serve every request: the launch sequence, or one graph replay */
 FFGPU_API int ffgpu_batch_launch(ffgpu_batch *batch, void *stream);
 FFGPU_API int ffgpu_batch_info(const ffgpu_batch *batch, int *tile_rs256, int *tile_rsi16, int *ctas_per_sm,
                                size_t *items, unsigned *grid);
