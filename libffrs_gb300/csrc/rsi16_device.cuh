@@ -1235,12 +1235,15 @@ static __device__ __noinline__ void rsi16_repair_known_block(const Rsi16Dev &c, 
     for (uint32_t k = lane; k < ecc; k += 32) deriv[k] = fmul(loc[k], k + 1);
     __syncwarp();
     const uint32_t dl = w_poly_len(deriv, ecc, lane);
-    // positions may repeat; apply sequentially in list order on lane 0
     __syncwarp();
-    if (lane == 0) {
-        for (uint32_t i = 0; i < count; ++i) {
-            const uint32_t p = bp[i];
-            uint16_t bb = (uint16_t)p;
+    // The corrections depend on the syndromes and the positions only: each
+    // lane computes those of its listed positions, then lane 0 applies them
+    // in list order (positions may repeat, and repeats accumulate).
+    for (uint32_t i0 = 0; i0 < count; i0 += 32) {
+        const uint32_t i = i0 + lane;
+        uint32_t q = 0, err = 0;
+        if (i < count) {
+            uint16_t bb = (uint16_t)bp[i];
             bb = (uint16_t)(((bb >> 1) & 0x5555) | ((bb & 0x5555) << 1));
             bb = (uint16_t)(((bb >> 2) & 0x3333) | ((bb & 0x3333) << 2));
             bb = (uint16_t)(((bb >> 4) & 0x0f0f) | ((bb & 0x0f0f) << 4));
@@ -1250,17 +1253,21 @@ static __device__ __noinline__ void rsi16_repair_known_block(const Rsi16Dev &c, 
             const uint32_t xi = finv(x);
             const uint32_t num = eval_poly(ev, ecc, xi);
             const uint32_t den = eval_poly(deriv, dl, xi);
-            const uint32_t err = fmul(fdiv(num, den), x);
+            err = fmul(fdiv(num, den), x);
             uint16_t cc = (uint16_t)pr;
             cc = (uint16_t)(((cc >> 1) & 0x5555) | ((cc & 0x5555) << 1));
             cc = (uint16_t)(((cc >> 2) & 0x3333) | ((cc & 0x3333) << 2));
             cc = (uint16_t)(((cc >> 4) & 0x0f0f) | ((cc & 0x0f0f) << 4));
             cc = (uint16_t)((cc >> 8) | (cc << 8));
-            const uint32_t q = (uint32_t)(cc >> c.rbo_shift);
-            put_pos(c, v, b, q, fadd(get_pos(c, v, b, q), err));
+            q = (uint32_t)(cc >> c.rbo_shift);
         }
-        if (status) status[b] = FFGPU_REPAIR_OK;
+        const uint32_t nj = count - i0 < 32 ? count - i0 : 32;
+        for (uint32_t j = 0; j < nj; ++j) {
+            const uint32_t qj = __shfl_sync(0xffffffffu, q, (int)j), ej = __shfl_sync(0xffffffffu, err, (int)j);
+            if (lane == 0) put_pos(c, v, b, qj, fadd(get_pos(c, v, b, qj), ej));
+        }
     }
+    if (lane == 0 && status) status[b] = FFGPU_REPAIR_OK;
     __syncwarp();
 }
 
