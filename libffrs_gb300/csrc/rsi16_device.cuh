@@ -802,6 +802,57 @@ static __device__ __forceinline__ void rsi16_encode_sub_pass(const Rsi16Dev &c, 
     }
 }
 
+// Syndromes (NTT::pntt over every chunk) of the one block b into
+// out[0 .. N) for ecc = N < 32: the warp's 32/N slots take every (32/N)-th
+// chunk on the sub-warp transforms and their sums are added (exact mod p, so
+// the order does not matter).
+template <int N>
+static __device__ __forceinline__ void sub_synd_one(const Rsi16Dev &c, const BlockView &v, size_t b, uint32_t *out,
+                                                    int lane) {
+    constexpr int G = 32 / N;
+    const int e = lane % N, s = lane / N;
+    SubTw<N> tw;
+    sub_twiddles<N>(c, e, tw);
+    const size_t mb = (b / v.group) * v.msg_gstride + (b % v.group) * v.msg_bstride;
+    const size_t pb = (b / v.group) * v.par_gstride + (b % v.group) * v.par_bstride;
+    const uint32_t nch = c.pntt_blocks ? c.pntt_blocks : 1;
+    uint32_t acc = 0;
+    for (uint32_t base = 0; base < nch; base += G) {
+        const uint32_t ch = base + (uint32_t)s;
+        const uint32_t k = ch * N + (uint32_t)e;
+        uint32_t w = 0;
+        if (ch < nch) {
+            if (k < c.message_len)
+                w = ld_word(v.msg, v.msg16, mb + (size_t)k * v.msg_estride);
+            else if (k < c.block_len)
+                w = ld_word(v.par, v.par16, pb + (size_t)(k - c.message_len) * v.par_estride);
+        }
+        w = sub_ct<N>(w, tw, e);
+        if (ch < nch) acc = fadd(acc, fmul(w, c.pntt_shift[k]));
+    }
+#pragma unroll
+    for (int o = N; o < 32; o <<= 1) acc = fadd(acc, __shfl_xor_sync(0xffffffffu, acc, o));
+    if (lane < N) out[lane] = acc;
+    __syncwarp();
+}
+
+// Syndromes of block b into temp[0 .. ecc) on one warp: the sub-warp
+// transforms for ecc 2..16, the block gathered into temp and the
+// shared-memory transforms otherwise.
+static __device__ __forceinline__ void w_synd_block(const Rsi16Dev &c, const BlockView &v, size_t b, uint32_t *temp,
+                                                    int lane) {
+    switch (c.ecc) {
+        case 2: sub_synd_one<2>(c, v, b, temp, lane); return;
+        case 4: sub_synd_one<4>(c, v, b, temp, lane); return;
+        case 8: sub_synd_one<8>(c, v, b, temp, lane); return;
+        case 16: sub_synd_one<16>(c, v, b, temp, lane); return;
+        default:
+            w_gather(c, v, b, temp, true, lane);
+            w_pntt(c, temp, c.pntt_blocks, lane);
+            return;
+    }
+}
+
 // ---------------------------------------------------------------- one block per warp
 
 // parity of block b (ws: block_len words)
@@ -914,8 +965,7 @@ static __device__ __noinline__ bool rsi16_repair_bm_block_t(const Rsi16Dev &c, c
             return true;
         }
     } else {
-        w_gather(c, v, b, temp, true, lane);
-        w_pntt(c, temp, c.pntt_blocks, lane);
+        w_synd_block(c, v, b, temp, lane);
         if (w_all_zero(S, ecc, lane)) {
             if (lane == 0) status[b] = FFGPU_NO_ERRORS;
             return true;
@@ -1195,8 +1245,7 @@ static __device__ __noinline__ void rsi16_repair_known_block(const Rsi16Dev &c, 
                                                       uint8_t *status, int lane) {
     const uint32_t ecc = c.ecc;
 
-    w_gather(c, v, b, temp, true, lane);
-    w_pntt(c, temp, c.pntt_blocks, lane);
+    w_synd_block(c, v, b, temp, lane);
     if (w_all_zero(temp, ecc, lane)) {
         if (lane == 0 && status) status[b] = FFGPU_NO_ERRORS;
         return;
