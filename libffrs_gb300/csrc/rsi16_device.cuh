@@ -836,6 +836,33 @@ static __device__ __forceinline__ void sub_synd_one(const Rsi16Dev &c, const Blo
     __syncwarp();
 }
 
+// Roots of C (degree L) for ecc = N < 32: the inverse partial NTT
+// (pintt_ecc, ntt.hpp:206-220) of every chunk on the sub-warp transforms,
+// slot s taking chunks s, s + 32/N, ...; the positions i = chunk * N + e with
+// a zero go to T in increasing order (at most n1 kept).  Returns their count.
+template <int N>
+static __device__ __forceinline__ uint32_t sub_roots(const Rsi16Dev &c, const uint32_t *C, uint32_t L, uint32_t *T,
+                                                     uint32_t n1, int lane) {
+    constexpr int G = 32 / N;
+    const int e = lane % N, s = lane / N;
+    SubTw<N> tw;
+    sub_twiddles<N>(c, e, tw);
+    const uint32_t cr = (uint32_t)e <= L ? C[e] : 0u;
+    const uint32_t nch = c.block_len / N;
+    uint32_t count = 0;
+    for (uint32_t base = 0; base < nch; base += G) {
+        const uint32_t ch = base + (uint32_t)s;
+        uint32_t x = ch < nch ? fmul(cr, c.pintt_shift[ch * N + (uint32_t)e]) : 1u;
+        x = sub_gs<N>(x, tw, e);
+        const bool hit = ch < nch && x == 0;
+        const uint32_t msk = __ballot_sync(0xffffffffu, hit);
+        const uint32_t at = count + __popc(msk & ((1u << lane) - 1u));
+        if (hit && at < n1) T[at] = ch * N + (uint32_t)e;
+        count += __popc(msk);
+    }
+    return count;
+}
+
 // Syndromes of block b into temp[0 .. ecc) on one warp: the sub-warp
 // transforms for ecc 2..16, the block gathered into temp and the
 // shared-memory transforms otherwise.
@@ -1035,6 +1062,13 @@ static __device__ __noinline__ bool rsi16_repair_bm_block_t(const Rsi16Dev &c, c
                 if (hit && at < n1) T[at] = ch * ecc + lane * EPL + h;
                 count += __popc(msk);
             }
+        }
+    } else if (ecc == 2 || ecc == 4 || ecc == 8 || ecc == 16) {
+        switch (ecc) {
+            case 2: count = sub_roots<2>(c, C, L, T, n1, lane); break;
+            case 4: count = sub_roots<4>(c, C, L, T, n1, lane); break;
+            case 8: count = sub_roots<8>(c, C, L, T, n1, lane); break;
+            default: count = sub_roots<16>(c, C, L, T, n1, lane); break;
         }
     } else {
         uint32_t *R = temp + ecc + 3 * n1;  // block_len words, past S, C, B and T
