@@ -496,7 +496,7 @@ void build_plan(ffgpu_batch &B, int tile_rs, int tile_rsi, int ctas_rs, int ctas
             if (r.kind == BK_RS256_ENC)
                 K.smem = std::max(K.smem, (size_t)256 * c.W * 4 + (size_t)kBatchThreads * r.msg_len);
             else {
-                const size_t sc = c.W <= 16 ? (size_t)kDecodeScratchCols * c.ecc * kBatchThreads : 0;
+                const size_t sc = c.W <= 16 ? decode_scratch_bytes(c.ecc) * kBatchThreads : 0;
                 K.smem = std::max(K.smem, (size_t)256 * c.W * 4 + 768 + sc);
                 any_rs_dec |= c.W > 16;  // only the widest class keeps its scratch in global memory
             }

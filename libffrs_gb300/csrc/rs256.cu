@@ -44,8 +44,8 @@ __global__ void __launch_bounds__(128) rs256_encode_table_kernel(const uint8_t *
 
 // Per-thread decode scratch, interleaved across threads so that lock-step
 // accesses of a warp fall on consecutive bytes: in shared memory after the
-// tables (gscratch == NULL, kDecodeScratchCols columns of ecc bytes for the
-// CTA's threads), else in global memory (256-byte columns across the launch).
+// tables (gscratch == NULL, decode_scratch_bytes(ecc) for each of the CTA's
+// threads), else in global memory (256-byte columns across the launch).
 template <int W>
 __global__ void __launch_bounds__(128) rs256_decode_table_kernel(uint8_t *__restrict__ data,
                                                                  uint8_t *__restrict__ parity, size_t nblocks,
@@ -196,7 +196,7 @@ static void launch_decode_table(const Rs256Code &c, uint8_t *data, uint8_t *pari
                                 uint8_t *status, uint8_t *synds, cudaStream_t st) {
     const unsigned threads = 128;
     const size_t tables = (size_t)256 * W * 4 + 768;
-    const size_t sm_scratch = (size_t)kDecodeScratchCols * c.ecc * threads;
+    const size_t sm_scratch = decode_scratch_bytes(c.ecc) * threads;
     const bool in_smem = tables + sm_scratch <= 100 * 1024;  // ecc <= 64
     const size_t smem = tables + (in_smem ? sm_scratch : 0);
     static bool attr = false;

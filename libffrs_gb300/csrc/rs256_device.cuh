@@ -82,27 +82,32 @@ struct ScratchBytes {
     __device__ __forceinline__ ScratchBytes operator+(int k) const { return {base + (size_t)k * stride, stride}; }
 };
 
-// Per-thread decode scratch: five byte columns of `cols` bytes (cols >= ecc).
-// Byte k of column c of thread tid sits at g[(c * cols + k) * nthreads + tid],
-// so that the lock-step accesses of a warp fall on consecutive bytes (global
-// memory: one sector; shared memory: no bank conflict).
-//   S: syndromes; A, B, C: the rotating Berlekamp-Massey polynomials (then
-//   the root positions in a free one); R: remainder logs, Chien exponents,
-//   then the evaluator.
+// Per-thread decode scratch: five byte columns.  Byte k of a column of thread
+// tid sits at column_base[k * nthreads + tid], so that the lock-step accesses
+// of a warp fall on consecutive bytes (global memory: one sector; shared
+// memory: no bank conflict).
+//   S (ecc bytes): syndromes;
+//   A, B, C (ecc/2 + 2 bytes each): the rotating Berlekamp-Massey polynomials
+//   (degree <= L <= ecc/2 while they are live), then the root positions in a
+//   free one;
+//   R (ecc bytes): remainder logs, Chien exponents, then the evaluator.
 struct DecodeScratchG {
     ScratchBytes S, A, B, C, R;
-    __device__ DecodeScratchG(uint8_t *g, size_t tid, size_t nthreads, int cols = 256) {
+    // cols == 0: the compact layout of decode_scratch_bytes(ecc) bytes per
+    // thread; else five columns of cols bytes
+    __device__ DecodeScratchG(uint8_t *g, size_t tid, size_t nthreads, int ecc = 0) {
         uint8_t *b = g + tid;
-        const size_t cs = (size_t)cols * nthreads;
+        const size_t s = ecc ? (size_t)ecc : 256, h = ecc ? (size_t)(ecc / 2 + 2) : 256;
         S = {b, nthreads};
-        A = {b + cs, nthreads};
-        B = {b + 2 * cs, nthreads};
-        C = {b + 3 * cs, nthreads};
-        R = {b + 4 * cs, nthreads};
+        A = {b + s * nthreads, nthreads};
+        B = {b + (s + h) * nthreads, nthreads};
+        C = {b + (s + 2 * h) * nthreads, nthreads};
+        R = {b + (s + 3 * h) * nthreads, nthreads};
     }
 };
-constexpr int kDecodeScratchCols = 5;
-constexpr size_t kDecodeScratchBytes = 2048;  // per thread at cols = 256
+constexpr size_t kDecodeScratchBytes = 2048;  // per thread, the 256-byte-column layout
+// per thread, the compact layout for ecc
+__host__ __device__ constexpr size_t decode_scratch_bytes(int ecc) { return 2 * (size_t)ecc + 3 * (size_t)(ecc / 2 + 2); }
 
 // Syndromes from the remainder: S_j = sum_m R[m] a^{-j(m+1)}, j-outer with
 // the exponent of each term stepped by j (no multiplications), the remainder
@@ -131,9 +136,12 @@ static __device__ void synds_from_rem(const uint32_t (&rem)[W], int ecc, const u
 // rs_decode::berlekamp_massey (reed_solomon.hpp:655-702) on normal-order
 // polynomials (A[k] = Lambda_k, degrees below ecc), with the same updates and
 // truncation as the reference's reversed layout.  Loops run over the live
-// degrees only, and the three buffers rotate instead of being copied.
-// Returns the number of errors L; *lam is left on the buffer holding Lambda
-// and *fr on a free one.
+// degrees only, and the three buffers rotate instead of being copied.  The
+// locator's degree never exceeds L (every update adds x^m B with
+// m + deg B <= the new L), and L never shrinks, so the run stops as soon as
+// L passes ecc/2 (the reference's decode then fails whatever follows) and
+// the buffers need ecc/2 + 1 coefficients.  Returns L; *lam is left on the
+// buffer holding Lambda and *fr on a free one.
 static __device__ int rs_bm(const DecodeScratchG &sc, int ecc, const uint8_t *ex, const uint8_t *lg,
                             ScratchBytes *lam, ScratchBytes *fr) {
     ScratchBytes A = sc.A, P = sc.B, T = sc.C;
@@ -153,6 +161,8 @@ static __device__ int rs_bm(const DecodeScratchG &sc, int ecc, const uint8_t *ex
         const int hi = m + degP < ecc - 1 ? m + degP : ecc - 1;
         const int nd = degA > hi ? degA : hi;
         if (2 * L <= n) {
+            // L only grows: past ecc/2 the block fails whatever follows
+            if (2 * (n + 1 - L) > ecc) return n + 1 - L;
             // T = A + s x^m P; P <- A; A <- T
             for (int k = 0; k <= nd; ++k) {
                 uint32_t v = k <= degA ? (uint32_t)A[k] : 0u;
