@@ -119,17 +119,29 @@ static __device__ void synds_from_rem(const uint32_t (&rem)[W], int ecc, const u
         const uint32_t r = rem_byte<W>(rem, m);
         sc.R[m] = r ? lg[r] % 255 : 255;  // logs may be stored as 1..255
     }
-    for (int j = 0; j < ecc; ++j) {
-        uint32_t acc = 0;
-        int sub = 0;  // j * (m + 1) mod 255
-        for (int m = 0; m < ecc; ++m) {
-            sub += j;
-            if (sub >= 255) sub -= 255;
-            const uint32_t lr = sc.R[m];
-            const uint32_t v = ex[lr + 255u - (uint32_t)sub];  // lr + 255 - sub <= 510
-            acc ^= lr != 255u ? v : 0u;
+    // eight syndromes per pass: one load of each remainder log serves them all
+    for (int j0 = 0; j0 < ecc; j0 += 8) {
+        uint32_t acc[8];
+        int sub[8], step[8];  // sub: j * (m + 1) mod 255
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            acc[q] = 0;
+            sub[q] = 0;
+            step[q] = j0 + q < ecc ? j0 + q : 0;  // j < 255; past ecc nothing is kept
         }
-        sc.S[j] = (uint8_t)acc;
+        for (int m = 0; m < ecc; ++m) {
+            const uint32_t lr = sc.R[m];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                sub[q] += step[q];
+                if (sub[q] >= 255) sub[q] -= 255;
+                const uint32_t v = ex[lr + 255u - (uint32_t)sub[q]];  // lr + 255 - sub <= 510
+                acc[q] ^= lr != 255u ? v : 0u;
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+            if (j0 + q < ecc) sc.S[j0 + q] = (uint8_t)acc[q];
     }
 }
 
