@@ -169,7 +169,8 @@ static __device__ int rs_bm(const DecodeScratchG &sc, int ecc, const uint8_t *ex
             ++m;
             continue;
         }
-        const uint32_t s = gdiv(ex, lg, d, b);
+        const uint32_t s = gdiv(ex, lg, d, b);  // non-zero: d and b are
+        const uint32_t lgs = lg[s];
         const int hi = m + degP < ecc - 1 ? m + degP : ecc - 1;
         const int nd = degA > hi ? degA : hi;
         if (2 * L <= n) {
@@ -178,7 +179,10 @@ static __device__ int rs_bm(const DecodeScratchG &sc, int ecc, const uint8_t *ex
             // T = A + s x^m P; P <- A; A <- T
             for (int k = 0; k <= nd; ++k) {
                 uint32_t v = k <= degA ? (uint32_t)A[k] : 0u;
-                if (k >= m && k <= hi) v ^= gmul(ex, lg, s, P[k - m]);
+                if (k >= m && k <= hi) {
+                    const uint32_t pk = P[k - m];
+                    v ^= pk ? (uint32_t)ex[lgs + lg[pk]] : 0u;  // gmul(s, pk)
+                }
                 T[k] = (uint8_t)v;
             }
             const ScratchBytes oldP = P;
@@ -192,7 +196,10 @@ static __device__ int rs_bm(const DecodeScratchG &sc, int ecc, const uint8_t *ex
             m = 1;
         } else {
             for (int k = degA + 1; k <= hi; ++k) A[k] = 0;  // stale bytes above the live degree
-            for (int k = m; k <= hi; ++k) A[k] ^= (uint8_t)gmul(ex, lg, s, P[k - m]);
+            for (int k = m; k <= hi; ++k) {
+                const uint32_t pk = P[k - m];
+                if (pk) A[k] ^= ex[lgs + lg[pk]];  // gmul(s, pk)
+            }
             degA = nd;
             ++m;
         }
@@ -304,13 +311,12 @@ static __device__ void decode_solve(uint8_t *d, uint8_t *p, int msg_len, int ecc
     for (int i = 0; i < errors; ++i) {
         const uint32_t xi = ex[pos[i]];
         const uint32_t xinv = ginv(ex, lg, xi);
+        const uint32_t lx = lg[xinv], lx2 = lx + lx;  // xinv != 0
         uint32_t num = 0;
-        for (int k = ecc - 1; k >= 0; --k) num = gmul(ex, lg, num, xinv) ^ sc.R[k];
+        for (int k = ecc - 1; k >= 0; --k) num = (num ? (uint32_t)ex[lg[num] + lx] : 0u) ^ sc.R[k];
         uint32_t den = 0;
-        for (int k = errors - ((errors & 1) ? 0 : 1); k >= 1; k -= 2) {
-            den = gmul(ex, lg, den, xinv);
-            den = gmul(ex, lg, den, xinv) ^ lam[k];
-        }
+        for (int k = errors - ((errors & 1) ? 0 : 1); k >= 1; k -= 2)
+            den = (den ? (uint32_t)ex[(lg[den] + lx2) % 255] : 0u) ^ lam[k];  // den xinv^2 + Lambda_k
         const uint8_t mag = (uint8_t)gmul(ex, lg, xi, gdiv(ex, lg, num, den));
         const int q = size - 1 - pos[i];
         if (q < msg_len)
