@@ -82,19 +82,19 @@ struct ScratchBytes {
     __device__ __forceinline__ ScratchBytes operator+(int k) const { return {base + (size_t)k * stride, stride}; }
 };
 
-// Per-thread decode scratch: five byte columns.  Byte k of a column of thread
+// Per-thread decode scratch: byte columns.  Byte k of a column of thread
 // tid sits at column_base[k * nthreads + tid], so that the lock-step accesses
 // of a warp fall on consecutive bytes (global memory: one sector; shared
 // memory: no bank conflict).
-//   S (ecc bytes): syndromes;
-//   A, B, C (ecc/2 + 2 bytes each): the rotating Berlekamp-Massey polynomials
-//   (degree <= L <= ecc/2 while they are live), then the root positions in a
-//   free one;
-//   R (ecc bytes): remainder logs, Chien exponents, then the evaluator.
+//   S (ecc bytes): syndromes, then the evaluator (written over them);
+//   A, B, C (ecc/2 + 2 bytes each, consecutive): the remainder logs while
+//   the syndromes are formed (R, spanning all three), then the rotating
+//   Berlekamp-Massey polynomials (degree <= L <= ecc/2 while they are live),
+//   then Lambda, the root positions and the Chien exponents.
 struct DecodeScratchG {
     ScratchBytes S, A, B, C, R;
-    // cols == 0: the compact layout of decode_scratch_bytes(ecc) bytes per
-    // thread; else five columns of cols bytes
+    // ecc == 0: 256-byte columns; else the compact layout of
+    // decode_scratch_bytes(ecc) bytes per thread
     __device__ DecodeScratchG(uint8_t *g, size_t tid, size_t nthreads, int ecc = 0) {
         uint8_t *b = g + tid;
         const size_t s = ecc ? (size_t)ecc : 256, h = ecc ? (size_t)(ecc / 2 + 2) : 256;
@@ -102,12 +102,12 @@ struct DecodeScratchG {
         A = {b + s * nthreads, nthreads};
         B = {b + (s + h) * nthreads, nthreads};
         C = {b + (s + 2 * h) * nthreads, nthreads};
-        R = {b + (s + 3 * h) * nthreads, nthreads};
+        R = A;  // 3h >= ecc bytes from A on
     }
 };
 constexpr size_t kDecodeScratchBytes = 2048;  // per thread, the 256-byte-column layout
 // per thread, the compact layout for ecc
-__host__ __device__ constexpr size_t decode_scratch_bytes(int ecc) { return 2 * (size_t)ecc + 3 * (size_t)(ecc / 2 + 2); }
+__host__ __device__ constexpr size_t decode_scratch_bytes(int ecc) { return (size_t)ecc + 3 * (size_t)(ecc / 2 + 2); }
 
 // Syndromes from the remainder: S_j = sum_m R[m] a^{-j(m+1)}, j-outer with
 // the exponent of each term stepped by j (no multiplications), the remainder
@@ -153,9 +153,9 @@ static __device__ void synds_from_rem(const uint32_t (&rem)[W], int ecc, const u
 // m + deg B <= the new L), and L never shrinks, so the run stops as soon as
 // L passes ecc/2 (the reference's decode then fails whatever follows) and
 // the buffers need ecc/2 + 1 coefficients.  Returns L; *lam is left on the
-// buffer holding Lambda and *fr on a free one.
+// buffer holding Lambda and *fr, *fr2 on the free ones.
 static __device__ int rs_bm(const DecodeScratchG &sc, int ecc, const uint8_t *ex, const uint8_t *lg,
-                            ScratchBytes *lam, ScratchBytes *fr) {
+                            ScratchBytes *lam, ScratchBytes *fr, ScratchBytes *fr2) {
     ScratchBytes A = sc.A, P = sc.B, T = sc.C;
     A[0] = 1;
     P[0] = 1;
@@ -208,6 +208,7 @@ static __device__ int rs_bm(const DecodeScratchG &sc, int ecc, const uint8_t *ex
     for (int k = degA + 1; k <= L; ++k) A[k] = 0;
     *lam = A;
     *fr = T;
+    *fr2 = P;
     return L;
 }
 
@@ -250,8 +251,8 @@ static __device__ void decode_one(uint8_t *d, uint8_t *p, int msg_len, int ecc, 
 // sums differs.
 static __device__ void decode_solve(uint8_t *d, uint8_t *p, int msg_len, int ecc, const uint8_t *ex, const uint8_t *lg,
                              const DecodeScratchG &sc, uint8_t *status) {
-    ScratchBytes lam, pos;
-    const int errors = rs_bm(sc, ecc, ex, lg, &lam, &pos);
+    ScratchBytes lam, pos, xp;
+    const int errors = rs_bm(sc, ecc, ex, lg, &lam, &pos, &xp);
     if (errors > ecc / 2) {
         *status = 0;
         return;
@@ -262,10 +263,11 @@ static __device__ void decode_solve(uint8_t *d, uint8_t *p, int msg_len, int ecc
     // zeros of Lambda at x = a^{-i}, i < size, in increasing i, stopping at
     // errors + 1 roots.  Term k at position i has exponent
     // log(Lambda_k) - i k (mod 255); eight positions per pass, each term's
-    // exponent kept in sc.R between passes (255: a zero coefficient).
+    // exponent kept in the free buffer xp between passes (255: a zero
+    // coefficient).
     for (int k = 0; k <= errors; ++k) {
         const uint32_t c = lam[k];
-        sc.R[k] = c ? lg[c] % 255 : 255;
+        xp[k] = c ? lg[c] % 255 : 255;
     }
     int roots = 0;
     for (int i0 = 0; i0 < npos && roots <= errors; i0 += 8) {
@@ -273,7 +275,7 @@ static __device__ void decode_solve(uint8_t *d, uint8_t *p, int msg_len, int ecc
 #pragma unroll
         for (int j = 0; j < 8; ++j) acc[j] = 0;
         for (int k = 0; k <= errors; ++k) {
-            int e = sc.R[k];
+            int e = xp[k];
             if (e == 255) continue;
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
@@ -281,7 +283,7 @@ static __device__ void decode_solve(uint8_t *d, uint8_t *p, int msg_len, int ecc
                 e -= k;
                 if (e < 0) e += 255;
             }
-            sc.R[k] = (uint8_t)e;
+            xp[k] = (uint8_t)e;
         }
 #pragma unroll
         for (int j = 0; j < 8; ++j)
@@ -291,13 +293,14 @@ static __device__ void decode_solve(uint8_t *d, uint8_t *p, int msg_len, int ecc
         *status = 0;
         return;
     }
-    // Forney: Omega = (S * Lambda) mod x^ecc (into sc.R), nonzero
+    // Forney: Omega = (S * Lambda) mod x^ecc, non-zero.  Omega_k needs
+    // S_0 .. S_k only, so it is written over S_k from the top down.
     uint32_t anyo = 0;
-    for (int k = 0; k < ecc; ++k) {
+    for (int k = ecc - 1; k >= 0; --k) {
         uint32_t v = 0;
         const int top = k < errors ? k : errors;
         for (int j = 0; j <= top; ++j) v ^= gmul(ex, lg, lam[j], sc.S[k - j]);
-        sc.R[k] = (uint8_t)v;
+        sc.S[k] = (uint8_t)v;
         anyo |= v;
     }
     if (!anyo) {
@@ -313,7 +316,7 @@ static __device__ void decode_solve(uint8_t *d, uint8_t *p, int msg_len, int ecc
         const uint32_t xinv = ginv(ex, lg, xi);
         const uint32_t lx = lg[xinv], lx2 = lx + lx;  // xinv != 0
         uint32_t num = 0;
-        for (int k = ecc - 1; k >= 0; --k) num = (num ? (uint32_t)ex[lg[num] + lx] : 0u) ^ sc.R[k];
+        for (int k = ecc - 1; k >= 0; --k) num = (num ? (uint32_t)ex[lg[num] + lx] : 0u) ^ sc.S[k];
         uint32_t den = 0;
         for (int k = errors - ((errors & 1) ? 0 : 1); k >= 1; k -= 2)
             den = (den ? (uint32_t)ex[(lg[den] + lx2) % 255] : 0u) ^ lam[k];  // den xinv^2 + Lambda_k
