@@ -504,16 +504,17 @@ void build_plan(ffgpu_batch &B, int tile_rs, int tile_rsi, int ctas_rs, int ctas
             const Rsi16Code &c = *static_cast<const ffgpu_rsi16 *>(r.handle)->code;
             bc.rsi = c.dev;
             const uint32_t ci = code_index(B, r.handle, bc);
-            // repairs of 16 blocks or more with a Berlekamp-Massey per lane go
-            // by 32-block batches (fewer would leave most lanes idle)
-            const bool lane_bm = r.kind == BK_RSI16_DEC && (c.ecc == 32 || c.ecc == 64) && r.nblocks >= 16;
-            const size_t tile = lane_bm ? 32 : (size_t)tile_rsi;
+            // repair items of 8 blocks or more run a Berlekamp-Massey per lane
+            // (one lane per block); the tile trades lanes busy per warp
+            // against warps busy per batch
+            const size_t tile = (size_t)tile_rsi;
+            const bool lane_bm = r.kind == BK_RSI16_DEC && (c.ecc == 32 || c.ecc == 64) && tile >= 8;
             for (size_t b0 = 0; b0 < r.nblocks; b0 += tile) {
                 BatchItem it{};
                 it.kind = r.kind;
                 it.code = ci;
                 it.nblocks = (uint32_t)std::min<size_t>(tile, r.nblocks - b0);
-                it.lane_bm = lane_bm && it.nblocks >= 16;
+                it.lane_bm = lane_bm && it.nblocks >= 8;
                 it.msg = static_cast<uint16_t *>(r.a) + b0 * c.message_len;
                 it.par = static_cast<uint16_t *>(r.b) + b0 * c.ecc;
                 it.status = r.status ? r.status + b0 : nullptr;
@@ -682,7 +683,7 @@ void autotune(ffgpu_batch &B, cudaStream_t st) {
         return ms;
     };
     const int tiles_rs[] = {128, 512, 2048};
-    const int tiles_rsi[] = {2, 8, 32};
+    const int tiles_rsi[] = {2, 4, 8, 16, 32};
     const int ctas[] = {1, 2, 4, 0};
     int bt_rs = B.tile_rs, bt_rsi = B.tile_rsi, bc_rs = B.ctas_rs, bc_rsi = B.ctas_rsi;
     bool any_rs = false;
