@@ -215,6 +215,8 @@ def bench_rs256_decode(args, torch, rank, world):
     nb, ml, ecc = args.blocks or (1 << 20), 223, 32
     data0, par0 = make_rs256_decode_inputs(torch, nb, 1000 + rank)
     code = capi.RS256Code(ecc)
+    if args.table_only:  # the per-thread table decoder instead of the bitsliced kernels
+        code.set_table_only(True)
     nbuf = max(1, min(args.steps, 4))
     bufs = [(data0.clone(), par0.clone(), torch.zeros(nb, dtype=torch.uint8, device="cuda")) for _ in range(nbuf)]
     stream = torch.cuda.current_stream()
@@ -292,6 +294,7 @@ def bench_rs256_decode(args, torch, rank, world):
         "e2e": e2e,
         "config": {"workload": "RS256 decode ecc_len=32, 1048576 blocks x (223+32) B, 0-16 errors/block, "
                                "1% 17-20 errors", "blocks": nb, "message_len": ml, "ecc_len": ecc,
+                   "decoder": "per-thread table decoder" if args.table_only else "bitsliced",
                    "l2": "inputs larger than L2 (268 MB per step; 4 rotating buffers)"},
         "dtype": "u8",
         "status_ok_fraction": float(st.float().mean().item()),
@@ -1116,6 +1119,8 @@ def main():
     ap.add_argument("--blocks", type=int, default=0,
                     help="override the block count (small cases for profiling; not a bench line)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer pass (profiling)")
+    ap.add_argument("--table-only", action="store_true",
+                    help="rs256-decode through the per-thread table decoder (profiling that kernel)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
