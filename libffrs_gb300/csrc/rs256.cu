@@ -73,66 +73,6 @@ __global__ void __launch_bounds__(128) rs256_decode_table_kernel(uint8_t *__rest
                       status ? status + blk : nullptr, synds_out ? synds_out + blk * (size_t)ecc : nullptr);
 }
 
-// Decode from precomputed syndromes (ecc bytes per block).
-__global__ void __launch_bounds__(128) rs256_solve_kernel(uint8_t *__restrict__ data, uint8_t *__restrict__ parity,
-                                                          size_t nblocks, int msg_len,
-                                                          const uint8_t *__restrict__ exp512,
-                                                          const uint8_t *__restrict__ log256, int ecc,
-                                                          const uint8_t *__restrict__ synds,
-                                                          uint8_t *__restrict__ status,
-                                                          uint8_t *__restrict__ gscratch) {
-    __shared__ uint8_t ex[512], lg[256];
-    for (int i = threadIdx.x; i < 512; i += blockDim.x) ex[i] = exp512[i];
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) lg[i] = log256[i];
-    __syncthreads();
-    const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const size_t nthreads = (size_t)gridDim.x * blockDim.x;
-    const DecodeScratchG sc(gscratch, tid, nthreads);
-    for (size_t blk = tid; blk < nblocks; blk += nthreads) {
-        const uint8_t *s = synds + blk * (size_t)ecc;
-        uint32_t any = 0;
-        if ((ecc & 3) == 0) {
-            for (int j = 0; j < ecc; j += 4) {
-                const uint32_t w = *reinterpret_cast<const uint32_t *>(s + j);
-                any |= w;
-                sc.S[j] = (uint8_t)w;
-                sc.S[j + 1] = (uint8_t)(w >> 8);
-                sc.S[j + 2] = (uint8_t)(w >> 16);
-                sc.S[j + 3] = (uint8_t)(w >> 24);
-            }
-        } else {
-            for (int j = 0; j < ecc; ++j) {
-                any |= s[j];
-                sc.S[j] = s[j];
-            }
-        }
-        if (!any) {
-            status[blk] = 1;
-            continue;
-        }
-        decode_solve(data + blk * (size_t)msg_len, parity + blk * (size_t)ecc, msg_len, ecc, ex, lg, sc,
-                     status + blk);
-    }
-}
-
-void rs256_solve(const Rs256Code &c, uint8_t *data, uint8_t *parity, size_t nblocks, int msg_len, const uint8_t *synds,
-                 uint8_t *status, cudaStream_t st) {
-    const unsigned threads = 128;
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const size_t grid = std::min<size_t>(grid_for(nblocks, threads), (size_t)(sms > 0 ? sms : 132) * 8);
-    void *scratch = nullptr;
-    FFGPU_CHECK_CUDA(cudaMallocAsync(&scratch, grid * threads * kDecodeScratchBytes, st));
-    KernelTimer kt_timer("rs256_solve_kernel", st);
-    rs256_solve_kernel<<<(unsigned)grid, threads, 0, st>>>(data, parity, nblocks, msg_len, c.d_exp512, c.d_log256,
-                                                          c.ecc, synds, status, (uint8_t *)scratch);
-    cudaError_t le = cudaGetLastError();
-    cudaFreeAsync(scratch, st);
-    if (le != cudaSuccess) throw Error(FFGPU_ECUDA, std::string("rs256_solve_kernel: ") + cudaGetErrorString(le));
-    launched();
-}
-
 // ---------------------------------------------------------------- host
 
 static int bucket_words(int ecc) {

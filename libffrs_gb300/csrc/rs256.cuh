@@ -45,9 +45,6 @@ void rs256_decode_table(const Rs256Code &c, uint8_t *data, uint8_t *parity, size
 // the request, else the table kernel
 void rs256_synds(const Rs256Code &c, const uint8_t *data, const uint8_t *parity, size_t nblocks, int msg_len,
                  uint8_t *synds, cudaStream_t st);
-// decode from syndromes already computed (ecc bytes per block)
-void rs256_solve(const Rs256Code &c, uint8_t *data, uint8_t *parity, size_t nblocks, int msg_len, const uint8_t *synds,
-                 uint8_t *status, cudaStream_t st);
 bool rs256_fast_synds(const Rs256Code &c, const uint8_t *data, const uint8_t *parity, size_t nblocks, int msg_len,
                       uint8_t *synds, cudaStream_t st);
 
