@@ -86,8 +86,7 @@ struct ScratchBytes {
 // tid sits at column_base[k * nthreads + tid], so that the lock-step accesses
 // of a warp fall on consecutive bytes (global memory: one sector; shared
 // memory: no bank conflict).
-//   S (ecc bytes): the syndromes' logs (mod 255; 255 marks a zero), then the
-//   evaluator's values (written over them);
+//   S (ecc bytes): syndromes, then the evaluator (written over them);
 //   A, B, C (ecc/2 + 2 bytes each, consecutive): the remainder logs while
 //   the syndromes are formed (R, spanning all three), then the rotating
 //   Berlekamp-Massey polynomials (degree <= L <= ecc/2 while they are live),
@@ -110,8 +109,7 @@ constexpr size_t kDecodeScratchBytes = 2048;  // per thread, the 256-byte-column
 // per thread, the compact layout for ecc
 __host__ __device__ constexpr size_t decode_scratch_bytes(int ecc) { return (size_t)ecc + 3 * (size_t)(ecc / 2 + 2); }
 
-// Syndromes from the remainder, S_j = sum_m R[m] a^{-j(m+1)}, stored as logs
-// (mod 255; 255 for a zero syndrome); j-outer with
+// Syndromes from the remainder: S_j = sum_m R[m] a^{-j(m+1)}, j-outer with
 // the exponent of each term stepped by j (no multiplications), the remainder
 // bytes' logs (mod 255) staged in sc.R (255 marks a zero byte).
 template <int W>
@@ -143,7 +141,7 @@ static __device__ void synds_from_rem(const uint32_t (&rem)[W], int ecc, const u
         }
 #pragma unroll
         for (int q = 0; q < 8; ++q)
-            if (j0 + q < ecc) sc.S[j0 + q] = (uint8_t)(acc[q] ? lg[acc[q]] % 255 : 255);
+            if (j0 + q < ecc) sc.S[j0 + q] = (uint8_t)acc[q];
     }
 }
 
@@ -164,13 +162,9 @@ static __device__ int rs_bm(const DecodeScratchG &sc, int ecc, const uint8_t *ex
     int degA = 0, degP = 0, L = 0, m = 1;
     uint32_t b = 1;
     for (int n = 0; n < ecc; ++n) {
-        const uint32_t ln = sc.S[n];
-        uint32_t d = ln != 255u ? (uint32_t)ex[ln] : 0u;
+        uint32_t d = sc.S[n];
         const int top = L < degA ? L : degA;
-        for (int i = 1; i <= top; ++i) {
-            const uint32_t a = A[i], ls = sc.S[n - i];
-            if (a && ls != 255u) d ^= ex[lg[a] + ls];  // Lambda_i S_{n-i}
-        }
+        for (int i = 1; i <= top; ++i) d ^= gmul(ex, lg, A[i], sc.S[n - i]);
         if (d == 0) {
             ++m;
             continue;
@@ -237,10 +231,7 @@ static __device__ void decode_one(uint8_t *d, uint8_t *p, int msg_len, int ecc, 
     if (synds_out) {
         if (any) {
             synds_from_rem<W>(rem, ecc, ex, lg, sc);
-            for (int j = 0; j < ecc; ++j) {
-                const uint32_t l = sc.S[j];
-                synds_out[j] = l != 255u ? ex[l] : 0;
-            }
+            for (int j = 0; j < ecc; ++j) synds_out[j] = sc.S[j];
         } else {
             for (int j = 0; j < ecc; ++j) synds_out[j] = 0;
         }
@@ -255,7 +246,7 @@ static __device__ void decode_one(uint8_t *d, uint8_t *p, int msg_len, int ecc, 
 }
 
 // The part of rs_decode::decode after the syndromes (reed_solomon.hpp:568-594),
-// with sc.S holding the logs of non-zero syndromes.  Every decision and every corrected
+// with sc.S holding non-zero syndromes.  Every decision and every corrected
 // byte is the reference's; only the evaluation order of the (exact) field
 // sums differs.
 static __device__ void decode_solve(uint8_t *d, uint8_t *p, int msg_len, int ecc, const uint8_t *ex, const uint8_t *lg,
@@ -308,11 +299,8 @@ static __device__ void decode_solve(uint8_t *d, uint8_t *p, int msg_len, int ecc
     for (int k = ecc - 1; k >= 0; --k) {
         uint32_t v = 0;
         const int top = k < errors ? k : errors;
-        for (int j = 0; j <= top; ++j) {
-            const uint32_t a = lam[j], ls = sc.S[k - j];
-            if (a && ls != 255u) v ^= ex[lg[a] + ls];  // Lambda_j S_{k-j}
-        }
-        sc.S[k] = (uint8_t)v;  // a value from here on, no longer a log
+        for (int j = 0; j <= top; ++j) v ^= gmul(ex, lg, lam[j], sc.S[k - j]);
+        sc.S[k] = (uint8_t)v;
         anyo |= v;
     }
     if (!anyo) {
