@@ -212,8 +212,8 @@ FFGPU_API int ffgpu_circ16_repair_host(const ffgpu_circ16 *code, uint16_t *msg, 
  * geometries and directions (device buffers, laid out as for the per-code
  * entry points above) and serves all of them in one launch sequence: the
  * CIRC16 requests gathered per code and direction through the staged
- * encode / repair, then one persistent kernel per item class (RS256 by
- * remainder width, RSi16) side by side on forked streams.  The sequence can
+ * encode / repair on a high-priority stream, beside one persistent kernel per
+ * item class (RS256 by remainder width, RSi16) on forked streams.  The sequence can
  * be captured into a CUDA graph and replayed.  Results are byte-identical to
  * calling the per-code entry point once per request.  A batch holds pointers:
  * the buffers must stay valid while it is planned, captured and launched. */

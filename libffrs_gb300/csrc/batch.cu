@@ -16,7 +16,7 @@
 // walk alone.  Their codewords are gathered (one copy kernel) into contiguous
 // arrays per code and direction, run through circ16_encode /
 // circ16_repair_many (every stage one launch over all of them) and scattered
-// back, ahead of the persistent kernel on the same stream.
+// back, on a high-priority side stream beside the persistent kernels.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -301,9 +301,10 @@ struct ffgpu_batch {
     std::vector<CircGroup> circ;
     size_t n_gather = 0, n_scatter = 0;
     DeviceBuffer d_cmsg, d_cecc, d_cst, d_cws, d_segs;
-    // side streams of the class launches (index 0 unused: the caller's)
-    cudaStream_t side[kClasses] = {};
-    cudaEvent_t ev_fork = nullptr, ev_join[kClasses] = {};
+    // side streams of the class launches (index 0 unused: the caller's) and
+    // of the CIRC16 chain
+    cudaStream_t side[kClasses] = {}, circ_st = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join[kClasses] = {}, ev_cfork = nullptr, ev_cjoin = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int graph_kernels = 1;
@@ -316,6 +317,9 @@ struct ffgpu_batch {
             if (ev_join[k]) cudaEventDestroy(ev_join[k]);
         }
         if (ev_fork) cudaEventDestroy(ev_fork);
+        if (circ_st) cudaStreamDestroy(circ_st);
+        if (ev_cfork) cudaEventDestroy(ev_cfork);
+        if (ev_cjoin) cudaEventDestroy(ev_cjoin);
     }
     void drop_graph() {
         if (exec) cudaGraphExecDestroy(exec);
@@ -591,8 +595,30 @@ constexpr int kRunRs256 = 7, kRunRsi16 = 8, kRunCirc = 16, kRunAll = 31;
 // The class launches run side by side (class k > 0 on side stream k, forked
 // from and joined back into st), so that one class's tail overlaps the
 // others' work.
+void launch_classes(ffgpu_batch &B, cudaStream_t st, bool timed, int which);
+
 void launch_plan(ffgpu_batch &B, cudaStream_t st, bool timed, int which = kRunAll) {
-    if ((which & kRunCirc) && !B.circ.empty()) launch_circ(B, st);
+    // the CIRC16 chain (many short dependent launches) on a high-priority
+    // side stream, beside the class launches
+    const bool circ = (which & kRunCirc) && !B.circ.empty();
+    if (circ) {
+        if (!B.circ_st) {
+            int lo = 0, hi = 0;
+            FFGPU_CHECK_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+            FFGPU_CHECK_CUDA(cudaStreamCreateWithPriority(&B.circ_st, cudaStreamNonBlocking, hi));
+            FFGPU_CHECK_CUDA(cudaEventCreateWithFlags(&B.ev_cfork, cudaEventDisableTiming));
+            FFGPU_CHECK_CUDA(cudaEventCreateWithFlags(&B.ev_cjoin, cudaEventDisableTiming));
+        }
+        FFGPU_CHECK_CUDA(cudaEventRecord(B.ev_cfork, st));
+        FFGPU_CHECK_CUDA(cudaStreamWaitEvent(B.circ_st, B.ev_cfork, 0));
+        launch_circ(B, B.circ_st);
+        FFGPU_CHECK_CUDA(cudaEventRecord(B.ev_cjoin, B.circ_st));
+    }
+    launch_classes(B, st, timed, which);
+    if (circ) FFGPU_CHECK_CUDA(cudaStreamWaitEvent(st, B.ev_cjoin, 0));
+}
+
+void launch_classes(ffgpu_batch &B, cudaStream_t st, bool timed, int which) {
     int run[kClasses], n = 0;
     for (int k = 0; k < kClasses; ++k)
         if ((which & (1 << k)) && !B.cls[k].items.empty()) run[n++] = k;
