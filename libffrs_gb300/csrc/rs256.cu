@@ -119,12 +119,13 @@ static void launch_encode_table(const Rs256Code &c, const uint8_t *data, size_t 
                                 cudaStream_t st) {
     const unsigned threads = 128;
     const size_t smem = (size_t)256 * W * 4 + (size_t)threads * msg_len + 16;
-    static bool attr = false;
-    if (!attr) {
+    // once per process (a thread-safe static initialiser)
+    static const bool attr = [] {
         FFGPU_CHECK_CUDA(cudaFuncSetAttribute(rs256_encode_table_kernel<W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               200 * 1024));
-        attr = true;
-    }
+        return true;
+    }();
+    (void)attr;
     KernelTimer kt_timer("rs256_encode_table_kernel", st);
     rs256_encode_table_kernel<W><<<grid_for(nblocks, threads), threads, smem, st>>>(data, nblocks, msg_len, c.d_lut,
                                                                                     c.ecc, parity);
@@ -139,12 +140,12 @@ static void launch_decode_table(const Rs256Code &c, uint8_t *data, uint8_t *pari
     const size_t sm_scratch = decode_scratch_bytes(c.ecc) * threads;
     const bool in_smem = tables + sm_scratch <= 100 * 1024;  // ecc <= 64
     const size_t smem = tables + (in_smem ? sm_scratch : 0);
-    static bool attr = false;
-    if (!attr) {
+    static const bool attr = [] {
         FFGPU_CHECK_CUDA(cudaFuncSetAttribute(rs256_decode_table_kernel<W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               200 * 1024));
-        attr = true;
-    }
+        return true;
+    }();
+    (void)attr;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

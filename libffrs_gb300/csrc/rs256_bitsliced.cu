@@ -1434,13 +1434,12 @@ void rs256_fast_free(Rs256Code &c) {
 }
 
 static int sm_count() {
-    static int n = 0;
-    if (!n) {
-        int dev = 0;
+    static const int n = [] {  // once per process (a thread-safe static initialiser)
+        int dev = 0, v = 0;
         cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        if (n <= 0) n = 132;
-    }
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        return v > 0 ? v : 132;
+    }();
     return n;
 }
 
