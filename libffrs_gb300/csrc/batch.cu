@@ -1,11 +1,13 @@
 // Fused batch path: requests of mixed codes (RS256, RSi16, CIRC16), uneven
-// geometries and both directions are cut into work items and served by ONE
-// persistent launch.  Every CTA (four warps) pulls the next item from a global
-// counter; items are ordered longest first so the tail stays short.  The
-// launch can be captured once in a CUDA graph and replayed.  The schedule --
-// RS256 blocks per item, RSi16 blocks per item and CTAs per SM -- is chosen by
-// timing candidate plans on the batch itself (decode buffers are restored
-// after every trial).
+// geometries and both directions are served by one launch sequence.  RS256
+// and RSi16 requests are cut into work items, grouped into classes (RS256 by
+// the width of the LFSR remainder, RSi16), and each class is served by one
+// persistent launch on its own forked stream: an RS256 CTA (four warps) or an
+// RSi16 warp pulls the next item from the class's counter; items are ordered
+// longest first so the tail stays short.  The sequence can be captured once
+// in a CUDA graph and replayed.  The schedule -- RS256 blocks per item, RSi16
+// blocks per item and CTAs per SM -- is chosen by timing candidate plans on
+// the batch itself (decode buffers are restored after every trial).
 //
 // Each item runs the same per-block device code as the standalone kernels
 // (rs256_device.cuh, rsi16_device.cuh), so the bytes are identical to the
