@@ -1,12 +1,14 @@
-/* Host stand-in for <cuda_runtime.h>: lets the per-thread RS256 decoder
- * (libffrs_gb300/csrc/rs256_device.cuh) compile as plain C++ so that a CPU
- * test can run it against the oracle.  Only what that header uses. */
+/* Host stand-in for <cuda_runtime.h>: lets the device headers
+ * (libffrs_gb300/csrc/rs256_device.cuh, rsi16_device.cuh) compile as plain
+ * C++ so that CPU tests can run their algorithms against the oracle.  Only
+ * what those headers use; warp intrinsics come from warp_emu.h. */
 #pragma once
 #include <cstddef>
 #include <cstdint>
 #define __device__
 #define __host__
 #define __forceinline__ inline
+#define __noinline__
 static inline unsigned __funnelshift_r(unsigned lo, unsigned hi, unsigned shift) {
     return (unsigned)((((unsigned long long)hi << 32) | lo) >> (shift & 31));
 }
@@ -14,6 +16,15 @@ static inline unsigned __funnelshift_r(unsigned lo, unsigned hi, unsigned shift)
 struct uint4 {
     unsigned x, y, z, w;
 };
+typedef struct CUstream_st *cudaStream_t;
+template <typename T>
+static inline T min(T a, T b) {
+    return a < b ? a : b;
+}
+template <typename T>
+static inline T max(T a, T b) {
+    return a < b ? b : a;
+}
 struct HostDim3 {
     unsigned x = 0, y = 0, z = 0;
 };
