@@ -5,9 +5,11 @@ the oracle: CPU parity checks of the GPU code itself.
   remainder, syndromes, Berlekamp-Massey, Chien search, Forney) over ecc
   1..254, shortened blocks and error counts past the capacity.
 * The RSi16 register transforms (rsi16_device.cuh: the sub-warp syndromes and
-  encodes for ecc 2..16, the two-block register ones for ecc 32 and 64) on
-  the oracle's own code tables, with the warp emulated by 32 host threads in
-  lock step."""
+  encodes for ecc 2..16, the two-block register ones for ecc 32 and 64) and
+  the RSi16 repair paths (lane-per-block Berlekamp-Massey batches, the
+  per-block bounded-distance path, the step-for-step mirror, known positions)
+  on the oracle's own code tables, with the warp emulated by 32 host threads
+  in lock step."""
 
 import os
 import shutil
@@ -42,5 +44,19 @@ def test_rsi16_transforms_on_host(tmp_path):
                     os.path.join(REPO, "tests", "host", "rsi16_transform_check.cpp"), str(obj), "-o", str(exe)],
                    check=True)
     r = subprocess.run([str(exe), "17", "64"], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True,
+                       timeout=600)
+    assert r.returncode == 0 and r.stdout.strip().endswith("bad 0"), r.stdout[-2000:]
+
+
+@pytest.mark.skipif(shutil.which("g++") is None or shutil.which("gcc") is None, reason="needs gcc/g++")
+def test_rsi16_repairs_on_host(tmp_path):
+    obj = tmp_path / "ffrs_oracle.o"
+    exe = tmp_path / "rsi16_repair_check"
+    subprocess.run(["gcc", "-O2", "-c", os.path.join(REPO, "oracle", "ffrs_oracle.c"), "-o", str(obj)], check=True)
+    subprocess.run(["g++", "-O2", "-std=c++20", "-pthread", "-I", os.path.join(REPO, "tests", "host", "stub"),
+                    "-I", os.path.join(REPO, "libffrs_gb300", "csrc"), "-I", os.path.join(REPO, "oracle"),
+                    os.path.join(REPO, "tests", "host", "rsi16_repair_check.cpp"), str(obj), "-o", str(exe)],
+                   check=True)
+    r = subprocess.run([str(exe), "19", "3"], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True,
                        timeout=600)
     assert r.returncode == 0 and r.stdout.strip().endswith("bad 0"), r.stdout[-2000:]
