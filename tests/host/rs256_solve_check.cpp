@@ -3,7 +3,8 @@
 // search, Forney), compiled for the host and run block by block against the
 // oracle's rs_decode::decode (reed_solomon.hpp:559-595): same status, same
 // bytes, both from the oracle's remainder and through decode_one with the
-// library's own tables (gf256.h).  Usage:
+// library's own tables (gf256.h); and the table encoder (rs256_encode_one)
+// against the oracle's encoder.  Usage:
 // rs256_solve_check <seed> <trials per ecc>; prints "bad N", exits 1 if N > 0.
 #include <cstdio>
 #include <cstdlib>
@@ -43,6 +44,15 @@ static int run(int ecc, int trials, std::mt19937 &g) {
         std::vector<uint8_t> cw(n), par(ecc), rem(ecc);
         for (int i = 0; i < ml; ++i) cw[i] = (uint8_t)g();
         orc_rs256_encode(rs, cw.data(), ml, par.data());
+        {
+            // the table encoder of the GPU path (rs256_encode_one) on the same message
+            std::vector<uint8_t> mine(ecc);
+            rs256_encode_one<W>(cw.data(), ml, lut16, mine.data(), ecc);
+            if (mine != par) {
+                if (bad < 5) std::printf("encode ecc %d msg_len %d: parity differs\n", ecc, ml);
+                ++bad;
+            }
+        }
         std::memcpy(cw.data() + ml, par.data(), ecc);
         // 0 .. ecc/2 + 3 corrupted bytes (some past the capacity)
         const int k = (int)(g() % (unsigned)(ecc / 2 + 4));
