@@ -35,6 +35,7 @@ extern "C" {
 #define FFGPU_ENOMEM (-3)   /* device or pinned allocation failed */
 #define FFGPU_EASSERT (-4)  /* a reference py_assert would fire: RuntimeError */
 #define FFGPU_ETIMEOUT (-5) /* a bounded device wait gave up */
+#define FFGPU_ECANCELLED (-6) /* a served request was withdrawn by ffgpu_server_cancel */
 
 /* RSi16 repair status (libffrs/rsi16v.hpp:32-38) */
 #define FFGPU_NO_ERRORS 0
@@ -113,7 +114,10 @@ FFGPU_API int ffgpu_rs256_synds_host(const ffgpu_rs256 *code, const uint8_t *dat
  * aligned buffers; at most 524,288 blocks per call at ecc_len 32 (1,048,576
  * at 16), else FFGPU_EINVAL.  One scratch per device: calls that may overlap
  * on the device (other streams or threads) race and must be ordered by the
- * caller.  Make the first call on a device outside stream capture. */
+ * caller.  Make the first call on a device outside stream capture.  The
+ * scratch is the current device's, so the stream must belong to it
+ * (checked); a code set to the table decoder (ffgpu_rs256_set_table_only)
+ * is rejected with FFGPU_EINVAL. */
 FFGPU_API int ffgpu_rs256_decode_noalloc(const ffgpu_rs256 *code, uint8_t *data, uint8_t *parity, size_t nblocks,
                                          size_t message_len, uint8_t *status, void *stream);
 /* No reference counterpart.  table_only != 0 makes this code use the
@@ -267,14 +271,26 @@ FFGPU_API int ffgpu_server_submit_rsi16(ffgpu_server *server, const ffgpu_rsi16 
                                         uint16_t *parity, size_t nblocks, uint8_t *status, uint64_t *ticket);
 FFGPU_API int ffgpu_server_submit_circ16(ffgpu_server *server, const ffgpu_circ16 *code, int op, uint16_t *msg,
                                          uint16_t *ecc, size_t nblocks, uint8_t *status, uint64_t *ticket);
-/* state: 0 queued, 1 running, 2 done, 3 failed; times are seconds since the
- * server was created (submitted, admitted into a slot, completion seen) */
+/* state: 0 queued, 1 running, 2 done, 3 failed, 4 cancelled; times are
+ * seconds since the server was created (submitted, admitted into a slot,
+ * completion seen) */
 FFGPU_API int ffgpu_server_poll(ffgpu_server *server, uint64_t ticket, int *state, double *t_submit,
                                 double *t_start, double *t_done);
-/* block until the request is done; timeout_s < 0 waits without limit */
+/* block until the request is done; timeout_s < 0 waits without limit.  A
+ * failed request returns its error (FFGPU_ENOMEM when its device buffers
+ * could not be allocated), a cancelled one FFGPU_ECANCELLED. */
 FFGPU_API int ffgpu_server_wait(ffgpu_server *server, uint64_t ticket, double timeout_s);
-/* forget a finished request */
+/* forget a finished (done, failed or cancelled) request */
 FFGPU_API int ffgpu_server_release(ffgpu_server *server, uint64_t ticket);
+/* withdraw a request that is still queued (state 0): it becomes state 4 and
+ * its buffers are never touched; ffgpu_server_wait on it returns
+ * FFGPU_ECANCELLED.  A request already admitted (state >= 1) is not
+ * withdrawn: FFGPU_EINVAL. */
+FFGPU_API int ffgpu_server_cancel(ffgpu_server *server, uint64_t ticket);
+/* Test hook for the failure path, no device involved: the next n slot
+ * allocations of any server report out-of-memory (FFGPU_ENOMEM) as a failed
+ * cudaMallocAsync would; their requests fail, the server keeps serving. */
+FFGPU_API int ffgpu_server_debug_fail_allocs(int n);
 
 #ifdef __cplusplus
 }

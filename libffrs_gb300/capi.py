@@ -1,8 +1,9 @@
 """ctypes view of the C ABI in include/ffgpu.h (libffgpu.so).
 
-This is the boundary a non-Python caller binds; tests and
-bench.py use it to drive the kernels with device pointers (e.g. torch tensors'
-data_ptr()) and CUDA streams.
+This is the boundary a non-Python caller binds (ctypes here; cgo, JNI and
+other FFIs bind the same symbols); tests and bench.py use it to drive the
+kernels with device pointers (e.g. torch tensors' data_ptr()) and CUDA
+streams.
 """
 
 import ctypes
@@ -19,6 +20,7 @@ ECUDA = -2
 ENOMEM = -3
 EASSERT = -4
 ETIMEOUT = -5
+ECANCELLED = -6
 STATUS_ASSERT = 0xFF
 
 
@@ -109,6 +111,8 @@ def _declare(L):
         "ffgpu_server_poll": (_I, [_P, ctypes.c_uint64, ctypes.POINTER(_I)] + [ctypes.POINTER(ctypes.c_double)] * 3),
         "ffgpu_server_wait": (_I, [_P, ctypes.c_uint64, ctypes.c_double]),
         "ffgpu_server_release": (_I, [_P, ctypes.c_uint64]),
+        "ffgpu_server_cancel": (_I, [_P, ctypes.c_uint64]),
+        "ffgpu_server_debug_fail_allocs": (_I, [_I]),
         "ffgpu_batch_create": (_I, [_PP]),
         "ffgpu_batch_destroy": (_I, [_P]),
         "ffgpu_batch_clear": (_I, [_P]),
@@ -312,6 +316,10 @@ class Server:
     def release(self, ticket):
         call("ffgpu_server_release", self.h, ticket)
         self._keep.pop(ticket, None)
+
+    def cancel(self, ticket):
+        """withdraw a request that is still queued (FFGPUError if admitted)"""
+        call("ffgpu_server_cancel", self.h, ticket)
 
 
 def rsi16_repair_counters(reset=False):

@@ -303,6 +303,16 @@ struct ffgpu_batch {
     std::vector<CircGroup> circ;
     size_t n_gather = 0, n_scatter = 0;
     DeviceBuffer d_cmsg, d_cecc, d_cst, d_cws, d_segs;
+    // the plan's table uploads, staged in page-locked memory and copied on
+    // the plan's stream (ev_stage: the last staged copies, waited for before
+    // the staging is rewritten)
+    struct Upload {
+        void *dst;
+        std::vector<uint8_t> bytes;
+    };
+    std::vector<Upload> uploads;
+    PinnedBuffer h_stage;
+    cudaEvent_t ev_stage = nullptr;
     // side streams of the class launches (index 0 unused: the caller's) and
     // of the CIRC16 chain
     cudaStream_t side[kClasses] = {}, circ_st = nullptr;
@@ -314,6 +324,10 @@ struct ffgpu_batch {
 
     ~ffgpu_batch() {
         drop_graph();
+        if (ev_stage) {
+            cudaEventSynchronize(ev_stage);
+            cudaEventDestroy(ev_stage);
+        }
         for (int k = 1; k < kClasses; ++k) {
             if (side[k]) cudaStreamDestroy(side[k]);
             if (ev_join[k]) cudaEventDestroy(ev_join[k]);
@@ -376,6 +390,32 @@ size_t circ_group(ffgpu_batch &B, const ffgpu_batch::Req &r) {
 // Gathered arrays, workspaces and copy ranges of the CIRC16 requests: an
 // encode gathers messages and scatters ecc; a repair gathers and scatters
 // both, and scatters the status.
+void queue_upload(ffgpu_batch &B, void *dst, const void *src, size_t n) {
+    const uint8_t *p = static_cast<const uint8_t *>(src);
+    B.uploads.push_back({dst, std::vector<uint8_t>(p, p + n)});
+}
+
+// Copies the queued tables to the device on `st` through the page-locked
+// staging buffer: the host never waits for the device, except for the
+// previous plan's staged copies before their buffer is reused.
+void flush_uploads(ffgpu_batch &B, cudaStream_t st) {
+    size_t total = 0;
+    for (const auto &u : B.uploads) total += (u.bytes.size() + 15) & ~(size_t)15;
+    if (total) {
+        if (!B.ev_stage) FFGPU_CHECK_CUDA(cudaEventCreateWithFlags(&B.ev_stage, cudaEventDisableTiming));
+        else FFGPU_CHECK_CUDA(cudaEventSynchronize(B.ev_stage));
+        uint8_t *h = static_cast<uint8_t *>(B.h_stage.get(total));
+        size_t off = 0;
+        for (const auto &u : B.uploads) {
+            std::memcpy(h + off, u.bytes.data(), u.bytes.size());
+            FFGPU_CHECK_CUDA(cudaMemcpyAsync(u.dst, h + off, u.bytes.size(), cudaMemcpyHostToDevice, st));
+            off += (u.bytes.size() + 15) & ~(size_t)15;
+        }
+        FFGPU_CHECK_CUDA(cudaEventRecord(B.ev_stage, st));
+    }
+    B.uploads.clear();
+}
+
 void plan_circ(ffgpu_batch &B) {
     B.circ.clear();
     B.n_gather = B.n_scatter = 0;
@@ -423,7 +463,7 @@ void plan_circ(ffgpu_batch &B) {
     B.n_scatter = sca.size();
     gat.insert(gat.end(), sca.begin(), sca.end());
     B.d_segs.get(gat.size() * sizeof(CopySeg));
-    FFGPU_CHECK_CUDA(cudaMemcpy(B.d_segs.ptr, gat.data(), gat.size() * sizeof(CopySeg), cudaMemcpyHostToDevice));
+    queue_upload(B, B.d_segs.ptr, gat.data(), gat.size() * sizeof(CopySeg));
 }
 
 // The CIRC16 chain: gather, encode / repair per group, scatter.
@@ -465,8 +505,11 @@ void size_class(ffgpu_batch::ItemClass &k, int ctas) {
     k.grid = (unsigned)std::max<size_t>(1, std::min<size_t>((size_t)sm_count_b() * k.per_sm, k.items.size()));
 }
 
-void build_plan(ffgpu_batch &B, int tile_rs, int tile_rsi, int ctas_rs, int ctas_rsi) {
+// The tables go to the device on `st`: launches of the plan must follow on
+// the same stream (or after a synchronisation of it).
+void build_plan(ffgpu_batch &B, int tile_rs, int tile_rsi, int ctas_rs, int ctas_rsi, cudaStream_t st) {
     B.drop_graph();
+    B.uploads.clear();
     B.codes.clear();
     B.code_keys.clear();
     for (auto &K : B.cls) {
@@ -559,13 +602,10 @@ void build_plan(ffgpu_batch &B, int tile_rs, int tile_rsi, int ctas_rs, int ctas
     if (any_rs_dec) B.d_rs_scratch.get((size_t)B.cls[2].grid * kBatchThreads * kDecodeScratchBytes);
     for (auto &K : B.cls) {
         K.d_items.get(std::max<size_t>(1, K.items.size()) * sizeof(BatchItem));
-        if (!K.items.empty())
-            FFGPU_CHECK_CUDA(cudaMemcpy(K.d_items.ptr, K.items.data(), K.items.size() * sizeof(BatchItem),
-                                        cudaMemcpyHostToDevice));
+        if (!K.items.empty()) queue_upload(B, K.d_items.ptr, K.items.data(), K.items.size() * sizeof(BatchItem));
     }
-    if (!B.codes.empty())
-        FFGPU_CHECK_CUDA(cudaMemcpy(B.d_codes.ptr, B.codes.data(), B.codes.size() * sizeof(BatchCode),
-                                    cudaMemcpyHostToDevice));
+    if (!B.codes.empty()) queue_upload(B, B.d_codes.ptr, B.codes.data(), B.codes.size() * sizeof(BatchCode));
+    flush_uploads(B, st);
     B.planned = true;
 }
 
@@ -720,7 +760,7 @@ void autotune(ffgpu_batch &B, cudaStream_t st) {
         float best = 1e30f;
         for (int t : tiles_rs)
             for (int cps : ctas) {
-                build_plan(B, t, bt_rsi, cps, bc_rsi);
+                build_plan(B, t, bt_rsi, cps, bc_rsi, st);
                 const float ms = trial(kRunRs256);
                 if (ms < best) {
                     best = ms;
@@ -733,7 +773,7 @@ void autotune(ffgpu_batch &B, cudaStream_t st) {
         float best = 1e30f;
         for (int t : tiles_rsi)
             for (int cps : ctas) {
-                build_plan(B, bt_rs, t, bc_rs, cps);
+                build_plan(B, bt_rs, t, bc_rs, cps, st);
                 const float ms = trial(kRunRsi16);
                 if (ms < best) {
                     best = ms;
@@ -746,7 +786,7 @@ void autotune(ffgpu_batch &B, cudaStream_t st) {
     cudaEventDestroy(e1);
     copy_regions(B, regions, false, st);
     FFGPU_CHECK_CUDA(cudaStreamSynchronize(st));
-    build_plan(B, bt_rs, bt_rsi, bc_rs, bc_rsi);
+    build_plan(B, bt_rs, bt_rsi, bc_rs, bc_rsi, st);
 }
 
 }  // namespace
@@ -825,7 +865,7 @@ int ffgpu_batch_plan(ffgpu_batch *b, int autotune_on, void *stream) {
         if (autotune_on)
             autotune(*b, st);
         else
-            build_plan(*b, b->tile_rs, b->tile_rsi, b->ctas_rs, b->ctas_rsi);
+            build_plan(*b, b->tile_rs, b->tile_rsi, b->ctas_rs, b->ctas_rsi, st);
     });
 }
 
@@ -833,9 +873,11 @@ int ffgpu_batch_capture(ffgpu_batch *b, void *stream) {
     return guarded([&] {
         FFGPU_REQUIRE(b, "batch is NULL");
         std::lock_guard<std::mutex> lk(b->mu);
-        if (!b->planned) build_plan(*b, b->tile_rs, b->tile_rsi, b->ctas_rs, b->ctas_rsi);
-        b->drop_graph();
         cudaStream_t st = (cudaStream_t)stream;
+        if (!b->planned) build_plan(*b, b->tile_rs, b->tile_rsi, b->ctas_rs, b->ctas_rsi, st);
+        // the tables are on the device before any replay reads them
+        if (b->ev_stage) FFGPU_CHECK_CUDA(cudaEventSynchronize(b->ev_stage));
+        b->drop_graph();
         cudaStream_t cap = st;
         bool own = false;
         if (!cap) {  // the legacy default stream cannot be captured
@@ -878,7 +920,9 @@ int ffgpu_batch_launch(ffgpu_batch *b, void *stream) {
             launched(b->graph_kernels);
             return;
         }
-        if (!b->planned) build_plan(*b, b->tile_rs, b->tile_rsi, b->ctas_rs, b->ctas_rsi);
+        if (!b->planned) build_plan(*b, b->tile_rs, b->tile_rsi, b->ctas_rs, b->ctas_rsi, st);
+        // a plan made on another stream: its table uploads come first
+        if (b->ev_stage) FFGPU_CHECK_CUDA(cudaStreamWaitEvent(st, b->ev_stage, 0));
         launch_plan(*b, st, true);
     });
 }

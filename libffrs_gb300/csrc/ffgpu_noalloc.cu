@@ -23,7 +23,10 @@
 //   threads -- race on it; callers must order them (one stream, or events);
 // * the scratch address is looked up once per device with
 //   cudaGetSymbolAddress; make the first call on a device outside any stream
-//   capture.
+//   capture;
+// * the scratch used is the current device's: the stream must belong to the
+//   current device (checked), and a code switched to the table decoder
+//   (ffgpu_rs256_set_table_only) is rejected.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -64,6 +67,9 @@ int ffgpu_rs256_decode_noalloc(const ffgpu_rs256 *code, uint8_t *data, uint8_t *
         FFGPU_REQUIRE(message_len >= 1 && message_len + (size_t)c.ecc <= 255, "block_len must be <= 255");
         FFGPU_REQUIRE(c.fast && (c.ecc == 16 || c.ecc == 32),
                       "decode without allocation covers ecc_len 16 and 32 with primitive 2 and polynomial 0x11d");
+        FFGPU_REQUIRE(!c.table_only,
+                      "decode without allocation runs the bitsliced kernels; this code is set to the table decoder "
+                      "(ffgpu_rs256_set_table_only)");
         FFGPU_REQUIRE((((uintptr_t)data | (uintptr_t)parity) & 3) == 0,
                       "decode without allocation needs 4-byte aligned data and parity");
         const size_t need = rs256_fast_scratch_bytes(c.ecc, nblocks);
@@ -72,6 +78,14 @@ int ffgpu_rs256_decode_noalloc(const ffgpu_rs256 *code, uint8_t *data, uint8_t *
                                           std::to_string(need) + " bytes of scratch, the fixed scratch holds " +
                                           std::to_string(kNoAllocScratchBytes) + "; split the request");
         if (nblocks == 0) return;
+        int dev = 0;
+        FFGPU_CHECK_CUDA(cudaGetDevice(&dev));
+        if (stream) {
+            int sdev = dev;
+            FFGPU_CHECK_CUDA(cudaStreamGetDevice((cudaStream_t)stream, &sdev));
+            FFGPU_REQUIRE(sdev == dev, "decode without allocation: the stream belongs to another device than the "
+                                       "current one, whose scratch array the call would use");
+        }
         void *scratch = scratch_address();
         if (!rs256_fast_decode_with(c, data, parity, nblocks, (int)message_len, status, scratch, (cudaStream_t)stream))
             throw Error(FFGPU_EINVAL, "decode without allocation: request not covered by the bitsliced kernels");

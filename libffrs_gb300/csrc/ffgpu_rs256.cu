@@ -188,11 +188,18 @@ cudaStream_t HostPipeline::to_down(size_t k) {
 
 void HostPipeline::sync() { FFGPU_CHECK_CUDA(cudaStreamSynchronize(down())); }
 
+// The library is bound to one device, the one ffgpu_init names (default 0):
+// its stream, the pipeline streams and the code tables live there.  The
+// caller's current device is left as it was.
 cudaStream_t lib_stream() {
     std::lock_guard<std::mutex> lk(g_stream_mu);
     if (!g_stream) {
+        int prev = 0;
+        FFGPU_CHECK_CUDA(cudaGetDevice(&prev));
         FFGPU_CHECK_CUDA(cudaSetDevice(g_device));
-        FFGPU_CHECK_CUDA(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking));
+        const cudaError_t e = cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking);
+        cudaSetDevice(prev);
+        FFGPU_CHECK_CUDA(e);
         // the per-call scratch comes from the stream-ordered pool; keep freed
         // blocks in the pool across synchronisations instead of unmapping them
         cudaMemPool_t pool;

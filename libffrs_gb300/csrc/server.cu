@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <array>
+#include <atomic>
 #include <string>
 #include <chrono>
 #include <condition_variable>
@@ -39,8 +40,9 @@ struct SrvReq {
     size_t nblocks = 0, msg_len = 0;
     size_t a_bytes = 0, b_bytes = 0, s_bytes = 0;
     double t_submit = 0, t_start = 0, t_done = 0;
-    int state = 0;  // 0 queued, 1 running, 2 done, 3 failed
+    int state = 0;  // 0 queued, 1 running, 2 done, 3 failed, 4 cancelled
     std::string error;
+    int error_code = FFGPU_ECUDA;
 };
 
 struct Slot {
@@ -93,19 +95,37 @@ size_t round16(size_t n) { return (n + 255) & ~(size_t)255; }
 // device bytes of one request (its buffers, 256-byte aligned)
 size_t dev_need(const SrvReq &r) { return round16(r.a_bytes) + round16(r.b_bytes) + round16(r.s_bytes); }
 
-void fail_slot_requests(ffgpu_server &S, Slot &sl, const std::string &msg) {
+void fail_slot_requests(ffgpu_server &S, Slot &sl, const std::string &msg, int code) {
     for (SrvReq *r : sl.reqs) {
         r->state = 3;
         r->error = msg;
+        r->error_code = code;
         r->t_done = S.now();
     }
 }
 
-// issue one micro-batch on a free slot (called with the lock released)
+// Allocation failures injected by ffgpu_server_debug_fail_allocs: the next n
+// slot allocations report out-of-memory without calling CUDA, so that tests
+// exercise the failure path on the host.
+std::atomic<int> g_fail_allocs{0};
+
+bool take_injected_failure() {
+    int n = g_fail_allocs.load();
+    while (n > 0)
+        if (g_fail_allocs.compare_exchange_weak(n, n - 1)) return true;
+    return false;
+}
+
+// issue one micro-batch on a free slot (called with the lock released): the
+// device buffers, the batch's work list (planned while the slot's stream is
+// idle, its tables uploaded on that stream), then copies in, the batch
+// launch, copies out, the stream-ordered free and the completion event.
 void issue(ffgpu_server &S, Slot &sl) {
     size_t total = 0;
     for (SrvReq *r : sl.reqs) total += dev_need(*r);
     sl.dev_bytes = total;
+    if (take_injected_failure())
+        throw ffgpu::Error(FFGPU_ENOMEM, "cudaMallocAsync: out of memory (injected)");
     FFGPU_CHECK_CUDA(cudaMallocAsync(&sl.dev, total, sl.st));
     uint8_t *base = static_cast<uint8_t *>(sl.dev);
     ffgpu_batch_clear(sl.batch);
@@ -119,9 +139,6 @@ void issue(ffgpu_server &S, Slot &sl) {
         uint8_t *ds = base + off;
         off += round16(r->s_bytes);
         dptr.push_back({da, db, ds});
-        FFGPU_CHECK_CUDA(cudaMemcpyAsync(da, r->a, r->a_bytes, cudaMemcpyHostToDevice, sl.st));
-        if (r->op == FFGPU_OP_DECODE)
-            FFGPU_CHECK_CUDA(cudaMemcpyAsync(db, r->b, r->b_bytes, cudaMemcpyHostToDevice, sl.st));
         int rc = 0;
         if (r->kind == SK_RS256)
             rc = ffgpu_batch_add_rs256(sl.batch, static_cast<const ffgpu_rs256 *>(r->code), r->op, da, db, r->nblocks,
@@ -136,7 +153,15 @@ void issue(ffgpu_server &S, Slot &sl) {
                                         r->nblocks, r->op == FFGPU_OP_DECODE ? ds : nullptr);
         if (rc) throw ffgpu::Error(rc, ffgpu_last_error());
     }
+    // the plan needs only the device pointers; the slot's stream holds
+    // nothing but the allocation yet, so its synchronisation returns at once
     if (int rc = ffgpu_batch_plan(sl.batch, 0, sl.st)) throw ffgpu::Error(rc, ffgpu_last_error());
+    for (size_t i = 0; i < sl.reqs.size(); ++i) {
+        SrvReq *r = sl.reqs[i];
+        FFGPU_CHECK_CUDA(cudaMemcpyAsync(dptr[i][0], r->a, r->a_bytes, cudaMemcpyHostToDevice, sl.st));
+        if (r->op == FFGPU_OP_DECODE)
+            FFGPU_CHECK_CUDA(cudaMemcpyAsync(dptr[i][1], r->b, r->b_bytes, cudaMemcpyHostToDevice, sl.st));
+    }
     if (int rc = ffgpu_batch_launch(sl.batch, sl.st)) throw ffgpu::Error(rc, ffgpu_last_error());
     for (size_t i = 0; i < sl.reqs.size(); ++i) {
         SrvReq *r = sl.reqs[i];
@@ -206,8 +231,19 @@ void worker_main(ffgpu_server *S) {
             try {
                 issue(*S, sl);
             } catch (const std::exception &e) {
+                // copies already queued on the slot's stream may still read
+                // or write the callers' host buffers: let them finish before
+                // the requests are reported failed, then return the memory
+                cudaStreamSynchronize(sl.st);
+                if (sl.dev) {
+                    cudaFreeAsync(sl.dev, sl.st);
+                    cudaStreamSynchronize(sl.st);
+                    sl.dev = nullptr;
+                }
+                cudaGetLastError();
+                const auto *fe = dynamic_cast<const ffgpu::Error *>(&e);
                 lk.lock();
-                fail_slot_requests(*S, sl, e.what());
+                fail_slot_requests(*S, sl, e.what(), fe ? fe->code : FFGPU_ECUDA);
                 S->in_use -= need;
                 sl.reqs.clear();
                 sl.busy = false;
@@ -385,7 +421,34 @@ int ffgpu_server_wait(ffgpu_server *S, uint64_t ticket, double timeout_s) {
             S->done_cv.wait(lk, pred);
         else if (!S->done_cv.wait_for(lk, std::chrono::duration<double>(timeout_s), pred))
             throw Error(FFGPU_ETIMEOUT, "request not finished within the timeout");
-        if (r->state == 3) throw Error(FFGPU_ECUDA, "request failed: " + r->error);
+        if (r->state == 3) throw Error(r->error_code, "request failed: " + r->error);
+        if (r->state == 4) throw Error(FFGPU_ECANCELLED, "request cancelled");
+    });
+}
+
+// withdraw a request that is still queued; one already admitted into a slot
+// runs to completion
+int ffgpu_server_cancel(ffgpu_server *S, uint64_t ticket) {
+    return guarded([&] {
+        FFGPU_REQUIRE(S, "server is NULL");
+        std::lock_guard<std::mutex> lk(S->mu);
+        auto it = S->reqs.find(ticket);
+        FFGPU_REQUIRE(it != S->reqs.end(), "unknown ticket");
+        SrvReq *r = it->second.get();
+        if (r->state == 4) return;
+        FFGPU_REQUIRE(r->state == 0, "request already admitted: it runs to completion");
+        auto q = std::find(S->queue.begin(), S->queue.end(), r);
+        if (q != S->queue.end()) S->queue.erase(q);
+        r->state = 4;
+        r->t_done = S->now();
+        S->done_cv.notify_all();
+    });
+}
+
+int ffgpu_server_debug_fail_allocs(int n) {
+    return guarded([&] {
+        FFGPU_REQUIRE(n >= 0, "n must be >= 0");
+        g_fail_allocs.store(n);
     });
 }
 

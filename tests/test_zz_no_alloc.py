@@ -56,6 +56,55 @@ def test_noalloc_matches_decode_twice(built, ecc, ml, nb):
         np.testing.assert_array_equal(got[0], od)
 
 
+def _pool_used_high():
+    """High-water mark of the device's default stream-ordered pool (the pool
+    ffgpu_rs256_decode allocates its scratch from), read through the driver
+    API; None where the query is not available."""
+    import ctypes
+
+    try:
+        cu = ctypes.CDLL("libcuda.so.1")
+    except OSError:
+        return None
+    dev = ctypes.c_int()
+    pool = ctypes.c_void_p()
+    val = ctypes.c_uint64()
+    if cu.cuCtxGetDevice(ctypes.byref(dev)) or cu.cuDeviceGetDefaultMemPool(ctypes.byref(pool), dev):
+        return None
+    CU_MEMPOOL_ATTR_USED_MEM_HIGH = 8
+    if cu.cuMemPoolGetAttribute(pool, CU_MEMPOOL_ATTR_USED_MEM_HIGH, ctypes.byref(val)):
+        return None
+    return pool, cu, val.value
+
+
+def test_noalloc_allocates_nothing(built):
+    """After the high-water mark of the stream-ordered pool is reset, a
+    decode through the no-allocation entry point leaves it at zero, while the
+    allocating entry point raises it."""
+    import ctypes
+
+    import torch
+
+    from libffrs_gb300 import capi
+
+    torch.zeros(1, device="cuda")
+    q = _pool_used_high()
+    if q is None:
+        pytest.skip("the driver's pool attribute query is not available")
+    pool, cu, _ = q
+    code = capi.RS256Code(32)
+    rng = np.random.Generator(np.random.PCG64(3))
+    data, par = _blocks(rng, 4096, 223, 32)
+    _decode(torch, code, "ffgpu_rs256_decode_noalloc", data, par)  # first call: scratch address set-up
+    zero = ctypes.c_uint64(0)
+    CU_MEMPOOL_ATTR_USED_MEM_HIGH = 8
+    assert cu.cuMemPoolSetAttribute(pool, CU_MEMPOOL_ATTR_USED_MEM_HIGH, ctypes.byref(zero)) == 0
+    _decode(torch, code, "ffgpu_rs256_decode_noalloc", data, par)
+    assert _pool_used_high()[2] == 0
+    _decode(torch, code, "ffgpu_rs256_decode", data, par)
+    assert _pool_used_high()[2] > 0
+
+
 def test_noalloc_limits(built):
     import torch
 
@@ -71,3 +120,7 @@ def test_noalloc_limits(built):
         capi.call("ffgpu_rs256_decode_noalloc", other.h, d.data_ptr(), d.data_ptr(), 1, 200, d.data_ptr(), None)
     with pytest.raises(capi.FFGPUError, match="aligned"):
         capi.call("ffgpu_rs256_decode_noalloc", code.h, d.data_ptr() + 1, d.data_ptr(), 1, 223, d.data_ptr(), None)
+    with pytest.raises(capi.FFGPUError, match="table decoder"):
+        tab = capi.RS256Code(32)
+        tab.set_table_only(True)
+        capi.call("ffgpu_rs256_decode_noalloc", tab.h, d.data_ptr(), d.data_ptr(), 1, 223, d.data_ptr(), None)
