@@ -960,15 +960,82 @@ static __device__ __noinline__ void rsi16_repair_block(const Rsi16Dev &c, const 
         status[b] = count > 0 ? FFGPU_REPAIR_OK : (lanes ? FFGPU_ERROR_LOCATION_FAIL : FFGPU_NO_ERRORS);
 }
 
+// When the bounded-distance path may stand in for the reference.  The
+// reference's key-equation solver (RSi16v::_sugiyama, rsi16v_impl.hpp:271-440)
+// runs the Euclidean algorithm on x^ecc and S(x) = sum_j S_j x^j in the NTT
+// domain, and takes every quotient to have degree one: its first step forms
+// Q = x^ecc // S(x) from the two top coefficients of S (rsi16v_impl.hpp:
+// 313-320), and its later divisions and products (NTT::poly_div_ntt,
+// ntt.hpp:471-564) alias in the cyclic NTT domain once a quotient is longer.
+// On such a block it returns a wrong locator -- typically with no root at
+// all, ErrorLocationFail -- although the errors are within the code's
+// capacity, and its bytes and status are only reproduced by the
+// step-for-step mirror.  All quotients of that Euclidean run have degree one
+// exactly when Berlekamp-Massey on the reversed sequence S_{ecc-1}, ...,
+// S_0 is normal: its length grows by one at every even step until it reaches
+// its final value (no zero discrepancy at an even step before that).  The
+// bounded-distance path accepts a block only then.
+//
+// Warp-wide Berlekamp-Massey over the syndromes S (forward: S_0 first;
+// reverse: S_{ecc-1} first) on the buffers C, B, T of n1 words; returns L,
+// C receives the connection polynomial (forward), `normal` the check above
+// (reverse).
+static __device__ uint32_t w_bm(const Rsi16Dev &c, const uint32_t *S, uint32_t *&C, uint32_t *&B, uint32_t *&T,
+                                uint32_t n1, uint32_t ecc, bool reverse, bool &normal, int lane) {
+    for (uint32_t k = lane; k < n1; k += 32) {
+        C[k] = k == 0;
+        B[k] = k == 0;
+    }
+    __syncwarp();
+    uint32_t L = 0, m = 1, binv = 1;
+    bool stalled = false, abnormal = false;
+    for (uint32_t n = 0; n < ecc; ++n) {
+        // discrepancy d = sum_{i <= L} C_i S_{n-i} (reverse: S_{ecc-1-(n-i)})
+        uint32_t acc = 0;
+        for (uint32_t i = lane; i <= L && i <= n; i += 32)
+            acc += fmul(C[i], reverse ? S[ecc - 1 - (n - i)] : S[n - i]);
+        acc = __reduce_add_sync(0xffffffffu, acc) % 0x10001u;
+        const uint32_t d = acc;
+        if (d == 0) {
+            if (!(n & 1) && 2 * L <= n) stalled = true;
+            ++m;
+            continue;
+        }
+        const uint32_t coef = fmul(d, binv);
+        const bool grow = 2 * L <= n;
+        if (grow) {
+            abnormal |= stalled;
+            for (uint32_t k = lane; k < n1; k += 32) T[k] = C[k];
+            __syncwarp();
+        }
+        for (uint32_t k = lane; k < n1; k += 32)
+            if (k >= m) C[k] = fsub(C[k], fmul(coef, B[k - m]));
+        __syncwarp();
+        if (grow) {
+            uint32_t *x = B;
+            B = T;
+            T = x;
+            L = n + 1 - L;
+            binv = c.inv_tab[d];
+            m = 1;
+        } else {
+            ++m;
+        }
+    }
+    normal = !abnormal && L > 0 && L <= ecc / 2;
+    return L;
+}
+
 // Bounded-distance repair of block b by Berlekamp-Massey, for the blocks whose
 // error pattern has weight at most t = ecc/2.  The syndromes are the
 // reference's (first ecc outputs of the partial NTT: S_j = sum_i r_i X_i^j,
 // X_i = w^rbo(i)).  When BM returns a connection polynomial C of length
 // L <= t that has exactly L roots X_i^-1 among the block positions, there is
 // exactly one error pattern of weight <= t with these syndromes, and every
-// correct bounded-distance decoder -- the reference's NTT-domain Sugiyama
-// included -- returns it: the corrections block[i] += X_i Omega(X_i^-1) /
-// C'(X_i^-1) and RepairOk.  Returns false (block untouched) otherwise; the
+// correct bounded-distance decoder returns it: the corrections block[i] +=
+// X_i Omega(X_i^-1) / C'(X_i^-1) and RepairOk.  The reference's NTT-domain
+// Sugiyama is such a decoder only on the blocks w_bm calls normal; the path
+// accepts no other block.  Returns false (block untouched) otherwise; the
 // caller then runs the reference's algorithm step for step.
 // temp: ntt_len + 6 * ecc words.
 template <int EPL>
@@ -999,42 +1066,13 @@ static __device__ __noinline__ bool rsi16_repair_bm_block_t(const Rsi16Dev &c, c
         }
     }
     uint32_t *C = temp + ecc, *B = C + n1, *T = B + n1;
-    for (uint32_t k = lane; k < n1; k += 32) {
-        C[k] = k == 0;
-        B[k] = k == 0;
-    }
-    __syncwarp();
-    uint32_t L = 0, m = 1, binv = 1;
-    for (uint32_t n = 0; n < ecc; ++n) {
-        // discrepancy d = sum_{i <= L} C_i S_{n-i}
-        uint32_t acc = 0;
-        for (uint32_t i = lane; i <= L && i <= n; i += 32) acc += fmul(C[i], S[n - i]);
-        acc = __reduce_add_sync(0xffffffffu, acc) % 0x10001u;
-        const uint32_t d = acc;
-        if (d == 0) {
-            ++m;
-            continue;
-        }
-        const uint32_t coef = fmul(d, binv);
-        const bool grow = 2 * L <= n;
-        if (grow) {
-            for (uint32_t k = lane; k < n1; k += 32) T[k] = C[k];
-            __syncwarp();
-        }
-        for (uint32_t k = lane; k < n1; k += 32)
-            if (k >= m) C[k] = fsub(C[k], fmul(coef, B[k - m]));
-        __syncwarp();
-        if (grow) {
-            uint32_t *x = B;
-            B = T;
-            T = x;
-            L = n + 1 - L;
-            binv = c.inv_tab[d];
-            m = 1;
-        } else {
-            ++m;
-        }
-    }
+    // the reference's solver is exact on this block only when the reversed
+    // syndrome sequence is normal (see rev_normal below); run that check first
+    // on the same buffers, then the locator itself
+    bool normal = false;
+    w_bm(c, S, C, B, T, n1, ecc, true, normal, lane);
+    if (!normal) return false;
+    uint32_t L = w_bm(c, S, C, B, T, n1, ecc, false, normal, lane);
     if (L == 0 || L > t) return false;
     // C must have degree exactly L (checked through the root count below)
     for (uint32_t k = lane; k < n1; k += 32)
@@ -1176,6 +1214,46 @@ static __device__ __forceinline__ uint32_t rsi16_bm_lane(const uint32_t *S, cons
         }
     }
     return L;
+}
+
+// The normality check of w_bm on one lane: Berlekamp-Massey over the
+// reversed column S_{ecc-1}, ..., S_0 with T + 1 coefficients, true when its
+// length grows by one at every even step up to its final value L <= T (the
+// truncation argument of rsi16_bm_lane holds unchanged: while L <= T the
+// polynomials stay within T + 1 coefficients).
+template <int T>
+static __device__ __forceinline__ bool rsi16_rev_normal_lane(const uint32_t *S, const uint32_t *inv_tab, uint32_t ecc) {
+    uint32_t C[T + 1], Bs[T + 1];
+#pragma unroll
+    for (int i = 0; i <= T; ++i) {
+        C[i] = i == 0 ? 1u : 0u;
+        Bs[i] = i == 1 ? 1u : 0u;
+    }
+    uint32_t L = 0, binv = 1;
+    bool stalled = false, abnormal = false;
+#pragma unroll 1
+    for (uint32_t n = 0; n < ecc; ++n) {
+        uint64_t acc = 0;
+#pragma unroll
+        for (int i = 0; i <= T; ++i)
+            if ((uint32_t)i <= n) acc += (uint64_t)C[i] * S[(ecc - 1 - (n - i)) * kColStride];
+        const uint32_t d = (uint32_t)(acc % 0x10001u);
+        const uint32_t coef = fmul(d, binv);
+        const bool grow = d != 0 && 2 * L <= n;
+        if (d == 0 && !(n & 1) && 2 * L <= n) stalled = true;
+        abnormal |= grow && stalled;
+#pragma unroll
+        for (int i = T; i >= 0; --i) {
+            const uint32_t bi = Bs[i];
+            Bs[i] = i == 0 ? 0u : (grow ? C[i - 1] : Bs[i - 1]);
+            C[i] = fsub(C[i], fmul(coef, bi));
+        }
+        if (grow) {
+            L = n + 1 - L;
+            binv = inv_tab[d];
+        }
+    }
+    return !abnormal && L > 0 && L <= (uint32_t)T;
 }
 
 // The rest of the bounded-distance path, from a block's syndromes (column S)
@@ -1394,6 +1472,9 @@ static __device__ __forceinline__ void rsi16_repair32(const Rsi16Dev &c, const B
     if ((nz >> lane) & 1u) {
         uint32_t C[T + 1];
         L = rsi16_bm_lane<T>(Ssm + lane, c.inv_tab, c.ecc, C);
+        // only where the reference's solver is exact (see w_bm); L = 0 sends
+        // the block to the mirror
+        if (!rsi16_rev_normal_lane<T>(Ssm + lane, c.inv_tab, c.ecc)) L = 0;
 #pragma unroll
         for (int i = 0; i <= T; ++i) Csm[i * kColStride + lane] = C[i];
     }

@@ -86,6 +86,48 @@ static void corrupt(std::mt19937 &g, uint16_t *w, size_t n, size_t k) {
     for (size_t q = 0; q < k; ++q) w[g() % n] = (uint16_t)g();
 }
 
+static uint32_t pmul(uint32_t a, uint32_t b) { return (uint32_t)((uint64_t)a * b % 65537u); }
+static uint32_t ppow(uint32_t a, uint32_t e) {
+    uint32_t r = 1;
+    for (; e; e >>= 1, a = pmul(a, a))
+        if (e & 1) r = pmul(r, a);
+    return r;
+}
+
+// A received word whose top syndrome S_{ecc-1} = sum_k e_k X_k^{ecc-1} is
+// zero (X_i = w^rbo(i), the reference's syndromes): k - 1 random errors and
+// a last one that cancels their top syndrome, all within the capacity.  The
+// reference's key-equation solver then meets a first quotient of degree two,
+// which it does not handle (its result is only reproduced by the mirror).
+static void corrupt_top_zero(std::mt19937 &g, const HostCode &h, uint16_t *w, size_t n, size_t ecc) {
+    for (int attempt = 0; attempt < 64; ++attempt) {
+        const size_t k = 2 + g() % (ecc / 2 - 1);
+        std::vector<uint32_t> pos;
+        while (pos.size() < k) {
+            const uint32_t p = g() % n;
+            bool seen = false;
+            for (uint32_t q : pos) seen |= q == p;
+            if (!seen) pos.push_back(p);
+        }
+        std::vector<uint32_t> nv(k);
+        uint32_t top = 0;
+        bool ok = true;
+        for (size_t q = 0; q + 1 < k; ++q) {
+            const uint32_t e = 1 + g() % 65536u;
+            nv[q] = (w[pos[q]] + e) % 65537u;
+            ok &= nv[q] != 65536u;
+            top = (top + pmul(e, ppow(h.c.roots_ntt[orc_rsi16_rbo(h.o, pos[q])], (uint32_t)ecc - 1))) % 65537u;
+        }
+        const uint32_t xl = ppow(h.c.roots_ntt[orc_rsi16_rbo(h.o, pos[k - 1])], (uint32_t)ecc - 1);
+        const uint32_t el = pmul(65537u - top, ppow(xl, 65535u));
+        nv[k - 1] = (w[pos[k - 1]] + el) % 65537u;
+        ok &= el != 0 && nv[k - 1] != 65536u;
+        if (!ok) continue;
+        for (size_t q = 0; q < k; ++q) w[pos[q]] = (uint16_t)nv[q];
+        return;
+    }
+}
+
 template <int EPL>
 static int run_unknown(size_t block_len, size_t ecc, size_t nbatch, std::mt19937 &g) {
     HostCode h(block_len, ecc);
@@ -97,7 +139,10 @@ static int run_unknown(size_t block_len, size_t ecc, size_t nbatch, std::mt19937
     for (size_t b = 0; b < nb; ++b) {
         std::memcpy(cw.data(), &msg[b * ml], ml * 2);
         std::memcpy(cw.data() + ml, &par[b * ecc], ecc * 2);
-        corrupt(g, cw.data(), block_len, g() % (ecc / 2 + 4));
+        if (b % 4 == 3 && ecc >= 4)
+            corrupt_top_zero(g, h, cw.data(), block_len, ecc);
+        else
+            corrupt(g, cw.data(), block_len, g() % (ecc / 2 + 4));
         std::memcpy(&msg[b * ml], cw.data(), ml * 2);
         std::memcpy(&par[b * ecc], cw.data() + ml, ecc * 2);
     }

@@ -11,8 +11,6 @@ import time
 import numpy as np
 import pytest
 
-import oracle_expect
-
 pytestmark = pytest.mark.gpu
 
 
@@ -96,7 +94,8 @@ def test_served_matches_oracle(stream_of_requests):
     from libffrs_gb300 import capi
 
     bench, reqs, _, kinds = stream_of_requests
-    want = [oracle_expect.serving(r) for r in reqs]
+    codes = {}
+    want = [bench.serving_expect(r, codes) for r in reqs]
     bench.serving_restore(reqs)
     srv = capi.Server(slots=4, max_batch=16)
     tickets = [bench.serve_submit(srv, r) for r in reqs]
