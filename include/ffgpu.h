@@ -108,7 +108,7 @@ FFGPU_API int ffgpu_rs256_decode_host(const ffgpu_rs256 *code, uint8_t *data, ui
 FFGPU_API int ffgpu_rs256_synds_host(const ffgpu_rs256 *code, const uint8_t *data, const uint8_t *parity, size_t nblocks,
                            size_t message_len, uint8_t *synds);
 /* No reference counterpart.  ffgpu_rs256_decode without any allocation: the
- * same kernels and results, on a fixed 16 MiB scratch array compiled into the
+ * same kernels and results, on a fixed 18 MiB scratch array compiled into the
  * library, for callers that cannot allocate device memory on their hot path.
  * Covers ecc_len 16/32 with primitive 2 and polynomial 0x11d and 4-byte
  * aligned buffers; at most 524,288 blocks per call at ecc_len 32 (1,048,576

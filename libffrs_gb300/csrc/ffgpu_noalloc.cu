@@ -1,23 +1,23 @@
 // C ABI: RS256 decode that allocates nothing.
 //
-// ffgpu_rs256_decode allocates its scratch (the bitsliced syndrome planes and
-// correction lists, 32 bytes per block at ecc_len 32) from the stream-ordered
-// pool on every call.  Some callers cannot allocate on their hot path: a
+// ffgpu_rs256_decode allocates its scratch (the bitsliced syndrome planes,
+// then the Berlekamp-Massey records: 36 bytes per block at ecc_len 32) from
+// the stream-ordered pool on every call.  Some callers cannot allocate on their hot path: a
 // framework that reserved all device memory up front and hands out buffers
 // itself (the pool allocation would fail or compete with it), and real-time
 // callers that must not see an allocation stall or an out-of-memory error in
-// the middle of a repair loop.  This entry point runs the same two kernels on
-// a fixed scratch array compiled into the library instead.
+// the middle of a repair loop.  This entry point runs the same kernels on a
+// fixed scratch array compiled into the library instead.
 //
 // Limits and rules:
-// * the scratch is kNoAllocScratchBytes (16 MiB): up to 524,288 blocks per
+// * the scratch is kNoAllocScratchBytes (18 MiB): up to 524,288 blocks per
 //   call at ecc_len 32 and 1,048,576 at ecc_len 16; larger requests are
 //   rejected with FFGPU_EINVAL, as are codes and buffers the bitsliced
 //   kernels do not cover (ecc_len 16 or 32, primitive 2, polynomial 0x11d,
 //   4-byte aligned data and parity);
 // * nothing in the scratch has to start at zero: the syndrome kernel writes
-//   every plane word of every group before the solve kernel reads it, and
-//   each correction list is written before it is read;
+//   every plane word of every group before the Berlekamp-Massey kernel reads
+//   it, and that kernel writes every record word the Chien kernel reads;
 // * there is one scratch per device for the whole process, so calls that can
 //   overlap on the device -- from different streams, or from different host
 //   threads -- race on it; callers must order them (one stream, or events);
@@ -39,7 +39,7 @@ using namespace ffgpu;
 
 namespace {
 
-constexpr size_t kNoAllocScratchBytes = (size_t)16 << 20;
+constexpr size_t kNoAllocScratchBytes = (size_t)18 << 20;
 __device__ __align__(256) uint8_t g_noalloc_scratch[kNoAllocScratchBytes];
 
 constexpr int kMaxDevices = 64;

@@ -453,6 +453,26 @@ __device__ __forceinline__ void crt_map(const uint32_t *rs, int stride, uint32_t
     (one(std::integral_constant<int, TM>{}), ...);
 }
 
+// Decode scratch of one tile (32 groups = 1024 blocks): kTileWords<E> words,
+// word w of group g at w * 32 + g.  It first holds the bitsliced syndromes
+// (w = 8j + b: bit b of S_j), then the record the Berlekamp-Massey kernel
+// leaves for the Chien kernel (RecLayout).
+template <int E>
+constexpr int kTileWords = E * 9 * 32;
+
+// The record of one group after Berlekamp-Massey: C_0..C_t (w = 8k + b),
+// Omega_0..Omega_{t-1}, the 6 planes of L, the mask of live blocks (non-zero
+// syndromes and inside the call).
+template <int E>
+struct RecLayout {
+    static constexpr int t = E / 2;
+    static constexpr int kC = 0;
+    static constexpr int kOm = 8 * (t + 1);
+    static constexpr int kL = kOm + 8 * t;
+    static constexpr int kLive = kL + 6;
+    static_assert(kLive < E * 9, "record larger than the tile scratch");
+};
+
 // ---------------------------------------------------------------- window loader
 
 // Tile geometry: G groups of 32 blocks per CTA.  A window is 32 consecutive
@@ -597,7 +617,7 @@ __device__ __forceinline__ void rem_to_synd_t(int t, const uint32_t *rs, int str
 // Syndromes of every block.  PLANES = false: E bytes per block, S_0 first.
 // PLANES = true: bitsliced, for the solve kernel: group G (blocks 32G ..
 // 32G+31) keeps plane word k = 8j + b (bit b of S_j) at
-// planes[(G / 32) * (E * 8 * 32) + k * 32 + G % 32], so that 32 consecutive
+// planes[(G / 32) * kTileWords<E> + k * 32 + G % 32], so that 32 consecutive
 // groups read or write one plane word with one coalesced access.
 template <int E, bool PLANES, int G = kSyndGroups>
 __global__ void __launch_bounds__(G * SyndCode<E>::T) bs_synd_kernel(const uint8_t *__restrict__ data,
@@ -634,7 +654,7 @@ __global__ void __launch_bounds__(G * SyndCode<E>::T) bs_synd_kernel(const uint8
         if constexpr (PLANES) {
             const size_t G = first / 32 + g;
             if ((int)(g * 32) < nb_tile) {
-                uint32_t *o = reinterpret_cast<uint32_t *>(synds) + (G / 32) * (size_t)(E * 8 * 32) + G % 32;
+                uint32_t *o = reinterpret_cast<uint32_t *>(synds) + (G / 32) * (size_t)kTileWords<E> + G % 32;
 #pragma unroll
                 for (int m = 0; m < D; ++m)
 #pragma unroll
@@ -1055,74 +1075,17 @@ struct SolveGeom {
     static constexpr int kXrows = P * 8 + (P - 1) * 16;
     static constexpr int kX = 2 * kXrows * 32;     // double-buffered
     static constexpr int kCp = (t + 1) * 8 * 32;   // C_0..C_t planes (Omega)
-    static constexpr int kCnt = 32 * 32;           // root counters [block][group]
-    static constexpr int kCx = P * P * 24 * 32;    // Chien exchange [position][warp][24][32]
-    static constexpr int kA = kS + (kX > kCp ? kX : kCp);
-    // the Chien exchange overlays the syndromes and the C planes, the root
-    // counters take the last kCnt words (both live only after Omega)
-    static constexpr int kWords = kA > kCx + kCnt ? kA : kCx + kCnt;
-    static constexpr size_t smem = (size_t)kWords * 4 + 768;
+    static constexpr int kWords = kS + (kX > kCp ? kX : kCp);
+    static constexpr size_t smem = (size_t)kWords * 4;
     static_assert(K % 2 == 0, "K must be even");
 };
 
-// C_i <- C_i a^{-i}, Omega_k <- Omega_k a^{-k} (i = HK+1+u, k = Pu+H)
-template <int E, int H, int... U>
-__device__ __forceinline__ void chien_advance(uint32_t (&Ct)[SolveGeom<E>::K][8], uint32_t (&Ot)[SolveGeom<E>::K][8],
-                                              std::integer_sequence<int, U...>) {
-    constexpr int K = SolveGeom<E>::K, P = SolveGeom<E>::P;
-    (cmul_inplace<apow(-(H * K + 1 + U))>(Ct[U]), ...);
-    (cmul_inplace<apow(-(P * U + H))>(Ot[U]), ...);
-}
-
-// One Chien position for warp H: partial sums of the even / odd C terms and of
-// the Omega terms, then every term advances by its constant a^{-i}.
-template <int E, int H>
-__device__ __forceinline__ void chien_step(uint32_t (&Ct)[SolveGeom<E>::K][8], uint32_t (&Ot)[SolveGeom<E>::K][8],
-                                           const uint32_t (&C0)[8], uint32_t *out) {
-    constexpr int K = SolveGeom<E>::K;
-    // with K even, C_i (i = HK+1+u) has odd degree exactly for even u
-#pragma unroll
-    for (int b = 0; b < 8; ++b) {
-        uint32_t po = Ct[0][b], pe = Ct[1][b];
-#pragma unroll
-        for (int u = 2; u < K; u += 4) {
-            if (u + 2 < K) {
-                po = xor3(po, Ct[u][b], Ct[u + 2][b]);
-                pe = xor3(pe, Ct[u + 1][b], Ct[u + 3][b]);
-            } else {
-                po ^= Ct[u][b];
-                pe ^= Ct[u + 1][b];
-            }
-        }
-        if (H == 0) pe ^= C0[b];
-        uint32_t pw = Ot[0][b];
-#pragma unroll
-        for (int v = 1; v < K; v += 2) {
-            if (v + 1 < K)
-                pw = xor3(pw, Ot[v][b], Ot[v + 1][b]);
-            else
-                pw ^= Ot[v][b];
-        }
-        out[b * 32] = pe;
-        out[(8 + b) * 32] = po;
-        out[(16 + b) * 32] = pw;
-    }
-    chien_advance<E, H>(Ct, Ot, std::make_integer_sequence<int, K>{});
-}
-
-// Partial sums of warp H for the P positions base .. base+P-1 of one step.
-template <int E, int H>
-__device__ __forceinline__ void chien_steps(uint32_t (&Ct)[SolveGeom<E>::K][8], uint32_t (&Ot)[SolveGeom<E>::K][8],
-                                            const uint32_t (&C0)[8], uint32_t *Xc, int lane) {
-    constexpr int P = SolveGeom<E>::P;
-#pragma unroll 1
-    for (int p = 0; p < P; ++p) chien_step<E, H>(Ct, Ot, C0, Xc + (p * P + H) * 24 * 32 + lane);
-}
-
-// One CTA = 32 groups (1024 blocks) and P = 4 warps: warp h keeps the
-// coefficients C_i, i = hK+1 .. hK+K (K = t/P), and the evaluator terms
-// Omega_k, k = Pv+h; warp 0 also keeps C_0.  The warps meet through shared
-// memory once per BM iteration and once per P Chien positions.
+// Berlekamp-Massey and the error evaluator of a tile.  One CTA = 32 groups
+// (1024 blocks) and P = 4 warps: warp h keeps the coefficients C_i, i = hK+1
+// .. hK+K (K = t/P), and computes the evaluator terms Omega_k, k = Pv+h; warp
+// 0 also keeps C_0.  The warps meet through shared memory once per BM
+// iteration.  The result goes to the tile's record (RecLayout) for
+// bs_chien_kernel.
 //
 // Berlekamp-Massey runs inversion-free: C <- b C + d x^m B, B <- C and b <- d
 // on a length change.  Every C it produces is a non-zero multiple (per block)
@@ -1132,28 +1095,20 @@ __device__ __forceinline__ void chien_steps(uint32_t (&Ct)[SolveGeom<E>::K][8], 
 // root count, L and the Forney values Omega(x) / Lodd(x) are the normalised
 // algorithm's.
 template <int E>
-__global__ void __launch_bounds__(128, 4) bs_solve_kernel(uint8_t *__restrict__ data, uint8_t *__restrict__ parity,
-                                                          size_t nblocks, int msg_len, uint32_t *__restrict__ planes,
-                                                          uint8_t *__restrict__ status,
-                                                          const uint8_t *__restrict__ exp512,
-                                                          const uint8_t *__restrict__ log256) {
+__global__ void __launch_bounds__(128, 4) bs_bm_kernel(size_t nblocks, uint32_t *__restrict__ planes) {
     using G = SolveGeom<E>;
     constexpr int t = G::t, K = G::K, P = G::P;
     extern __shared__ __align__(16) uint32_t sm[];
     uint32_t *Ssm = sm;           // [E*8][32] syndrome planes
     uint32_t *Xb = sm + G::kS;    // BM exchange, then the C planes
     uint32_t *Csm = Xb;
-    uint32_t *Xc = sm;            // Chien exchange (after Omega)
-    uint32_t *cnt = sm + G::kWords - G::kCnt;
-    uint8_t *ex = reinterpret_cast<uint8_t *>(sm + G::kWords);  // exp[512], log[256]
-    uint8_t *lg = ex + 512;
 
     const int lane = threadIdx.x & 31, h = threadIdx.x >> 5;
     const size_t ngroups = (nblocks + 31) / 32;
     const size_t tile = blockIdx.x;
     const size_t grp = tile * 32 + lane;
     const bool valid = grp < ngroups;
-    uint32_t *tplanes = planes + tile * (size_t)G::kS;
+    uint32_t *tplanes = planes + tile * (size_t)kTileWords<E>;
 
     // phase 0: syndrome planes of the 32 groups, one contiguous region of
     // E * 1024 bytes, copied asynchronously 16 bytes per thread and round
@@ -1166,8 +1121,6 @@ __global__ void __launch_bounds__(128, 4) bs_solve_kernel(uint8_t *__restrict__ 
             asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst + off), "l"(src + off) : "memory");
         asm volatile("cp.async.commit_group;" ::: "memory");
     }
-    for (int i = threadIdx.x; i < 512; i += 128) ex[i] = exp512[i];
-    for (int i = threadIdx.x; i < 256; i += 128) lg[i] = log256[i];
     asm volatile("cp.async.wait_group 0;" ::: "memory");
     __syncthreads();
     uint32_t anyS = 0u;
@@ -1300,116 +1253,252 @@ __global__ void __launch_bounds__(128, 4) bs_solve_kernel(uint8_t *__restrict__ 
         }
         reduce15(p15, Ot[v]);
     }
-    if (h != 0) {
+    // the record (RecLayout) over this tile's syndromes: every syndrome of the
+    // tile was read into shared memory in phase 0, by this CTA only
+    using R = RecLayout<E>;
+    uint32_t *rec = tplanes + lane;
+    if (h == 0) {
 #pragma unroll
-        for (int b = 0; b < 8; ++b) C0[b] = 0u;  // only warp 0 adds the C_0 term
+        for (int b = 0; b < 8; ++b) rec[(R::kC + b) * 32] = C0[b];
+#pragma unroll
+        for (int b = 0; b < 6; ++b) rec[(R::kL + b) * 32] = L[b];
+        rec[R::kLive * 32] = anyS & vmask;
     }
-    __syncthreads();  // the syndromes and C planes become the Chien exchange
-    for (int i = threadIdx.x; i < G::kCnt; i += 128) cnt[i] = 0u;
+#pragma unroll
+    for (int u = 0; u < K; ++u)
+#pragma unroll
+        for (int b = 0; b < 8; ++b) rec[(R::kC + 8 * (h * K + 1 + u) + b) * 32] = C[u][b];
+#pragma unroll
+    for (int v = 0; v < K; ++v)
+#pragma unroll
+        for (int b = 0; b < 8; ++b) rec[(R::kOm + 8 * (P * v + h) + b) * 32] = Ot[v][b];
+}
+
+// ---------------------------------------------------------------- Chien search and Forney
+//
+// bs_chien_kernel: one CTA per tile (32 groups, 1024 blocks) and four warps;
+// lane = group.  From the Berlekamp-Massey record of every group:
+//   1. Chien search over the scan indices i = 0 .. size-1 (x = a^{-i}, the
+//      error degree; byte position size-1-i, as the reference scans them):
+//      warp h takes i = 64h .. 64h+63 and holds all t + 1 terms C_k x^k, so a
+//      position needs no exchange between warps; the blocks whose locator
+//      vanishes there form one root-mask word.
+//   2. The 256 root masks of a group become 8 words per block (32 x 32 bit
+//      transposes).
+//   3. Per block: the root count and the roots in scan order, one slot each.
+//   4. Forney per slot, bitsliced over the 32 blocks of a group: x of the
+//      slot's root, e = Omega(x) / Lodd(x) (Horner on both, one inversion).
+//   5. Status and corrections, as rs_decode::decode (reed_solomon.hpp:
+//      559-595): a block with non-zero syndromes is repaired exactly when
+//      L <= t and it has L roots; otherwise it is left untouched.
+template <int E>
+struct ChienGeom {
+    static constexpr int t = E / 2;
+    static constexpr int R = t / 4;                 // slots per thread (phase 4)
+    static constexpr int kA = 256 * 33;             // root masks, then their transposes, then coefficients
+    static constexpr int kCoef = (t + t / 2) * 8;   // Omega_0..t-1, C_1, C_3, .., C_{t-1}: planes per group
+    static_assert(kCoef * 32 <= kA, "coefficients do not fit");
+    static constexpr int kX = 32 * 4 * 32;          // packed x (then e) bytes [block][4][group]
+    static constexpr int kDeg = t * 32 * 32 / 4;    // root scan indices, bytes [slot][block][group]
+    static constexpr int kCnt = 32 * 32 / 4;        // root counts, bytes [block][group]
+    static constexpr int kExp = 256 / 4;            // a^0 .. a^254 (bytes)
+    static constexpr int kWords = kA + kX + kDeg + kCnt + kExp;
+    static constexpr size_t smem = (size_t)kWords * 4;
+};
+
+template <int E, int H, int... K>
+__device__ __forceinline__ void chien_start(uint32_t (&T)[E / 2 + 1][8], std::integer_sequence<int, K...>) {
+    // T_k <- C_k a^{-64 H k}, k = 1..t
+    (cmul_inplace<apow(-(64 * H * (K + 1)))>(T[K + 1]), ...);
+}
+
+template <int E, int... K>
+__device__ __forceinline__ void chien_next(uint32_t (&T)[E / 2 + 1][8], std::integer_sequence<int, K...>) {
+    // T_k <- T_k a^{-k}, k = 1..t
+    (cmul_inplace<apow(-(K + 1))>(T[K + 1]), ...);
+}
+
+// positions 64H .. 64H+63 of one group: root-mask words into rm[i * 32]
+template <int E, int H>
+__device__ __forceinline__ void chien_scan(uint32_t (&T)[E / 2 + 1][8], int size, uint32_t live, uint32_t *rm) {
+    constexpr int t = E / 2;
+    chien_start<E, H>(T, std::make_integer_sequence<int, t>{});
+#pragma unroll 1
+    for (int p = 0; p < 64; ++p) {
+        const int i = 64 * H + p;
+        uint32_t nz = 0u;
+#pragma unroll
+        for (int b = 0; b < 8; ++b) {
+            uint32_t v = T[0][b];
+#pragma unroll
+            for (int k = 1; k <= t; k += 2) v = (k + 1 <= t) ? xor3(v, T[k][b], T[k + 1][b]) : (v ^ T[k][b]);
+            nz |= v;
+        }
+        rm[i * 32] = i < size ? (~nz & live) : 0u;
+        chien_next<E>(T, std::make_integer_sequence<int, t>{});
+    }
+}
+
+template <int E>
+__global__ void __launch_bounds__(128, 3) bs_chien_kernel(uint8_t *__restrict__ data, uint8_t *__restrict__ parity,
+                                                          size_t nblocks, int msg_len,
+                                                          const uint32_t *__restrict__ planes,
+                                                          uint8_t *__restrict__ status,
+                                                          const uint8_t *__restrict__ exp512) {
+    using G = ChienGeom<E>;
+    using Rl = RecLayout<E>;
+    constexpr int t = G::t, RS = G::R;
+    extern __shared__ __align__(16) uint32_t sm[];
+    uint32_t *A = sm;                   // [256][32] masks; [32 blocks * 8][33] transposed; coefficients
+    uint32_t *Xv = sm + G::kA;          // [block][4][group] packed x, then e
+    uint8_t *deg = reinterpret_cast<uint8_t *>(Xv + G::kX);         // [slot][block][group]
+    uint8_t *cnt = deg + G::kDeg * 4;                                // [block][group]
+    uint8_t *ex = cnt + G::kCnt * 4;                                 // a^0 .. a^254
+
+    const int lane = threadIdx.x & 31, h = threadIdx.x >> 5;
+    const size_t tile = blockIdx.x;
+    const uint32_t *rec = planes + tile * (size_t)kTileWords<E> + lane;
+    const int size = msg_len + E;
+    for (int i = threadIdx.x; i < 255; i += 128) ex[i] = exp512[i];
+    const uint32_t live = rec[Rl::kLive * 32];
+
+    // phase 1: Chien search
+    {
+        uint32_t T[t + 1][8];
+#pragma unroll
+        for (int k = 0; k <= t; ++k)
+#pragma unroll
+            for (int b = 0; b < 8; ++b) T[k][b] = rec[(Rl::kC + 8 * k + b) * 32];
+        switch (h) {
+            case 0: chien_scan<E, 0>(T, size, live, A + lane); break;
+            case 1: chien_scan<E, 1>(T, size, live, A + lane); break;
+            case 2: chien_scan<E, 2>(T, size, live, A + lane); break;
+            default: chien_scan<E, 3>(T, size, live, A + lane); break;
+        }
+    }
     __syncthreads();
 
-    // phase 3: Chien search and Forney, P positions per exchange; warp h
-    // takes position base + h
-    const int size = msg_len + E;
-    uint8_t *corr = reinterpret_cast<uint8_t *>(tplanes) + (size_t)lane * (E * 32);  // [32 blocks][t][2]
-    const uint32_t live = anyS & vmask;
-#pragma unroll 1
-    for (int base = 0; base < size; base += P) {
-        switch (h) {
-            case 0: chien_steps<E, 0>(C, Ot, C0, Xc, lane); break;
-            case 1: chien_steps<E, 1>(C, Ot, C0, Xc, lane); break;
-            case 2: chien_steps<E, 2>(C, Ot, C0, Xc, lane); break;
-            default: chien_steps<E, 3>(C, Ot, C0, Xc, lane); break;
+    // phase 2: masks of positions 32q .. 32q+31 (q = 2h, 2h+1) to one word per
+    // block (bit r: a root at position 32q + r), stored at [(j * 8 + q)][33]
+    {
+        uint32_t a[2][32];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+#pragma unroll
+            for (int r = 0; r < 32; ++r) a[u][r] = A[((2 * h + u) * 32 + r) * 32 + lane];
+            transpose32(a[u]);
         }
         __syncthreads();
-        const int i = base + h;
-        uint32_t lo[8], om[8], nz = 0u;
-        {
-            const uint32_t *A = Xc + (h * P) * 24 * 32 + lane;
 #pragma unroll
-            for (int b = 0; b < 8; ++b) {
-                uint32_t ce = A[b * 32], co = A[(8 + b) * 32], cw = A[(16 + b) * 32];
+        for (int u = 0; u < 2; ++u)
 #pragma unroll
-                for (int w = 1; w < P; ++w) {
-                    ce ^= A[(w * 24 + b) * 32];
-                    co ^= A[(w * 24 + 8 + b) * 32];
-                    cw ^= A[(w * 24 + 16 + b) * 32];
-                }
-                nz |= ce ^ co;
-                lo[b] = co;
-                om[b] = cw;
-            }
-        }
-        __syncthreads();  // every warp has read its position before the next writes
-        if (i < size) {
-            uint32_t roots = ~nz & live;
-            const int pos = size - 1 - i;
-            while (roots) {
-                const int j = __ffs(roots) - 1;
-                roots &= roots - 1;
-                uint32_t ob = 0u, lb = 0u;
-#pragma unroll
-                for (int b = 0; b < 8; ++b) {
-                    ob |= ((om[b] >> j) & 1u) << b;
-                    lb |= ((lo[b] >> j) & 1u) << b;
-                }
-                const uint32_t e = (ob && lb) ? ex[lg[ob] + 255 - lg[lb]] : 0u;
-                const int slot = (int)atomicAdd(&cnt[j * 32 + lane], 1u);
-                if (slot < t) {
-                    corr[(j * t + slot) * 2] = (uint8_t)pos;
-                    corr[(j * t + slot) * 2 + 1] = (uint8_t)e;
-                }
-            }
-        }
+            for (int j = 0; j < 32; ++j) A[(j * 8 + 2 * h + u) * 33 + lane] = a[u][j];
     }
     __syncthreads();
 
-    // phase 4: status and corrections, warp h takes blocks 8h .. 8h+7.
-    // Each block's list is 2t bytes (16-byte aligned); four blocks' lists are
-    // fetched together so that their L2 round trips overlap.
-    constexpr int NV = (2 * t) / 16;  // uint4 per block list
-    constexpr int BPW = 32 / P;       // blocks per warp
+    // phase 3: per block (j = 8h .. 8h+7) the root count and the roots in scan
+    // order; slot s keeps the scan index and x = a^{-i} (packed: word
+    // [j][s % 4], byte s / 4)
 #pragma unroll 1
-    for (int j0 = h * BPW; j0 < h * BPW + BPW; j0 += 4) {
-        uint4 cv[4][NV];
-#pragma unroll
-        for (int r = 0; r < 4; ++r)
-#pragma unroll
-            for (int v = 0; v < NV; ++v)
-                cv[r][v] = reinterpret_cast<const uint4 *>(corr + (size_t)(j0 + r) * t * 2)[v];
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            const int j = j0 + r;
-            if (!((vmask >> j) & 1u)) continue;
-            const size_t blk = blk0 + j;
-            if (!((anyS >> j) & 1u)) {
-                status[blk] = 1;
-                continue;
+    for (int j = 8 * h; j < 8 * h + 8; ++j) {
+        int c = 0;
+#pragma unroll 1
+        for (int q = 0; q < 8; ++q) {
+            uint32_t w = A[(j * 8 + q) * 33 + lane];
+            while (w) {
+                const int r = __ffs(w) - 1;
+                w &= w - 1;
+                if (c < t) {
+                    const int i = 32 * q + r;
+                    deg[(c * 32 + j) * 32 + lane] = (uint8_t)i;
+                    reinterpret_cast<uint8_t *>(Xv + (j * 4 + (c & 3)) * 32 + lane)[c >> 2] = ex[(255 - i) % 255];
+                }
+                ++c;
             }
-            int l = 0;
-#pragma unroll
-            for (int b = 0; b < 6; ++b) l |= (int)((L[b] >> j) & 1u) << b;
-            const int c = (int)cnt[j * 32 + lane];
-            if (l > t || c != l) {
-                status[blk] = 0;
-                continue;
-            }
-            // the corrections go out as fire-and-forget word XORs (both buffers
-            // are 4-byte aligned on this path; neighbouring blocks share words)
-#pragma unroll
-            for (int sl = 0; sl < t; ++sl) {
-                if (sl >= c) continue;
-                const uint4 q = cv[r][sl / 8];
-                const uint32_t wv = (sl % 8) < 2 ? q.x : (sl % 8) < 4 ? q.y : (sl % 8) < 6 ? q.z : q.w;
-                const uint32_t pe = wv >> (16 * (sl & 1));
-                const int p = (int)(pe & 0xffu);
-                const uint32_t e = (pe >> 8) & 0xffu;
-                uint8_t *a = p < msg_len ? data + blk * (size_t)msg_len + p : parity + blk * (size_t)E + (p - msg_len);
-                const uintptr_t w = reinterpret_cast<uintptr_t>(a);
-                atomicXor(reinterpret_cast<unsigned int *>(w & ~(uintptr_t)3), e << (8 * (w & 3)));
-            }
-            status[blk] = 1;
         }
+        cnt[j * 32 + lane] = (uint8_t)(c < 255 ? c : 255);
+    }
+    __syncthreads();
+
+    // phase 4: Forney.  The coefficient planes go to shared memory first
+    // (Omega_0..t-1, then C_1, C_3, ..., C_{t-1}); thread h evaluates the
+    // slots 4r + h (r < t/4) of all 32 blocks of its group.
+    for (int w = h; w < G::kCoef; w += 4)
+        A[w * 32 + lane] = w < 8 * t ? rec[(Rl::kOm + w) * 32] : rec[(Rl::kC + 8 * (2 * ((w - 8 * t) / 8) + 1) + (w & 7)) * 32];
+    __syncthreads();
+    {
+        uint32_t a[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) a[j] = Xv[(j * 4 + h) * 32 + lane];
+        transpose32(a);  // a[8r + b]: bit b of x, slot 4r + h, bit j = block j
+#pragma unroll
+        for (int r = 0; r < RS; ++r) {
+            uint32_t x[8], om[8], lo[8], y[8], cf[8];
+#pragma unroll
+            for (int b = 0; b < 8; ++b) x[b] = a[8 * r + b];
+            // Omega(x), Horner from the top coefficient
+#pragma unroll
+            for (int b = 0; b < 8; ++b) om[b] = A[(8 * (t - 1) + b) * 32 + lane];
+#pragma unroll 1
+            for (int k = t - 2; k >= 0; --k) {
+                vmul(om, x, om);
+#pragma unroll
+                for (int b = 0; b < 8; ++b) om[b] ^= A[(8 * k + b) * 32 + lane];
+            }
+            // Lodd(x) = x * sum_m C_{2m+1} (x^2)^m
+            vsqr(x, y);
+#pragma unroll
+            for (int b = 0; b < 8; ++b) lo[b] = A[(8 * t + 8 * (t / 2 - 1) + b) * 32 + lane];
+#pragma unroll 1
+            for (int m = t / 2 - 2; m >= 0; --m) {
+                vmul(lo, y, lo);
+#pragma unroll
+                for (int b = 0; b < 8; ++b) lo[b] ^= A[(8 * t + 8 * m + b) * 32 + lane];
+            }
+            vmul(lo, x, lo);
+            vinv(lo, cf);
+            vmul(om, cf, om);
+#pragma unroll
+            for (int b = 0; b < 8; ++b) a[8 * r + b] = om[b];
+        }
+        transpose32(a);  // byte r of word j: e of block j, slot 4r + h
+#pragma unroll
+        for (int j = 0; j < 32; ++j) Xv[(j * 4 + h) * 32 + lane] = a[j];
+    }
+    __syncthreads();
+
+    // phase 5: statuses and corrections of blocks j = 8h .. 8h+7
+    const size_t grp = tile * 32 + lane;
+    uint32_t Lp[6];
+#pragma unroll
+    for (int b = 0; b < 6; ++b) Lp[b] = rec[(Rl::kL + b) * 32];
+#pragma unroll 1
+    for (int j = 8 * h; j < 8 * h + 8; ++j) {
+        const size_t blk = grp * 32 + j;
+        if (blk >= nblocks) break;
+        if (!((live >> j) & 1u)) {
+            status[blk] = 1;
+            continue;
+        }
+        int l = 0;
+#pragma unroll
+        for (int b = 0; b < 6; ++b) l |= (int)((Lp[b] >> j) & 1u) << b;
+        const int c = cnt[j * 32 + lane];
+        if (l > t || c != l) {
+            status[blk] = 0;
+            continue;
+        }
+        // fire-and-forget word XORs: both buffers are 4-byte aligned on this
+        // path, and neighbouring blocks share words
+        for (int sl = 0; sl < c; ++sl) {
+            const int i = deg[(sl * 32 + j) * 32 + lane];
+            const uint32_t e = reinterpret_cast<const uint8_t *>(Xv + (j * 4 + (sl & 3)) * 32 + lane)[sl >> 2];
+            const int p = size - 1 - i;
+            uint8_t *ad = p < msg_len ? data + blk * (size_t)msg_len + p : parity + blk * (size_t)E + (p - msg_len);
+            const uintptr_t w = reinterpret_cast<uintptr_t>(ad);
+            atomicXor(reinterpret_cast<unsigned int *>(w & ~(uintptr_t)3), e << (8 * (w & 3)));
+        }
+        status[blk] = 1;
     }
 }
 
@@ -1497,7 +1586,7 @@ bool rs256_fast_synds(const Rs256Code &c, const uint8_t *data, const uint8_t *pa
 // nblocks blocks: whole tiles of 32 groups
 size_t rs256_fast_scratch_bytes(int ecc, size_t nblocks) {
     const size_t ngroups = (nblocks + 31) / 32, ntiles = (ngroups + 31) / 32;
-    return ntiles * (size_t)ecc * 8 * 32 * 4;
+    return ntiles * (size_t)(ecc == 32 ? bs::kTileWords<32> : bs::kTileWords<16>) * 4;
 }
 
 template <int E>
@@ -1510,16 +1599,27 @@ static void launch_bs_decode(const Rs256Code &c, uint8_t *data, uint8_t *parity,
             data, parity, nblocks, msg_len, reinterpret_cast<uint8_t *>(planes));
         check_launch("bs_synd_kernel");
     }
-    FFGPU_CHECK_CUDA(cudaFuncSetAttribute(bs::bs_solve_kernel<E>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)bs::SolveGeom<E>::smem));
-    // four CTAs of 128 threads per SM need the largest shared-memory carveout
-    FFGPU_CHECK_CUDA(
-        cudaFuncSetAttribute(bs::bs_solve_kernel<E>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    static const bool attrs = [] {  // once per process (a thread-safe static initialiser)
+        cudaFuncSetAttribute(bs::bs_bm_kernel<E>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)bs::SolveGeom<E>::smem);
+        cudaFuncSetAttribute(bs::bs_chien_kernel<E>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)bs::ChienGeom<E>::smem);
+        // several CTAs of 128 threads per SM need the largest shared-memory carveout
+        cudaFuncSetAttribute(bs::bs_bm_kernel<E>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        cudaFuncSetAttribute(bs::bs_chien_kernel<E>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        return true;
+    }();
+    (void)attrs;
     const size_t ntiles = ((nblocks + 31) / 32 + 31) / 32;
-    KernelTimer kt_timer("bs_solve_kernel", st);
-    bs::bs_solve_kernel<E><<<(unsigned)ntiles, 128, bs::SolveGeom<E>::smem, st>>>(
-        data, parity, nblocks, msg_len, planes, status, c.d_exp512, c.d_log256);
-    check_launch("bs_solve_kernel");
+    {
+        KernelTimer kt_timer("bs_bm_kernel", st);
+        bs::bs_bm_kernel<E><<<(unsigned)ntiles, 128, bs::SolveGeom<E>::smem, st>>>(nblocks, planes);
+        check_launch("bs_bm_kernel");
+    }
+    KernelTimer kt_timer("bs_chien_kernel", st);
+    bs::bs_chien_kernel<E><<<(unsigned)ntiles, 128, bs::ChienGeom<E>::smem, st>>>(data, parity, nblocks, msg_len,
+                                                                                    planes, status, c.d_exp512);
+    check_launch("bs_chien_kernel");
 }
 
 // decode with caller-provided scratch of rs256_fast_scratch_bytes(ecc, nblocks)

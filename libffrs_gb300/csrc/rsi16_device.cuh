@@ -978,8 +978,8 @@ static __device__ __noinline__ void rsi16_repair_block(const Rsi16Dev &c, const 
 //
 // Warp-wide Berlekamp-Massey over the syndromes S (forward: S_0 first;
 // reverse: S_{ecc-1} first) on the buffers C, B, T of n1 words; returns L,
-// C receives the connection polynomial (forward), `normal` the check above
-// (reverse).
+// C receives the connection polynomial, `normal` the check above (meaningful
+// for the reverse run).
 static __device__ uint32_t w_bm(const Rsi16Dev &c, const uint32_t *S, uint32_t *&C, uint32_t *&B, uint32_t *&T,
                                 uint32_t n1, uint32_t ecc, bool reverse, bool &normal, int lane) {
     for (uint32_t k = lane; k < n1; k += 32) {
@@ -1066,14 +1066,17 @@ static __device__ __noinline__ bool rsi16_repair_bm_block_t(const Rsi16Dev &c, c
         }
     }
     uint32_t *C = temp + ecc, *B = C + n1, *T = B + n1;
-    // the reference's solver is exact on this block only when the reversed
-    // syndrome sequence is normal (see rev_normal below); run that check first
-    // on the same buffers, then the locator itself
+    // Berlekamp-Massey on the reversed syndromes: the reference's solver is
+    // exact on this block only when that run is normal (w_bm), and its
+    // connection polynomial, read backwards, is the locator up to a scalar
+    // (the roots and Omega / C' do not depend on the scalar)
     bool normal = false;
-    w_bm(c, S, C, B, T, n1, ecc, true, normal, lane);
-    if (!normal) return false;
-    uint32_t L = w_bm(c, S, C, B, T, n1, ecc, false, normal, lane);
-    if (L == 0 || L > t) return false;
+    uint32_t L = w_bm(c, S, C, B, T, n1, ecc, true, normal, lane);
+    if (!normal || L == 0 || L > t) return false;
+    for (uint32_t k = lane; k < n1; k += 32) T[k] = C[k];  // T is free after the run
+    __syncwarp();
+    for (uint32_t k = lane; k < n1; k += 32) C[k] = k <= L ? T[L - k] : 0u;
+    __syncwarp();
     // C must have degree exactly L (checked through the root count below)
     for (uint32_t k = lane; k < n1; k += 32)
         if (k > L && C[k]) L = 0xffffffffu;
@@ -1173,57 +1176,19 @@ static __device__ __forceinline__ bool rsi16_repair_bm_block(const Rsi16Dev &c, 
 // transforms and the column reads of the lanes avoid bank conflicts.
 constexpr uint32_t kColStride = 33;
 
-// Normalised Berlekamp-Massey over GF(65537) for one block (lane): the same
-// iteration as rsi16_repair_bm_block_t, C <- C - (d / b) x^m B, with x^m B kept
-// pre-shifted and T + 1 = ecc/2 + 1 coefficients.  A block that the
-// bounded-distance path accepts ends with L <= T; while L <= T the locator has
-// degree <= L and every shifted B that is used has degree <= L, and once L
-// exceeds T it never comes back below (the block then goes to the mirror), so
-// the dropped terms never change an accepted result.  S points at S_0 of the
-// block's column (stride kColStride).  Returns L; C receives the locator.
+// Berlekamp-Massey of w_bm's reverse run for one block (lane), normalised
+// (C <- C - (d / b) x^m B, with x^m B kept pre-shifted), over the reversed
+// column S_{ecc-1}, ..., S_0 (stride kColStride), with T + 1 = ecc/2 + 1
+// coefficients on registers.  A block the bounded-distance path accepts ends
+// with L <= T; while L <= T the connection polynomial has degree <= L and
+// every shifted B used has degree <= L, and once L exceeds T it never comes
+// back below (the block then goes to the mirror), so the dropped terms never
+// change an accepted result.  Returns L, or 0 when the run is not normal or
+// L > T; C receives the connection polynomial of the reversed sequence.
 template <int T>
-static __device__ __forceinline__ uint32_t rsi16_bm_lane(const uint32_t *S, const uint32_t *inv_tab, uint32_t ecc,
-                                                         uint32_t (&C)[T + 1]) {
+static __device__ __forceinline__ uint32_t rsi16_rev_bm_lane(const uint32_t *S, const uint32_t *inv_tab, uint32_t ecc,
+                                                             uint32_t (&C)[T + 1]) {
     uint32_t Bs[T + 1];
-#pragma unroll
-    for (int i = 0; i <= T; ++i) {
-        C[i] = i == 0 ? 1u : 0u;
-        Bs[i] = i == 1 ? 1u : 0u;  // x^1 * B, B = 1
-    }
-    uint32_t L = 0, binv = 1;
-#pragma unroll 1
-    for (uint32_t n = 0; n < ecc; ++n) {
-        // d = sum_i C_i S_{n-i}: products below 2^33, 64-bit sum, one reduction
-        uint64_t acc = 0;
-#pragma unroll
-        for (int i = 0; i <= T; ++i)
-            if ((uint32_t)i <= n) acc += (uint64_t)C[i] * S[(n - i) * kColStride];
-        const uint32_t d = (uint32_t)(acc % 0x10001u);
-        const uint32_t coef = fmul(d, binv);
-        const bool grow = d != 0 && 2 * L <= n;
-        // C_i <- C_i - coef Bs_i and Bs_i <- grow ? C_{i-1} : Bs_{i-1}, top down
-#pragma unroll
-        for (int i = T; i >= 0; --i) {
-            const uint32_t bi = Bs[i];
-            Bs[i] = i == 0 ? 0u : (grow ? C[i - 1] : Bs[i - 1]);
-            C[i] = fsub(C[i], fmul(coef, bi));
-        }
-        if (grow) {
-            L = n + 1 - L;
-            binv = inv_tab[d];
-        }
-    }
-    return L;
-}
-
-// The normality check of w_bm on one lane: Berlekamp-Massey over the
-// reversed column S_{ecc-1}, ..., S_0 with T + 1 coefficients, true when its
-// length grows by one at every even step up to its final value L <= T (the
-// truncation argument of rsi16_bm_lane holds unchanged: while L <= T the
-// polynomials stay within T + 1 coefficients).
-template <int T>
-static __device__ __forceinline__ bool rsi16_rev_normal_lane(const uint32_t *S, const uint32_t *inv_tab, uint32_t ecc) {
-    uint32_t C[T + 1], Bs[T + 1];
 #pragma unroll
     for (int i = 0; i <= T; ++i) {
         C[i] = i == 0 ? 1u : 0u;
@@ -1253,7 +1218,7 @@ static __device__ __forceinline__ bool rsi16_rev_normal_lane(const uint32_t *S, 
             binv = inv_tab[d];
         }
     }
-    return !abnormal && L > 0 && L <= (uint32_t)T;
+    return (abnormal || L > (uint32_t)T) ? 0u : L;
 }
 
 // The rest of the bounded-distance path, from a block's syndromes (column S)
@@ -1470,13 +1435,16 @@ static __device__ __forceinline__ void rsi16_repair32(const Rsi16Dev &c, const B
     __syncwarp();
     uint32_t L = 0;
     if ((nz >> lane) & 1u) {
+        // Berlekamp-Massey on the reversed syndromes: only a normal run is
+        // accepted (w_bm; L = 0 sends the block to the mirror), and its
+        // connection polynomial read backwards is the locator up to a scalar
         uint32_t C[T + 1];
-        L = rsi16_bm_lane<T>(Ssm + lane, c.inv_tab, c.ecc, C);
-        // only where the reference's solver is exact (see w_bm); L = 0 sends
-        // the block to the mirror
-        if (!rsi16_rev_normal_lane<T>(Ssm + lane, c.inv_tab, c.ecc)) L = 0;
+        L = rsi16_rev_bm_lane<T>(Ssm + lane, c.inv_tab, c.ecc, C);
 #pragma unroll
-        for (int i = 0; i <= T; ++i) Csm[i * kColStride + lane] = C[i];
+        for (int i = 0; i <= T; ++i) {
+            if ((uint32_t)i <= L) Csm[(L - i) * kColStride + lane] = C[i];
+            if ((uint32_t)i > L) Csm[i * kColStride + lane] = 0u;
+        }
     }
     __syncwarp();
     // blocks whose locator passes the checks get their roots searched in
