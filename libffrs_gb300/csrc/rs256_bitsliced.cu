@@ -27,6 +27,7 @@
 
 #include "common.cuh"
 #include "rs256.cuh"
+#include "rs256_synd_gen.cuh"
 
 namespace ffgpu {
 namespace bs {
@@ -1274,6 +1275,132 @@ __global__ void __launch_bounds__(128, 4) bs_bm_kernel(size_t nblocks, uint32_t 
         for (int b = 0; b < 8; ++b) rec[(R::kOm + 8 * (P * v + h) + b) * 32] = Ot[v][b];
 }
 
+// ---------------------------------------------------------------- syndromes by bit plane (ecc 32)
+//
+// bs_synd32_kernel: the bitsliced syndromes of ecc_len 32 through the
+// generated networks of rs256_synd_gen.cuh (split by bit plane, odd j and
+// j = 0 evaluated per plane, Horner in steps of 32 degrees).  One CTA per
+// tile (32 groups, 1024 blocks), eight warps: warp w evaluates bit plane w
+// of every group, lane = group.  Per window of 32 degrees (255 .. 0):
+//   * load: the window's bytes of every block as 4-byte words (cp.async, one
+//     window ahead of the arithmetic; zeros before the block's first degree);
+//   * transpose: thread (w, group) turns column w (window bytes 4w .. 4w+3)
+//     of the group's 32 blocks into 8 planes x 4 degrees;
+//   * Horner step: warp w reads plane w of the window's 32 degrees.
+// The rows of the eight planes are then combined into S_0 .. S_31 (two
+// halves through shared memory) and stored as the tile's syndrome planes.
+struct Synd32Geom {
+    static constexpr int kRawStride = 32 * 9 + 1;   // words per group: 32 blocks x 9 words, + 1 against conflicts
+    static constexpr int kRaw = 32 * kRawStride;    // one window of the tile
+    static constexpr int kP = 8 * 32 * 32;          // planes [bit][degree][group]
+    static constexpr int kWords = 2 * kRaw + kP;
+    static_assert(kSyndRowsB * 8 * 32 <= 2 * kRaw && kSyndRowsA <= kSyndRowsB, "exchange does not fit");
+    static constexpr size_t smem = (size_t)kWords * 4;
+};
+
+// cp.async of window w's words of the tile into raw: block b's word k at
+// raw[(b / 32) * kRawStride + (b % 32) * 9 + k]; words outside the array are
+// zero-filled (no read)
+__device__ __forceinline__ void synd32_load(uint32_t *raw, const uint8_t *__restrict__ data,
+                                            const uint8_t *__restrict__ parity, size_t nblocks, int msg_len,
+                                            size_t first, int w) {
+    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(raw);
+    const long long p0 = (long long)msg_len - 224 + 32 * w;  // first data byte of the window (windows 0..6)
+    const long long total = w < 7 ? (long long)(nblocks * (size_t)msg_len) : (long long)(nblocks * 32);
+    const uint8_t *base = w < 7 ? data : parity;
+#pragma unroll 4
+    for (int q = threadIdx.x; q < 1024 * 9; q += 256) {
+        const int b = q / 9, k = q - 9 * (q / 9);
+        const long long blk = (long long)(first + b);
+        const long long a = w < 7 ? (((blk * msg_len + p0) & ~3LL) + 4 * k) : blk * 32 + 4 * k;
+        const bool in = a >= 0 && a < total && (w < 7 || k < 8);
+        const uint32_t dst = sbase + (uint32_t)(((b >> 5) * Synd32Geom::kRawStride + (b & 31) * 9 + k) * 4);
+        const uint8_t *src = base + (in ? a : 0);
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src), "r"(in ? 4 : 0)
+                     : "memory");
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(256, 1) bs_synd32_kernel(const uint8_t *__restrict__ data,
+                                                           const uint8_t *__restrict__ parity, size_t nblocks,
+                                                           int msg_len, uint32_t *__restrict__ planes) {
+    using G = Synd32Geom;
+    extern __shared__ __align__(16) uint32_t sm[];
+    uint32_t *raw0 = sm, *P = sm + 2 * G::kRaw;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const size_t tile = blockIdx.x, first = tile * 1024;
+    uint32_t s[kSyndRows];
+#pragma unroll
+    for (int i = 0; i < kSyndRows; ++i) s[i] = 0u;
+    const long long p0 = (long long)msg_len - 224;  // first data byte of window 0
+    synd32_load(raw0, data, parity, nblocks, msg_len, first, 0);
+#pragma unroll 1
+    for (int win = 0; win < 8; ++win) {
+        uint32_t *raw = raw0 + (win & 1) * G::kRaw;
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        __syncthreads();
+        // transpose column w of group `lane`: bytes 4w .. 4w+3 of the window
+        {
+            uint32_t a[32];
+            const uint32_t *rg = raw + lane * G::kRawStride + w;
+            if (win < 7) {
+                const long long c0 = p0 + 32 * win + 4 * w;  // position of the column's first byte
+                const uint32_t keep = c0 >= 0 ? ~0u : (c0 <= -4 ? 0u : (~0u << (8 * (int)(-c0))));
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const long long blk = (long long)(first + lane * 32 + j);
+                    const uint32_t sh = (uint32_t)((blk * msg_len + p0) & 3) * 8;
+                    a[j] = __funnelshift_r(rg[j * 9], rg[j * 9 + 1], sh) & keep;
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < 32; ++j) a[j] = rg[j * 9];
+            }
+            transpose32(a);  // a[8r + b]: bit b of window byte 4w + r, bit j = block j
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+#pragma unroll
+                for (int b = 0; b < 8; ++b) P[(b * 32 + 4 * w + r) * 32 + lane] = a[8 * r + b];
+        }
+        __syncthreads();
+        if (win < 7) synd32_load(raw0 + ((win + 1) & 1) * G::kRaw, data, parity, nblocks, msg_len, first, win + 1);
+        const uint32_t *Pw = P + w * 32 * 32 + lane;
+        synd_step32([&](int k) { return Pw[k * 32]; }, s);
+    }
+    // the rows of all planes into S_j, in two halves through shared memory
+    uint32_t *X = raw0 + lane;
+    uint32_t *out = planes + tile * (size_t)kTileWords<32> + lane;
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < kSyndRowsA; ++i) X[(i * 8 + w) * 32] = s[i];
+    __syncthreads();
+    switch (w) {
+        case 0: synd_combine_A0(X, out); break;
+        case 1: synd_combine_A1(X, out); break;
+        case 2: synd_combine_A2(X, out); break;
+        case 3: synd_combine_A3(X, out); break;
+        case 4: synd_combine_A4(X, out); break;
+        case 5: synd_combine_A5(X, out); break;
+        case 6: synd_combine_A6(X, out); break;
+        default: synd_combine_A7(X, out); break;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < kSyndRowsB; ++i) X[(i * 8 + w) * 32] = s[kSyndRowsA + i];
+    __syncthreads();
+    switch (w) {
+        case 0: synd_combine_B0(X, out); break;
+        case 1: synd_combine_B1(X, out); break;
+        case 2: synd_combine_B2(X, out); break;
+        case 3: synd_combine_B3(X, out); break;
+        case 4: synd_combine_B4(X, out); break;
+        case 5: synd_combine_B5(X, out); break;
+        case 6: synd_combine_B6(X, out); break;
+        default: synd_combine_B7(X, out); break;
+    }
+}
+
 // ---------------------------------------------------------------- Chien search and Forney
 //
 // bs_chien_kernel: one CTA per tile (32 groups, 1024 blocks) and four warps;
@@ -1593,7 +1720,19 @@ template <int E>
 static void launch_bs_decode(const Rs256Code &c, uint8_t *data, uint8_t *parity, size_t nblocks, int msg_len,
                              uint8_t *status, uint32_t *planes, cudaStream_t st) {
     constexpr int T = bs::SyndCode<E>::T;
-    {
+    const size_t ntiles = ((nblocks + 31) / 32 + 31) / 32;
+    if constexpr (E == 32) {
+        static const bool synd_attrs = [] {
+            cudaFuncSetAttribute(bs::bs_synd32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)bs::Synd32Geom::smem);
+            return true;
+        }();
+        (void)synd_attrs;
+        KernelTimer kt_timer("bs_synd32_kernel", st);
+        bs::bs_synd32_kernel<<<(unsigned)ntiles, 256, bs::Synd32Geom::smem, st>>>(data, parity, nblocks, msg_len,
+                                                                                  planes);
+        check_launch("bs_synd32_kernel");
+    } else {
         KernelTimer kt_timer("bs_synd_kernel", st);
         bs::bs_synd_kernel<E, true><<<synd_grid(nblocks, T), bs::kSyndGroups * T, 0, st>>>(
             data, parity, nblocks, msg_len, reinterpret_cast<uint8_t *>(planes));
@@ -1610,7 +1749,6 @@ static void launch_bs_decode(const Rs256Code &c, uint8_t *data, uint8_t *parity,
         return true;
     }();
     (void)attrs;
-    const size_t ntiles = ((nblocks + 31) / 32 + 31) / 32;
     {
         KernelTimer kt_timer("bs_bm_kernel", st);
         bs::bs_bm_kernel<E><<<(unsigned)ntiles, 128, bs::SolveGeom<E>::smem, st>>>(nblocks, planes);

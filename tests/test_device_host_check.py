@@ -60,3 +60,31 @@ def test_rsi16_repairs_on_host(tmp_path):
     r = subprocess.run([str(exe), "19", "3"], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True,
                        timeout=600)
     assert r.returncode == 0 and r.stdout.strip().endswith("bad 0"), r.stdout[-2000:]
+
+
+@pytest.mark.skipif(shutil.which("g++") is None or shutil.which("gcc") is None, reason="needs gcc/g++")
+def test_rs256_syndrome_networks_on_host(tmp_path):
+    """The generated bitsliced syndrome networks (rs256_synd_gen.cuh) against
+    the oracle's syndromes, full and shortened blocks."""
+    obj = tmp_path / "ffrs_oracle.o"
+    exe = tmp_path / "rs256_synd_check"
+    subprocess.run(["gcc", "-O2", "-c", os.path.join(REPO, "oracle", "ffrs_oracle.c"), "-o", str(obj)], check=True)
+    subprocess.run(["g++", "-O2", "-std=c++17", "-I", os.path.join(REPO, "tests", "host", "stub"),
+                    "-I", os.path.join(REPO, "libffrs_gb300", "csrc"), "-I", os.path.join(REPO, "oracle"),
+                    os.path.join(REPO, "tests", "host", "rs256_synd_check.cpp"), str(obj), "-o", str(exe)],
+                   check=True)
+    r = subprocess.run([str(exe), "5", "300"], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True,
+                       timeout=600)
+    assert r.returncode == 0 and r.stdout.strip().endswith("bad 0"), r.stdout[-2000:]
+
+
+def test_generated_syndrome_header_is_current():
+    """rs256_synd_gen.cuh is exactly what gen_rs256_synd.py emits."""
+    import importlib.util
+
+    path = os.path.join(REPO, "libffrs_gb300", "csrc", "gen_rs256_synd.py")
+    spec = importlib.util.spec_from_file_location("gen_rs256_synd", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    with open(mod.OUT) as f:
+        assert f.read() == mod.generate()
