@@ -1065,6 +1065,21 @@ __device__ __forceinline__ void l_update(uint32_t (&L)[6], int a, uint32_t cond)
     }
 }
 
+// the largest L of the 32 x 32 blocks of a warp (bit-serial per lane, then
+// across the lanes): warp-uniform
+__device__ __forceinline__ int max_len(const uint32_t (&L)[6]) {
+    uint32_t cand = ~0u;
+    int res = 0;
+#pragma unroll
+    for (int b = 5; b >= 0; --b) {
+        const uint32_t t = cand & L[b];
+        const bool nz = t != 0u;
+        res |= (int)nz << b;
+        cand = nz ? t : cand;
+    }
+    return (int)__reduce_max_sync(0xffffffffu, (unsigned)res);
+}
+
 template <int E>
 struct SolveGeom {
     static constexpr int P = 4;              // warps per tile
@@ -1143,6 +1158,7 @@ __global__ void __launch_bounds__(128, 4) bs_bm_kernel(size_t nblocks, uint32_t 
 #pragma unroll
     for (int b = 0; b < 6; ++b) L[b] = 0u;
     constexpr int kTop = P * 8;  // first exchange row of the warp tops
+    int lmax = 0;                // the tile's largest L (every warp holds the same L planes)
 #pragma unroll 1
     for (int n = 0; n < E; ++n) {
         // partial discrepancy, one reduction for all products; at the start
@@ -1159,7 +1175,7 @@ __global__ void __launch_bounds__(128, 4) bs_bm_kernel(size_t nblocks, uint32_t 
 #pragma unroll
         for (int u = 0; u < K; ++u) {
             const int j = n - (h * K + 1 + u);
-            if (j >= 0) {
+            if (j >= 0 && h * K + 1 + u <= lmax) {
                 uint32_t sj[8];
 #pragma unroll
                 for (int b = 0; b < 8; ++b) sj[b] = Ssm[(j * 8 + b) * 32 + lane];
@@ -1189,9 +1205,13 @@ __global__ void __launch_bounds__(128, 4) bs_bm_kernel(size_t nblocks, uint32_t 
             nzd |= s;
         }
         const uint32_t cond = nzd & le_const(L, n >> 1);
+        // the new lengths first: every block's new C has degree at most its
+        // new L, so the products above the tile's largest new L are zero
+        l_update(L, n + 1, cond);
+        lmax = max_len(L);
         // C_i <- b C_i + d Bs_i and Bs_i <- cond ? C_{i-1} : Bs_{i-1}, from
         // the top down; C_i = Bs_i = 0 for i > n+1, so those products are
-        // skipped
+        // skipped, and so are those above lmax
 #pragma unroll
         for (int u = K - 1; u >= 0; --u) {
             uint32_t lc[8], lb[8];
@@ -1208,7 +1228,7 @@ __global__ void __launch_bounds__(128, 4) bs_bm_kernel(size_t nblocks, uint32_t 
                     lb[b] = X[(kTop + (h - 1) * 16 + 8 + b) * 32 + lane];
                 }
             }
-            if (h * K + 1 + u <= n + 1) {
+            if (h * K + 1 + u <= n + 1 && h * K + 1 + u <= lmax) {
                 uint32_t pr[15];
 #pragma unroll
                 for (int k = 0; k < 15; ++k) pr[k] = 0u;
@@ -1222,7 +1242,6 @@ __global__ void __launch_bounds__(128, 4) bs_bm_kernel(size_t nblocks, uint32_t 
         if (h == 0) vmul(bb, C0, C0);
 #pragma unroll
         for (int b = 0; b < 8; ++b) bb[b] = bitsel(cond, d[b], bb[b]);
-        l_update(L, n + 1, cond);
     }
     __syncthreads();  // BM exchange reads done before the C planes overwrite it
 
@@ -1299,25 +1318,52 @@ struct Synd32Geom {
 };
 
 // cp.async of window w's words of the tile into raw: block b's word k at
-// raw[(b / 32) * kRawStride + (b % 32) * 9 + k]; words outside the array are
-// zero-filled (no read)
+// raw[(b / 32) * kRawStride + (b % 32) * 9 + k].  Words outside the array
+// are zero-filled (no read).
 __device__ __forceinline__ void synd32_load(uint32_t *raw, const uint8_t *__restrict__ data,
                                             const uint8_t *__restrict__ parity, size_t nblocks, int msg_len,
                                             size_t first, int w) {
     const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(raw);
-    const long long p0 = (long long)msg_len - 224 + 32 * w;  // first data byte of the window (windows 0..6)
-    const long long total = w < 7 ? (long long)(nblocks * (size_t)msg_len) : (long long)(nblocks * 32);
-    const uint8_t *base = w < 7 ? data : parity;
+    const int t = threadIdx.x;
+    if (w < 7) {
+        // offsets relative to the tile's first data byte fit in 32 bits;
+        // word q = 9 b + k of the window goes to thread q % 256, so that a
+        // warp reads whole consecutive stretches of the tile
+        const long long tile0 = (long long)first * msg_len;
+        const long long total = (long long)(nblocks * (size_t)msg_len) - tile0;  // bytes from tile0 to the end
+        const int c = msg_len - 224 + 32 * w;
+        const uint8_t *tb = data + tile0;
+        int b = t / 9, k = t - 9 * (t / 9);
 #pragma unroll 4
-    for (int q = threadIdx.x; q < 1024 * 9; q += 256) {
-        const int b = q / 9, k = q - 9 * (q / 9);
-        const long long blk = (long long)(first + b);
-        const long long a = w < 7 ? (((blk * msg_len + p0) & ~3LL) + 4 * k) : blk * 32 + 4 * k;
-        const bool in = a >= 0 && a < total && (w < 7 || k < 8);
-        const uint32_t dst = sbase + (uint32_t)(((b >> 5) * Synd32Geom::kRawStride + (b & 31) * 9 + k) * 4);
-        const uint8_t *src = base + (in ? a : 0);
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src), "r"(in ? 4 : 0)
-                     : "memory");
+        for (int i = 0; i < 36; ++i) {
+            const long long ak = (long long)((b * msg_len + c) & ~3) + 4 * k;  // may precede the array
+            const bool in = ak >= -tile0 && ak < total;
+            const uint32_t dst = sbase + (uint32_t)(((b >> 5) * Synd32Geom::kRawStride + (b & 31) * 9 + k) * 4);
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(in ? tb + ak : data),
+                         "r"(in ? 4 : 0)
+                         : "memory");
+            // q += 256 = 9 * 28 + 4
+            b += 28;
+            k += 4;
+            if (k >= 9) {
+                k -= 9;
+                ++b;
+            }
+        }
+    } else {
+        // the parity bytes of the tile are one contiguous stretch: word q of it
+        // (block q / 8, word q % 8) goes to thread q % 256
+        const long long total = (long long)(nblocks * 32) - (long long)first * 32;
+        const uint8_t *tb = parity + first * 32;
+#pragma unroll 4
+        for (int i = 0; i < 32; ++i) {
+            const int q = t + 256 * i, b = q >> 3, k = q & 7;
+            const bool in = (long long)q * 4 < total;
+            const uint32_t dst = sbase + (uint32_t)(((b >> 5) * Synd32Geom::kRawStride + (b & 31) * 9 + k) * 4);
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(in ? tb + 4 * q : parity),
+                         "r"(in ? 4 : 0)
+                         : "memory");
+        }
     }
     asm volatile("cp.async.commit_group;" ::: "memory");
 }
@@ -1347,11 +1393,12 @@ __global__ void __launch_bounds__(256, 1) bs_synd32_kernel(const uint8_t *__rest
             if (win < 7) {
                 const long long c0 = p0 + 32 * win + 4 * w;  // position of the column's first byte
                 const uint32_t keep = c0 >= 0 ? ~0u : (c0 <= -4 ? 0u : (~0u << (8 * (int)(-c0))));
+                // byte offset (mod 4) of block j's window: (first + 32 lane + j) * msg_len + p0
+                uint32_t off = (uint32_t)((((long long)first * msg_len + p0) & 3) + (uint32_t)(lane * 32 * msg_len));
 #pragma unroll
                 for (int j = 0; j < 32; ++j) {
-                    const long long blk = (long long)(first + lane * 32 + j);
-                    const uint32_t sh = (uint32_t)((blk * msg_len + p0) & 3) * 8;
-                    a[j] = __funnelshift_r(rg[j * 9], rg[j * 9 + 1], sh) & keep;
+                    a[j] = __funnelshift_r(rg[j * 9], rg[j * 9 + 1], (off & 3) * 8) & keep;
+                    off += (uint32_t)msg_len;
                 }
             } else {
 #pragma unroll
@@ -1486,6 +1533,29 @@ __global__ void __launch_bounds__(128, 3) bs_chien_kernel(uint8_t *__restrict__ 
     const size_t tile = blockIdx.x;
     const uint32_t *rec = planes + tile * (size_t)kTileWords<E> + lane;
     const int size = msg_len + E;
+    // The corrections of phase 5 change a few bytes in most lines of the
+    // tile's data, which the syndrome kernel read long before (evicted from
+    // L2 by then).  The tile's data and parity are two contiguous stretches:
+    // prefetch them into L2 now, so that the phases in between hide the DRAM
+    // reads and the final XORs hit L2.  Bulk prefetches need 16-byte aligned
+    // addresses and sizes: each stretch is trimmed inwards to that, in pieces
+    // of at most 2 KiB.
+    {
+        const size_t first = tile * 1024;
+        const size_t nb = nblocks - first < 1024 ? nblocks - first : 1024;
+        const uintptr_t d0 = reinterpret_cast<uintptr_t>(data + first * (size_t)msg_len);
+        const uintptr_t p0 = reinterpret_cast<uintptr_t>(parity + first * E);
+        const uintptr_t db = (d0 + 15) & ~(uintptr_t)15, de = (d0 + nb * (size_t)msg_len) & ~(uintptr_t)15;
+        const uintptr_t pb = (p0 + 15) & ~(uintptr_t)15, pe = (p0 + nb * E) & ~(uintptr_t)15;
+        const size_t dn = de > db ? de - db : 0, pn = pe > pb ? pe - pb : 0;
+        const size_t dpieces = (dn + 2047) / 2048, ppieces = (pn + 2047) / 2048;
+        for (size_t q = threadIdx.x; q < dpieces + ppieces; q += 128) {
+            const bool isd = q < dpieces;
+            const size_t off = (isd ? q : q - dpieces) * 2048, len = isd ? dn : pn;
+            const uint32_t n = (uint32_t)(len - off < 2048 ? len - off : 2048);  // a multiple of 16
+            asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"((isd ? db : pb) + off), "r"(n) : "memory");
+        }
+    }
     for (int i = threadIdx.x; i < 255; i += 128) ex[i] = exp512[i];
     const uint32_t live = rec[Rl::kLive * 32];
 
@@ -1558,35 +1628,60 @@ __global__ void __launch_bounds__(128, 3) bs_chien_kernel(uint8_t *__restrict__ 
 #pragma unroll
         for (int j = 0; j < 32; ++j) a[j] = Xv[(j * 4 + h) * 32 + lane];
         transpose32(a);  // a[8r + b]: bit b of x, slot 4r + h, bit j = block j
+        // Horner for all RS slots at once: each coefficient is read once and
+        // feeds RS independent products
+        uint32_t om[RS][8], y[RS][8], lo[RS][8];
+#pragma unroll
+        for (int r = 0; r < RS; ++r)
+#pragma unroll
+            for (int b = 0; b < 8; ++b) om[r][b] = A[(8 * (t - 1) + b) * 32 + lane];
+#pragma unroll 1
+        for (int k = t - 2; k >= 0; --k) {
+            uint32_t cf[8];
+#pragma unroll
+            for (int b = 0; b < 8; ++b) cf[b] = A[(8 * k + b) * 32 + lane];
+#pragma unroll
+            for (int r = 0; r < RS; ++r) {
+                uint32_t x[8];
+#pragma unroll
+                for (int b = 0; b < 8; ++b) x[b] = a[8 * r + b];
+                vmul(om[r], x, om[r]);
+#pragma unroll
+                for (int b = 0; b < 8; ++b) om[r][b] ^= cf[b];
+            }
+        }
+        // Lodd(x) = x * sum_m C_{2m+1} (x^2)^m
 #pragma unroll
         for (int r = 0; r < RS; ++r) {
-            uint32_t x[8], om[8], lo[8], y[8], cf[8];
+            uint32_t x[8];
 #pragma unroll
             for (int b = 0; b < 8; ++b) x[b] = a[8 * r + b];
-            // Omega(x), Horner from the top coefficient
+            vsqr(x, y[r]);
 #pragma unroll
-            for (int b = 0; b < 8; ++b) om[b] = A[(8 * (t - 1) + b) * 32 + lane];
+            for (int b = 0; b < 8; ++b) lo[r][b] = A[(8 * t + 8 * (t / 2 - 1) + b) * 32 + lane];
+        }
 #pragma unroll 1
-            for (int k = t - 2; k >= 0; --k) {
-                vmul(om, x, om);
+        for (int m = t / 2 - 2; m >= 0; --m) {
+            uint32_t cf[8];
 #pragma unroll
-                for (int b = 0; b < 8; ++b) om[b] ^= A[(8 * k + b) * 32 + lane];
+            for (int b = 0; b < 8; ++b) cf[b] = A[(8 * t + 8 * m + b) * 32 + lane];
+#pragma unroll
+            for (int r = 0; r < RS; ++r) {
+                vmul(lo[r], y[r], lo[r]);
+#pragma unroll
+                for (int b = 0; b < 8; ++b) lo[r][b] ^= cf[b];
             }
-            // Lodd(x) = x * sum_m C_{2m+1} (x^2)^m
-            vsqr(x, y);
+        }
 #pragma unroll
-            for (int b = 0; b < 8; ++b) lo[b] = A[(8 * t + 8 * (t / 2 - 1) + b) * 32 + lane];
-#pragma unroll 1
-            for (int m = t / 2 - 2; m >= 0; --m) {
-                vmul(lo, y, lo);
+        for (int r = 0; r < RS; ++r) {
+            uint32_t x[8], inv[8];
 #pragma unroll
-                for (int b = 0; b < 8; ++b) lo[b] ^= A[(8 * t + 8 * m + b) * 32 + lane];
-            }
-            vmul(lo, x, lo);
-            vinv(lo, cf);
-            vmul(om, cf, om);
+            for (int b = 0; b < 8; ++b) x[b] = a[8 * r + b];
+            vmul(lo[r], x, lo[r]);
+            vinv(lo[r], inv);
+            vmul(om[r], inv, om[r]);
 #pragma unroll
-            for (int b = 0; b < 8; ++b) a[8 * r + b] = om[b];
+            for (int b = 0; b < 8; ++b) a[8 * r + b] = om[r][b];
         }
         transpose32(a);  // byte r of word j: e of block j, slot 4r + h
 #pragma unroll
@@ -1594,38 +1689,56 @@ __global__ void __launch_bounds__(128, 3) bs_chien_kernel(uint8_t *__restrict__ 
     }
     __syncthreads();
 
-    // phase 5: statuses and corrections of blocks j = 8h .. 8h+7
+    // phase 5: statuses and corrections of blocks j = 8h .. 8h+7, two blocks
+    // per pass.  Every corrected byte belongs to one block alone, so plain byte
+    // loads and stores do (neighbouring blocks share words, not bytes); all
+    // loads of a pass are issued before its stores.
     const size_t grp = tile * 32 + lane;
     uint32_t Lp[6];
 #pragma unroll
     for (int b = 0; b < 6; ++b) Lp[b] = rec[(Rl::kL + b) * 32];
 #pragma unroll 1
-    for (int j = 8 * h; j < 8 * h + 8; ++j) {
-        const size_t blk = grp * 32 + j;
-        if (blk >= nblocks) break;
-        if (!((live >> j) & 1u)) {
-            status[blk] = 1;
-            continue;
-        }
-        int l = 0;
+    for (int j0 = 8 * h; j0 < 8 * h + 8; j0 += 2) {
+        int c[2];
+        uint8_t *ad[2][t];
+        uint8_t v[2][t];
 #pragma unroll
-        for (int b = 0; b < 6; ++b) l |= (int)((Lp[b] >> j) & 1u) << b;
-        const int c = cnt[j * 32 + lane];
-        if (l > t || c != l) {
-            status[blk] = 0;
-            continue;
+        for (int u = 0; u < 2; ++u) {
+            const int j = j0 + u;
+            const size_t blk = grp * 32 + j;
+            c[u] = 0;
+            if (blk >= nblocks) continue;
+            if (!((live >> j) & 1u)) {
+                status[blk] = 1;
+                continue;
+            }
+            int l = 0;
+#pragma unroll
+            for (int b = 0; b < 6; ++b) l |= (int)((Lp[b] >> j) & 1u) << b;
+            const int cj = cnt[j * 32 + lane];
+            if (l > t || cj != l) {
+                status[blk] = 0;
+                continue;
+            }
+            status[blk] = 1;
+            c[u] = cj;
+#pragma unroll
+            for (int sl = 0; sl < t; ++sl) {
+                if (sl < cj) {
+                    const int p = size - 1 - deg[(sl * 32 + j) * 32 + lane];
+                    ad[u][sl] = p < msg_len ? data + blk * (size_t)msg_len + p
+                                            : parity + blk * (size_t)E + (p - msg_len);
+                    v[u][sl] = *ad[u][sl];
+                }
+            }
         }
-        // fire-and-forget word XORs: both buffers are 4-byte aligned on this
-        // path, and neighbouring blocks share words
-        for (int sl = 0; sl < c; ++sl) {
-            const int i = deg[(sl * 32 + j) * 32 + lane];
-            const uint32_t e = reinterpret_cast<const uint8_t *>(Xv + (j * 4 + (sl & 3)) * 32 + lane)[sl >> 2];
-            const int p = size - 1 - i;
-            uint8_t *ad = p < msg_len ? data + blk * (size_t)msg_len + p : parity + blk * (size_t)E + (p - msg_len);
-            const uintptr_t w = reinterpret_cast<uintptr_t>(ad);
-            atomicXor(reinterpret_cast<unsigned int *>(w & ~(uintptr_t)3), e << (8 * (w & 3)));
-        }
-        status[blk] = 1;
+#pragma unroll
+        for (int u = 0; u < 2; ++u)
+#pragma unroll
+            for (int sl = 0; sl < t; ++sl)
+                if (sl < c[u])
+                    *ad[u][sl] =
+                        v[u][sl] ^ reinterpret_cast<const uint8_t *>(Xv + ((j0 + u) * 4 + (sl & 3)) * 32 + lane)[sl >> 2];
     }
 }
 
