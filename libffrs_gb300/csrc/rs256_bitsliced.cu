@@ -940,7 +940,9 @@ __global__ void __launch_bounds__(64 * kSegs) bs_encode32_seg_kernel(const uint8
 // number of roots equals L; this is exactly when the reference returns true
 // (with roots == L, C has L distinct roots and Omega != 0).
 //
-// One CTA = 32 groups (1024 blocks) and four warps (see bs_solve_kernel).
+// bs_bm_kernel runs Berlekamp-Massey and the evaluator, bs_chien_kernel the
+// Chien search, Forney and the corrections; one CTA = one tile of 32 groups
+// (1024 blocks) in both.
 
 __device__ __forceinline__ void reduce15(uint32_t (&p)[15], uint32_t (&r)[8]) {
 #pragma unroll
