@@ -330,6 +330,21 @@ def torch_rsi16_apply_errors(torch, cw, pos_h, d_h, step=1 << 15):
 
 # ---------------------------------------------------------------- GPU arms
 
+class TimedRange:
+    """An NVTX range named "timed" around a timed region, so that a profiler
+    can be restricted to it (ncu --nvtx --nvtx-include timed/)."""
+
+    def __init__(self, torch):
+        self.nvtx = torch.cuda.nvtx
+
+    def __enter__(self):
+        self.nvtx.range_push("timed")
+        return self
+
+    def __exit__(self, *exc):
+        self.nvtx.range_pop()
+
+
 def timed_steps(torch, args, world, run, restore, nbuf):
     """K timed steps over nbuf rotating buffers: buffer j is restored (when
     `restore` is given) in an untimed gap before each batch of nbuf steps;
@@ -346,7 +361,7 @@ def timed_steps(torch, args, world, run, restore, nbuf):
     launches0 = capi.kernel_launches()
     capi.timing_collect()
     capi.timing_enable(True)
-    with ClockSampler(torch.cuda.current_device()) as clk:
+    with ClockSampler(torch.cuda.current_device()) as clk, TimedRange(torch):
         done = 0
         while done < args.steps:
             batch = min(nbuf, args.steps - done)
@@ -1228,7 +1243,7 @@ def bench_batch_mixed(args, torch, rank, world):
     launches0 = capi.kernel_launches()
     capi.timing_collect()
     capi.timing_enable(True)
-    with ClockSampler(torch.cuda.current_device()) as clk:
+    with ClockSampler(torch.cuda.current_device()) as clk, TimedRange(torch):
         kern_ms = run_timed(lambda: b.launch(sp), args.steps)
     launches = capi.kernel_launches() - launches0
     kernels = capi.timing_collect()

@@ -18,6 +18,7 @@
 #include "rsi16.cuh"
 
 #include "rsi16_device.cuh"
+#include "rsi16_bt.cuh"
 
 namespace ffgpu {
 
@@ -188,6 +189,38 @@ __global__ void rsi16_encode_warp_kernel(Rsi16Dev c, BlockView v, size_t nblocks
     }
 }
 
+// ecc = N: one block per thread (rsi16_bt.cuh), 32 blocks per warp.  Blocks
+// are contiguous uint16 words (message_len words of message, N of parity).
+template <int N>
+__global__ void __launch_bounds__(128, 3) rsi16_encode_bt_kernel(Rsi16Dev c, const __grid_constant__ BtTw<N> tw,
+                                                                 const uint16_t *__restrict__ msg,
+                                                                 uint16_t *__restrict__ par, size_t nblocks) {
+    extern __shared__ __align__(16) uint8_t bt_smem[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpc = blockDim.x >> 5;
+    uint8_t *bufs = bt_smem + wib * bt_warp_smem<N>();
+    const size_t ntiles = (nblocks + 31) / 32;
+    for (size_t t = (size_t)blockIdx.x * wpc + wib; t < ntiles; t += (size_t)gridDim.x * wpc) {
+        const size_t blk0 = t * 32;
+        int32_t acc[N];
+        // NTT::pntt_message (libffrs/ntt.hpp:160-180): the message chunks only
+        bt_pntt<N>(c, tw, bufs, msg, c.message_len, nullptr, blk0, nblocks, c.pntt_blocks - 1, lane, acc);
+#pragma unroll
+        for (int k = 0; k < N; ++k) acc[k] = lmul(acc[k], tw.mix[k]);
+        bt_gs<N>(acc, tw);
+        const size_t b = blk0 + lane;
+        if (b < nblocks) {
+            uint4 *o = reinterpret_cast<uint4 *>(par + b * N);
+#pragma unroll
+            for (int q = 0; q < N / 8; ++q) {
+                uint32_t w[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) w[i] = lcanon(acc[8 * q + 2 * i]) & 0xffffu | lcanon(acc[8 * q + 2 * i + 1]) << 16;
+                o[q] = make_uint4(w[0], w[1], w[2], w[3]);
+            }
+        }
+    }
+}
+
 // syndromes of block b go to synds[(b / out_group) * out_gstride + (b % out_group) * ecc]
 __global__ void rsi16_synd_warp_kernel(Rsi16Dev c, BlockView v, size_t nblocks, uint32_t *synds, size_t out_group,
                                        size_t out_gstride, uint32_t *gscratch, uint32_t ws_words) {
@@ -311,6 +344,41 @@ __global__ void __launch_bounds__(128, 4) rsi16_repair_batch_kernel(Rsi16Dev c, 
     }
     if (w.lane == 0 && (nfast | nmirror)) {
         atomicAdd(&g_repair_fast_blocks, nfast);
+        atomicAdd(&g_repair_mirror_blocks, nmirror);
+    }
+}
+
+// ecc = N: the repair with one block per thread (bt_repair_tile); warps take
+// tiles of 32 blocks from a counter, blocks the bounded-distance path does
+// not accept go to the step-for-step mirror on the warp's slice of mirror_ws.
+template <int N>
+__global__ void __launch_bounds__(128, 3) rsi16_repair_bt_kernel(Rsi16Dev c, const __grid_constant__ BtTw<N> tw,
+                                                                 BlockView v, size_t nblocks, uint8_t *status,
+                                                                 const uint8_t *active, unsigned int *next_tile,
+                                                                 uint32_t *mirror_ws, uint32_t mirror_words) {
+    extern __shared__ __align__(16) uint32_t bt_rsmem[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpc = blockDim.x >> 5;
+    uint32_t *ws = bt_rsmem + wib * BtRepairSmem<N>::kWords;
+    uint32_t *mws = mirror_ws + ((size_t)blockIdx.x * wpc + wib) * mirror_words;
+    uint16_t *msg = (uint16_t *)v.msg, *par = (uint16_t *)v.par;
+    const size_t ntiles = (nblocks + 31) / 32;
+    unsigned long long nfast = 0, nmirror = 0;
+    for (;;) {
+        unsigned int t = 0;
+        if (lane == 0) t = atomicAdd(next_tile, 1u);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= ntiles) break;
+        const size_t blk0 = (size_t)t * 32;
+        for (uint32_t m = bt_repair_tile<N>(c, tw, msg, par, blk0, nblocks, status, active, ws, lane, nfast); m;
+             m &= m - 1) {
+            __syncwarp();
+            rsi16_repair_block(c, v, blk0 + (__ffs(m) - 1), mws, status, lane);
+            ++nmirror;
+        }
+    }
+    const unsigned int f = __reduce_add_sync(0xffffffffu, (unsigned int)nfast);
+    if (lane == 0 && (f | nmirror)) {
+        atomicAdd(&g_repair_fast_blocks, (unsigned long long)f);
         atomicAdd(&g_repair_mirror_blocks, nmirror);
     }
 }
@@ -479,8 +547,42 @@ static void launch_synd_reg(const Rsi16Code &c, const BlockView &v, size_t nbloc
     check_launch("rsi16_synd_reg_kernel");
 }
 
+// The one-block-per-thread encoder applies to ecc 64 on contiguous uint16
+// blocks whose rows start on 16-byte boundaries (message_len is a multiple of
+// ecc, so every row does when the base pointers do).
+static bool bt_view(const Rsi16Code &c, const BlockView &v) {
+    return c.ecc == 64 && c.pntt_blocks >= 2 && v.group == 1 && v.msg16 && v.par16 && v.msg_estride == 1 &&
+           v.par_estride == 1 && v.msg_gstride == c.message_len && v.par_gstride == c.ecc &&
+           ((uintptr_t)v.msg & 15) == 0 && ((uintptr_t)v.par & 15) == 0 && ((uintptr_t)c.dev.pntt_shift & 15) == 0;
+}
+
+template <int N>
+static BtTw<N> bt_twiddles(const Rsi16Code &c) {
+    BtTw<N> tw;
+    for (int i = 0; i < N / 2; ++i) {
+        tw.ct[i] = c.roots_ecc[i];
+        tw.gs[i] = c.roots_i_ecc[i];
+    }
+    for (int i = 0; i < N; ++i) tw.mix[i] = c.ecc_mix[i];
+    return tw;
+}
+
+template <int N>
+static void launch_encode_bt(const Rsi16Code &c, const BlockView &v, size_t nblocks, cudaStream_t st) {
+    const size_t ntiles = (nblocks + 31) / 32;
+    const unsigned grid = (unsigned)std::max<size_t>(1, std::min<size_t>((ntiles + 3) / 4, (size_t)num_sms() * 24));
+    KernelTimer kt_timer("rsi16_encode_bt_kernel", st);
+    rsi16_encode_bt_kernel<N><<<grid, 128, 4 * bt_warp_smem<N>(), st>>>(
+        c.dev, bt_twiddles<N>(c), (const uint16_t *)v.msg, (uint16_t *)v.par, nblocks);
+    check_launch("rsi16_encode_bt_kernel");
+}
+
 void rsi16_encode(const Rsi16Code &c, const BlockView &v, size_t nblocks, cudaStream_t st) {
     if (!nblocks) return;
+    if (bt_view(c, v)) {
+        launch_encode_bt<64>(c, v, nblocks, st);
+        return;
+    }
     switch (reg_epl(c)) {
         case 1: launch_encode<1>(c, v, nblocks, st); return;
         case 2: launch_encode<2>(c, v, nblocks, st); return;
@@ -524,9 +626,43 @@ void rsi16_synd_grouped(const Rsi16Code &c, const BlockView &v, size_t nblocks, 
     check_launch("rsi16_synd_warp_kernel");
 }
 
+template <int N>
+static void launch_repair_bt(const Rsi16Code &c, const BlockView &v, size_t nblocks, uint8_t *status,
+                             const uint8_t *active, cudaStream_t st) {
+    const size_t smem = 4 * (size_t)BtRepairSmem<N>::kWords * 4;  // four warps per CTA
+    const size_t ntiles = (nblocks + 31) / 32;
+    const unsigned grid = (unsigned)std::max<size_t>(1, std::min<size_t>((ntiles + 3) / 4, (size_t)num_sms() * 3));
+    // the tile counter and the mirror workspaces (one per warp), stream-ordered
+    const uint32_t mwords = c.dev.temp_len + 1;
+    const size_t mbytes = 256 + (size_t)grid * 4 * mwords * 4;
+    void *scratch = nullptr;
+    FFGPU_CHECK_CUDA(cudaMallocAsync(&scratch, mbytes, st));
+    FFGPU_CHECK_CUDA(cudaMemsetAsync(scratch, 0, 4, st));
+    static const bool attr = [] {
+        FFGPU_CHECK_CUDA(cudaFuncSetAttribute(rsi16_repair_bt_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)(4 * BtRepairSmem<N>::kWords * 4)));
+        return true;
+    }();
+    (void)attr;
+    {
+        KernelTimer kt_timer("rsi16_repair_bt_kernel", st);
+        rsi16_repair_bt_kernel<N><<<grid, 128, smem, st>>>(c.dev, bt_twiddles<N>(c), v, nblocks, status, active,
+                                                          (unsigned int *)scratch,
+                                                          (uint32_t *)((char *)scratch + 256), mwords);
+    }
+    cudaError_t e = cudaGetLastError();
+    cudaFreeAsync(scratch, st);
+    if (e != cudaSuccess) throw Error(FFGPU_ECUDA, std::string("rsi16_repair_bt_kernel: ") + cudaGetErrorString(e));
+    launched();
+}
+
 void rsi16_repair(const Rsi16Code &c, const BlockView &v, size_t nblocks, uint8_t *status, cudaStream_t st,
                   const uint8_t *active) {
     if (!nblocks) return;
+    if (bt_view(c, v)) {
+        launch_repair_bt<64>(c, v, nblocks, status, active, st);
+        return;
+    }
     auto go = [&](auto epl) {
         constexpr int E = decltype(epl)::value;
         if constexpr (E == 1 || E == 2) {

@@ -1,0 +1,365 @@
+// RSi16 with one block per thread: the ecc-point NTTs of a block run in one
+// thread's registers, 32 blocks per warp, so that every butterfly is a
+// register operation (no shuffles, no selects, no duplicated multiplies) and
+// the field values are reduced lazily.
+//
+// Lazy GF(65537) values.  A value is an int32 congruent to the field element
+// mod p = 2^16 + 1, kept well inside (-2^30, 2^30).  Since 2^16 = -1 and
+// 2^32 = 1 (mod p), a product x = a w (|a| < 2^31, 0 <= w <= 65536, taken to
+// 64 bits) written as x = h 2^32 + l1 2^16 + l0 (l0, l1 in [0, 65535], h the
+// signed high word) is congruent to l0 - l1 + h: one wide multiply and three
+// integer operations, and the result lies within 65535 + |h| of zero.  Sums
+// and differences are plain int32 adds; only the final values are brought
+// to [0, p).  Every operation keeps the value's residue mod p, so the result
+// is the exact field value that the reference's canonical arithmetic
+// (libffrs/galois.hpp:258-346) gives.
+//
+// Range bound for a block of C chunks of N = 64 words (inputs in [0, 65535]):
+// a CT stage adds at most 65551 in magnitude (products of |b| < 2^20 have
+// |h| <= 16), so after 6 stages |v| < 2^19; chunk 0 enters the accumulator
+// unmultiplied, every later chunk adds at most 65551, so for C <= 1024
+// |acc| < 2^26; after the mix product (|h| < 2^10) and 6 GS stages (the sum
+// side doubles per stage) |v| < 2^23.  All far inside int32.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "rsi16.cuh"
+#include "rsi16_device.cuh"
+
+namespace ffgpu {
+
+static __device__ __forceinline__ int32_t lmul(int32_t a, uint32_t w) {
+    const long long x = (long long)a * (long long)(int32_t)w;
+    const uint32_t lo = (uint32_t)x;
+    return (int32_t)(lo & 0xffffu) - (int32_t)(lo >> 16) + (int32_t)(x >> 32);
+}
+
+// [0, p) from a lazy value with |v| < 2^30: v = (v >> 16) 2^16 + (v & 0xffff)
+// with an arithmetic shift, so v = (v & 0xffff) - (v >> 16), which lies in
+// [-2^14, 65535 + 2^14]; one conditional add and one conditional subtract.
+static __device__ __forceinline__ uint32_t lcanon(int32_t v) {
+    int32_t r = (v & 0xffff) - (v >> 16);
+    r = r < 0 ? r + 0x10001 : r;
+    r = r >= 0x10001 ? r - 0x10001 : r;
+    return (uint32_t)r;
+}
+
+// Twiddles of one code, passed as a kernel parameter: with every index a
+// compile-time constant they are read as constant-bank operands.
+//   ct[ef * i]: roots_ecc (the CT stages, index < N / 2)
+//   gs[i << ef]: roots_i_ecc (the GS stages, index < N / 2)
+//   mix: ecc_mix (RSi16v::_mix_ecc, libffrs/rsi16v_impl.hpp:100-119)
+template <int N>
+struct BtTw {
+    uint32_t ct[N / 2];
+    uint32_t gs[N / 2];
+    uint32_t mix[N];
+};
+
+template <int N>
+constexpr int bt_log() {
+    return N == 32 ? 5 : (N == 64 ? 6 : 7);
+}
+
+// ct_butterfly (libffrs/ntt.hpp:225-249) on one thread's vector: RBO input,
+// normal order output.  Butterflies with twiddle index 0 (a factor of 1)
+// take no product.
+template <int N>
+static __device__ __forceinline__ void bt_ct(int32_t (&x)[N], const BtTw<N> &tw) {
+#pragma unroll
+    for (int st = 0; st < bt_log<N>(); ++st) {
+        const int stride = 1 << st, ef = (N >> 1) >> st;
+#pragma unroll
+        for (int j = 0; j < N; ++j) {
+            if (j & stride) continue;
+            const int i = j & (stride - 1);
+            const int32_t a = x[j], m = i ? lmul(x[j + stride], tw.ct[ef * i]) : x[j + stride];
+            x[j] = a + m;
+            x[j + stride] = a - m;
+        }
+    }
+}
+
+// gs_butterfly (libffrs/ntt.hpp:280-302) on one thread's vector: normal order
+// input, RBO output.
+template <int N>
+static __device__ __forceinline__ void bt_gs(int32_t (&x)[N], const BtTw<N> &tw) {
+#pragma unroll
+    for (int st = 0; st < bt_log<N>(); ++st) {
+        const int stride = (N >> 1) >> st, ef = st;
+#pragma unroll
+        for (int j = 0; j < N; ++j) {
+            if (j & stride) continue;
+            const int i = j & (stride - 1);
+            const int32_t a = x[j], b = x[j + stride];
+            x[j] = a + b;
+            x[j + stride] = i ? lmul(a - b, tw.gs[i << ef]) : a - b;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- warp tile staging
+//
+// A warp's 32 blocks are staged chunk by chunk: chunk ch of block r (N uint16
+// words, 2N bytes) lands in row r of a warp-private shared buffer.  The copy
+// is coalesced (each 16-byte cp.async of a warp instruction covers whole
+// rows: for N = 64, 4 rows of 128 bytes) and the 16-byte segments of row r
+// are stored at segment s ^ (r & 7), so that the row reads below (one row
+// per thread, 16 bytes at a time) hit distinct banks within each quarter
+// warp.  Rows of blocks past the end are zero-filled.
+
+template <int N>
+struct BtTile {
+    static constexpr int kRowBytes = 2 * N;
+    static constexpr int kSegs = kRowBytes / 16;      // 16-byte segments per row
+    static constexpr int kRowsPerIssue = 32 / kSegs;  // rows one warp instruction covers
+    static constexpr int kBufBytes = 32 * kRowBytes;  // one chunk of 32 blocks
+};
+
+static __device__ __forceinline__ uint32_t smem_addr(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// cp.async of chunk `ch` of the warp's blocks [blk0, blk0 + 32) into buf.
+// Block r's words start at words + (blk0 + r) * row_stride (uint16 units).
+template <int N>
+static __device__ __forceinline__ void bt_issue(uint8_t *buf, const uint16_t *words, size_t row_stride, size_t blk0,
+                                                size_t nblocks, uint32_t ch, int lane) {
+    using T = BtTile<N>;
+    static_assert(T::kSegs == 8, "the swizzle assumes 8 segments per row");
+    const int seg = lane % T::kSegs;
+#pragma unroll
+    for (int it = 0; it < 32 / T::kRowsPerIssue; ++it) {
+        const int r = it * T::kRowsPerIssue + lane / T::kSegs;
+        const bool in = blk0 + r < nblocks;
+        const uint16_t *src = in ? words + (blk0 + r) * row_stride + (size_t)ch * N + seg * 8 : words;
+        const uint32_t dst = smem_addr(buf + r * T::kRowBytes + ((seg ^ (r & 7)) << 4));
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(in ? 16 : 0)
+                     : "memory");
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+// row `lane` of buf as N values
+template <int N>
+static __device__ __forceinline__ void bt_read_row(const uint8_t *buf, int lane, int32_t (&x)[N]) {
+    using T = BtTile<N>;
+#pragma unroll
+    for (int s = 0; s < T::kSegs; ++s) {
+        const uint4 q = *reinterpret_cast<const uint4 *>(buf + lane * T::kRowBytes + ((s ^ (lane & 7)) << 4));
+        const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            x[8 * s + 2 * i] = (int32_t)(w[i] & 0xffffu);
+            x[8 * s + 2 * i + 1] = (int32_t)(w[i] >> 16);
+        }
+    }
+}
+
+// NTT::pntt (libffrs/ntt.hpp:133-152) of the warp's 32 blocks over chunks
+// [0, nch), one block per lane: acc = sum_ch ct(chunk_ch) * pntt_shift_ch.
+// `words` / `row_stride` give chunk ch of block b at
+// words + b * row_stride + ch * N; when `par` is given, chunk nch - 1 is read
+// from par + b * N instead (the parity chunk of a codeword).
+template <int N>
+static __device__ __forceinline__ void bt_pntt(const Rsi16Dev &c, const BtTw<N> &tw, uint8_t *bufs,
+                                               const uint16_t *words, size_t row_stride, const uint16_t *par,
+                                               size_t blk0, size_t nblocks, uint32_t nch, int lane,
+                                               int32_t (&acc)[N]) {
+    using T = BtTile<N>;
+    auto issue = [&](uint32_t ch) {
+        uint8_t *buf = bufs + (ch & 1) * T::kBufBytes;
+        if (par && ch == nch - 1)
+            bt_issue<N>(buf, par, N, blk0, nblocks, 0, lane);
+        else
+            bt_issue<N>(buf, words, row_stride, blk0, nblocks, ch, lane);
+    };
+    issue(0);
+    for (uint32_t ch = 0; ch < nch; ++ch) {
+        if (ch + 1 < nch) {
+            issue(ch + 1);
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
+        }
+        __syncwarp();
+        int32_t x[N];
+        bt_read_row<N>(bufs + (ch & 1) * T::kBufBytes, lane, x);
+        __syncwarp();  // every lane has read the buffer before the next issue refills it
+        bt_ct<N>(x, tw);
+        if (ch == 0) {
+            // pntt_shift of chunk 0 is root^(j * rbo(0)) = 1
+#pragma unroll
+            for (int k = 0; k < N; ++k) acc[k] = x[k];
+        } else {
+            const uint4 *sh = reinterpret_cast<const uint4 *>(c.pntt_shift + (size_t)ch * N);
+#pragma unroll
+            for (int q = 0; q < N / 4; ++q) {
+                const uint4 s = __ldg(sh + q);
+                acc[4 * q] += lmul(x[4 * q], s.x);
+                acc[4 * q + 1] += lmul(x[4 * q + 1], s.y);
+                acc[4 * q + 2] += lmul(x[4 * q + 2], s.z);
+                acc[4 * q + 3] += lmul(x[4 * q + 3], s.w);
+            }
+        }
+    }
+}
+
+// v == 0 (mod p) for a lazy value with |v| < 2^30 whose reduced form
+// r = (v & 0xffff) - (v >> 16) lies in (-p, 2p): r is 0 or p
+static __device__ __forceinline__ bool lzero(int32_t v) {
+    const int32_t r = (v & 0xffff) - (v >> 16);
+    return r == 0 || r == 0x10001;
+}
+
+// ---------------------------------------------------------------- one-block-per-thread repair
+//
+// RSi16v::_repair, unknown locations (libffrs/rsi16v_impl.hpp:122-168), on
+// the bounded-distance path of the warp kernels: syndromes by bt_pntt over
+// every chunk (the parity chunk last), Berlekamp-Massey on the reversed
+// syndromes per lane (rsi16_rev_bm_lane: a normal run's connection
+// polynomial read backwards is the locator), the roots by inverse partial
+// NTT per lane (_find_roots_ntt, :443-497) and Forney per lane (_forney,
+// :500-512).  A block the path does not accept (abnormal run, L out of range,
+// root count not L) is repaired by the step-for-step mirror on the warp.
+//
+// Shared memory of one warp, in words: the syndrome columns S[N][33] (lane j
+// owns column j; Omega later replaces S in place), then a region that first
+// holds the two staging buffers of bt_pntt and afterwards the locator
+// columns Loc[N/2 + 1][33] (the derivative later replaces them in place) and
+// the root lists Rts[N/2 + 1][33].
+
+template <int N>
+struct BtRepairSmem {
+    static constexpr int kCol = 33;
+    static constexpr int kS = N * kCol;
+    static constexpr int kLoc = (N / 2 + 1) * kCol;
+    static constexpr int kStage = 2 * BtTile<N>::kBufBytes / 4;
+    static constexpr int kR = kStage > 2 * kLoc ? kStage : 2 * kLoc;
+    // rounded to 16 bytes: every warp's staging buffers start on a 16-byte
+    // boundary (cp.async of 16 bytes)
+    static constexpr int kWords = (kS + kR + 3) / 4 * 4;
+    static_assert(kS % 4 == 0, "the staging buffers start on a 16-byte boundary");
+};
+
+// Horner in lazy arithmetic: sum_{i < n} col[i * 33] x^i, |result| < 2^18
+static __device__ __forceinline__ int32_t bt_eval_col(const uint32_t *col, uint32_t n, uint32_t x) {
+    int32_t sum = 0;
+    for (uint32_t i = n; i-- > 0;) sum = lmul(sum, x) + (int32_t)col[i * 33];
+    return sum;
+}
+
+// position i of block b (message words, then parity words)
+static __device__ __forceinline__ uint16_t *bt_word(uint16_t *msg, uint16_t *par, uint32_t ml, uint32_t ecc,
+                                                    size_t b, uint32_t i) {
+    return i < ml ? msg + b * ml + i : par + b * ecc + (i - ml);
+}
+
+// The repair of the warp's tile [blk0, blk0 + 32), lane = block.  Returns the
+// lanes whose block goes to the mirror; adds the accepted blocks (and the
+// clean ones) to nfast.
+template <int N>
+static __device__ __forceinline__ uint32_t bt_repair_tile(const Rsi16Dev &c, const BtTw<N> &tw, uint16_t *msg,
+                                                          uint16_t *par, size_t blk0, size_t nblocks,
+                                                          uint8_t *status, const uint8_t *active, uint32_t *ws,
+                                                          int lane, unsigned long long &nfast) {
+    using M = BtRepairSmem<N>;
+    constexpr int T = N / 2;
+    constexpr int K = M::kCol;
+    uint32_t *Ssm = ws, *R = ws + M::kS;
+    uint32_t *Lsm = R, *Rts = R + M::kLoc;
+    const size_t b = blk0 + lane;
+    const bool in = b < nblocks && (!active || active[b]);
+
+    // syndromes: S_k = pntt(codeword)_k
+    bool nz = false;
+    {
+        int32_t acc[N];
+        bt_pntt<N>(c, tw, reinterpret_cast<uint8_t *>(R), msg, c.message_len, par, blk0, nblocks, c.pntt_blocks,
+                   lane, acc);
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            const uint32_t s = lcanon(acc[k]);
+            Ssm[k * K + lane] = s;
+            nz |= s != 0;
+        }
+    }
+    __syncwarp();
+    // 0: nothing to do, 1: bounded-distance path, 2: mirror
+    int path = 0;
+    uint32_t L = 0;
+    if (in && !nz) {
+        status[b] = FFGPU_NO_ERRORS;
+        ++nfast;
+    } else if (in) {
+        uint32_t C[T + 1];
+        L = rsi16_rev_bm_lane<T>(Ssm + lane, c.inv_tab, c.ecc, C);
+#pragma unroll
+        for (int i = 0; i <= T; ++i) {
+            if ((uint32_t)i <= L) Lsm[(L - i) * K + lane] = C[i];
+            if ((uint32_t)i > L) Lsm[i * K + lane] = 0u;
+        }
+        path = L ? 1 : 2;
+    }
+    // roots: positions ch * N + k with Loc(X^-1) = 0, by inverse partial NTT
+    // of the locator (pintt_shift, then gs_butterfly) chunk by chunk
+    uint32_t cnt = 0;
+    if (path == 1) {
+        int32_t loc[T + 1];
+#pragma unroll
+        for (int k = 0; k <= T; ++k) loc[k] = (int32_t)Lsm[k * K + lane];
+        for (uint32_t ch = 0; ch < c.pntt_blocks; ++ch) {
+            int32_t x[N];
+            const uint32_t *sh = c.pintt_shift + (size_t)ch * N;
+#pragma unroll
+            for (int k = 0; k < N; ++k) x[k] = k <= T ? lmul(loc[k], __ldg(sh + k)) : 0;
+            bt_gs<N>(x, tw);
+#pragma unroll
+            for (int k = 0; k < N; ++k) {
+                if (lzero(x[k])) {
+                    if (cnt <= (uint32_t)T) Rts[cnt * K + lane] = ch * N + k;
+                    ++cnt;
+                }
+            }
+        }
+        if (cnt != L) path = 2;
+    }
+    if (path == 1) {
+        // Omega = S * Loc mod x^L, in place over S (high degrees first, so
+        // that S_0 .. S_j are still there for Omega_j)
+        for (uint32_t j = L; j-- > 0;) {
+            uint64_t sum = 0;
+            for (uint32_t k = 0; k <= j; ++k) sum += (uint64_t)Lsm[k * K + lane] * Ssm[(j - k) * K + lane];
+            Ssm[j * K + lane] = (uint32_t)(sum % 0x10001u);
+        }
+        // the derivative Loc'_j = (j + 1) Loc_{j+1}, in place over Loc
+        for (uint32_t j = 0; j < L; ++j) Lsm[j * K + lane] = fmul(Lsm[(j + 1) * K + lane], j + 1);
+        const uint32_t NN = c.ntt_len;
+        for (uint32_t r = 0; r < L; ++r) {
+            const uint32_t i = Rts[r * K + lane];
+            const uint32_t e = (__brev(i) >> 16) >> c.rbo_shift;
+            const uint32_t x = c.roots_ntt[e];
+            const uint32_t xi = c.roots_ntt[(NN - e) & (NN - 1)];
+            const uint32_t num = lcanon(bt_eval_col(Ssm + lane, L, xi));
+            const uint32_t den = lcanon(bt_eval_col(Lsm + lane, L, xi));
+            const uint32_t err = fmul(fmul(num, c.inv_tab[den]), x);
+            uint16_t *w = bt_word(msg, par, c.message_len, N, b, i);
+            *w = (uint16_t)fadd(*w, err);
+        }
+        status[b] = FFGPU_REPAIR_OK;
+        ++nfast;
+    }
+    __syncwarp();  // the columns are read before the next tile's staging overwrites them
+    return __ballot_sync(0xffffffffu, path == 2);
+}
+
+// Shared memory of one warp of the bt kernels: two chunk buffers.
+template <int N>
+constexpr int bt_warp_smem() {
+    return 2 * BtTile<N>::kBufBytes;
+}
+
+}  // namespace ffgpu
