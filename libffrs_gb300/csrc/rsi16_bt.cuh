@@ -208,11 +208,19 @@ static __device__ __forceinline__ void bt_pntt(const Rsi16Dev &c, const BtTw<N> 
     }
 }
 
-// v == 0 (mod p) for a lazy value with |v| < 2^30 whose reduced form
-// r = (v & 0xffff) - (v >> 16) lies in (-p, 2p): r is 0 or p
+// v == 0 (mod p) for any int32 v.  p is odd, so multiplication by its
+// inverse mod 2^32 (0xffff0001: 65537 * 0xffff0001 = 2^48 + 1) permutes the
+// 32-bit words and sends the multiple k p to k; the multiples of p in the
+// int32 range are k p with |k| <= 32767, so v is one of them exactly when
+// v * p^-1 + 32767 (mod 2^32) is at most 65534.
 static __device__ __forceinline__ bool lzero(int32_t v) {
-    const int32_t r = (v & 0xffff) - (v >> 16);
-    return r == 0 || r == 0x10001;
+    return (uint32_t)v * 0xffff0001u + 32767u <= 65534u;
+}
+
+// [0, p) from a lazy 64-bit value with |x| < 2^62: x = h 2^32 + l1 2^16 + l0
+static __device__ __forceinline__ uint32_t lcanon64(long long x) {
+    const uint32_t lo = (uint32_t)x;
+    return lcanon((int32_t)(lo & 0xffffu) - (int32_t)(lo >> 16) + (int32_t)(x >> 32));
 }
 
 // ---------------------------------------------------------------- one-block-per-thread repair
@@ -220,11 +228,12 @@ static __device__ __forceinline__ bool lzero(int32_t v) {
 // RSi16v::_repair, unknown locations (libffrs/rsi16v_impl.hpp:122-168), on
 // the bounded-distance path of the warp kernels: syndromes by bt_pntt over
 // every chunk (the parity chunk last), Berlekamp-Massey on the reversed
-// syndromes per lane (rsi16_rev_bm_lane: a normal run's connection
-// polynomial read backwards is the locator), the roots by inverse partial
-// NTT per lane (_find_roots_ntt, :443-497) and Forney per lane (_forney,
-// :500-512).  A block the path does not accept (abnormal run, L out of range,
-// root count not L) is repaired by the step-for-step mirror on the warp.
+// syndromes per lane (bt_rev_bm: a normal run's connection polynomial read
+// backwards is the locator), the roots by inverse partial NTT per lane
+// (_find_roots_ntt, :443-497) and Forney (_forney, :500-512) block by block
+// across the warp, one root per lane.  A block the path does not accept
+// (abnormal run, L out of range, root count not L) is repaired by the
+// step-for-step mirror on the warp.
 //
 // Shared memory of one warp, in words: the syndrome columns S[N][33] (lane j
 // owns column j; Omega later replaces S in place), then a region that first
@@ -245,11 +254,48 @@ struct BtRepairSmem {
     static_assert(kS % 4 == 0, "the staging buffers start on a 16-byte boundary");
 };
 
-// Horner in lazy arithmetic: sum_{i < n} col[i * 33] x^i, |result| < 2^18
-static __device__ __forceinline__ int32_t bt_eval_col(const uint32_t *col, uint32_t n, uint32_t x) {
-    int32_t sum = 0;
-    for (uint32_t i = n; i-- > 0;) sum = lmul(sum, x) + (int32_t)col[i * 33];
-    return sum;
+// Berlekamp-Massey on the reversed syndrome column S_{ecc-1}, ..., S_0
+// (stride 33): the same steps and the same normality and length checks as
+// rsi16_rev_bm_lane, with the connection polynomial C and the shifted
+// previous one (Bs) kept lazily reduced (|C_i| < 2^23 after ecc <= 64 steps)
+// and each discrepancy summed exactly in 64 bits.  Returns L, or 0 when the
+// run is not normal or L > T; C is left in [0, p).
+template <int T>
+static __device__ __forceinline__ uint32_t bt_rev_bm(const uint32_t *S, const uint32_t *inv_tab, uint32_t ecc,
+                                                     int32_t (&C)[T + 1]) {
+    int32_t Bs[T + 1];
+#pragma unroll
+    for (int i = 0; i <= T; ++i) {
+        C[i] = i == 0 ? 1 : 0;
+        Bs[i] = i == 1 ? 1 : 0;
+    }
+    uint32_t L = 0, binv = 1;
+    bool stalled = false, abnormal = false;
+#pragma unroll 1
+    for (uint32_t n = 0; n < ecc; ++n) {
+        long long acc = 0;
+#pragma unroll
+        for (int i = 0; i <= T; ++i)
+            if ((uint32_t)i <= n) acc += (long long)C[i] * (long long)S[(ecc - 1 - (n - i)) * 33];
+        const uint32_t d = lcanon64(acc);
+        const uint32_t coef = fmul(d, binv);
+        const bool grow = d != 0 && 2 * L <= n;
+        if (d == 0 && !(n & 1) && 2 * L <= n) stalled = true;
+        abnormal |= grow && stalled;
+#pragma unroll
+        for (int i = T; i >= 0; --i) {
+            const int32_t bi = Bs[i];
+            Bs[i] = i == 0 ? 0 : (grow ? C[i - 1] : Bs[i - 1]);
+            C[i] -= lmul(bi, coef);
+        }
+        if (grow) {
+            L = n + 1 - L;
+            binv = inv_tab[d];
+        }
+    }
+#pragma unroll
+    for (int i = 0; i <= T; ++i) C[i] = (int32_t)lcanon(C[i]);
+    return (abnormal || L > (uint32_t)T) ? 0u : L;
 }
 
 // position i of block b (message words, then parity words)
@@ -295,32 +341,39 @@ static __device__ __forceinline__ uint32_t bt_repair_tile(const Rsi16Dev &c, con
         status[b] = FFGPU_NO_ERRORS;
         ++nfast;
     } else if (in) {
-        uint32_t C[T + 1];
-        L = rsi16_rev_bm_lane<T>(Ssm + lane, c.inv_tab, c.ecc, C);
+        int32_t C[T + 1];
+        L = bt_rev_bm<T>(Ssm + lane, c.inv_tab, c.ecc, C);
 #pragma unroll
         for (int i = 0; i <= T; ++i) {
-            if ((uint32_t)i <= L) Lsm[(L - i) * K + lane] = C[i];
+            if ((uint32_t)i <= L) Lsm[(L - i) * K + lane] = (uint32_t)C[i];
             if ((uint32_t)i > L) Lsm[i * K + lane] = 0u;
         }
         path = L ? 1 : 2;
     }
     // roots: positions ch * N + k with Loc(X^-1) = 0, by inverse partial NTT
     // of the locator (pintt_shift, then gs_butterfly) chunk by chunk
-    uint32_t cnt = 0;
     if (path == 1) {
         int32_t loc[T + 1];
 #pragma unroll
         for (int k = 0; k <= T; ++k) loc[k] = (int32_t)Lsm[k * K + lane];
+        uint32_t cnt = 0;
         for (uint32_t ch = 0; ch < c.pntt_blocks; ++ch) {
             int32_t x[N];
             const uint32_t *sh = c.pintt_shift + (size_t)ch * N;
 #pragma unroll
             for (int k = 0; k < N; ++k) x[k] = k <= T ? lmul(loc[k], __ldg(sh + k)) : 0;
             bt_gs<N>(x, tw);
+            uint32_t z[N / 32];
 #pragma unroll
-            for (int k = 0; k < N; ++k) {
-                if (lzero(x[k])) {
-                    if (cnt <= (uint32_t)T) Rts[cnt * K + lane] = ch * N + k;
+            for (int h = 0; h < N / 32; ++h) {
+                z[h] = 0;
+#pragma unroll
+                for (int k = 0; k < 32; ++k) z[h] |= (uint32_t)lzero(x[32 * h + k]) << k;
+            }
+#pragma unroll
+            for (int h = 0; h < N / 32; ++h) {
+                for (uint32_t m = z[h]; m; m &= m - 1) {
+                    if (cnt <= (uint32_t)T) Rts[cnt * K + lane] = ch * N + 32 * h + (__ffs(m) - 1);
                     ++cnt;
                 }
             }
@@ -337,20 +390,29 @@ static __device__ __forceinline__ uint32_t bt_repair_tile(const Rsi16Dev &c, con
         }
         // the derivative Loc'_j = (j + 1) Loc_{j+1}, in place over Loc
         for (uint32_t j = 0; j < L; ++j) Lsm[j * K + lane] = fmul(Lsm[(j + 1) * K + lane], j + 1);
-        const uint32_t NN = c.ntt_len;
-        for (uint32_t r = 0; r < L; ++r) {
-            const uint32_t i = Rts[r * K + lane];
+        status[b] = FFGPU_REPAIR_OK;
+        ++nfast;
+    }
+    __syncwarp();
+    // Forney block by block, lane r on root r: e_i = X_i Omega(X_i^-1) / Loc'(X_i^-1)
+    const uint32_t NN = c.ntt_len;
+    for (uint32_t todo = __ballot_sync(0xffffffffu, path == 1); todo; todo &= todo - 1) {
+        const int j = __ffs(todo) - 1;
+        const uint32_t Lj = __shfl_sync(0xffffffffu, L, j);
+        if ((uint32_t)lane < Lj) {
+            const uint32_t i = Rts[lane * K + j];
             const uint32_t e = (__brev(i) >> 16) >> c.rbo_shift;
             const uint32_t x = c.roots_ntt[e];
             const uint32_t xi = c.roots_ntt[(NN - e) & (NN - 1)];
-            const uint32_t num = lcanon(bt_eval_col(Ssm + lane, L, xi));
-            const uint32_t den = lcanon(bt_eval_col(Lsm + lane, L, xi));
-            const uint32_t err = fmul(fmul(num, c.inv_tab[den]), x);
-            uint16_t *w = bt_word(msg, par, c.message_len, N, b, i);
+            int32_t num = 0, den = 0;
+            for (uint32_t k = Lj; k-- > 0;) {
+                num = lmul(num, xi) + (int32_t)Ssm[k * K + j];
+                den = lmul(den, xi) + (int32_t)Lsm[k * K + j];
+            }
+            const uint32_t err = fmul(fmul(lcanon(num), c.inv_tab[lcanon(den)]), x);
+            uint16_t *w = bt_word(msg, par, c.message_len, N, blk0 + j, i);
             *w = (uint16_t)fadd(*w, err);
         }
-        status[b] = FFGPU_REPAIR_OK;
-        ++nfast;
     }
     __syncwarp();  // the columns are read before the next tile's staging overwrites them
     return __ballot_sync(0xffffffffu, path == 2);
