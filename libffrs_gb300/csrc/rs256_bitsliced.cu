@@ -19,6 +19,7 @@
 // remainder R = r * x^d mod g_t into its syndromes S_j = r(a^j) = R(a^j) a^{-jd}.
 // All selector tables are computed at compile time and reach the code as
 // template constants, so every plane index is resolved to a register.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -832,19 +833,27 @@ __device__ __forceinline__ void seg_map(uint32_t *rs, int stride) {
         }
 }
 
-// CTA: 32 groups (1024 blocks), warp w = (factor t = w & 1, segment s = w >> 1)
-__global__ void __launch_bounds__(64 * kSegs) bs_encode32_seg_kernel(const uint8_t *__restrict__ data,
-                                                                     size_t nblocks, int msg_len,
-                                                                     uint8_t *__restrict__ parity) {
+// The segmented encoder on thread-block clusters: one cluster of kSegs CTAs
+// per tile of 32 groups (1024 blocks), CTA rank s running segment s for both
+// factors (warp t = factor t) with its own window buffer, so that a batch of
+// N blocks spreads over N / 256 CTAs instead of N / 1024.  Each rank maps its
+// remainders by x^(kSegLen s) mod g_t in its own shared memory; after a
+// cluster barrier rank 0 adds the kSegs mapped remainders through
+// distributed shared memory, applies the Chinese remainder map and writes the
+// parity; a second barrier keeps the other ranks' shared memory alive until
+// rank 0 has read it.
+__global__ void __cluster_dims__(kSegs, 1, 1) __launch_bounds__(64)
+    bs_encode32_cl_kernel(const uint8_t *__restrict__ data, size_t nblocks, int msg_len, uint8_t *__restrict__ parity) {
+    namespace cg = cooperative_groups;
     constexpr int E = 32, D = 16, G = 32;
-    extern __shared__ __align__(16) uint32_t sm[];  // kSegs window buffers of G * 256 words
-    const int warp = threadIdx.x >> 5, g = threadIdx.x & 31;
-    const int t = warp & 1, s = warp >> 1;
-    const size_t first = (size_t)blockIdx.x * G * 32;
+    extern __shared__ __align__(16) uint32_t sm[];  // the window buffer (G * 256 words), then the stash
+    cg::cluster_group cl = cg::this_cluster();
+    const int s = (int)cl.block_rank();
+    const int t = threadIdx.x >> 5, g = threadIdx.x & 31;
+    const size_t first = (size_t)(blockIdx.x / kSegs) * G * 32;
     const int nb_tile = (int)min((size_t)G * 32, nblocks - first);
     const int end_s = msg_len - kSegLen * s;
     const int start_s = max(0, msg_len - kSegLen * (s + 1));
-    uint32_t *mybuf = sm + s * (G * 256);
     uint32_t R[D][8];
 #pragma unroll
     for (int m = 0; m < D; ++m)
@@ -852,75 +861,75 @@ __global__ void __launch_bounds__(64 * kSegs) bs_encode32_seg_kernel(const uint8
         for (int b = 0; b < 8; ++b) R[m][b] = 0u;
     const size_t total = nblocks * (size_t)msg_len;
     for (int w0 = 0; w0 < kSegLen; w0 += 32) {
+        const int p0 = start_s + w0;
+        const int npos = min(32, end_s - p0);
+        if (npos <= 0) break;  // uniform over the CTA
         __syncthreads();
-        for (int ss = 0; ss < kSegs; ++ss) {
-            const int p0 = max(0, msg_len - kSegLen * (ss + 1)) + w0;
-            if (p0 < msg_len - kSegLen * ss) load_window(sm + ss * (G * 256), data, (size_t)msg_len, total, first,
-                                                         nb_tile, p0, G);
-        }
+        load_window(sm, data, (size_t)msg_len, total, first, nb_tile, p0, G);
         __syncthreads();
-        const int npos = min(32, end_s - (start_s + w0));
-        if (npos > 0) transpose_window<2>(mybuf, g, t);
+        transpose_window<2>(sm, g, t);
         __syncthreads();
-        if (npos > 0) {
-            if (t == 0)
-                run_lfsr_window<Code<E>, 0>(mybuf, g, npos, R);
-            else
-                run_lfsr_window<Code<E>, 1>(mybuf, g, npos, R);
-        }
+        if (t == 0)
+            run_lfsr_window<Code<E>, 0>(sm, g, npos, R);
+        else
+            run_lfsr_window<Code<E>, 1>(sm, g, npos, R);
     }
-    __syncthreads();
-    // stash: [warp][m*8+b][g], stride G
-    uint32_t *rs = sm + warp * (128 * G) + g;
+    __syncthreads();  // window reads done before the stash overwrites the buffer
+    // stash [t][m*8+b][g], stride G, mapped in place by x^(kSegLen s) mod g_t
+    uint32_t *rs = sm + t * (128 * G) + g;
 #pragma unroll
     for (int m = 0; m < D; ++m)
 #pragma unroll
         for (int b = 0; b < 8; ++b) rs[(m * 8 + b) * G] = R[m][b];
-    // segment maps (each thread rewrites only its own stash)
-    switch (warp) {
-        case 2: seg_map<0, 1>(rs, G); break;
-        case 3: seg_map<1, 1>(rs, G); break;
-        case 4: seg_map<0, 2>(rs, G); break;
-        case 5: seg_map<1, 2>(rs, G); break;
-        case 6: seg_map<0, 3>(rs, G); break;
-        case 7: seg_map<1, 3>(rs, G); break;
+    // (each case with its own stash address: a shared one kept live across
+    // the six maps costs registers)
+    switch (s * 2 + t) {
+        case 2: seg_map<0, 1>(sm + g, G); break;
+        case 3: seg_map<1, 1>(sm + 128 * G + g, G); break;
+        case 4: seg_map<0, 2>(sm + g, G); break;
+        case 5: seg_map<1, 2>(sm + 128 * G + g, G); break;
+        case 6: seg_map<0, 3>(sm + g, G); break;
+        case 7: seg_map<1, 3>(sm + 128 * G + g, G); break;
         default: break;
     }
-    __syncthreads();
-    // sum the segments of each factor into the CRT layout [(t*16+m)*8+b][g]
-    uint32_t *crt = sm + 2 * kSegs * 128 * G;  // past the stashes
+    cl.sync();
     if (s == 0) {
+        // the segment sum in place over rank 0's stash: the CRT layout
+        // [(t*16+m)*8+b][g]
+        const uint32_t *rem[kSegs];
+#pragma unroll
+        for (int ss = 1; ss < kSegs; ++ss) rem[ss] = cl.map_shared_rank(sm, ss) + t * (128 * G) + g;
 #pragma unroll 4
         for (int k = 0; k < 128; ++k) {
-            uint32_t v = 0u;
+            uint32_t v = rs[k * G];
 #pragma unroll
-            for (int ss = 0; ss < kSegs; ++ss) v ^= sm[(ss * 2 + t) * (128 * G) + k * G + g];
-            crt[(t * 128 + k) * G + g] = v;
+            for (int ss = 1; ss < kSegs; ++ss) v ^= rem[ss][k * G];
+            rs[k * G] = v;
+        }
+        __syncthreads();
+        uint32_t Pp[16][8];
+#pragma unroll
+        for (int p = 0; p < 16; ++p)
+#pragma unroll
+            for (int o = 0; o < 8; ++o) Pp[p][o] = 0u;
+        if (t == 0)
+            crt_map<0>(sm + g, G, Pp, std::make_integer_sequence<int, 32>{});
+        else
+            crt_map<16>(sm + g, G, Pp, std::make_integer_sequence<int, 32>{});
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            uint32_t a[32];
+#pragma unroll
+            for (int k = 0; k < 32; ++k) a[k] = Pp[q * 4 + k / 8][k % 8];
+            transpose32(a);
+            const int pb = t * 16 + q * 4;
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+                if ((int)(g * 32 + j) < nb_tile)
+                    *reinterpret_cast<uint32_t *>(parity + (first + (size_t)g * 32 + j) * E + pb) = a[j];
         }
     }
-    __syncthreads();
-    if (s != 0) return;
-    uint32_t Pp[16][8];
-#pragma unroll
-    for (int p = 0; p < 16; ++p)
-#pragma unroll
-        for (int o = 0; o < 8; ++o) Pp[p][o] = 0u;
-    if (t == 0)
-        crt_map<0>(crt + g, G, Pp, std::make_integer_sequence<int, 32>{});
-    else
-        crt_map<16>(crt + g, G, Pp, std::make_integer_sequence<int, 32>{});
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        uint32_t a[32];
-#pragma unroll
-        for (int k = 0; k < 32; ++k) a[k] = Pp[q * 4 + k / 8][k % 8];
-        transpose32(a);
-        const int pb = t * 16 + q * 4;
-#pragma unroll
-        for (int j = 0; j < 32; ++j)
-            if ((int)(g * 32 + j) < nb_tile)
-                *reinterpret_cast<uint32_t *>(parity + (first + (size_t)g * 32 + j) * E + pb) = a[j];
-    }
+    cl.sync();
 }
 
 // ---------------------------------------------------------------- bitsliced solve
@@ -1794,13 +1803,12 @@ bool rs256_fast_encode(const Rs256Code &c, const uint8_t *data, size_t nblocks, 
     if (!nblocks) return true;
     const size_t seg_ctas = (nblocks + 1023) / 1024;
     if (msg_len <= bs::kSegs * bs::kSegLen && seg_ctas <= (size_t)sm_count() * 4) {
-        // too few groups to fill the GPU: split the messages into segments too
-        constexpr size_t smem = (size_t)(4 * 32 * 256 + 2 * 128 * 32) * 4;
-        FFGPU_CHECK_CUDA(
-            cudaFuncSetAttribute(bs::bs_encode32_seg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        KernelTimer kt_timer("bs_encode32_seg_kernel", st);
-        bs::bs_encode32_seg_kernel<<<(unsigned)seg_ctas, 64 * bs::kSegs, smem, st>>>(data, nblocks, msg_len, parity);
-        check_launch("bs_encode32_seg_kernel");
+        // too few groups to fill the GPU: split the messages into segments
+        // too, one CTA per (tile, segment) in clusters of kSegs
+        constexpr size_t smem = (size_t)(32 * 256) * 4;
+        KernelTimer kt_timer("bs_encode32_cl_kernel", st);
+        bs::bs_encode32_cl_kernel<<<(unsigned)(seg_ctas * bs::kSegs), 64, smem, st>>>(data, nblocks, msg_len, parity);
+        check_launch("bs_encode32_cl_kernel");
         return true;
     }
     KernelTimer kt_timer("bs_encode32_kernel", st);

@@ -273,11 +273,13 @@ static __device__ __forceinline__ uint32_t bt_rev_bm(const uint32_t *S, const ui
     bool stalled = false, abnormal = false;
 #pragma unroll 1
     for (uint32_t n = 0; n < ecc; ++n) {
-        long long acc = 0;
+        // four independent partial sums: a dependent chain of T + 1 wide
+        // multiply-adds would leave the lane waiting on each one
+        long long acc[4] = {0, 0, 0, 0};
 #pragma unroll
         for (int i = 0; i <= T; ++i)
-            if ((uint32_t)i <= n) acc += (long long)C[i] * (long long)S[(ecc - 1 - (n - i)) * 33];
-        const uint32_t d = lcanon64(acc);
+            if ((uint32_t)i <= n) acc[i & 3] += (long long)C[i] * (long long)S[(ecc - 1 - (n - i)) * 33];
+        const uint32_t d = lcanon64((acc[0] + acc[1]) + (acc[2] + acc[3]));
         const uint32_t coef = fmul(d, binv);
         const bool grow = d != 0 && 2 * L <= n;
         if (d == 0 && !(n & 1) && 2 * L <= n) stalled = true;
@@ -384,9 +386,14 @@ static __device__ __forceinline__ uint32_t bt_repair_tile(const Rsi16Dev &c, con
         // Omega = S * Loc mod x^L, in place over S (high degrees first, so
         // that S_0 .. S_j are still there for Omega_j)
         for (uint32_t j = L; j-- > 0;) {
-            uint64_t sum = 0;
-            for (uint32_t k = 0; k <= j; ++k) sum += (uint64_t)Lsm[k * K + lane] * Ssm[(j - k) * K + lane];
-            Ssm[j * K + lane] = (uint32_t)(sum % 0x10001u);
+            uint64_t s0 = 0, s1 = 0;
+            uint32_t k = 0;
+            for (; k + 1 <= j; k += 2) {
+                s0 += (uint64_t)Lsm[k * K + lane] * Ssm[(j - k) * K + lane];
+                s1 += (uint64_t)Lsm[(k + 1) * K + lane] * Ssm[(j - k - 1) * K + lane];
+            }
+            if (k == j) s0 += (uint64_t)Lsm[k * K + lane] * Ssm[0 * K + lane];
+            Ssm[j * K + lane] = lcanon64((long long)(s0 + s1));
         }
         // the derivative Loc'_j = (j + 1) Loc_{j+1}, in place over Loc
         for (uint32_t j = 0; j < L; ++j) Lsm[j * K + lane] = fmul(Lsm[(j + 1) * K + lane], j + 1);
