@@ -13,6 +13,11 @@
 #include <thread>
 #include <vector>
 
+#include <sys/mman.h>
+#include <unistd.h>
+
+#include <cerrno>
+
 #include "common.cuh"
 #include "handles.h"
 #include "rs256.cuh"
@@ -74,14 +79,16 @@ CopyPool &copy_pool() {
 }
 }  // namespace
 
-void host_copy(void *dst, const void *src, size_t n) {
-    constexpr size_t kPart = 4u << 20;
-    if (n <= 2 * kPart) {
-        std::memcpy(dst, src, n);
+// Runs job(off, len) over [0, n) split into parts of at least min_part bytes
+// (page multiples): the calling thread takes the first part, the copy pool
+// the others; returns when every part is done.
+static void split_run(size_t n, size_t min_part, const std::function<void(size_t, size_t)> &job) {
+    CopyPool &pool = copy_pool();
+    const size_t parts = std::max<size_t>(1, std::min<size_t>(n / min_part, pool.workers + 1));
+    if (parts == 1) {
+        job(0, n);
         return;
     }
-    CopyPool &pool = copy_pool();
-    const size_t parts = std::min<size_t>((n + kPart - 1) / kPart, pool.workers + 1);
     const size_t each = ((n + parts - 1) / parts + 4095) & ~(size_t)4095;
     std::mutex m;
     std::condition_variable done;
@@ -91,14 +98,42 @@ void host_copy(void *dst, const void *src, size_t n) {
     for (size_t p = 1; p <= helpers; ++p) {
         const size_t off = p * each, len = std::min(each, n - off);
         pool.push([&, off, len] {
-            std::memcpy((char *)dst + off, (const char *)src + off, len);
+            job(off, len);
             std::lock_guard<std::mutex> lk(m);
             if (--left == 0) done.notify_one();
         });
     }
-    std::memcpy(dst, src, std::min(each, n));
+    job(0, std::min(each, n));
     std::unique_lock<std::mutex> lk(m);
     done.wait(lk, [&] { return left == 0; });
+}
+
+void host_copy(void *dst, const void *src, size_t n) {
+    split_run(n, 1u << 20, [&](size_t off, size_t len) { std::memcpy((char *)dst + off, (const char *)src + off, len); });
+}
+
+// Maps in the pages of [p, p + n) ahead of the copies into them: a fresh
+// pageable output (a new bytearray) otherwise takes its page faults, and the
+// kernel's zeroing of every page, inside the copies at the end of a host
+// pipeline.  madvise(MADV_POPULATE_WRITE) faults the pages in writable
+// without changing their contents (so outputs that alias inputs are safe), a
+// part per pool thread; kernels without it (before Linux 5.14) skip this.
+#ifndef MADV_POPULATE_WRITE
+#define MADV_POPULATE_WRITE 23
+#endif
+static void host_prefault(void *p, size_t n) {
+    static const size_t page = [] {
+        const long v = sysconf(_SC_PAGESIZE);
+        return v > 0 ? (size_t)v : (size_t)4096;
+    }();
+    static std::atomic<bool> unsupported{false};
+    if (unsupported.load(std::memory_order_relaxed)) return;
+    split_run(n, 2u << 20, [&](size_t off, size_t len) {
+        const uintptr_t a = ((uintptr_t)p + off + page - 1) & ~(uintptr_t)(page - 1);
+        const uintptr_t b = ((uintptr_t)p + off + len) & ~(uintptr_t)(page - 1);
+        if (b > a && madvise((void *)a, b - a, MADV_POPULATE_WRITE) != 0 && errno == EINVAL)
+            unsupported.store(true, std::memory_order_relaxed);
+    });
 }
 
 // Ordering events of the host pipelines, reused across calls (creating and
@@ -144,6 +179,23 @@ void OutputDrain::chunk(cudaStream_t st) {
 }
 
 void OutputDrain::finish() {
+    // the outputs' pages are mapped in (in parallel) while the GPU still
+    // works on the chunks, before any chunk is copied out
+    // (adjacent parts, such as one output's chunks, are merged first, so that
+    // each output is one parallel pass)
+    std::vector<std::pair<char *, size_t>> runs;
+    for (auto &pt : parts_) runs.push_back({(char *)pt.dst, pt.n});
+    std::sort(runs.begin(), runs.end());
+    size_t w = 0;
+    for (size_t i = 0; i < runs.size(); ++i) {
+        if (w && runs[w - 1].first + runs[w - 1].second == runs[i].first)
+            runs[w - 1].second += runs[i].second;
+        else
+            runs[w++] = runs[i];
+    }
+    runs.resize(w);
+    for (auto &r : runs)
+        if (r.second >= (1u << 20)) host_prefault(r.first, r.second);
     for (auto &c : chunks_) {
         FFGPU_CHECK_CUDA(cudaEventSynchronize(c.ev));
         for (size_t i = c.first; i < c.first + c.count; ++i) host_copy(parts_[i].dst, parts_[i].src, parts_[i].n);

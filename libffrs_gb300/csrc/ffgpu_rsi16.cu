@@ -148,7 +148,7 @@ int ffgpu_rsi16_encode_host(const ffgpu_rsi16 *code, const uint16_t *msg, size_t
         if (interleave == 1) {
             // chunks of blocks on the pipeline streams: copies in, encodes and
             // copies out of different chunks overlap
-            const size_t chunk = host_chunk_blocks(nblocks, 8192, 4);
+            const size_t chunk = host_chunk_blocks(nblocks, 8192, 16);
             uint16_t *hp = pipeline_out(parity, chunk < nblocks, h->h_par, np * 2);
             OutputDrain drain;
             HostPipeline pl;

@@ -361,9 +361,19 @@ static __device__ __forceinline__ uint32_t bt_repair_tile(const Rsi16Dev &c, con
         uint32_t cnt = 0;
         for (uint32_t ch = 0; ch < c.pntt_blocks; ++ch) {
             int32_t x[N];
-            const uint32_t *sh = c.pintt_shift + (size_t)ch * N;
+            // pintt_shift of chunk ch, 16 bytes at a time (the last load also
+            // reads the chunk's entries T + 1 .. T + 3, unused)
+            const uint4 *sh = reinterpret_cast<const uint4 *>(c.pintt_shift + (size_t)ch * N);
 #pragma unroll
-            for (int k = 0; k < N; ++k) x[k] = k <= T ? lmul(loc[k], __ldg(sh + k)) : 0;
+            for (int q = 0; q <= T / 4; ++q) {
+                const uint4 s4 = __ldg(sh + q);
+                const uint32_t sv[4] = {s4.x, s4.y, s4.z, s4.w};
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+                    if (4 * q + i <= T) x[4 * q + i] = lmul(loc[4 * q + i], sv[i]);
+            }
+#pragma unroll
+            for (int k = T + 1; k < N; ++k) x[k] = 0;
             bt_gs<N>(x, tw);
             uint32_t z[N / 32];
 #pragma unroll
