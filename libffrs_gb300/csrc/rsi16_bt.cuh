@@ -254,14 +254,18 @@ struct BtRepairSmem {
     static_assert(kS % 4 == 0, "the staging buffers start on a 16-byte boundary");
 };
 
-// Berlekamp-Massey on the reversed syndrome column S_{ecc-1}, ..., S_0
-// (stride 33): the same steps and the same normality and length checks as
+// Berlekamp-Massey on the reversed syndrome column S_{E-1}, ..., S_0 (stride
+// 33): the same steps and the same normality and length checks as
 // rsi16_rev_bm_lane, with the connection polynomial C and the shifted
-// previous one (Bs) kept lazily reduced (|C_i| < 2^23 after ecc <= 64 steps)
-// and each discrepancy summed exactly in 64 bits.  Returns L, or 0 when the
-// run is not normal or L > T; C is left in [0, p).
-template <int T>
-static __device__ __forceinline__ uint32_t bt_rev_bm(const uint32_t *S, const uint32_t *inv_tab, uint32_t ecc,
+// previous one (Bs) kept lazily reduced (|C_i| < 2^23 after E <= 64 steps)
+// and each discrepancy summed exactly in 64 bits.  Before step n, C has
+// degree at most n and Bs at most n + 1, so the discrepancy takes the terms
+// i <= n and the update the coefficients i <= n + 2; groups of four
+// coefficients beyond that are skipped by branches on n (uniform across the
+// warp).  Returns L, or 0 when the run is not normal or L > T; C is left in
+// [0, p).
+template <int T, int E>
+static __device__ __forceinline__ uint32_t bt_rev_bm(const uint32_t *S, const uint32_t *inv_tab,
                                                      int32_t (&C)[T + 1]) {
     int32_t Bs[T + 1];
 #pragma unroll
@@ -272,23 +276,35 @@ static __device__ __forceinline__ uint32_t bt_rev_bm(const uint32_t *S, const ui
     uint32_t L = 0, binv = 1;
     bool stalled = false, abnormal = false;
 #pragma unroll 1
-    for (uint32_t n = 0; n < ecc; ++n) {
+    for (int n = 0; n < E; ++n) {
         // four independent partial sums: a dependent chain of T + 1 wide
         // multiply-adds would leave the lane waiting on each one
         long long acc[4] = {0, 0, 0, 0};
 #pragma unroll
-        for (int i = 0; i <= T; ++i)
-            if ((uint32_t)i <= n) acc[i & 3] += (long long)C[i] * (long long)S[(ecc - 1 - (n - i)) * 33];
+        for (int g = 0; g <= T / 4; ++g) {
+            if (4 * g > n) break;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int i = 4 * g + u;
+                if (i <= T && i <= n) acc[u] += (long long)C[i] * (int32_t)S[(E - 1 - (n - i)) * 33];
+            }
+        }
         const uint32_t d = lcanon64((acc[0] + acc[1]) + (acc[2] + acc[3]));
         const uint32_t coef = fmul(d, binv);
-        const bool grow = d != 0 && 2 * L <= n;
-        if (d == 0 && !(n & 1) && 2 * L <= n) stalled = true;
+        const bool grow = d != 0 && 2 * L <= (uint32_t)n;
+        if (d == 0 && !(n & 1) && 2 * L <= (uint32_t)n) stalled = true;
         abnormal |= grow && stalled;
 #pragma unroll
-        for (int i = T; i >= 0; --i) {
-            const int32_t bi = Bs[i];
-            Bs[i] = i == 0 ? 0 : (grow ? C[i - 1] : Bs[i - 1]);
-            C[i] -= lmul(bi, coef);
+        for (int g = T / 4; g >= 0; --g) {
+            if (4 * g > n + 2) continue;
+#pragma unroll
+            for (int u = 3; u >= 0; --u) {
+                const int i = 4 * g + u;
+                if (i > T) continue;
+                const int32_t bi = Bs[i];
+                Bs[i] = i == 0 ? 0 : (grow ? C[i - 1] : Bs[i - 1]);
+                C[i] -= lmul(bi, coef);
+            }
         }
         if (grow) {
             L = n + 1 - L;
@@ -344,7 +360,7 @@ static __device__ __forceinline__ uint32_t bt_repair_tile(const Rsi16Dev &c, con
         ++nfast;
     } else if (in) {
         int32_t C[T + 1];
-        L = bt_rev_bm<T>(Ssm + lane, c.inv_tab, c.ecc, C);
+        L = bt_rev_bm<T, N>(Ssm + lane, c.inv_tab, C);
 #pragma unroll
         for (int i = 0; i <= T; ++i) {
             if ((uint32_t)i <= L) Lsm[(L - i) * K + lane] = (uint32_t)C[i];
@@ -411,24 +427,52 @@ static __device__ __forceinline__ uint32_t bt_repair_tile(const Rsi16Dev &c, con
         ++nfast;
     }
     __syncwarp();
-    // Forney block by block, lane r on root r: e_i = X_i Omega(X_i^-1) / Loc'(X_i^-1)
+    // Forney, e_i = X_i Omega(X_i^-1) / Loc'(X_i^-1), in two passes.  First
+    // block by block, lane r on root r: Omega(X^-1) into row 32 + r of the
+    // block's syndrome column (rows 32 .. 63 are free once Omega is built)
+    // and Loc'(X^-1) into row r of its locator column (the derivative is dead
+    // once the block's evaluations are done).  Then every lane finishes its
+    // own block's roots four at a time: the inverse, the product and the
+    // read-modify-write of the word, with the loads of four roots in flight.
     const uint32_t NN = c.ntt_len;
     for (uint32_t todo = __ballot_sync(0xffffffffu, path == 1); todo; todo &= todo - 1) {
         const int j = __ffs(todo) - 1;
         const uint32_t Lj = __shfl_sync(0xffffffffu, L, j);
+        uint32_t den = 0;
         if ((uint32_t)lane < Lj) {
             const uint32_t i = Rts[lane * K + j];
             const uint32_t e = (__brev(i) >> 16) >> c.rbo_shift;
-            const uint32_t x = c.roots_ntt[e];
             const uint32_t xi = c.roots_ntt[(NN - e) & (NN - 1)];
-            int32_t num = 0, den = 0;
+            int32_t num = 0, dn = 0;
             for (uint32_t k = Lj; k-- > 0;) {
                 num = lmul(num, xi) + (int32_t)Ssm[k * K + j];
-                den = lmul(den, xi) + (int32_t)Lsm[k * K + j];
+                dn = lmul(dn, xi) + (int32_t)Lsm[k * K + j];
             }
-            const uint32_t err = fmul(fmul(lcanon(num), c.inv_tab[lcanon(den)]), x);
-            uint16_t *w = bt_word(msg, par, c.message_len, N, blk0 + j, i);
-            *w = (uint16_t)fadd(*w, err);
+            Ssm[(32 + lane) * K + j] = lcanon(num);
+            den = lcanon(dn);
+        }
+        __syncwarp();  // every lane has read the derivative before it is overwritten
+        if ((uint32_t)lane < Lj) Lsm[lane * K + j] = den;
+    }
+    __syncwarp();
+    if (path == 1) {
+        for (uint32_t r0 = 0; r0 < L; r0 += 4) {
+            uint32_t pos[4], x[4], inv[4], num[4], old[4];
+            uint16_t *w[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const uint32_t r = r0 + q < L ? r0 + q : r0;
+                pos[q] = Rts[r * K + lane];
+                num[q] = Ssm[(32 + r) * K + lane];
+                const uint32_t e = (__brev(pos[q]) >> 16) >> c.rbo_shift;
+                x[q] = c.roots_ntt[e];
+                inv[q] = c.inv_tab[Lsm[r * K + lane]];
+                w[q] = bt_word(msg, par, c.message_len, N, b, pos[q]);
+                old[q] = *w[q];
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (r0 + q < L) *w[q] = (uint16_t)fadd(old[q], fmul(fmul(num[q], inv[q]), x[q]));
         }
     }
     __syncwarp();  // the columns are read before the next tile's staging overwrites them
