@@ -114,6 +114,14 @@ Rsi16Code::Rsi16Code(size_t block_len_, size_t ecc_len, uint32_t primitive_)
     const uint32_t w_i = inv(w);
     for (size_t i = 0; i < ecc; ++i) ecc_mix[i] = neg(div(pow(w_i, (uint32_t)i), (uint32_t)ecc));
 
+    auto shoup = [](const std::vector<uint32_t> &v) {
+        std::vector<uint32_t> o(v.size());
+        for (size_t i = 0; i < v.size(); ++i) o[i] = (uint32_t)(((uint64_t)v[i] << 32) / 0x10001u);
+        return o;
+    };
+    pntt_shift_s = shoup(pntt_shift);
+    pintt_shift_s = shoup(pintt_shift);
+
     // one device allocation for all tables
     std::vector<uint32_t> all;
     auto put = [&](const std::vector<uint32_t> &v) {
@@ -126,7 +134,7 @@ Rsi16Code::Rsi16Code(size_t block_len_, size_t ecc_len, uint32_t primitive_)
     for (uint32_t a = 0; a < 65537; ++a) inv_tab[a] = inv(a);
     const size_t o_rn = put(roots_ntt), o_re = put(roots_ecc), o_rie = put(roots_i_ecc), o_re2 = put(roots_ecc2),
                  o_rie2 = put(roots_i_ecc2), o_ps = put(pntt_shift), o_pis = put(pintt_shift), o_rbo = put(rbo_ecc),
-                 o_mix = put(ecc_mix), o_inv = put(inv_tab);
+                 o_mix = put(ecc_mix), o_inv = put(inv_tab), o_pss = put(pntt_shift_s), o_piss = put(pintt_shift_s);
     FFGPU_CHECK_CUDA(cudaMalloc(&d_tables, all.size() * 4));
     FFGPU_CHECK_CUDA(cudaMemcpy(d_tables, all.data(), all.size() * 4, cudaMemcpyHostToDevice));
     dev.roots_ntt = d_tables + o_rn;
@@ -139,6 +147,8 @@ Rsi16Code::Rsi16Code(size_t block_len_, size_t ecc_len, uint32_t primitive_)
     dev.rbo_ecc = d_tables + o_rbo;
     dev.ecc_mix = d_tables + o_mix;
     dev.inv_tab = d_tables + o_inv;
+    dev.pntt_shift_s = d_tables + o_pss;
+    dev.pintt_shift_s = d_tables + o_piss;
     dev.block_len = (uint32_t)block_len;
     dev.message_len = (uint32_t)message_len;
     dev.ecc = (uint32_t)ecc;
@@ -201,12 +211,12 @@ __global__ void __launch_bounds__(128, 3) rsi16_encode_bt_kernel(Rsi16Dev c, con
     const size_t ntiles = (nblocks + 31) / 32;
     for (size_t t = (size_t)blockIdx.x * wpc + wib; t < ntiles; t += (size_t)gridDim.x * wpc) {
         const size_t blk0 = t * 32;
-        int32_t acc[N];
+        uint32_t acc[N];
         // NTT::pntt_message (libffrs/ntt.hpp:160-180): the message chunks only
         bt_pntt<N>(c, tw, bufs, msg, c.message_len, nullptr, blk0, nblocks, c.pntt_blocks - 1, lane, acc);
 #pragma unroll
-        for (int k = 0; k < N; ++k) acc[k] = lmul(acc[k], tw.mix[k]);
-        bt_gs<N>(acc, tw);
+        for (int k = 0; k < N; ++k) acc[k] = smul(acc[k], tw.mix[k], tw.mix_s[k]);
+        bt_gs_u<N>(acc, tw);
         const size_t b = blk0 + lane;
         if (b < nblocks) {
             uint4 *o = reinterpret_cast<uint4 *>(par + b * N);
@@ -214,7 +224,7 @@ __global__ void __launch_bounds__(128, 3) rsi16_encode_bt_kernel(Rsi16Dev c, con
             for (int q = 0; q < N / 8; ++q) {
                 uint32_t w[4];
 #pragma unroll
-                for (int i = 0; i < 4; ++i) w[i] = lcanon(acc[8 * q + 2 * i]) & 0xffffu | lcanon(acc[8 * q + 2 * i + 1]) << 16;
+                for (int i = 0; i < 4; ++i) w[i] = ucanon(acc[8 * q + 2 * i]) & 0xffffu | ucanon(acc[8 * q + 2 * i + 1]) << 16;
                 o[q] = make_uint4(w[0], w[1], w[2], w[3]);
             }
         }
@@ -564,6 +574,12 @@ static BtTw<N> bt_twiddles(const Rsi16Code &c) {
         tw.gs[i] = c.roots_i_ecc[i];
     }
     for (int i = 0; i < N; ++i) tw.mix[i] = c.ecc_mix[i];
+    auto shoup = [](uint32_t w) { return (uint32_t)(((uint64_t)w << 32) / 0x10001u); };
+    for (int i = 0; i < N / 2; ++i) {
+        tw.ct_s[i] = shoup(tw.ct[i]);
+        tw.gs_s[i] = shoup(tw.gs[i]);
+    }
+    for (int i = 0; i < N; ++i) tw.mix_s[i] = shoup(tw.mix[i]);
     return tw;
 }
 

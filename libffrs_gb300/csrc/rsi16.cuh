@@ -15,6 +15,9 @@ namespace ffgpu {
 struct Rsi16Dev {
     const uint32_t *roots_ntt, *roots_ecc, *roots_i_ecc, *roots_ecc2, *roots_i_ecc2;
     const uint32_t *pntt_shift, *pintt_shift, *rbo_ecc, *ecc_mix;
+    // floor(w 2^32 / p) of every pntt_shift / pintt_shift entry w (the
+    // Shoup companions used by the one-block-per-thread kernels)
+    const uint32_t *pntt_shift_s, *pintt_shift_s;
     const uint32_t *inv_tab;  // inverse of every field element (inv(0) == 1, as the reference's table)
     uint32_t block_len, message_len, ecc, ntt_len, pntt_blocks, ecc_mask, rbo_shift;
     uint32_t ecc_len_i, ecc2_len_i;
@@ -29,6 +32,7 @@ struct Rsi16Code {
     std::vector<uint32_t> exp_, log_;
     std::vector<uint32_t> roots_ntt, roots_i_ntt, roots_ecc, roots_i_ecc, roots_ecc2, roots_i_ecc2;
     std::vector<uint32_t> pntt_shift, pintt_shift, rbo_ecc, ecc_mix;
+    std::vector<uint32_t> pntt_shift_s, pintt_shift_s;
     uint32_t ntt_len_i, ecc_len_i, ecc2_len_i;
     uint32_t *d_tables = nullptr;
     Rsi16Dev dev{};

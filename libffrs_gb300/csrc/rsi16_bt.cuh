@@ -3,23 +3,25 @@
 // register operation (no shuffles, no selects, no duplicated multiplies) and
 // the field values are reduced lazily.
 //
-// Lazy GF(65537) values.  A value is an int32 congruent to the field element
-// mod p = 2^16 + 1, kept well inside (-2^30, 2^30).  Since 2^16 = -1 and
-// 2^32 = 1 (mod p), a product x = a w (|a| < 2^31, 0 <= w <= 65536, taken to
-// 64 bits) written as x = h 2^32 + l1 2^16 + l0 (l0, l1 in [0, 65535], h the
-// signed high word) is congruent to l0 - l1 + h: one wide multiply and three
-// integer operations, and the result lies within 65535 + |h| of zero.  Sums
-// and differences are plain int32 adds; only the final values are brought
-// to [0, p).  Every operation keeps the value's residue mod p, so the result
-// is the exact field value that the reference's canonical arithmetic
-// (libffrs/galois.hpp:258-346) gives.
+// Lazy GF(65537) values, p = 2^16 + 1.  Every operation keeps the value's
+// residue mod p, so the results are the exact field values that the
+// reference's canonical arithmetic (libffrs/galois.hpp:258-346) gives; only
+// outputs are brought to [0, p).  Two forms:
 //
-// Range bound for a block of C chunks of N = 64 words (inputs in [0, 65535]):
-// a CT stage adds at most 65551 in magnitude (products of |b| < 2^20 have
-// |h| <= 16), so after 6 stages |v| < 2^19; chunk 0 enters the accumulator
-// unmultiplied, every later chunk adds at most 65551, so for C <= 1024
-// |acc| < 2^26; after the mix product (|h| < 2^10) and 6 GS stages (the sum
-// side doubles per stage) |v| < 2^23.  All far inside int32.
+// * The transforms (bt_ct_u, bt_gs_u) keep uint32 values below a bound known
+//   at compile time for each stage.  A product by a table constant w uses
+//   Shoup's method with w' = floor(w 2^32 / p): for any x < 2^32,
+//   x w - floor(x w' / 2^32) p lies in [0, 2p), and the 32-bit wraparound
+//   gives it exactly (smul: three multiply instructions).  A butterfly's
+//   difference adds K, a multiple of p at least the stage's input bound, so
+//   it stays non-negative.  For 64-point transforms the bounds stay below
+//   2^25 (the stage-by-stage counts are at bt_ct_u and bt_gs_u).
+// * The other steps (Berlekamp-Massey, Horner, Forney) keep signed int32
+//   values within (-2^30, 2^30).  A product x = a w (|a| < 2^31,
+//   0 <= w <= 65536, taken to 64 bits) written as x = h 2^32 + l1 2^16 + l0
+//   (l0, l1 in [0, 65535], h the signed high word) is congruent to
+//   l0 - l1 + h, since 2^16 = -1 and 2^32 = 1 (mod p) (lmul: one wide
+//   multiply and three integer operations).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -47,8 +49,23 @@ static __device__ __forceinline__ uint32_t lcanon(int32_t v) {
     return (uint32_t)r;
 }
 
+// x w mod p into [0, 2p) for any x < 2^32 and w < p, w' = floor(w 2^32 / p)
+static __device__ __forceinline__ uint32_t smul(uint32_t x, uint32_t w, uint32_t ws) {
+    return x * w - __umulhi(x, ws) * 0x10001u;
+}
+
+// [0, p) from an unsigned lazy value v < 2^31
+static __device__ __forceinline__ uint32_t ucanon(uint32_t v) {
+    const int32_t r = (int32_t)(v & 0xffffu) - (int32_t)(v >> 16);
+    return (uint32_t)(r < 0 ? r + 0x10001 : r);
+}
+
+// the least multiple of p that is at least b
+__host__ __device__ constexpr uint32_t pmul_ceil(uint32_t b) { return (b + 0x10000u) / 0x10001u * 0x10001u; }
+
 // Twiddles of one code, passed as a kernel parameter: with every index a
-// compile-time constant they are read as constant-bank operands.
+// compile-time constant they are read as constant-bank operands.  Each has
+// its Shoup companion.
 //   ct[ef * i]: roots_ecc (the CT stages, index < N / 2)
 //   gs[i << ef]: roots_i_ecc (the GS stages, index < N / 2)
 //   mix: ecc_mix (RSi16v::_mix_ecc, libffrs/rsi16v_impl.hpp:100-119)
@@ -57,6 +74,7 @@ struct BtTw {
     uint32_t ct[N / 2];
     uint32_t gs[N / 2];
     uint32_t mix[N];
+    uint32_t ct_s[N / 2], gs_s[N / 2], mix_s[N];  // the Shoup companions floor(w 2^32 / p)
 };
 
 template <int N>
@@ -65,39 +83,53 @@ constexpr int bt_log() {
 }
 
 // ct_butterfly (libffrs/ntt.hpp:225-249) on one thread's vector: RBO input,
-// normal order output.  Butterflies with twiddle index 0 (a factor of 1)
-// take no product.
+// normal order output, inputs below 2^16 (message words).  Butterflies with
+// twiddle index 0 (a factor of 1) take no product.  With inputs below B, a
+// stage's outputs are below B + K, K = the least multiple of p at least
+// max(B, 2p): a + m < B + 2p, a - m + K < B + K (m < 2p after a product, m < B
+// without).  From B = 2^16 the six stages of 64 points end below 6.3 * 10^6.
 template <int N>
-static __device__ __forceinline__ void bt_ct(int32_t (&x)[N], const BtTw<N> &tw) {
+static __device__ __forceinline__ void bt_ct_u(uint32_t (&x)[N], const BtTw<N> &tw) {
+    uint32_t B = 0x10000u;
 #pragma unroll
     for (int st = 0; st < bt_log<N>(); ++st) {
         const int stride = 1 << st, ef = (N >> 1) >> st;
+        const uint32_t K = pmul_ceil(B > 0x20002u ? B : 0x20002u);
 #pragma unroll
         for (int j = 0; j < N; ++j) {
             if (j & stride) continue;
             const int i = j & (stride - 1);
-            const int32_t a = x[j], m = i ? lmul(x[j + stride], tw.ct[ef * i]) : x[j + stride];
+            const uint32_t a = x[j];
+            const uint32_t m = i ? smul(x[j + stride], tw.ct[ef * i], tw.ct_s[ef * i]) : x[j + stride];
             x[j] = a + m;
-            x[j + stride] = a - m;
+            x[j + stride] = a - m + K;
         }
+        B += K;
     }
 }
 
 // gs_butterfly (libffrs/ntt.hpp:280-302) on one thread's vector: normal order
-// input, RBO output.
+// input, RBO output, inputs below 2p (products).  With inputs below B a stage's
+// outputs are below B + K, K = the least multiple of p at least B: a + b < 2B,
+// a - b + K < B + K, a product < 2p.  From B = 2p the six stages of 64 points
+// end below 2^6 * 2p < 2^24.
 template <int N>
-static __device__ __forceinline__ void bt_gs(int32_t (&x)[N], const BtTw<N> &tw) {
+static __device__ __forceinline__ void bt_gs_u(uint32_t (&x)[N], const BtTw<N> &tw) {
+    uint32_t B = 0x20002u;
 #pragma unroll
     for (int st = 0; st < bt_log<N>(); ++st) {
         const int stride = (N >> 1) >> st, ef = st;
+        const uint32_t K = pmul_ceil(B);
 #pragma unroll
         for (int j = 0; j < N; ++j) {
             if (j & stride) continue;
             const int i = j & (stride - 1);
-            const int32_t a = x[j], b = x[j + stride];
+            const uint32_t a = x[j], b = x[j + stride];
             x[j] = a + b;
-            x[j + stride] = i ? lmul(a - b, tw.gs[i << ef]) : a - b;
+            const uint32_t d = a - b + K;
+            x[j + stride] = i ? smul(d, tw.gs[i << ef], tw.gs_s[i << ef]) : d;
         }
+        B += K;
     }
 }
 
@@ -145,7 +177,7 @@ static __device__ __forceinline__ void bt_issue(uint8_t *buf, const uint16_t *wo
 
 // row `lane` of buf as N values
 template <int N>
-static __device__ __forceinline__ void bt_read_row(const uint8_t *buf, int lane, int32_t (&x)[N]) {
+static __device__ __forceinline__ void bt_read_row(const uint8_t *buf, int lane, uint32_t (&x)[N]) {
     using T = BtTile<N>;
 #pragma unroll
     for (int s = 0; s < T::kSegs; ++s) {
@@ -153,14 +185,15 @@ static __device__ __forceinline__ void bt_read_row(const uint8_t *buf, int lane,
         const uint32_t w[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-            x[8 * s + 2 * i] = (int32_t)(w[i] & 0xffffu);
-            x[8 * s + 2 * i + 1] = (int32_t)(w[i] >> 16);
+            x[8 * s + 2 * i] = w[i] & 0xffffu;
+            x[8 * s + 2 * i + 1] = w[i] >> 16;
         }
     }
 }
 
 // NTT::pntt (libffrs/ntt.hpp:133-152) of the warp's 32 blocks over chunks
-// [0, nch), one block per lane: acc = sum_ch ct(chunk_ch) * pntt_shift_ch.
+// [0, nch), one block per lane: acc = sum_ch ct(chunk_ch) * pntt_shift_ch,
+// lazily reduced: below 6.3 * 10^6 + (nch - 1) 2p < 2^28 for nch <= 1024.
 // `words` / `row_stride` give chunk ch of block b at
 // words + b * row_stride + ch * N; when `par` is given, chunk nch - 1 is read
 // from par + b * N instead (the parity chunk of a codeword).
@@ -168,7 +201,7 @@ template <int N>
 static __device__ __forceinline__ void bt_pntt(const Rsi16Dev &c, const BtTw<N> &tw, uint8_t *bufs,
                                                const uint16_t *words, size_t row_stride, const uint16_t *par,
                                                size_t blk0, size_t nblocks, uint32_t nch, int lane,
-                                               int32_t (&acc)[N]) {
+                                               uint32_t (&acc)[N]) {
     using T = BtTile<N>;
     auto issue = [&](uint32_t ch) {
         uint8_t *buf = bufs + (ch & 1) * T::kBufBytes;
@@ -186,23 +219,24 @@ static __device__ __forceinline__ void bt_pntt(const Rsi16Dev &c, const BtTw<N> 
             asm volatile("cp.async.wait_group 0;" ::: "memory");
         }
         __syncwarp();
-        int32_t x[N];
+        uint32_t x[N];
         bt_read_row<N>(bufs + (ch & 1) * T::kBufBytes, lane, x);
         __syncwarp();  // every lane has read the buffer before the next issue refills it
-        bt_ct<N>(x, tw);
+        bt_ct_u<N>(x, tw);
         if (ch == 0) {
             // pntt_shift of chunk 0 is root^(j * rbo(0)) = 1
 #pragma unroll
             for (int k = 0; k < N; ++k) acc[k] = x[k];
         } else {
             const uint4 *sh = reinterpret_cast<const uint4 *>(c.pntt_shift + (size_t)ch * N);
+            const uint4 *shs = reinterpret_cast<const uint4 *>(c.pntt_shift_s + (size_t)ch * N);
 #pragma unroll
             for (int q = 0; q < N / 4; ++q) {
-                const uint4 s = __ldg(sh + q);
-                acc[4 * q] += lmul(x[4 * q], s.x);
-                acc[4 * q + 1] += lmul(x[4 * q + 1], s.y);
-                acc[4 * q + 2] += lmul(x[4 * q + 2], s.z);
-                acc[4 * q + 3] += lmul(x[4 * q + 3], s.w);
+                const uint4 s = __ldg(sh + q), ss = __ldg(shs + q);
+                acc[4 * q] += smul(x[4 * q], s.x, ss.x);
+                acc[4 * q + 1] += smul(x[4 * q + 1], s.y, ss.y);
+                acc[4 * q + 2] += smul(x[4 * q + 2], s.z, ss.z);
+                acc[4 * q + 3] += smul(x[4 * q + 3], s.w, ss.w);
             }
         }
     }
@@ -341,12 +375,12 @@ static __device__ __forceinline__ uint32_t bt_repair_tile(const Rsi16Dev &c, con
     // syndromes: S_k = pntt(codeword)_k
     bool nz = false;
     {
-        int32_t acc[N];
+        uint32_t acc[N];
         bt_pntt<N>(c, tw, reinterpret_cast<uint8_t *>(R), msg, c.message_len, par, blk0, nblocks, c.pntt_blocks,
                    lane, acc);
 #pragma unroll
         for (int k = 0; k < N; ++k) {
-            const uint32_t s = lcanon(acc[k]);
+            const uint32_t s = ucanon(acc[k]);
             Ssm[k * K + lane] = s;
             nz |= s != 0;
         }
@@ -376,27 +410,28 @@ static __device__ __forceinline__ uint32_t bt_repair_tile(const Rsi16Dev &c, con
         for (int k = 0; k <= T; ++k) loc[k] = (int32_t)Lsm[k * K + lane];
         uint32_t cnt = 0;
         for (uint32_t ch = 0; ch < c.pntt_blocks; ++ch) {
-            int32_t x[N];
+            uint32_t x[N];
             // pintt_shift of chunk ch, 16 bytes at a time (the last load also
             // reads the chunk's entries T + 1 .. T + 3, unused)
             const uint4 *sh = reinterpret_cast<const uint4 *>(c.pintt_shift + (size_t)ch * N);
+            const uint4 *shs = reinterpret_cast<const uint4 *>(c.pintt_shift_s + (size_t)ch * N);
 #pragma unroll
             for (int q = 0; q <= T / 4; ++q) {
-                const uint4 s4 = __ldg(sh + q);
-                const uint32_t sv[4] = {s4.x, s4.y, s4.z, s4.w};
+                const uint4 s4 = __ldg(sh + q), ss4 = __ldg(shs + q);
+                const uint32_t sv[4] = {s4.x, s4.y, s4.z, s4.w}, svs[4] = {ss4.x, ss4.y, ss4.z, ss4.w};
 #pragma unroll
                 for (int i = 0; i < 4; ++i)
-                    if (4 * q + i <= T) x[4 * q + i] = lmul(loc[4 * q + i], sv[i]);
+                    if (4 * q + i <= T) x[4 * q + i] = smul((uint32_t)loc[4 * q + i], sv[i], svs[i]);
             }
 #pragma unroll
             for (int k = T + 1; k < N; ++k) x[k] = 0;
-            bt_gs<N>(x, tw);
+            bt_gs_u<N>(x, tw);
             uint32_t z[N / 32];
 #pragma unroll
             for (int h = 0; h < N / 32; ++h) {
                 z[h] = 0;
 #pragma unroll
-                for (int k = 0; k < 32; ++k) z[h] |= (uint32_t)lzero(x[32 * h + k]) << k;
+                for (int k = 0; k < 32; ++k) z[h] |= (uint32_t)lzero((int32_t)x[32 * h + k]) << k;
             }
 #pragma unroll
             for (int h = 0; h < N / 32; ++h) {
