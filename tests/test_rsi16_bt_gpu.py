@@ -106,3 +106,43 @@ def test_bt_repair_vs_oracle(built, bl, nb):
     np.testing.assert_array_equal(ds.cpu().numpy(), np.where(so < 0, 255, so.astype(np.int16)).astype(np.uint8))
     np.testing.assert_array_equal(dm.cpu().numpy().view(np.uint16), mo)
     np.testing.assert_array_equal(dp.cpu().numpy().view(np.uint16), po)
+
+
+@pytest.mark.parametrize("nb,k", [(1, 16), (40, 16), (1000, 48), (300, 64)])
+def test_known_location_repair_many_blocks(built, nb, k):
+    """ffgpu_rsi16_repair_known: nblocks blocks sharing one list of k known
+    error positions (device memory), every block against the oracle."""
+    import torch
+
+    from libffrs_gb300 import capi
+
+    bl, ecc = 1024, 64
+    rng = np.random.Generator(np.random.PCG64(nb * 11 + k))
+    o = O.RSi16(bl, ecc)
+    msg = rng.integers(0, 65536, size=(nb, bl - ecc), dtype=np.uint16)
+    cw = np.concatenate([msg, o.encode_blocks(msg)], axis=1)
+    pos = np.sort(rng.choice(bl, size=k, replace=False)).astype(np.uint32)
+    for i in range(nb):
+        for q in pos:
+            while True:
+                v = (int(cw[i, q]) + int(rng.integers(1, 65537))) % 65537
+                if v != 65536:
+                    break
+            cw[i, q] = v
+    m, p = np.ascontiguousarray(cw[:, :bl - ecc]), np.ascontiguousarray(cw[:, bl - ecc:])
+    dm = torch.from_numpy(m.view(np.int16)).cuda()
+    dp = torch.from_numpy(p.view(np.int16)).cuda()
+    ds = torch.zeros(nb, dtype=torch.uint8, device="cuda")
+    dpos = torch.from_numpy(pos.view(np.int32)).cuda()
+    code = capi.RSi16Code(bl, ecc)  # held: its handle is freed with the object
+    capi.call("ffgpu_rsi16_repair_known", code.h, dm.data_ptr(), dp.data_ptr(), nb, dpos.data_ptr(), k,
+              ds.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    want_m, want_p, want_s = m.copy(), p.copy(), []
+    for i in range(nb):
+        mi, pi = want_m[i].copy(), want_p[i].copy()
+        want_s.append(int(o.repair(mi, pi, [int(x) for x in pos])))
+        want_m[i], want_p[i] = mi, pi
+    np.testing.assert_array_equal(ds.cpu().numpy(), np.array(want_s, dtype=np.uint8))
+    np.testing.assert_array_equal(dm.cpu().numpy().view(np.uint16), want_m)
+    np.testing.assert_array_equal(dp.cpu().numpy().view(np.uint16), want_p)
