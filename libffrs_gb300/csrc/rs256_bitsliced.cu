@@ -1544,29 +1544,6 @@ __global__ void __launch_bounds__(128, 3) bs_chien_kernel(uint8_t *__restrict__ 
     const size_t tile = blockIdx.x;
     const uint32_t *rec = planes + tile * (size_t)kTileWords<E> + lane;
     const int size = msg_len + E;
-    // The corrections of phase 5 change a few bytes in most lines of the
-    // tile's data, which the syndrome kernel read long before (evicted from
-    // L2 by then).  The tile's data and parity are two contiguous stretches:
-    // prefetch them into L2 now, so that the phases in between hide the DRAM
-    // reads and the final XORs hit L2.  Bulk prefetches need 16-byte aligned
-    // addresses and sizes: each stretch is trimmed inwards to that, in pieces
-    // of at most 2 KiB.
-    {
-        const size_t first = tile * 1024;
-        const size_t nb = nblocks - first < 1024 ? nblocks - first : 1024;
-        const uintptr_t d0 = reinterpret_cast<uintptr_t>(data + first * (size_t)msg_len);
-        const uintptr_t p0 = reinterpret_cast<uintptr_t>(parity + first * E);
-        const uintptr_t db = (d0 + 15) & ~(uintptr_t)15, de = (d0 + nb * (size_t)msg_len) & ~(uintptr_t)15;
-        const uintptr_t pb = (p0 + 15) & ~(uintptr_t)15, pe = (p0 + nb * E) & ~(uintptr_t)15;
-        const size_t dn = de > db ? de - db : 0, pn = pe > pb ? pe - pb : 0;
-        const size_t dpieces = (dn + 2047) / 2048, ppieces = (pn + 2047) / 2048;
-        for (size_t q = threadIdx.x; q < dpieces + ppieces; q += 128) {
-            const bool isd = q < dpieces;
-            const size_t off = (isd ? q : q - dpieces) * 2048, len = isd ? dn : pn;
-            const uint32_t n = (uint32_t)(len - off < 2048 ? len - off : 2048);  // a multiple of 16
-            asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"((isd ? db : pb) + off), "r"(n) : "memory");
-        }
-    }
     for (int i = threadIdx.x; i < 255; i += 128) ex[i] = exp512[i];
     const uint32_t live = rec[Rl::kLive * 32];
 
@@ -1628,6 +1605,30 @@ __global__ void __launch_bounds__(128, 3) bs_chien_kernel(uint8_t *__restrict__ 
     }
     __syncthreads();
 
+    // The corrections of phase 5 change a few bytes in most lines of the
+    // tile's data, which the syndrome kernel read long before (evicted from
+    // L2 by then).  The tile's data and parity are two contiguous stretches:
+    // prefetch them into L2 now, so that phase 4 hides the DRAM reads and the
+    // final XORs hit L2 (issued at the kernel's start, the prefetches of all
+    // resident tiles held about as much as L2 and were partly evicted again).  Bulk prefetches need 16-byte aligned
+    // addresses and sizes: each stretch is trimmed inwards to that, in pieces
+    // of at most 2 KiB.
+    {
+        const size_t first = tile * 1024;
+        const size_t nb = nblocks - first < 1024 ? nblocks - first : 1024;
+        const uintptr_t d0 = reinterpret_cast<uintptr_t>(data + first * (size_t)msg_len);
+        const uintptr_t p0 = reinterpret_cast<uintptr_t>(parity + first * E);
+        const uintptr_t db = (d0 + 15) & ~(uintptr_t)15, de = (d0 + nb * (size_t)msg_len) & ~(uintptr_t)15;
+        const uintptr_t pb = (p0 + 15) & ~(uintptr_t)15, pe = (p0 + nb * E) & ~(uintptr_t)15;
+        const size_t dn = de > db ? de - db : 0, pn = pe > pb ? pe - pb : 0;
+        const size_t dpieces = (dn + 2047) / 2048, ppieces = (pn + 2047) / 2048;
+        for (size_t q = threadIdx.x; q < dpieces + ppieces; q += 128) {
+            const bool isd = q < dpieces;
+            const size_t off = (isd ? q : q - dpieces) * 2048, len = isd ? dn : pn;
+            const uint32_t n = (uint32_t)(len - off < 2048 ? len - off : 2048);  // a multiple of 16
+            asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"((isd ? db : pb) + off), "r"(n) : "memory");
+        }
+    }
     // phase 4: Forney.  The coefficient planes go to shared memory first
     // (Omega_0..t-1, then C_1, C_3, ..., C_{t-1}); thread h evaluates the
     // slots 4r + h (r < t/4) of all 32 blocks of its group.
