@@ -202,7 +202,7 @@ __global__ void rsi16_encode_warp_kernel(Rsi16Dev c, BlockView v, size_t nblocks
 // ecc = N: one block per thread (rsi16_bt.cuh), 32 blocks per warp.  Blocks
 // are contiguous uint16 words (message_len words of message, N of parity).
 template <int N>
-__global__ void __launch_bounds__(128, 3) rsi16_encode_bt_kernel(Rsi16Dev c, const __grid_constant__ BtTw<N> tw,
+__global__ void __launch_bounds__(128, N == 64 ? 3 : 4) rsi16_encode_bt_kernel(Rsi16Dev c, const __grid_constant__ BtTw<N> tw,
                                                                  const uint16_t *__restrict__ msg,
                                                                  uint16_t *__restrict__ par, size_t nblocks) {
     extern __shared__ __align__(16) uint8_t bt_smem[];
@@ -362,7 +362,7 @@ __global__ void __launch_bounds__(128, 4) rsi16_repair_batch_kernel(Rsi16Dev c, 
 // tiles of 32 blocks from a counter, blocks the bounded-distance path does
 // not accept go to the step-for-step mirror on the warp's slice of mirror_ws.
 template <int N>
-__global__ void __launch_bounds__(128, 3) rsi16_repair_bt_kernel(Rsi16Dev c, const __grid_constant__ BtTw<N> tw,
+__global__ void __launch_bounds__(128, N == 64 ? 3 : 4) rsi16_repair_bt_kernel(Rsi16Dev c, const __grid_constant__ BtTw<N> tw,
                                                                  BlockView v, size_t nblocks, uint8_t *status,
                                                                  const uint8_t *active, unsigned int *next_tile,
                                                                  uint32_t *mirror_ws, uint32_t mirror_words) {
@@ -557,11 +557,11 @@ static void launch_synd_reg(const Rsi16Code &c, const BlockView &v, size_t nbloc
     check_launch("rsi16_synd_reg_kernel");
 }
 
-// The one-block-per-thread encoder applies to ecc 64 on contiguous uint16
-// blocks whose rows start on 16-byte boundaries (message_len is a multiple of
-// ecc, so every row does when the base pointers do).
+// The one-block-per-thread kernels apply to ecc 32 and 64 on contiguous
+// uint16 blocks whose rows start on 16-byte boundaries (message_len is a
+// multiple of ecc, so every row does when the base pointers do).
 static bool bt_view(const Rsi16Code &c, const BlockView &v) {
-    return c.ecc == 64 && c.pntt_blocks >= 2 && v.group == 1 && v.msg16 && v.par16 && v.msg_estride == 1 &&
+    return (c.ecc == 64 || c.ecc == 32) && c.pntt_blocks >= 2 && v.group == 1 && v.msg16 && v.par16 && v.msg_estride == 1 &&
            v.par_estride == 1 && v.msg_gstride == c.message_len && v.par_gstride == c.ecc &&
            ((uintptr_t)v.msg & 15) == 0 && ((uintptr_t)v.par & 15) == 0 && ((uintptr_t)c.dev.pntt_shift & 15) == 0;
 }
@@ -596,7 +596,10 @@ static void launch_encode_bt(const Rsi16Code &c, const BlockView &v, size_t nblo
 void rsi16_encode(const Rsi16Code &c, const BlockView &v, size_t nblocks, cudaStream_t st) {
     if (!nblocks) return;
     if (bt_view(c, v)) {
-        launch_encode_bt<64>(c, v, nblocks, st);
+        if (c.ecc == 64)
+            launch_encode_bt<64>(c, v, nblocks, st);
+        else
+            launch_encode_bt<32>(c, v, nblocks, st);
         return;
     }
     switch (reg_epl(c)) {
@@ -647,7 +650,8 @@ static void launch_repair_bt(const Rsi16Code &c, const BlockView &v, size_t nblo
                              const uint8_t *active, cudaStream_t st) {
     const size_t smem = 4 * (size_t)BtRepairSmem<N>::kWords * 4;  // four warps per CTA
     const size_t ntiles = (nblocks + 31) / 32;
-    const unsigned grid = (unsigned)std::max<size_t>(1, std::min<size_t>((ntiles + 3) / 4, (size_t)num_sms() * 3));
+    const unsigned grid =
+        (unsigned)std::max<size_t>(1, std::min<size_t>((ntiles + 3) / 4, (size_t)num_sms() * (N == 64 ? 3 : 4)));
     // the tile counter and the mirror workspaces (one per warp), stream-ordered
     const uint32_t mwords = c.dev.temp_len + 1;
     const size_t mbytes = 256 + (size_t)grid * 4 * mwords * 4;
@@ -676,7 +680,10 @@ void rsi16_repair(const Rsi16Code &c, const BlockView &v, size_t nblocks, uint8_
                   const uint8_t *active) {
     if (!nblocks) return;
     if (bt_view(c, v)) {
-        launch_repair_bt<64>(c, v, nblocks, status, active, st);
+        if (c.ecc == 64)
+            launch_repair_bt<64>(c, v, nblocks, status, active, st);
+        else
+            launch_repair_bt<32>(c, v, nblocks, status, active, st);
         return;
     }
     auto go = [&](auto epl) {

@@ -149,6 +149,13 @@ struct BtTile {
     static constexpr int kSegs = kRowBytes / 16;      // 16-byte segments per row
     static constexpr int kRowsPerIssue = 32 / kSegs;  // rows one warp instruction covers
     static constexpr int kBufBytes = 32 * kRowBytes;  // one chunk of 32 blocks
+    static_assert(kSegs == 8 || kSegs == 4, "rows of 128 or 64 bytes");
+    // the slot of segment s of row r.  A quarter warp reads one segment of 8
+    // consecutive rows; they must hit the 8 distinct 16-byte bank groups of a
+    // 128-byte bank cycle.  128-byte rows: s ^ (r & 7).  64-byte rows, two per
+    // cycle: the even rows take groups 0-3 and the odd rows 4-7, so
+    // s ^ ((r >> 1) & 3).
+    static __device__ __forceinline__ int swz(int s, int r) { return kSegs == 8 ? s ^ (r & 7) : s ^ ((r >> 1) & 3); }
 };
 
 static __device__ __forceinline__ uint32_t smem_addr(const void *p) {
@@ -161,14 +168,13 @@ template <int N>
 static __device__ __forceinline__ void bt_issue(uint8_t *buf, const uint16_t *words, size_t row_stride, size_t blk0,
                                                 size_t nblocks, uint32_t ch, int lane) {
     using T = BtTile<N>;
-    static_assert(T::kSegs == 8, "the swizzle assumes 8 segments per row");
     const int seg = lane % T::kSegs;
 #pragma unroll
     for (int it = 0; it < 32 / T::kRowsPerIssue; ++it) {
         const int r = it * T::kRowsPerIssue + lane / T::kSegs;
         const bool in = blk0 + r < nblocks;
         const uint16_t *src = in ? words + (blk0 + r) * row_stride + (size_t)ch * N + seg * 8 : words;
-        const uint32_t dst = smem_addr(buf + r * T::kRowBytes + ((seg ^ (r & 7)) << 4));
+        const uint32_t dst = smem_addr(buf + r * T::kRowBytes + (T::swz(seg, r) << 4));
         asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(in ? 16 : 0)
                      : "memory");
     }
@@ -181,7 +187,7 @@ static __device__ __forceinline__ void bt_read_row(const uint8_t *buf, int lane,
     using T = BtTile<N>;
 #pragma unroll
     for (int s = 0; s < T::kSegs; ++s) {
-        const uint4 q = *reinterpret_cast<const uint4 *>(buf + lane * T::kRowBytes + ((s ^ (lane & 7)) << 4));
+        const uint4 q = *reinterpret_cast<const uint4 *>(buf + lane * T::kRowBytes + (T::swz(s, lane) << 4));
         const uint32_t w[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
@@ -463,8 +469,8 @@ static __device__ __forceinline__ uint32_t bt_repair_tile(const Rsi16Dev &c, con
     }
     __syncwarp();
     // Forney, e_i = X_i Omega(X_i^-1) / Loc'(X_i^-1), in two passes.  First
-    // block by block, lane r on root r: Omega(X^-1) into row 32 + r of the
-    // block's syndrome column (rows 32 .. 63 are free once Omega is built)
+    // block by block, lane r on root r: Omega(X^-1) into row T + r of the
+    // block's syndrome column (rows T .. N - 1 are free once Omega is built)
     // and Loc'(X^-1) into row r of its locator column (the derivative is dead
     // once the block's evaluations are done).  Then every lane finishes its
     // own block's roots four at a time: the inverse, the product and the
@@ -483,7 +489,7 @@ static __device__ __forceinline__ uint32_t bt_repair_tile(const Rsi16Dev &c, con
                 num = lmul(num, xi) + (int32_t)Ssm[k * K + j];
                 dn = lmul(dn, xi) + (int32_t)Lsm[k * K + j];
             }
-            Ssm[(32 + lane) * K + j] = lcanon(num);
+            Ssm[(T + lane) * K + j] = lcanon(num);
             den = lcanon(dn);
         }
         __syncwarp();  // every lane has read the derivative before it is overwritten
@@ -498,7 +504,7 @@ static __device__ __forceinline__ uint32_t bt_repair_tile(const Rsi16Dev &c, con
             for (int q = 0; q < 4; ++q) {
                 const uint32_t r = r0 + q < L ? r0 + q : r0;
                 pos[q] = Rts[r * K + lane];
-                num[q] = Ssm[(32 + r) * K + lane];
+                num[q] = Ssm[(T + r) * K + lane];
                 const uint32_t e = (__brev(pos[q]) >> 16) >> c.rbo_shift;
                 x[q] = c.roots_ntt[e];
                 inv[q] = c.inv_tab[Lsm[r * K + lane]];

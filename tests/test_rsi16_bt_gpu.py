@@ -1,5 +1,5 @@
-"""The one-block-per-thread RSi16 kernels (ecc 64 on contiguous, 16-byte
-aligned uint16 blocks) against the oracle: ragged block counts around the
+"""The one-block-per-thread RSi16 kernels (ecc 32 and 64 on contiguous,
+16-byte aligned uint16 blocks) against the oracle: ragged block counts around the
 32-block warp tile, the shortest and longest block lengths, extreme words
 (the lazy reduction's largest magnitudes), and the fallback taken when the
 buffers are not 16-byte aligned."""
@@ -24,25 +24,26 @@ def _encode(torch, capi, bl, ecc, msg, offset_words=0):
     return p.cpu().numpy().view(np.uint16).reshape(nb, ecc)
 
 
+@pytest.mark.parametrize("ecc", [32, 64])
 @pytest.mark.parametrize("bl,nb", [(128, 1), (128, 33), (1024, 31), (1024, 32), (1024, 33), (1024, 1000),
                                    (4096, 70), (65536, 3)])
-def test_bt_encode_vs_oracle(built, bl, nb):
+def test_bt_encode_vs_oracle(built, bl, nb, ecc):
     import torch
 
     from libffrs_gb300 import capi
 
-    ecc = 64
-    rng = np.random.Generator(np.random.PCG64(bl * 3 + nb))
+    rng = np.random.Generator(np.random.PCG64(bl * 3 + nb + ecc))
     msg = rng.integers(0, 65536, size=(nb, bl - ecc), dtype=np.uint16)
     np.testing.assert_array_equal(_encode(torch, capi, bl, ecc, msg), O.RSi16(bl, ecc).encode_blocks(msg))
 
 
-def test_bt_encode_extreme_words(built):
+@pytest.mark.parametrize("ecc", [32, 64])
+def test_bt_encode_extreme_words(built, ecc):
     import torch
 
     from libffrs_gb300 import capi
 
-    bl, ecc = 1024, 64
+    bl = 1024
     rng = np.random.Generator(np.random.PCG64(77))
     msg = np.empty((96, bl - ecc), dtype=np.uint16)
     msg[:32] = 65535
@@ -51,12 +52,13 @@ def test_bt_encode_extreme_words(built):
     np.testing.assert_array_equal(_encode(torch, capi, bl, ecc, msg), O.RSi16(bl, ecc).encode_blocks(msg))
 
 
-def test_bt_unaligned_falls_back(built):
+@pytest.mark.parametrize("ecc", [32, 64])
+def test_bt_unaligned_falls_back(built, ecc):
     import torch
 
     from libffrs_gb300 import capi
 
-    bl, ecc, nb = 1024, 64, 45
+    bl, nb = 1024, 45
     rng = np.random.Generator(np.random.PCG64(78))
     msg = rng.integers(0, 65536, size=(nb, bl - ecc), dtype=np.uint16)
     want = O.RSi16(bl, ecc).encode_blocks(msg)
@@ -75,17 +77,17 @@ def _corrupt(rng, cw, k):
         cw[q] = v
 
 
+@pytest.mark.parametrize("ecc", [32, 64])
 @pytest.mark.parametrize("bl,nb", [(128, 33), (1024, 1), (1024, 95), (4096, 40), (65536, 3)])
-def test_bt_repair_vs_oracle(built, bl, nb):
+def test_bt_repair_vs_oracle(built, bl, nb, ecc):
     """Statuses and repaired words of every block, 0 to ecc/2 + 4 errors (the
     ones past ecc/2 go to the mirror), and the path counters."""
     import torch
 
     from libffrs_gb300 import capi
 
-    ecc = 64
     ml = bl - ecc
-    rng = np.random.Generator(np.random.PCG64(bl * 5 + nb))
+    rng = np.random.Generator(np.random.PCG64(bl * 5 + nb + ecc))
     o = O.RSi16(bl, ecc)
     msg = rng.integers(0, 65536, size=(nb, ml), dtype=np.uint16)
     cw = np.concatenate([msg, o.encode_blocks(msg)], axis=1)
