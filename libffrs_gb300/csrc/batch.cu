@@ -31,6 +31,7 @@
 #include "handles.h"
 #include "rs256_device.cuh"
 #include "rsi16_device.cuh"
+#include "rsi16_bt.cuh"
 
 namespace ffgpu {
 
@@ -58,7 +59,8 @@ struct BatchCode {
 struct BatchItem {
     uint8_t kind;
     uint8_t lane_bm;  // RSi16 repair by 32-block batches with a Berlekamp-Massey per lane
-    uint8_t pad[2];
+    uint8_t bt;       // RSi16 ecc 32 / 64 on 16-byte aligned blocks: one block per thread
+    uint8_t pad;
     uint32_t code;
     uint32_t nblocks;
     int32_t msg_len;
@@ -159,6 +161,38 @@ __device__ void rsi16_encode_item_sub(const Rsi16Dev &c, const BatchItem &it) {
     for (size_t b0 = 0; b0 < it.nblocks; b0 += 32 / N) rsi16_encode_sub_pass<N>(c, v, b0, it.nblocks, tw, lane);
 }
 
+// A whole RSi16 ecc-N item on the calling warp with one block per lane
+// (rsi16_bt.cuh), 32 blocks at a time.  The code's twiddles are copied to the
+// end of the warp's workspace; the tile's columns and staging buffers start
+// at its beginning, and so does the step-for-step mirror, which runs after
+// the tile's columns are dead.
+template <int N>
+__device__ void rsi16_bt_item(const Rsi16Dev &c, const BatchItem &it, uint32_t *ws, uint32_t ws_words,
+                              bool decode) {
+    constexpr int TW = (int)(sizeof(BtTw<N>) / 4);
+    const int lane = threadIdx.x & 31;
+    uint32_t *twp = ws + ws_words - TW;
+    for (int i = lane; i < TW; i += 32) twp[i] = c.bt_tw[i];
+    __syncwarp();
+    const BtTw<N> &tw = *reinterpret_cast<const BtTw<N> *>(twp);
+    uint16_t *msg = static_cast<uint16_t *>(it.msg), *par = static_cast<uint16_t *>(it.par);
+    const size_t nb = it.nblocks;
+    const BlockView v = contiguous_view(it.msg, true, c.message_len, it.par, true, c.ecc);
+    unsigned long long nf = 0;
+    for (size_t blk0 = 0; blk0 < nb; blk0 += 32) {
+        if (decode) {
+            for (uint32_t m = bt_repair_tile<N>(c, tw, msg, par, blk0, nb, it.status, nullptr, ws, lane, nf); m;
+                 m &= m - 1) {
+                __syncwarp();
+                rsi16_repair_block(c, v, blk0 + (__ffs(m) - 1), ws, it.status, lane);
+            }
+        } else {
+            bt_encode_tile<N>(c, tw, reinterpret_cast<uint8_t *>(ws), msg, par, blk0, nb, lane);
+        }
+    }
+    __syncwarp();  // the twiddles are read before the next item overwrites them
+}
+
 __device__ void rsi16_item(const Rsi16Dev &c, const BatchItem &it, uint32_t *ws, bool decode) {
     switch (c.ecc) {
         case 32: rsi16_item_t<1>(c, it, ws, decode); return;
@@ -201,8 +235,9 @@ __global__ void __launch_bounds__(256) seg_copy_kernel(const CopySeg *segs) {
 // Item classes, one persistent launch each with its own registers, shared
 // memory and CTAs per SM: RS256 items by the width W of their LFSR remainder
 // (W <= 4: ecc <= 16; W <= 16: ecc <= 64; wider), then the RSi16 items.
-constexpr int kClasses = 4;
+constexpr int kClasses = 5;
 constexpr int kClsRsi16 = 3;
+constexpr int kClsRsi16Bt = 4;  // RSi16 ecc 32 / 64 items, one block per thread (its own register budget)
 
 __host__ __device__ constexpr int rs256_class(int W) { return W <= 4 ? 0 : (W <= 16 ? 1 : 2); }
 
@@ -228,7 +263,7 @@ __host__ __device__ constexpr int rs256_class(int W) { return W <= 4 ? 0 : (W <=
 template <int CLS>
 __global__ void __launch_bounds__(kBatchThreads) batch_kernel(BatchArgs a) {
     extern __shared__ __align__(16) uint32_t sm[];
-    if constexpr (CLS == kClsRsi16) {
+    if constexpr (CLS == kClsRsi16 || CLS == kClsRsi16Bt) {
         // RSi16 items are warp-sized: every warp pulls whole items
         const int lane = threadIdx.x & 31;
         uint32_t *wws = sm + (size_t)(threadIdx.x >> 5) * a.ws_words;
@@ -238,7 +273,15 @@ __global__ void __launch_bounds__(kBatchThreads) batch_kernel(BatchArgs a) {
             idx = __shfl_sync(0xffffffffu, idx, 0);
             if (idx >= a.nitems) break;
             const BatchItem it = a.items[idx];
-            rsi16_item(a.codes[it.code].rsi, it, wws, it.kind == BK_RSI16_DEC);
+            const Rsi16Dev &c = a.codes[it.code].rsi;
+            if constexpr (CLS == kClsRsi16Bt) {
+                if (c.ecc == 64)
+                    rsi16_bt_item<64>(c, it, wws, a.ws_words, it.kind == BK_RSI16_DEC);
+                else
+                    rsi16_bt_item<32>(c, it, wws, a.ws_words, it.kind == BK_RSI16_DEC);
+            } else {
+                rsi16_item(c, it, wws, it.kind == BK_RSI16_DEC);
+            }
         }
         return;
     }
@@ -518,7 +561,8 @@ void build_plan(ffgpu_batch &B, int tile_rs, int tile_rsi, int ctas_rs, int ctas
         K.ws_words = 0;
     }
     auto &K1 = B.cls[kClsRsi16];
-    uint32_t ws_words = 0;
+    auto &K2 = B.cls[kClsRsi16Bt];
+    uint32_t ws_words = 0, ws_words_bt = 0;
     bool any_rs_dec = false;
     for (const auto &r : B.reqs) {
         BatchCode bc{};
@@ -556,22 +600,38 @@ void build_plan(ffgpu_batch &B, int tile_rs, int tile_rsi, int ctas_rs, int ctas
             // repair items of 8 blocks or more run a Berlekamp-Massey per lane
             // (one lane per block); the tile trades lanes busy per warp
             // against warps busy per batch
-            const size_t tile = (size_t)tile_rsi;
-            const bool lane_bm = r.kind == BK_RSI16_DEC && (c.ecc == 32 || c.ecc == 64) && tile >= 8;
+            // ecc 32 / 64 on 16-byte aligned buffers: one block per thread,
+            // 64 blocks per item (rows stay aligned: message_len is a
+            // multiple of ecc)
+            const bool bt = (c.ecc == 32 || c.ecc == 64) && c.pntt_blocks >= 2 && c.dev.bt_tw &&
+                            ((uintptr_t)r.a & 15) == 0 && ((uintptr_t)r.b & 15) == 0;
+            const size_t tile = bt ? 64 : (size_t)tile_rsi;
+            const bool lane_bm = !bt && r.kind == BK_RSI16_DEC && (c.ecc == 32 || c.ecc == 64) && tile >= 8;
             for (size_t b0 = 0; b0 < r.nblocks; b0 += tile) {
                 BatchItem it{};
                 it.kind = r.kind;
                 it.code = ci;
                 it.nblocks = (uint32_t)std::min<size_t>(tile, r.nblocks - b0);
                 it.lane_bm = lane_bm && it.nblocks >= 8;
+                it.bt = bt;
                 it.msg = static_cast<uint16_t *>(r.a) + b0 * c.message_len;
                 it.par = static_cast<uint16_t *>(r.b) + b0 * c.ecc;
                 it.status = r.status ? r.status + b0 : nullptr;
-                K1.items.push_back(it);
+                (bt ? K2 : K1).items.push_back(it);
             }
-            ws_words = std::max(ws_words, r.kind == BK_RSI16_DEC ? c.dev.temp_len + 1 : (uint32_t)c.block_len);
+            if (!bt)
+                ws_words = std::max(ws_words, r.kind == BK_RSI16_DEC ? c.dev.temp_len + 1 : (uint32_t)c.block_len);
             if (lane_bm)  // the batch's columns (the mirror overlays them)
                 ws_words = std::max(ws_words, (uint32_t)((c.ecc + c.ecc / 2 + 1) * kColStride + 3 * c.ecc + 4));
+            if (bt) {
+                // the tile's columns and staging (or the mirror) at the start,
+                // the twiddles at the end
+                const uint32_t tw = c.ecc == 64 ? (uint32_t)(sizeof(BtTw<64>) / 4) : (uint32_t)(sizeof(BtTw<32>) / 4);
+                const uint32_t tile_words = c.ecc == 64 ? (uint32_t)BtRepairSmem<64>::kWords
+                                                        : (uint32_t)BtRepairSmem<32>::kWords;
+                const uint32_t lead = std::max(tile_words, r.kind == BK_RSI16_DEC ? c.dev.temp_len + 1 : 0u);
+                ws_words_bt = std::max(ws_words_bt, ((lead + 3) & ~3u) + tw);
+            }
         }
     }
     plan_circ(B);
@@ -586,17 +646,20 @@ void build_plan(ffgpu_batch &B, int tile_rs, int tile_rsi, int ctas_rs, int ctas
     }
     K1.ws_words = (ws_words + 3) & ~3u;
     K1.smem = (size_t)kBatchWarps * K1.ws_words * 4;
+    K2.ws_words = (ws_words_bt + 3) & ~3u;
+    K2.smem = (size_t)kBatchWarps * K2.ws_words * 4;
     size_class<0>(B.cls[0], ctas_rs);
     size_class<1>(B.cls[1], ctas_rs);
     size_class<2>(B.cls[2], ctas_rs);
     size_class<kClsRsi16>(K1, ctas_rsi);
+    size_class<kClsRsi16Bt>(K2, 0);
     B.tile_rs = tile_rs;
     B.tile_rsi = tile_rsi;
     B.ctas_rs = ctas_rs;
     B.ctas_rsi = ctas_rsi;
 
     B.d_codes.get(std::max<size_t>(1, B.codes.size()) * sizeof(BatchCode));
-    B.d_counter.get(256);
+    B.d_counter.get(kClasses * 32 * 4);
     // global decode scratch: one slice per CTA of the widest RS256 class
     // (the narrower ones keep theirs in shared memory)
     if (any_rs_dec) B.d_rs_scratch.get((size_t)B.cls[2].grid * kBatchThreads * kDecodeScratchBytes);
@@ -631,9 +694,9 @@ void launch_class(ffgpu_batch &B, cudaStream_t st, bool timed) {
     check_launch("batch_kernel");
 }
 
-// which: bit k the items of class k, bit 4 the CIRC16 chain (the autotuner
-// times the RS256 classes and the RSi16 class apart)
-constexpr int kRunRs256 = 7, kRunRsi16 = 8, kRunCirc = 16, kRunAll = 31;
+// which: bit k the items of class k, bit 5 the CIRC16 chain (the autotuner
+// times the RS256 classes and the RSi16 classes apart)
+constexpr int kRunRs256 = 7, kRunRsi16 = 8 | 16, kRunCirc = 32, kRunAll = 63;
 // The class launches run side by side (class k > 0 on side stream k, forked
 // from and joined back into st), so that one class's tail overlaps the
 // others' work.
@@ -683,7 +746,8 @@ void launch_classes(ffgpu_batch &B, cudaStream_t st, bool timed, int which) {
             case 0: launch_class<0>(B, s, timed); break;
             case 1: launch_class<1>(B, s, timed); break;
             case 2: launch_class<2>(B, s, timed); break;
-            default: launch_class<kClsRsi16>(B, s, timed); break;
+            case kClsRsi16: launch_class<kClsRsi16>(B, s, timed); break;
+            default: launch_class<kClsRsi16Bt>(B, s, timed); break;
         }
         if (i > 0) FFGPU_CHECK_CUDA(cudaEventRecord(B.ev_join[i], s));
     }

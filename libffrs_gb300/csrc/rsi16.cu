@@ -35,6 +35,25 @@ uint32_t Rsi16Code::rbo(uint32_t i) const {
 
 static uint32_t neg(uint32_t a) { return a == 0 ? 0 : 0x10001u - a; }
 
+// the twiddles of the one-block-per-thread kernels (rsi16_bt.cuh), with their
+// Shoup companions
+template <int N>
+static BtTw<N> bt_twiddles(const Rsi16Code &c) {
+    BtTw<N> tw;
+    for (int i = 0; i < N / 2; ++i) {
+        tw.ct[i] = c.roots_ecc[i];
+        tw.gs[i] = c.roots_i_ecc[i];
+    }
+    for (int i = 0; i < N; ++i) tw.mix[i] = c.ecc_mix[i];
+    auto shoup = [](uint32_t w) { return (uint32_t)(((uint64_t)w << 32) / 0x10001u); };
+    for (int i = 0; i < N / 2; ++i) {
+        tw.ct_s[i] = shoup(tw.ct[i]);
+        tw.gs_s[i] = shoup(tw.gs[i]);
+    }
+    for (int i = 0; i < N; ++i) tw.mix_s[i] = shoup(tw.mix[i]);
+    return tw;
+}
+
 Rsi16Code::Rsi16Code(size_t block_len_, size_t ecc_len, uint32_t primitive_)
     : primitive(primitive_), block_len(block_len_), ecc(ecc_len) {
     if (ecc_len < 2 || (ecc_len & (ecc_len - 1)))
@@ -135,6 +154,19 @@ Rsi16Code::Rsi16Code(size_t block_len_, size_t ecc_len, uint32_t primitive_)
     const size_t o_rn = put(roots_ntt), o_re = put(roots_ecc), o_rie = put(roots_i_ecc), o_re2 = put(roots_ecc2),
                  o_rie2 = put(roots_i_ecc2), o_ps = put(pntt_shift), o_pis = put(pintt_shift), o_rbo = put(rbo_ecc),
                  o_mix = put(ecc_mix), o_inv = put(inv_tab), o_pss = put(pntt_shift_s), o_piss = put(pintt_shift_s);
+    // the block-per-thread twiddles of ecc 32 / 64, for launches that cannot
+    // take them as a kernel parameter (the mixed batch)
+    std::vector<uint32_t> btw;
+    if (ecc == 64 || ecc == 32) {
+        if (ecc == 64) {
+            const BtTw<64> tw = bt_twiddles<64>(*this);
+            btw.assign((const uint32_t *)&tw, (const uint32_t *)&tw + sizeof tw / 4);
+        } else {
+            const BtTw<32> tw = bt_twiddles<32>(*this);
+            btw.assign((const uint32_t *)&tw, (const uint32_t *)&tw + sizeof tw / 4);
+        }
+    }
+    const size_t o_btw = btw.empty() ? 0 : put(btw);
     FFGPU_CHECK_CUDA(cudaMalloc(&d_tables, all.size() * 4));
     FFGPU_CHECK_CUDA(cudaMemcpy(d_tables, all.data(), all.size() * 4, cudaMemcpyHostToDevice));
     dev.roots_ntt = d_tables + o_rn;
@@ -148,6 +180,7 @@ Rsi16Code::Rsi16Code(size_t block_len_, size_t ecc_len, uint32_t primitive_)
     dev.ecc_mix = d_tables + o_mix;
     dev.inv_tab = d_tables + o_inv;
     dev.pntt_shift_s = d_tables + o_pss;
+    dev.bt_tw = btw.empty() ? nullptr : d_tables + o_btw;
     dev.pintt_shift_s = d_tables + o_piss;
     dev.block_len = (uint32_t)block_len;
     dev.message_len = (uint32_t)message_len;
@@ -209,26 +242,8 @@ __global__ void __launch_bounds__(128, N == 64 ? 3 : 4) rsi16_encode_bt_kernel(R
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpc = blockDim.x >> 5;
     uint8_t *bufs = bt_smem + wib * bt_warp_smem<N>();
     const size_t ntiles = (nblocks + 31) / 32;
-    for (size_t t = (size_t)blockIdx.x * wpc + wib; t < ntiles; t += (size_t)gridDim.x * wpc) {
-        const size_t blk0 = t * 32;
-        uint32_t acc[N];
-        // NTT::pntt_message (libffrs/ntt.hpp:160-180): the message chunks only
-        bt_pntt<N>(c, tw, bufs, msg, c.message_len, nullptr, blk0, nblocks, c.pntt_blocks - 1, lane, acc);
-#pragma unroll
-        for (int k = 0; k < N; ++k) acc[k] = smul(acc[k], tw.mix[k], tw.mix_s[k]);
-        bt_gs_u<N>(acc, tw);
-        const size_t b = blk0 + lane;
-        if (b < nblocks) {
-            uint4 *o = reinterpret_cast<uint4 *>(par + b * N);
-#pragma unroll
-            for (int q = 0; q < N / 8; ++q) {
-                uint32_t w[4];
-#pragma unroll
-                for (int i = 0; i < 4; ++i) w[i] = ucanon(acc[8 * q + 2 * i]) & 0xffffu | ucanon(acc[8 * q + 2 * i + 1]) << 16;
-                o[q] = make_uint4(w[0], w[1], w[2], w[3]);
-            }
-        }
-    }
+    for (size_t t = (size_t)blockIdx.x * wpc + wib; t < ntiles; t += (size_t)gridDim.x * wpc)
+        bt_encode_tile<N>(c, tw, bufs, msg, par, t * 32, nblocks, lane);
 }
 
 // syndromes of block b go to synds[(b / out_group) * out_gstride + (b % out_group) * ecc]
@@ -566,22 +581,6 @@ static bool bt_view(const Rsi16Code &c, const BlockView &v) {
            ((uintptr_t)v.msg & 15) == 0 && ((uintptr_t)v.par & 15) == 0 && ((uintptr_t)c.dev.pntt_shift & 15) == 0;
 }
 
-template <int N>
-static BtTw<N> bt_twiddles(const Rsi16Code &c) {
-    BtTw<N> tw;
-    for (int i = 0; i < N / 2; ++i) {
-        tw.ct[i] = c.roots_ecc[i];
-        tw.gs[i] = c.roots_i_ecc[i];
-    }
-    for (int i = 0; i < N; ++i) tw.mix[i] = c.ecc_mix[i];
-    auto shoup = [](uint32_t w) { return (uint32_t)(((uint64_t)w << 32) / 0x10001u); };
-    for (int i = 0; i < N / 2; ++i) {
-        tw.ct_s[i] = shoup(tw.ct[i]);
-        tw.gs_s[i] = shoup(tw.gs[i]);
-    }
-    for (int i = 0; i < N; ++i) tw.mix_s[i] = shoup(tw.mix[i]);
-    return tw;
-}
 
 template <int N>
 static void launch_encode_bt(const Rsi16Code &c, const BlockView &v, size_t nblocks, cudaStream_t st) {

@@ -18,6 +18,8 @@ struct Rsi16Dev {
     // floor(w 2^32 / p) of every pntt_shift / pintt_shift entry w (the
     // Shoup companions used by the one-block-per-thread kernels)
     const uint32_t *pntt_shift_s, *pintt_shift_s;
+    // ecc 32 / 64: the BtTw of the block-per-thread kernels, else NULL
+    const uint32_t *bt_tw;
     const uint32_t *inv_tab;  // inverse of every field element (inv(0) == 1, as the reference's table)
     uint32_t block_len, message_len, ecc, ntt_len, pntt_blocks, ecc_mask, rbo_shift;
     uint32_t ecc_len_i, ecc2_len_i;

@@ -520,6 +520,31 @@ static __device__ __forceinline__ uint32_t bt_repair_tile(const Rsi16Dev &c, con
     return __ballot_sync(0xffffffffu, path == 2);
 }
 
+// Parity of the warp's tile [blk0, blk0 + 32), one block per lane:
+// NTT::pntt_message (libffrs/ntt.hpp:160-180) over the message chunks,
+// RSi16v::_mix_ecc and the GS transform; msg / par are contiguous blocks.
+template <int N>
+static __device__ __forceinline__ void bt_encode_tile(const Rsi16Dev &c, const BtTw<N> &tw, uint8_t *bufs,
+                                                      const uint16_t *msg, uint16_t *par, size_t blk0,
+                                                      size_t nblocks, int lane) {
+    uint32_t acc[N];
+    bt_pntt<N>(c, tw, bufs, msg, c.message_len, nullptr, blk0, nblocks, c.pntt_blocks - 1, lane, acc);
+#pragma unroll
+    for (int k = 0; k < N; ++k) acc[k] = smul(acc[k], tw.mix[k], tw.mix_s[k]);
+    bt_gs_u<N>(acc, tw);
+    const size_t b = blk0 + lane;
+    if (b < nblocks) {
+        uint4 *o = reinterpret_cast<uint4 *>(par + b * N);
+#pragma unroll
+        for (int q = 0; q < N / 8; ++q) {
+            uint32_t w[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) w[i] = ucanon(acc[8 * q + 2 * i]) & 0xffffu | ucanon(acc[8 * q + 2 * i + 1]) << 16;
+            o[q] = make_uint4(w[0], w[1], w[2], w[3]);
+        }
+    }
+}
+
 // Shared memory of one warp of the bt kernels: two chunk buffers.
 template <int N>
 constexpr int bt_warp_smem() {
