@@ -165,32 +165,44 @@ __device__ void rsi16_encode_item_sub(const Rsi16Dev &c, const BatchItem &it) {
 // (rsi16_bt.cuh), 32 blocks at a time.  The code's twiddles are copied to the
 // end of the warp's workspace; the tile's columns and staging buffers start
 // at its beginning, and so does the step-for-step mirror, which runs after
-// the tile's columns are dead.
+// the tile's columns are dead.  Encode and repair are separate functions, not
+// inlined, so that each gets the registers of its own path.
 template <int N>
-__device__ void rsi16_bt_item(const Rsi16Dev &c, const BatchItem &it, uint32_t *ws, uint32_t ws_words,
-                              bool decode) {
+__device__ __forceinline__ BtTwShared<N> bt_item_twiddles(const Rsi16Dev &c, uint32_t *ws, uint32_t ws_words) {
     constexpr int TW = (int)(sizeof(BtTw<N>) / 4);
-    const int lane = threadIdx.x & 31;
     uint32_t *twp = ws + ws_words - TW;
-    for (int i = lane; i < TW; i += 32) twp[i] = c.bt_tw[i];
+    for (int i = threadIdx.x & 31; i < TW; i += 32) twp[i] = c.bt_tw[i];
     __syncwarp();
-    const BtTw<N> &tw = *reinterpret_cast<const BtTw<N> *>(twp);
+    return BtTwShared<N>{(uint32_t)__cvta_generic_to_shared(twp)};
+}
+
+template <int N>
+__device__ __noinline__ void rsi16_bt_enc_item(const Rsi16Dev &c, const BatchItem &it, uint32_t *ws,
+                                               uint32_t ws_words) {
+    const int lane = threadIdx.x & 31;
+    const BtTwShared<N> tw = bt_item_twiddles<N>(c, ws, ws_words);
+    for (size_t blk0 = 0; blk0 < it.nblocks; blk0 += 32)
+        bt_encode_tile<N>(c, tw, reinterpret_cast<uint8_t *>(ws), static_cast<const uint16_t *>(it.msg),
+                          static_cast<uint16_t *>(it.par), blk0, it.nblocks, lane);
+    __syncwarp();  // the twiddles are read before the next item overwrites them
+}
+
+template <int N>
+__device__ __noinline__ void rsi16_bt_dec_item(const Rsi16Dev &c, const BatchItem &it, uint32_t *ws,
+                                               uint32_t ws_words) {
+    const int lane = threadIdx.x & 31;
+    const BtTwShared<N> tw = bt_item_twiddles<N>(c, ws, ws_words);
     uint16_t *msg = static_cast<uint16_t *>(it.msg), *par = static_cast<uint16_t *>(it.par);
-    const size_t nb = it.nblocks;
-    const BlockView v = contiguous_view(it.msg, true, c.message_len, it.par, true, c.ecc);
     unsigned long long nf = 0;
-    for (size_t blk0 = 0; blk0 < nb; blk0 += 32) {
-        if (decode) {
-            for (uint32_t m = bt_repair_tile<N>(c, tw, msg, par, blk0, nb, it.status, nullptr, ws, lane, nf); m;
-                 m &= m - 1) {
-                __syncwarp();
-                rsi16_repair_block(c, v, blk0 + (__ffs(m) - 1), ws, it.status, lane);
-            }
-        } else {
-            bt_encode_tile<N>(c, tw, reinterpret_cast<uint8_t *>(ws), msg, par, blk0, nb, lane);
+    for (size_t blk0 = 0; blk0 < it.nblocks; blk0 += 32) {
+        for (uint32_t m = bt_repair_tile<N>(c, tw, msg, par, blk0, it.nblocks, it.status, nullptr, ws, lane, nf); m;
+             m &= m - 1) {
+            __syncwarp();
+            rsi16_repair_block(c, contiguous_view(it.msg, true, c.message_len, it.par, true, c.ecc),
+                               blk0 + (__ffs(m) - 1), ws, it.status, lane);
         }
     }
-    __syncwarp();  // the twiddles are read before the next item overwrites them
+    __syncwarp();
 }
 
 __device__ void rsi16_item(const Rsi16Dev &c, const BatchItem &it, uint32_t *ws, bool decode) {
@@ -275,10 +287,15 @@ __global__ void __launch_bounds__(kBatchThreads) batch_kernel(BatchArgs a) {
             const BatchItem it = a.items[idx];
             const Rsi16Dev &c = a.codes[it.code].rsi;
             if constexpr (CLS == kClsRsi16Bt) {
-                if (c.ecc == 64)
-                    rsi16_bt_item<64>(c, it, wws, a.ws_words, it.kind == BK_RSI16_DEC);
+                const bool dec = it.kind == BK_RSI16_DEC;
+                if (c.ecc == 64 && dec)
+                    rsi16_bt_dec_item<64>(c, it, wws, a.ws_words);
+                else if (c.ecc == 64)
+                    rsi16_bt_enc_item<64>(c, it, wws, a.ws_words);
+                else if (dec)
+                    rsi16_bt_dec_item<32>(c, it, wws, a.ws_words);
                 else
-                    rsi16_bt_item<32>(c, it, wws, a.ws_words, it.kind == BK_RSI16_DEC);
+                    rsi16_bt_enc_item<32>(c, it, wws, a.ws_words);
             } else {
                 rsi16_item(c, it, wws, it.kind == BK_RSI16_DEC);
             }

@@ -75,6 +75,33 @@ struct BtTw {
     uint32_t gs[N / 2];
     uint32_t mix[N];
     uint32_t ct_s[N / 2], gs_s[N / 2], mix_s[N];  // the Shoup companions floor(w 2^32 / p)
+    // the accessors the transforms use (a twiddle source; BtTwShared is the other)
+    __device__ __forceinline__ uint32_t get_ct(int i) const { return ct[i]; }
+    __device__ __forceinline__ uint32_t get_cts(int i) const { return ct_s[i]; }
+    __device__ __forceinline__ uint32_t get_gs(int i) const { return gs[i]; }
+    __device__ __forceinline__ uint32_t get_gss(int i) const { return gs_s[i]; }
+    __device__ __forceinline__ uint32_t get_mix(int i) const { return mix[i]; }
+    __device__ __forceinline__ uint32_t get_mixs(int i) const { return mix_s[i]; }
+};
+
+// A BtTw in shared memory, read at every use.  The kernels that take the
+// twiddles as a parameter read them as constant-bank operands; from shared
+// memory the compiler would hoist all 4N of them into registers ahead of the
+// transforms and spill, so each read here is a volatile load.
+template <int N>
+struct BtTwShared {
+    uint32_t base;  // shared-window address of the BtTw<N>
+    __device__ __forceinline__ uint32_t ld(int w) const {
+        uint32_t v;
+        asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(base + 4u * (uint32_t)w));
+        return v;
+    }
+    __device__ __forceinline__ uint32_t get_ct(int i) const { return ld(i); }
+    __device__ __forceinline__ uint32_t get_gs(int i) const { return ld(N / 2 + i); }
+    __device__ __forceinline__ uint32_t get_mix(int i) const { return ld(N + i); }
+    __device__ __forceinline__ uint32_t get_cts(int i) const { return ld(2 * N + i); }
+    __device__ __forceinline__ uint32_t get_gss(int i) const { return ld(2 * N + N / 2 + i); }
+    __device__ __forceinline__ uint32_t get_mixs(int i) const { return ld(3 * N + i); }
 };
 
 template <int N>
@@ -88,8 +115,8 @@ constexpr int bt_log() {
 // stage's outputs are below B + K, K = the least multiple of p at least
 // max(B, 2p): a + m < B + 2p, a - m + K < B + K (m < 2p after a product, m < B
 // without).  From B = 2^16 the six stages of 64 points end below 6.3 * 10^6.
-template <int N>
-static __device__ __forceinline__ void bt_ct_u(uint32_t (&x)[N], const BtTw<N> &tw) {
+template <int N, class TW>
+static __device__ __forceinline__ void bt_ct_u(uint32_t (&x)[N], const TW &tw) {
     uint32_t B = 0x10000u;
 #pragma unroll
     for (int st = 0; st < bt_log<N>(); ++st) {
@@ -100,7 +127,7 @@ static __device__ __forceinline__ void bt_ct_u(uint32_t (&x)[N], const BtTw<N> &
             if (j & stride) continue;
             const int i = j & (stride - 1);
             const uint32_t a = x[j];
-            const uint32_t m = i ? smul(x[j + stride], tw.ct[ef * i], tw.ct_s[ef * i]) : x[j + stride];
+            const uint32_t m = i ? smul(x[j + stride], tw.get_ct(ef * i), tw.get_cts(ef * i)) : x[j + stride];
             x[j] = a + m;
             x[j + stride] = a - m + K;
         }
@@ -113,8 +140,8 @@ static __device__ __forceinline__ void bt_ct_u(uint32_t (&x)[N], const BtTw<N> &
 // outputs are below B + K, K = the least multiple of p at least B: a + b < 2B,
 // a - b + K < B + K, a product < 2p.  From B = 2p the six stages of 64 points
 // end below 2^6 * 2p < 2^24.
-template <int N>
-static __device__ __forceinline__ void bt_gs_u(uint32_t (&x)[N], const BtTw<N> &tw) {
+template <int N, class TW>
+static __device__ __forceinline__ void bt_gs_u(uint32_t (&x)[N], const TW &tw) {
     uint32_t B = 0x20002u;
 #pragma unroll
     for (int st = 0; st < bt_log<N>(); ++st) {
@@ -127,7 +154,7 @@ static __device__ __forceinline__ void bt_gs_u(uint32_t (&x)[N], const BtTw<N> &
             const uint32_t a = x[j], b = x[j + stride];
             x[j] = a + b;
             const uint32_t d = a - b + K;
-            x[j + stride] = i ? smul(d, tw.gs[i << ef], tw.gs_s[i << ef]) : d;
+            x[j + stride] = i ? smul(d, tw.get_gs(i << ef), tw.get_gss(i << ef)) : d;
         }
         B += K;
     }
@@ -203,8 +230,8 @@ static __device__ __forceinline__ void bt_read_row(const uint8_t *buf, int lane,
 // `words` / `row_stride` give chunk ch of block b at
 // words + b * row_stride + ch * N; when `par` is given, chunk nch - 1 is read
 // from par + b * N instead (the parity chunk of a codeword).
-template <int N>
-static __device__ __forceinline__ void bt_pntt(const Rsi16Dev &c, const BtTw<N> &tw, uint8_t *bufs,
+template <int N, class TW>
+static __device__ __forceinline__ void bt_pntt(const Rsi16Dev &c, const TW &tw, uint8_t *bufs,
                                                const uint16_t *words, size_t row_stride, const uint16_t *par,
                                                size_t blk0, size_t nblocks, uint32_t nch, int lane,
                                                uint32_t (&acc)[N]) {
@@ -365,8 +392,8 @@ static __device__ __forceinline__ uint16_t *bt_word(uint16_t *msg, uint16_t *par
 // The repair of the warp's tile [blk0, blk0 + 32), lane = block.  Returns the
 // lanes whose block goes to the mirror; adds the accepted blocks (and the
 // clean ones) to nfast.
-template <int N>
-static __device__ __forceinline__ uint32_t bt_repair_tile(const Rsi16Dev &c, const BtTw<N> &tw, uint16_t *msg,
+template <int N, class TW>
+static __device__ __forceinline__ uint32_t bt_repair_tile(const Rsi16Dev &c, const TW &tw, uint16_t *msg,
                                                           uint16_t *par, size_t blk0, size_t nblocks,
                                                           uint8_t *status, const uint8_t *active, uint32_t *ws,
                                                           int lane, unsigned long long &nfast) {
@@ -523,14 +550,14 @@ static __device__ __forceinline__ uint32_t bt_repair_tile(const Rsi16Dev &c, con
 // Parity of the warp's tile [blk0, blk0 + 32), one block per lane:
 // NTT::pntt_message (libffrs/ntt.hpp:160-180) over the message chunks,
 // RSi16v::_mix_ecc and the GS transform; msg / par are contiguous blocks.
-template <int N>
-static __device__ __forceinline__ void bt_encode_tile(const Rsi16Dev &c, const BtTw<N> &tw, uint8_t *bufs,
+template <int N, class TW>
+static __device__ __forceinline__ void bt_encode_tile(const Rsi16Dev &c, const TW &tw, uint8_t *bufs,
                                                       const uint16_t *msg, uint16_t *par, size_t blk0,
                                                       size_t nblocks, int lane) {
     uint32_t acc[N];
     bt_pntt<N>(c, tw, bufs, msg, c.message_len, nullptr, blk0, nblocks, c.pntt_blocks - 1, lane, acc);
 #pragma unroll
-    for (int k = 0; k < N; ++k) acc[k] = smul(acc[k], tw.mix[k], tw.mix_s[k]);
+    for (int k = 0; k < N; ++k) acc[k] = smul(acc[k], tw.get_mix(k), tw.get_mixs(k));
     bt_gs_u<N>(acc, tw);
     const size_t b = blk0 + lane;
     if (b < nblocks) {
