@@ -224,6 +224,41 @@ static __device__ __forceinline__ void bt_read_row(const uint8_t *buf, int lane,
     }
 }
 
+// One chunk of NTT::pntt (libffrs/ntt.hpp:133-152) on one thread: x (chunk
+// ch of a block, words below 2^16) is transformed and added to acc times
+// pntt_shift of the chunk; chunk 0 initialises acc.
+template <int N, class TW>
+static __device__ __forceinline__ void bt_pntt_chunk(const Rsi16Dev &c, const TW &tw, uint32_t (&x)[N], uint32_t ch,
+                                                     uint32_t (&acc)[N]) {
+    bt_ct_u<N>(x, tw);
+    if (ch == 0) {
+        // pntt_shift of chunk 0 is root^(j * rbo(0)) = 1
+#pragma unroll
+        for (int k = 0; k < N; ++k) acc[k] = x[k];
+    } else {
+        const uint4 *sh = reinterpret_cast<const uint4 *>(c.pntt_shift + (size_t)ch * N);
+        const uint4 *shs = reinterpret_cast<const uint4 *>(c.pntt_shift_s + (size_t)ch * N);
+#pragma unroll
+        for (int q = 0; q < N / 4; ++q) {
+            const uint4 s = __ldg(sh + q), ss = __ldg(shs + q);
+            acc[4 * q] += smul(x[4 * q], s.x, ss.x);
+            acc[4 * q + 1] += smul(x[4 * q + 1], s.y, ss.y);
+            acc[4 * q + 2] += smul(x[4 * q + 2], s.z, ss.z);
+            acc[4 * q + 3] += smul(x[4 * q + 3], s.w, ss.w);
+        }
+    }
+}
+
+// the parity of a block from its pntt_message accumulator: RSi16v::_mix_ecc
+// (libffrs/rsi16v_impl.hpp:100-119), then gs_butterfly; acc ends lazily
+// reduced (below 2^24), in storage order
+template <int N, class TW>
+static __device__ __forceinline__ void bt_parity(const TW &tw, uint32_t (&acc)[N]) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) acc[k] = smul(acc[k], tw.get_mix(k), tw.get_mixs(k));
+    bt_gs_u<N>(acc, tw);
+}
+
 // NTT::pntt (libffrs/ntt.hpp:133-152) of the warp's 32 blocks over chunks
 // [0, nch), one block per lane: acc = sum_ch ct(chunk_ch) * pntt_shift_ch,
 // lazily reduced: below 6.3 * 10^6 + (nch - 1) 2p < 2^28 for nch <= 1024.
@@ -255,23 +290,7 @@ static __device__ __forceinline__ void bt_pntt(const Rsi16Dev &c, const TW &tw, 
         uint32_t x[N];
         bt_read_row<N>(bufs + (ch & 1) * T::kBufBytes, lane, x);
         __syncwarp();  // every lane has read the buffer before the next issue refills it
-        bt_ct_u<N>(x, tw);
-        if (ch == 0) {
-            // pntt_shift of chunk 0 is root^(j * rbo(0)) = 1
-#pragma unroll
-            for (int k = 0; k < N; ++k) acc[k] = x[k];
-        } else {
-            const uint4 *sh = reinterpret_cast<const uint4 *>(c.pntt_shift + (size_t)ch * N);
-            const uint4 *shs = reinterpret_cast<const uint4 *>(c.pntt_shift_s + (size_t)ch * N);
-#pragma unroll
-            for (int q = 0; q < N / 4; ++q) {
-                const uint4 s = __ldg(sh + q), ss = __ldg(shs + q);
-                acc[4 * q] += smul(x[4 * q], s.x, ss.x);
-                acc[4 * q + 1] += smul(x[4 * q + 1], s.y, ss.y);
-                acc[4 * q + 2] += smul(x[4 * q + 2], s.z, ss.z);
-                acc[4 * q + 3] += smul(x[4 * q + 3], s.w, ss.w);
-            }
-        }
+        bt_pntt_chunk<N>(c, tw, x, ch, acc);
     }
 }
 
@@ -556,9 +575,7 @@ static __device__ __forceinline__ void bt_encode_tile(const Rsi16Dev &c, const T
                                                       size_t nblocks, int lane) {
     uint32_t acc[N];
     bt_pntt<N>(c, tw, bufs, msg, c.message_len, nullptr, blk0, nblocks, c.pntt_blocks - 1, lane, acc);
-#pragma unroll
-    for (int k = 0; k < N; ++k) acc[k] = smul(acc[k], tw.get_mix(k), tw.get_mixs(k));
-    bt_gs_u<N>(acc, tw);
+    bt_parity<N>(tw, acc);
     const size_t b = blk0 + lane;
     if (b < nblocks) {
         uint4 *o = reinterpret_cast<uint4 *>(par + b * N);

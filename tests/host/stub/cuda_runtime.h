@@ -29,3 +29,15 @@ struct HostDim3 {
     unsigned x = 0, y = 0, z = 0;
 };
 static HostDim3 threadIdx, blockDim;
+static inline uint4 make_uint4(unsigned x, unsigned y, unsigned z, unsigned w) { return uint4{x, y, z, w}; }
+static inline unsigned __umulhi(unsigned a, unsigned b) { return (unsigned)(((unsigned long long)a * b) >> 32); }
+static inline unsigned __brev(unsigned x) {
+    unsigned r = 0;
+    for (int i = 0; i < 32; ++i) r |= ((x >> i) & 1u) << (31 - i);
+    return r;
+}
+template <typename T>
+static inline T __ldg(const T *p) {
+    return *p;
+}
+static inline size_t __cvta_generic_to_shared(const void *p) { return (size_t)p; }

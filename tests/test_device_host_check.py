@@ -9,7 +9,10 @@ the oracle: CPU parity checks of the GPU code itself.
   the RSi16 repair paths (lane-per-block Berlekamp-Massey batches, the
   per-block bounded-distance path, the step-for-step mirror, known positions)
   on the oracle's own code tables, with the warp emulated by 32 host threads
-  in lock step."""
+  in lock step.
+* The lazily reduced arithmetic of the one-block-per-thread RSi16 kernels
+  (rsi16_bt.cuh, ecc 32 and 64): parity, syndromes and the lane
+  Berlekamp-Massey."""
 
 import os
 import shutil
@@ -88,3 +91,20 @@ def test_generated_syndrome_header_is_current():
     spec.loader.exec_module(mod)
     with open(mod.OUT) as f:
         assert f.read() == mod.generate()
+
+
+@pytest.mark.skipif(shutil.which("g++") is None or shutil.which("gcc") is None, reason="needs gcc/g++")
+def test_rsi16_block_per_thread_arithmetic_on_host(tmp_path):
+    """The lazily reduced transforms and Berlekamp-Massey of the one-block-per-
+    thread RSi16 kernels (rsi16_bt.cuh): parity, syndromes and the lane
+    Berlekamp-Massey against the oracle, ecc 32 and 64, up to 65536 words."""
+    obj = tmp_path / "ffrs_oracle.o"
+    exe = tmp_path / "rsi16_bt_check"
+    subprocess.run(["gcc", "-O2", "-c", os.path.join(REPO, "oracle", "ffrs_oracle.c"), "-o", str(obj)], check=True)
+    subprocess.run(["g++", "-O2", "-std=c++20", "-pthread", "-I", os.path.join(REPO, "tests", "host", "stub"),
+                    "-I", os.path.join(REPO, "libffrs_gb300", "csrc"), "-I", os.path.join(REPO, "oracle"),
+                    os.path.join(REPO, "tests", "host", "rsi16_bt_check.cpp"), str(obj), "-o", str(exe)],
+                   check=True)
+    r = subprocess.run([str(exe), "23", "96"], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True,
+                       timeout=600)
+    assert r.returncode == 0 and r.stdout.strip().endswith("bad 0"), r.stdout[-2000:]
