@@ -460,8 +460,10 @@ int ffgpu_rs256_encode_host(const ffgpu_rs256 *code, const uint8_t *buf, size_t 
         uint8_t *d_out = (uint8_t *)h->d_parity.get(nout);
         // chunks of full blocks on the pipeline streams (copy in, encode and
         // copy out of different chunks overlap); the ragged tail block goes
-        // with the last chunk.  An encode launch of fewer blocks than about a
-        // quarter million is latency-bound, so smaller calls stay whole.
+        // with the last chunk.  Each chunk costs fixed host work (events, the
+        // staged output copy); below about a quarter million blocks that
+        // costs more than the overlap gains (65,536 blocks: 109 GB/s whole,
+        // 75 GB/s in four chunks), so smaller calls stay whole.
         const size_t chunk = std::max<size_t>(1, host_chunk_blocks(full, 262144, 4));
         uint8_t *h_out = pipeline_out(out, chunk < full, h->h_parity, nout);
         OutputDrain drain;

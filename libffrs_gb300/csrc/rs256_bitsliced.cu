@@ -19,7 +19,9 @@
 // remainder R = r * x^d mod g_t into its syndromes S_j = r(a^j) = R(a^j) a^{-jd}.
 // All selector tables are computed at compile time and reach the code as
 // template constants, so every plane index is resolved to a register.
-#include <cooperative_groups.h>
+//
+// Encode batches too small to fill the GPU with that LFSR (ecc 32) take the
+// byte-parallel nibble-table kernel instead (rs256_encode_nib_kernel).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -741,197 +743,6 @@ __global__ void __launch_bounds__(kGroups * 2) bs_encode32_kernel(const uint8_t 
 }
 
 
-// ---------------------------------------------------------------- segmented encode
-//
-// For batches too small to fill the GPU at one thread per (group, factor), the
-// message is also cut into kSegs segments of kSegLen bytes counted from its
-// end: with seg_s the bytes of segment s (s = 0 last),
-//   data * x^16 mod g_t = sum_s (seg_s * x^16 mod g_t) * x^(kSegLen * s) mod g_t,
-// so every (group, factor, segment) runs its own LFSR from zero and the
-// results meet through the fixed linear maps x^(kSegLen * s) mod g_t (compile
-// time, one four-Russians pass like the syndrome map), then the Chinese
-// remainder map of the unsegmented kernel.
-
-constexpr int kSegs = 4, kSegLen = 56;  // 4 * 56 >= 223, the largest ecc-32 message
-
-// SegSel: [t][s][m][p][o] input-bit mask of output bit o of R'[p] for input byte m
-struct SegSel {
-    uint8_t s[2][kSegs][16][16][8];
-};
-
-constexpr SegSel make_seg_sel() {
-    SegSel S{};
-    for (int t = 0; t < 2; ++t) {
-        const Poly<16> g = factor_poly<16>(16 * t);
-        // r = x^k mod g_t, highest degree first (r[p]: coefficient of x^(15-p))
-        uint8_t r[16] = {};
-        r[15] = 1;
-        for (int k = 0; k <= 15 + kSegLen * (kSegs - 1); ++k) {
-            // record x^k for every (s, m) with 15 - m + kSegLen * s == k
-            for (int s = 0; s < kSegs; ++s) {
-                const int m = 15 + kSegLen * s - k;
-                if (m >= 0 && m < 16)
-                    for (int p = 0; p < 16; ++p)
-                        for (int o = 0; o < 8; ++o) S.s[t][s][m][p][o] = sel_of(r[p], o);
-            }
-            // r <- r * x mod g_t
-            const uint8_t top = r[0];
-            for (int p = 0; p < 15; ++p) r[p] = r[p + 1];
-            r[15] = 0;
-            for (int p = 0; p < 16; ++p) r[p] ^= gm(top, g.c[p + 1]);
-        }
-    }
-    return S;
-}
-
-struct SegHolder {
-    static constexpr SegSel seg = make_seg_sel();
-};
-
-// out[p][o] (p = 8h .. 8h+7) ^= (x^(kSegLen s) mod g_t applied to input byte M)
-template <int T, int S, int M, int H, int... K>
-__device__ __forceinline__ void seg_accum(uint32_t (&out)[8][8], const uint32_t (&lo)[16], const uint32_t (&hi)[16],
-                                          std::integer_sequence<int, K...>) {
-    ((out[K / 8][K % 8] = pickx<SegHolder::seg.s[T][S][M][H * 8 + K / 8][K % 8]>(out[K / 8][K % 8], lo, hi)), ...);
-}
-
-// half H of R' = R * x^(kSegLen S) mod g_T, R read from the stash (16 bytes x 8 planes)
-template <int T, int S, int H, int... M>
-__device__ __forceinline__ void seg_map_half(const uint32_t *rs, int stride, uint32_t (&out)[8][8],
-                                             std::integer_sequence<int, M...>) {
-    auto one = [&](auto mc) {
-        constexpr int m = decltype(mc)::value;
-        uint32_t r[8];
-#pragma unroll
-        for (int b = 0; b < 8; ++b) r[b] = rs[(m * 8 + b) * stride];
-        uint32_t lo[16], hi[16];
-        combos(r, lo, hi);
-        seg_accum<T, S, m, H>(out, lo, hi, std::make_integer_sequence<int, 64>{});
-    };
-    (one(std::integral_constant<int, M>{}), ...);
-}
-
-// maps this thread's stashed remainder in place (both halves)
-template <int T, int S>
-__device__ __forceinline__ void seg_map(uint32_t *rs, int stride) {
-    uint32_t o0[8][8], o1[8][8];
-#pragma unroll
-    for (int p = 0; p < 8; ++p)
-#pragma unroll
-        for (int o = 0; o < 8; ++o) {
-            o0[p][o] = 0u;
-            o1[p][o] = 0u;
-        }
-    seg_map_half<T, S, 0>(rs, stride, o0, std::make_integer_sequence<int, 16>{});
-    seg_map_half<T, S, 1>(rs, stride, o1, std::make_integer_sequence<int, 16>{});
-#pragma unroll
-    for (int p = 0; p < 8; ++p)
-#pragma unroll
-        for (int o = 0; o < 8; ++o) {
-            rs[(p * 8 + o) * stride] = o0[p][o];
-            rs[((8 + p) * 8 + o) * stride] = o1[p][o];
-        }
-}
-
-// The segmented encoder on thread-block clusters: one cluster of kSegs CTAs
-// per tile of 32 groups (1024 blocks), CTA rank s running segment s for both
-// factors (warp t = factor t) with its own window buffer, so that a batch of
-// N blocks spreads over N / 256 CTAs instead of N / 1024.  Each rank maps its
-// remainders by x^(kSegLen s) mod g_t in its own shared memory; after a
-// cluster barrier rank 0 adds the kSegs mapped remainders through
-// distributed shared memory, applies the Chinese remainder map and writes the
-// parity; a second barrier keeps the other ranks' shared memory alive until
-// rank 0 has read it.
-__global__ void __cluster_dims__(kSegs, 1, 1) __launch_bounds__(64)
-    bs_encode32_cl_kernel(const uint8_t *__restrict__ data, size_t nblocks, int msg_len, uint8_t *__restrict__ parity) {
-    namespace cg = cooperative_groups;
-    constexpr int E = 32, D = 16, G = 32;
-    extern __shared__ __align__(16) uint32_t sm[];  // the window buffer (G * 256 words), then the stash
-    cg::cluster_group cl = cg::this_cluster();
-    const int s = (int)cl.block_rank();
-    const int t = threadIdx.x >> 5, g = threadIdx.x & 31;
-    const size_t first = (size_t)(blockIdx.x / kSegs) * G * 32;
-    const int nb_tile = (int)min((size_t)G * 32, nblocks - first);
-    const int end_s = msg_len - kSegLen * s;
-    const int start_s = max(0, msg_len - kSegLen * (s + 1));
-    uint32_t R[D][8];
-#pragma unroll
-    for (int m = 0; m < D; ++m)
-#pragma unroll
-        for (int b = 0; b < 8; ++b) R[m][b] = 0u;
-    const size_t total = nblocks * (size_t)msg_len;
-    for (int w0 = 0; w0 < kSegLen; w0 += 32) {
-        const int p0 = start_s + w0;
-        const int npos = min(32, end_s - p0);
-        if (npos <= 0) break;  // uniform over the CTA
-        __syncthreads();
-        load_window(sm, data, (size_t)msg_len, total, first, nb_tile, p0, G);
-        __syncthreads();
-        transpose_window<2>(sm, g, t);
-        __syncthreads();
-        if (t == 0)
-            run_lfsr_window<Code<E>, 0>(sm, g, npos, R);
-        else
-            run_lfsr_window<Code<E>, 1>(sm, g, npos, R);
-    }
-    __syncthreads();  // window reads done before the stash overwrites the buffer
-    // stash [t][m*8+b][g], stride G, mapped in place by x^(kSegLen s) mod g_t
-    uint32_t *rs = sm + t * (128 * G) + g;
-#pragma unroll
-    for (int m = 0; m < D; ++m)
-#pragma unroll
-        for (int b = 0; b < 8; ++b) rs[(m * 8 + b) * G] = R[m][b];
-    // (each case with its own stash address: a shared one kept live across
-    // the six maps costs registers)
-    switch (s * 2 + t) {
-        case 2: seg_map<0, 1>(sm + g, G); break;
-        case 3: seg_map<1, 1>(sm + 128 * G + g, G); break;
-        case 4: seg_map<0, 2>(sm + g, G); break;
-        case 5: seg_map<1, 2>(sm + 128 * G + g, G); break;
-        case 6: seg_map<0, 3>(sm + g, G); break;
-        case 7: seg_map<1, 3>(sm + 128 * G + g, G); break;
-        default: break;
-    }
-    cl.sync();
-    if (s == 0) {
-        // the segment sum in place over rank 0's stash: the CRT layout
-        // [(t*16+m)*8+b][g]
-        const uint32_t *rem[kSegs];
-#pragma unroll
-        for (int ss = 1; ss < kSegs; ++ss) rem[ss] = cl.map_shared_rank(sm, ss) + t * (128 * G) + g;
-#pragma unroll 4
-        for (int k = 0; k < 128; ++k) {
-            uint32_t v = rs[k * G];
-#pragma unroll
-            for (int ss = 1; ss < kSegs; ++ss) v ^= rem[ss][k * G];
-            rs[k * G] = v;
-        }
-        __syncthreads();
-        uint32_t Pp[16][8];
-#pragma unroll
-        for (int p = 0; p < 16; ++p)
-#pragma unroll
-            for (int o = 0; o < 8; ++o) Pp[p][o] = 0u;
-        if (t == 0)
-            crt_map<0>(sm + g, G, Pp, std::make_integer_sequence<int, 32>{});
-        else
-            crt_map<16>(sm + g, G, Pp, std::make_integer_sequence<int, 32>{});
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            uint32_t a[32];
-#pragma unroll
-            for (int k = 0; k < 32; ++k) a[k] = Pp[q * 4 + k / 8][k % 8];
-            transpose32(a);
-            const int pb = t * 16 + q * 4;
-#pragma unroll
-            for (int j = 0; j < 32; ++j)
-                if ((int)(g * 32 + j) < nb_tile)
-                    *reinterpret_cast<uint32_t *>(parity + (first + (size_t)g * 32 + j) * E + pb) = a[j];
-        }
-    }
-    cl.sync();
-}
-
 // ---------------------------------------------------------------- bitsliced solve
 //
 // Decoding from the bitsliced syndromes, 32 blocks per plane word, following
@@ -1379,56 +1190,43 @@ __device__ __forceinline__ void synd32_load(uint32_t *raw, const uint8_t *__rest
     asm volatile("cp.async.commit_group;" ::: "memory");
 }
 
-__global__ void __launch_bounds__(256, 1) bs_synd32_kernel(const uint8_t *__restrict__ data,
-                                                           const uint8_t *__restrict__ parity, size_t nblocks,
-                                                           int msg_len, uint32_t *__restrict__ planes) {
+// Thread (w, lane) of a tile's CTA: column w (window bytes 4w .. 4w+3) of the
+// 32 blocks of group `lane`, staged in raw by synd32_load, into the bit
+// planes P[(b * 32 + k) * 32 + lane] (bit b of window byte k, bit j = block
+// j).  Message windows (win < 7) are realigned from the staged words and
+// cleared before the block's first byte.
+__device__ __forceinline__ void synd32_transpose(const uint32_t *raw, uint32_t *P, int win, size_t first,
+                                                 int msg_len, int lane, int w) {
     using G = Synd32Geom;
-    extern __shared__ __align__(16) uint32_t sm[];
-    uint32_t *raw0 = sm, *P = sm + 2 * G::kRaw;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const size_t tile = blockIdx.x, first = tile * 1024;
-    uint32_t s[kSyndRows];
+    uint32_t a[32];
+    const uint32_t *rg = raw + lane * G::kRawStride + w;
+    if (win < 7) {
+        const long long p0 = (long long)msg_len - 224;  // first data byte of window 0
+        const long long c0 = p0 + 32 * win + 4 * w;     // position of the column's first byte
+        const uint32_t keep = c0 >= 0 ? ~0u : (c0 <= -4 ? 0u : (~0u << (8 * (int)(-c0))));
+        // byte offset (mod 4) of block j's window: (first + 32 lane + j) * msg_len + p0
+        uint32_t off = (uint32_t)((((long long)first * msg_len + p0) & 3) + (uint32_t)(lane * 32 * msg_len));
 #pragma unroll
-    for (int i = 0; i < kSyndRows; ++i) s[i] = 0u;
-    const long long p0 = (long long)msg_len - 224;  // first data byte of window 0
-    synd32_load(raw0, data, parity, nblocks, msg_len, first, 0);
-#pragma unroll 1
-    for (int win = 0; win < 8; ++win) {
-        uint32_t *raw = raw0 + (win & 1) * G::kRaw;
-        asm volatile("cp.async.wait_group 0;" ::: "memory");
-        __syncthreads();
-        // transpose column w of group `lane`: bytes 4w .. 4w+3 of the window
-        {
-            uint32_t a[32];
-            const uint32_t *rg = raw + lane * G::kRawStride + w;
-            if (win < 7) {
-                const long long c0 = p0 + 32 * win + 4 * w;  // position of the column's first byte
-                const uint32_t keep = c0 >= 0 ? ~0u : (c0 <= -4 ? 0u : (~0u << (8 * (int)(-c0))));
-                // byte offset (mod 4) of block j's window: (first + 32 lane + j) * msg_len + p0
-                uint32_t off = (uint32_t)((((long long)first * msg_len + p0) & 3) + (uint32_t)(lane * 32 * msg_len));
-#pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    a[j] = __funnelshift_r(rg[j * 9], rg[j * 9 + 1], (off & 3) * 8) & keep;
-                    off += (uint32_t)msg_len;
-                }
-            } else {
-#pragma unroll
-                for (int j = 0; j < 32; ++j) a[j] = rg[j * 9];
-            }
-            transpose32(a);  // a[8r + b]: bit b of window byte 4w + r, bit j = block j
-#pragma unroll
-            for (int r = 0; r < 4; ++r)
-#pragma unroll
-                for (int b = 0; b < 8; ++b) P[(b * 32 + 4 * w + r) * 32 + lane] = a[8 * r + b];
+        for (int j = 0; j < 32; ++j) {
+            a[j] = __funnelshift_r(rg[j * 9], rg[j * 9 + 1], (off & 3) * 8) & keep;
+            off += (uint32_t)msg_len;
         }
-        __syncthreads();
-        if (win < 7) synd32_load(raw0 + ((win + 1) & 1) * G::kRaw, data, parity, nblocks, msg_len, first, win + 1);
-        const uint32_t *Pw = P + w * 32 * 32 + lane;
-        synd_step32([&](int k) { return Pw[k * 32]; }, s);
+    } else {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) a[j] = rg[j * 9];
     }
-    // the rows of all planes into S_j, in two halves through shared memory
-    uint32_t *X = raw0 + lane;
-    uint32_t *out = planes + tile * (size_t)kTileWords<32> + lane;
+    transpose32(a);  // a[8r + b]: bit b of window byte 4w + r, bit j = block j
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int b = 0; b < 8; ++b) P[(b * 32 + 4 * w + r) * 32 + lane] = a[8 * r + b];
+}
+
+// The rows s of the eight planes (thread (w, lane) holds plane w of group
+// lane) into the syndrome planes out[(8j + b) * 32] (bit b of S_j; out is
+// offset by lane), in two halves through X (offset by lane).  Starts and ends
+// with a barrier.
+__device__ __forceinline__ void synd32_combine(const uint32_t (&s)[kSyndRows], uint32_t *X, uint32_t *out, int w) {
     __syncthreads();
 #pragma unroll
     for (int i = 0; i < kSyndRowsA; ++i) X[(i * 8 + w) * 32] = s[i];
@@ -1456,6 +1254,155 @@ __global__ void __launch_bounds__(256, 1) bs_synd32_kernel(const uint8_t *__rest
         case 5: synd_combine_B5(X, out); break;
         case 6: synd_combine_B6(X, out); break;
         default: synd_combine_B7(X, out); break;
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(256, 1) bs_synd32_kernel(const uint8_t *__restrict__ data,
+                                                           const uint8_t *__restrict__ parity, size_t nblocks,
+                                                           int msg_len, uint32_t *__restrict__ planes) {
+    using G = Synd32Geom;
+    extern __shared__ __align__(16) uint32_t sm[];
+    uint32_t *raw0 = sm, *P = sm + 2 * G::kRaw;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const size_t tile = blockIdx.x, first = tile * 1024;
+    uint32_t s[kSyndRows];
+#pragma unroll
+    for (int i = 0; i < kSyndRows; ++i) s[i] = 0u;
+    synd32_load(raw0, data, parity, nblocks, msg_len, first, 0);
+#pragma unroll 1
+    for (int win = 0; win < 8; ++win) {
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        __syncthreads();
+        synd32_transpose(raw0 + (win & 1) * G::kRaw, P, win, first, msg_len, lane, w);
+        __syncthreads();
+        if (win < 7) synd32_load(raw0 + ((win + 1) & 1) * G::kRaw, data, parity, nblocks, msg_len, first, win + 1);
+        const uint32_t *Pw = P + w * 32 * 32 + lane;
+        synd_step32([&](int k) { return Pw[k * 32]; }, s);
+    }
+    // the rows of all planes into S_j
+    synd32_combine(s, raw0 + lane, planes + tile * (size_t)kTileWords<32> + lane, w);
+}
+
+// ---------------------------------------------------------------- encode by nibble tables (ecc 32)
+//
+// rs_encode (libffrs/reed_solomon.hpp:225-297) is linear: the parity of a
+// message is the XOR over its bytes m_i of m_i * U_e, U_e = x^(32 + e) mod
+// g(x) for the byte's degree index e = message_len - 1 - i.  With each byte
+// split into nibbles, m * U_e = (m & 15) U_e + (m & 0xf0) U_e, so a degree
+// takes two tables of 16 entries of 32 bytes (1 KB); the 223 degrees of the
+// longest message fit in one CTA's shared memory.  There is no dependence
+// between bytes, which suits batches too small to fill the GPU with the
+// bitsliced LFSR (sequential over the message for each 32-block group).
+//
+// Bank layout: one 128-byte line holds the entries of one nibble value for
+// four consecutive degrees 4G .. 4G+3, 32 bytes each.  A quarter warp (the 8
+// lanes that one 16-byte shared load serves per wavefront) takes one block:
+// lane (r, h) the bytes of degree index e = r (mod 4) and parity half h
+// (bytes 16h .. 16h+15).  Its reads land on bank group 2r + h whatever the
+// byte values, so a warp's four quarters read their 512 bytes in four
+// wavefronts.  The four residues are then XORed by two shuffles.
+
+constexpr int kNibDegrees = 224;                      // degree indices 0 .. 223 (223 used)
+constexpr int kNibLineQ = 8;                          // 16-byte words per line: [r][h]
+constexpr int kNibGroupQ = 2 * 16 * kNibLineQ;        // words per group of 4 degrees: [part][v][line]
+constexpr int kNibWords = kNibDegrees / 4 * kNibGroupQ;
+
+// the XOR into acc of the entries of the four bytes of w (one per word,
+// byte k0 of each) at message indices p0 + 4j + k0, j < 4 (degree indices
+// e0 - 4j, e0 = ml - 1 - p0 - k0 = r mod 4); MASK: some indices fall
+// outside [0, ml) and those bytes count as zero
+template <bool MASK>
+__device__ __forceinline__ void nib_chunk(const uint4 *T, int ml, int p0, int k0, int rh, const uint32_t (&w)[4],
+                                          uint4 &acc) {
+    // entry (G, part, v, r, h) at T[((G * 2 + part) * 16 + v) * 8 + 2r + h]
+    const int G0 = (ml - 1 - p0 - k0) >> 2;
+    const uint4 *Tb = T + (ptrdiff_t)G0 * kNibGroupQ + rh;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        uint32_t v = (w[j] >> (8 * k0)) & 0xffu;
+        const uint4 *Te = Tb - j * kNibGroupQ;
+        if (MASK) {
+            const int p = p0 + 4 * j + k0;
+            const bool in = p >= 0 && p < ml;
+            v = in ? v : 0u;
+            Te = in ? Te : T + rh;
+        }
+        const uint4 lo = Te[(v & 15u) * kNibLineQ], hi = Te[(16 + (v >> 4)) * kNibLineQ];
+        acc.x ^= lo.x ^ hi.x;
+        acc.y ^= lo.y ^ hi.y;
+        acc.z ^= lo.z ^ hi.z;
+        acc.w ^= lo.w ^ hi.w;
+    }
+}
+
+// tab: kNibWords words (all degree groups); dynamic shared memory holds the
+// groups of degree indices 0 .. ml - 1.  Each warp takes four blocks at a
+// time, one per quarter.
+__global__ void __launch_bounds__(1024, 1) rs256_encode_nib_kernel(const uint8_t *__restrict__ data, size_t nblocks,
+                                                                    int ml, const uint4 *__restrict__ tab,
+                                                                    uint8_t *__restrict__ parity) {
+    extern __shared__ __align__(16) uint4 T[];
+    {
+        const uint32_t tb = (uint32_t)__cvta_generic_to_shared(T);
+        const int nq = (ml + 3) / 4 * kNibGroupQ;
+        for (int q = threadIdx.x; q < nq; q += blockDim.x)
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(tb + 16u * q), "l"(tab + q) : "memory");
+        asm volatile("cp.async.commit_group;" ::: "memory");
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        __syncthreads();
+    }
+    const int lane = threadIdx.x & 31, quarter = lane >> 3, rh = lane & 7, r = rh >> 1, h = rh & 1;
+    const uintptr_t d0 = (uintptr_t)data, d1 = d0 + nblocks * (size_t)ml;
+    const bool out16 = ((uintptr_t)parity & 15) == 0;
+    const size_t nwarps = (size_t)gridDim.x * (blockDim.x >> 5);
+    for (size_t base = ((size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 4; base < nblocks;
+         base += nwarps * 4) {
+        const size_t b = base + quarter;
+        uint4 acc = make_uint4(0u, 0u, 0u, 0u);
+        if (b < nblocks) {
+            const uintptr_t a = d0 + b * (size_t)ml, a0 = a & ~(uintptr_t)15;
+            const int nch = (int)((a + ml - a0 + 15) >> 4);
+            for (int c = 0; c < nch; ++c) {
+                const uintptr_t ac = a0 + 16 * (uintptr_t)c;
+                uint32_t w[4];
+                if (ac >= d0 && ac + 16 <= d1) {
+                    const uint4 q = __ldg(reinterpret_cast<const uint4 *>(ac));
+                    w[0] = q.x, w[1] = q.y, w[2] = q.z, w[3] = q.w;
+                } else {
+                    // the first or last 16 bytes of the buffer: its 4-byte
+                    // words (data is 4-byte aligned), zero outside it
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        const uintptr_t aw = ac + 4 * i;
+                        w[i] = (aw >= d0 && aw < d1) ? __ldg(reinterpret_cast<const uint32_t *>(aw)) : 0u;
+                    }
+                }
+                const int p0 = (int)((intptr_t)ac - (intptr_t)a);  // message index of the chunk's first byte
+                const int k0 = (ml - 1 - p0 - r) & 3;              // this lane's byte of each word
+                if (p0 >= 0 && p0 + 16 <= ml)
+                    nib_chunk<false>(T, ml, p0, k0, rh, w, acc);
+                else
+                    nib_chunk<true>(T, ml, p0, k0, rh, w, acc);
+            }
+        }
+        // XOR of the four residues r (lane bits 1 and 2)
+#pragma unroll
+        for (int m = 2; m <= 4; m <<= 1) {
+            acc.x ^= __shfl_xor_sync(0xffffffffu, acc.x, m);
+            acc.y ^= __shfl_xor_sync(0xffffffffu, acc.y, m);
+            acc.z ^= __shfl_xor_sync(0xffffffffu, acc.z, m);
+            acc.w ^= __shfl_xor_sync(0xffffffffu, acc.w, m);
+        }
+        if (b < nblocks && r == 0) {
+            uint8_t *o = parity + b * 32 + 16 * h;
+            if (out16) {
+                *reinterpret_cast<uint4 *>(o) = acc;
+            } else {
+                uint32_t *o4 = reinterpret_cast<uint32_t *>(o);
+                o4[0] = acc.x, o4[1] = acc.y, o4[2] = acc.z, o4[3] = acc.w;
+            }
+        }
     }
 }
 
@@ -1760,7 +1707,38 @@ __global__ void __launch_bounds__(128, 3) bs_chien_kernel(uint8_t *__restrict__ 
 
 struct FastState {
     int ecc;
+    std::once_flag nib_once;
+    uint4 *nib_tab = nullptr;  // the encoder's nibble tables (ecc 32), built at first use
 };
+
+// The tables of rs256_encode_nib_kernel: for degree index e (degree 32 + e),
+// entry (part, v) is val * U_e with val = v (part 0) or v << 4 (part 1),
+// U_e = x^(32 + e) mod g(x) as 32 bytes (byte k: the coefficient of x^(31 -
+// k)), g = prod_{j < 32} (x - a^j); stored at word ((e / 4 * 2 + part) * 16
+// + v) * 8 + 2 (e % 4) + h for its halves h (bytes 16h .. 16h + 15).
+static std::vector<uint32_t> nib_tables() {
+    constexpr bs::Poly<32> g = bs::factor_poly<32>(0);
+    uint8_t U[32], U32[32];
+    for (int k = 0; k < 32; ++k) U32[k] = U[k] = g.c[k + 1];  // x^32 mod g
+    std::vector<uint32_t> t((size_t)bs::kNibWords * 4);
+    for (int e = 0; e < bs::kNibDegrees; ++e) {
+        for (int part = 0; part < 2; ++part)
+            for (int v = 0; v < 16; ++v) {
+                const uint8_t val = (uint8_t)(part ? v << 4 : v);
+                for (int h = 0; h < 2; ++h) {
+                    const size_t word = (((size_t)(e / 4) * 2 + part) * 16 + v) * bs::kNibLineQ + 2 * (e % 4) + h;
+                    uint32_t *q = &t[word * 4];
+                    for (int k = 0; k < 16; ++k) q[k / 4] |= (uint32_t)bs::gm(val, U[16 * h + k]) << (8 * (k % 4));
+                }
+            }
+        // U <- x U mod g
+        const uint8_t top = U[0];
+        for (int k = 0; k < 31; ++k) U[k] = U[k + 1];
+        U[31] = 0;
+        for (int k = 0; k < 32; ++k) U[k] ^= bs::gm(top, U32[k]);
+    }
+    return t;
+}
 
 bool rs256_fast_init(Rs256Code &c) {
     if (c.primitive != 2 || (c.polynomial & 0xff) != 0x1d) return false;
@@ -1770,7 +1748,9 @@ bool rs256_fast_init(Rs256Code &c) {
 }
 
 void rs256_fast_free(Rs256Code &c) {
-    delete static_cast<FastState *>(c.fast_state);
+    auto *fs = static_cast<FastState *>(c.fast_state);
+    if (fs && fs->nib_tab) cudaFree(fs->nib_tab);
+    delete fs;
     c.fast_state = nullptr;
 }
 
@@ -1802,14 +1782,28 @@ bool rs256_fast_encode(const Rs256Code &c, const uint8_t *data, size_t nblocks, 
                        cudaStream_t st) {
     if (!c.fast || c.table_only || c.ecc != 32 || !aligned4(data) || !aligned4(parity)) return false;
     if (!nblocks) return true;
-    const size_t seg_ctas = (nblocks + 1023) / 1024;
-    if (msg_len <= bs::kSegs * bs::kSegLen && seg_ctas <= (size_t)sm_count() * 4) {
-        // too few groups to fill the GPU: split the messages into segments
-        // too, one CTA per (tile, segment) in clusters of kSegs
-        constexpr size_t smem = (size_t)(32 * 256) * 4;
-        KernelTimer kt_timer("bs_encode32_cl_kernel", st);
-        bs::bs_encode32_cl_kernel<<<(unsigned)(seg_ctas * bs::kSegs), 64, smem, st>>>(data, nblocks, msg_len, parity);
-        check_launch("bs_encode32_cl_kernel");
+    const size_t ntiles = (nblocks + 1023) / 1024;
+    if (3 * ntiles < 4 * (size_t)sm_count() && msg_len >= 1 && msg_len <= 223) {
+        // the LFSR kernel takes one wave (about 0.12 ms on 152 SMs) for any
+        // batch up to 2048 blocks per SM; the nibble tables take time in
+        // proportion to the blocks and are faster below about 1,365 per SM
+        auto *fs = static_cast<FastState *>(c.fast_state);
+        std::call_once(fs->nib_once, [&] {
+            const std::vector<uint32_t> t = nib_tables();
+            FFGPU_CHECK_CUDA(cudaMalloc(&fs->nib_tab, t.size() * 4));
+            FFGPU_CHECK_CUDA(cudaMemcpy(fs->nib_tab, t.data(), t.size() * 4, cudaMemcpyHostToDevice));
+            FFGPU_CHECK_CUDA(cudaFuncSetAttribute(bs::rs256_encode_nib_kernel,
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                  bs::kNibWords * 16));
+        });
+        // four blocks per warp, one CTA per SM
+        const size_t warps = (nblocks + 3) / 4, sms = (size_t)sm_count();
+        const unsigned threads = (unsigned)std::min<size_t>(1024, (warps + sms - 1) / sms * 32);
+        const unsigned grid = (unsigned)std::min(sms, (warps * 32 + threads - 1) / threads);
+        KernelTimer kt_timer("rs256_encode_nib_kernel", st);
+        bs::rs256_encode_nib_kernel<<<grid, threads, (size_t)(msg_len + 3) / 4 * bs::kNibGroupQ * 16, st>>>(
+            data, nblocks, msg_len, fs->nib_tab, parity);
+        check_launch("rs256_encode_nib_kernel");
         return true;
     }
     KernelTimer kt_timer("bs_encode32_kernel", st);

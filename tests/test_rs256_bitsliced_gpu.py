@@ -123,3 +123,25 @@ def test_bitsliced_unaligned_buffers(built, offset):
     np.testing.assert_array_equal(st, so)
     np.testing.assert_array_equal(d, od)
     np.testing.assert_array_equal(p, op)
+
+
+@pytest.mark.parametrize("ml,nb", [(223, 180000 + 3), (223, 2 * 152 * 1024 + 1000), (100, 2 * 160 * 1024 + 5)])
+def test_encode_large_batches(built, ml, nb):
+    """Batches on either side of the switch from the nibble-table encoder
+    (each warp four blocks at a time) to the bitsliced LFSR (2048-block
+    tiles), at about 1,365 blocks per SM."""
+    import torch
+    from libffrs_gb300 import capi
+
+    rng = np.random.Generator(np.random.PCG64(ml * 7 + nb))
+    data = rng.integers(0, 256, size=(nb, ml), dtype=np.uint8)
+    data[:64] = 255
+    o = O.RS256(32, block_len=ml + 32)
+    want = o.encode_blocks(data, threads=16)
+    code = capi.RS256Code(32)
+    stream = torch.cuda.current_stream().cuda_stream
+    d = torch.from_numpy(data.reshape(-1)).cuda()
+    p = torch.zeros(nb * 32, dtype=torch.uint8, device="cuda")
+    code.encode(d.data_ptr(), nb, ml, p.data_ptr(), stream)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(p.cpu().numpy().reshape(nb, 32), want)
