@@ -1309,18 +1309,17 @@ constexpr int kNibGroupQ = 2 * 16 * kNibLineQ;        // words per group of 4 de
 constexpr int kNibWords = kNibDegrees / 4 * kNibGroupQ;
 
 // the XOR into acc of the entries of the four bytes of w (one per word,
-// byte k0 of each) at message indices p0 + 4j + k0, j < 4 (degree indices
-// e0 - 4j, e0 = ml - 1 - p0 - k0 = r mod 4); MASK: some indices fall
-// outside [0, ml) and those bytes count as zero
+// byte k0 of each) at message indices p0 + 4j + k0, j < 4, whose degree
+// indices e0 - 4j lie in line group G0 - j (e0 = ml - 1 - p0 - k0 = r mod 4,
+// G0 = e0 >> 2, Tb = T + G0 * kNibGroupQ + 2r + h); MASK: some of the
+// indices fall outside [0, ml) and those bytes count as zero
 template <bool MASK>
-__device__ __forceinline__ void nib_chunk(const uint4 *T, int ml, int p0, int k0, int rh, const uint32_t (&w)[4],
-                                          uint4 &acc) {
+__device__ __forceinline__ void nib_chunk(const uint4 *T, const uint4 *Tb, int ml, int p0, int k0, int rh,
+                                          const uint32_t (&w)[4], uint4 &acc) {
     // entry (G, part, v, r, h) at T[((G * 2 + part) * 16 + v) * 8 + 2r + h]
-    const int G0 = (ml - 1 - p0 - k0) >> 2;
-    const uint4 *Tb = T + (ptrdiff_t)G0 * kNibGroupQ + rh;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-        uint32_t v = (w[j] >> (8 * k0)) & 0xffu;
+        uint32_t v = w[j] >> (8 * k0);
         const uint4 *Te = Tb - j * kNibGroupQ;
         if (MASK) {
             const int p = p0 + 4 * j + k0;
@@ -1328,11 +1327,27 @@ __device__ __forceinline__ void nib_chunk(const uint4 *T, int ml, int p0, int k0
             v = in ? v : 0u;
             Te = in ? Te : T + rh;
         }
-        const uint4 lo = Te[(v & 15u) * kNibLineQ], hi = Te[(16 + (v >> 4)) * kNibLineQ];
+        const uint4 lo = Te[(v & 15u) * kNibLineQ], hi = Te[(16 + ((v >> 4) & 15u)) * kNibLineQ];
         acc.x ^= lo.x ^ hi.x;
         acc.y ^= lo.y ^ hi.y;
         acc.z ^= lo.z ^ hi.z;
         acc.w ^= lo.w ^ hi.w;
+    }
+}
+
+// the 16-byte chunk at address ac as four words; chunks that reach past
+// either end of the buffer [d0, d1) are read by 4-byte words (data is
+// 4-byte aligned), zero outside it
+__device__ __forceinline__ void nib_load(uintptr_t ac, uintptr_t d0, uintptr_t d1, uint32_t (&w)[4]) {
+    if (ac >= d0 && ac + 16 <= d1) {
+        const uint4 q = __ldg(reinterpret_cast<const uint4 *>(ac));
+        w[0] = q.x, w[1] = q.y, w[2] = q.z, w[3] = q.w;
+    } else {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const uintptr_t aw = ac + 4 * i;
+            w[i] = (aw >= d0 && aw < d1) ? __ldg(reinterpret_cast<const uint32_t *>(aw)) : 0u;
+        }
     }
 }
 
@@ -1361,29 +1376,27 @@ __global__ void __launch_bounds__(1024, 1) rs256_encode_nib_kernel(const uint8_t
         const size_t b = base + quarter;
         uint4 acc = make_uint4(0u, 0u, 0u, 0u);
         if (b < nblocks) {
+            // chunk c: the 16 bytes at a0 + 16c, message indices p00 + 16c ..
+            // (p00 in [-15, 0]); this lane's bytes are k0, k0 + 4, .. of each
             const uintptr_t a = d0 + b * (size_t)ml, a0 = a & ~(uintptr_t)15;
-            const int nch = (int)((a + ml - a0 + 15) >> 4);
-            for (int c = 0; c < nch; ++c) {
-                const uintptr_t ac = a0 + 16 * (uintptr_t)c;
-                uint32_t w[4];
-                if (ac >= d0 && ac + 16 <= d1) {
-                    const uint4 q = __ldg(reinterpret_cast<const uint4 *>(ac));
-                    w[0] = q.x, w[1] = q.y, w[2] = q.z, w[3] = q.w;
-                } else {
-                    // the first or last 16 bytes of the buffer: its 4-byte
-                    // words (data is 4-byte aligned), zero outside it
+            const int p00 = (int)((intptr_t)a0 - (intptr_t)a);
+            const int nch = (ml - p00 + 15) >> 4;
+            const int k0 = (ml - 1 - p00 - r) & 3;
+            const uint4 *Tb = T + (ptrdiff_t)((ml - 1 - p00 - k0) >> 2) * kNibGroupQ + rh;
+            uint32_t w[4], wn[4];
+            nib_load(a0, d0, d1, w);
+            if (nch > 1) nib_load(a0 + 16, d0, d1, wn);
+            nib_chunk<true>(T, Tb, ml, p00, k0, rh, w, acc);
+            for (int c = 1; c < nch; ++c) {
 #pragma unroll
-                    for (int i = 0; i < 4; ++i) {
-                        const uintptr_t aw = ac + 4 * i;
-                        w[i] = (aw >= d0 && aw < d1) ? __ldg(reinterpret_cast<const uint32_t *>(aw)) : 0u;
-                    }
-                }
-                const int p0 = (int)((intptr_t)ac - (intptr_t)a);  // message index of the chunk's first byte
-                const int k0 = (ml - 1 - p0 - r) & 3;              // this lane's byte of each word
-                if (p0 >= 0 && p0 + 16 <= ml)
-                    nib_chunk<false>(T, ml, p0, k0, rh, w, acc);
+                for (int i = 0; i < 4; ++i) w[i] = wn[i];
+                if (c + 1 < nch) nib_load(a0 + 16 * (uintptr_t)(c + 1), d0, d1, wn);
+                const int p0 = p00 + 16 * c;
+                const uint4 *Tc = Tb - 4 * c * kNibGroupQ;
+                if (p0 + 16 <= ml)
+                    nib_chunk<false>(T, Tc, ml, p0, k0, rh, w, acc);
                 else
-                    nib_chunk<true>(T, ml, p0, k0, rh, w, acc);
+                    nib_chunk<true>(T, Tc, ml, p0, k0, rh, w, acc);
             }
         }
         // XOR of the four residues r (lane bits 1 and 2)
