@@ -103,9 +103,12 @@ def test_bitsliced_vs_oracle(built, ecc, ml, nb):
         np.testing.assert_array_equal(p, op)
 
 
-@pytest.mark.parametrize("offset", [1, 2, 3])
+@pytest.mark.parametrize("offset", [1, 2, 3, 4, 8, 12])
 def test_bitsliced_unaligned_buffers(built, offset):
-    """Buffers not on a 4-byte boundary are still decoded correctly."""
+    """Buffers off a 4-byte boundary (table kernels) and off a 16-byte one
+    (offsets 4, 8, 12: the nibble-table encoder's first chunk starts before
+    the buffer and its parity goes out in 4-byte words) give the oracle's
+    results."""
     from libffrs_gb300 import capi
 
     ecc, ml, nb = 32, 223, 300
