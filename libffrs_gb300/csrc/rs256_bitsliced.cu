@@ -30,6 +30,7 @@
 
 #include "common.cuh"
 #include "rs256.cuh"
+#include "rs256_nib.cuh"
 #include "rs256_synd_gen.cuh"
 
 namespace ffgpu {
@@ -1286,70 +1287,9 @@ __global__ void __launch_bounds__(256, 1) bs_synd32_kernel(const uint8_t *__rest
 
 // ---------------------------------------------------------------- encode by nibble tables (ecc 32)
 //
-// rs_encode (libffrs/reed_solomon.hpp:225-297) is linear: the parity of a
-// message is the XOR over its bytes m_i of m_i * U_e, U_e = x^(32 + e) mod
-// g(x) for the byte's degree index e = message_len - 1 - i.  With each byte
-// split into nibbles, m * U_e = (m & 15) U_e + (m & 0xf0) U_e, so a degree
-// takes two tables of 16 entries of 32 bytes (1 KB); the 223 degrees of the
-// longest message fit in one CTA's shared memory.  There is no dependence
-// between bytes, which suits batches too small to fill the GPU with the
-// bitsliced LFSR (sequential over the message for each 32-block group).
-//
-// Bank layout: one 128-byte line holds the entries of one nibble value for
-// four consecutive degrees 4G .. 4G+3, 32 bytes each.  A quarter warp (the 8
-// lanes that one 16-byte shared load serves per wavefront) takes one block:
-// lane (r, h) the bytes of degree index e = r (mod 4) and parity half h
-// (bytes 16h .. 16h+15).  Its reads land on bank group 2r + h whatever the
-// byte values, so a warp's four quarters read their 512 bytes in four
-// wavefronts.  The four residues are then XORed by two shuffles.
-
-constexpr int kNibDegrees = 224;                      // degree indices 0 .. 223 (223 used)
-constexpr int kNibLineQ = 8;                          // 16-byte words per line: [r][h]
-constexpr int kNibGroupQ = 2 * 16 * kNibLineQ;        // words per group of 4 degrees: [part][v][line]
-constexpr int kNibWords = kNibDegrees / 4 * kNibGroupQ;
-
-// the XOR into acc of the entries of the four bytes of w (one per word,
-// byte k0 of each) at message indices p0 + 4j + k0, j < 4, whose degree
-// indices e0 - 4j lie in line group G0 - j (e0 = ml - 1 - p0 - k0 = r mod 4,
-// G0 = e0 >> 2, Tb = T + G0 * kNibGroupQ + 2r + h); MASK: some of the
-// indices fall outside [0, ml) and those bytes count as zero
-template <bool MASK>
-__device__ __forceinline__ void nib_chunk(const uint4 *T, const uint4 *Tb, int ml, int p0, int k0, int rh,
-                                          const uint32_t (&w)[4], uint4 &acc) {
-    // entry (G, part, v, r, h) at T[((G * 2 + part) * 16 + v) * 8 + 2r + h]
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        uint32_t v = w[j] >> (8 * k0);
-        const uint4 *Te = Tb - j * kNibGroupQ;
-        if (MASK) {
-            const int p = p0 + 4 * j + k0;
-            const bool in = p >= 0 && p < ml;
-            v = in ? v : 0u;
-            Te = in ? Te : T + rh;
-        }
-        const uint4 lo = Te[(v & 15u) * kNibLineQ], hi = Te[(16 + ((v >> 4) & 15u)) * kNibLineQ];
-        acc.x ^= lo.x ^ hi.x;
-        acc.y ^= lo.y ^ hi.y;
-        acc.z ^= lo.z ^ hi.z;
-        acc.w ^= lo.w ^ hi.w;
-    }
-}
-
-// the 16-byte chunk at address ac as four words; chunks that reach past
-// either end of the buffer [d0, d1) are read by 4-byte words (data is
-// 4-byte aligned), zero outside it
-__device__ __forceinline__ void nib_load(uintptr_t ac, uintptr_t d0, uintptr_t d1, uint32_t (&w)[4]) {
-    if (ac >= d0 && ac + 16 <= d1) {
-        const uint4 q = __ldg(reinterpret_cast<const uint4 *>(ac));
-        w[0] = q.x, w[1] = q.y, w[2] = q.z, w[3] = q.w;
-    } else {
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            const uintptr_t aw = ac + 4 * i;
-            w[i] = (aw >= d0 && aw < d1) ? __ldg(reinterpret_cast<const uint32_t *>(aw)) : 0u;
-        }
-    }
-}
+// The tables, their layout and one lane's part of a block are in
+// rs256_nib.cuh; the kernel stages the tables and gives each quarter warp a
+// block.
 
 // tab: kNibWords words (all degree groups); dynamic shared memory holds the
 // groups of degree indices 0 .. ml - 1.  Each warp takes four blocks at a
@@ -1375,30 +1315,7 @@ __global__ void __launch_bounds__(1024, 1) rs256_encode_nib_kernel(const uint8_t
          base += nwarps * 4) {
         const size_t b = base + quarter;
         uint4 acc = make_uint4(0u, 0u, 0u, 0u);
-        if (b < nblocks) {
-            // chunk c: the 16 bytes at a0 + 16c, message indices p00 + 16c ..
-            // (p00 in [-15, 0]); this lane's bytes are k0, k0 + 4, .. of each
-            const uintptr_t a = d0 + b * (size_t)ml, a0 = a & ~(uintptr_t)15;
-            const int p00 = (int)((intptr_t)a0 - (intptr_t)a);
-            const int nch = (ml - p00 + 15) >> 4;
-            const int k0 = (ml - 1 - p00 - r) & 3;
-            const uint4 *Tb = T + (ptrdiff_t)((ml - 1 - p00 - k0) >> 2) * kNibGroupQ + rh;
-            uint32_t w[4], wn[4];
-            nib_load(a0, d0, d1, w);
-            if (nch > 1) nib_load(a0 + 16, d0, d1, wn);
-            nib_chunk<true>(T, Tb, ml, p00, k0, rh, w, acc);
-            for (int c = 1; c < nch; ++c) {
-#pragma unroll
-                for (int i = 0; i < 4; ++i) w[i] = wn[i];
-                if (c + 1 < nch) nib_load(a0 + 16 * (uintptr_t)(c + 1), d0, d1, wn);
-                const int p0 = p00 + 16 * c;
-                const uint4 *Tc = Tb - 4 * c * kNibGroupQ;
-                if (p0 + 16 <= ml)
-                    nib_chunk<false>(T, Tc, ml, p0, k0, rh, w, acc);
-                else
-                    nib_chunk<true>(T, Tc, ml, p0, k0, rh, w, acc);
-            }
-        }
+        if (b < nblocks) acc = nib_lane(T, d0, d1, b, ml, r, h);
         // XOR of the four residues r (lane bits 1 and 2)
 #pragma unroll
         for (int m = 2; m <= 4; m <<= 1) {
@@ -1724,35 +1641,6 @@ struct FastState {
     uint4 *nib_tab = nullptr;  // the encoder's nibble tables (ecc 32), built at first use
 };
 
-// The tables of rs256_encode_nib_kernel: for degree index e (degree 32 + e),
-// entry (part, v) is val * U_e with val = v (part 0) or v << 4 (part 1),
-// U_e = x^(32 + e) mod g(x) as 32 bytes (byte k: the coefficient of x^(31 -
-// k)), g = prod_{j < 32} (x - a^j); stored at word ((e / 4 * 2 + part) * 16
-// + v) * 8 + 2 (e % 4) + h for its halves h (bytes 16h .. 16h + 15).
-static std::vector<uint32_t> nib_tables() {
-    constexpr bs::Poly<32> g = bs::factor_poly<32>(0);
-    uint8_t U[32], U32[32];
-    for (int k = 0; k < 32; ++k) U32[k] = U[k] = g.c[k + 1];  // x^32 mod g
-    std::vector<uint32_t> t((size_t)bs::kNibWords * 4);
-    for (int e = 0; e < bs::kNibDegrees; ++e) {
-        for (int part = 0; part < 2; ++part)
-            for (int v = 0; v < 16; ++v) {
-                const uint8_t val = (uint8_t)(part ? v << 4 : v);
-                for (int h = 0; h < 2; ++h) {
-                    const size_t word = (((size_t)(e / 4) * 2 + part) * 16 + v) * bs::kNibLineQ + 2 * (e % 4) + h;
-                    uint32_t *q = &t[word * 4];
-                    for (int k = 0; k < 16; ++k) q[k / 4] |= (uint32_t)bs::gm(val, U[16 * h + k]) << (8 * (k % 4));
-                }
-            }
-        // U <- x U mod g
-        const uint8_t top = U[0];
-        for (int k = 0; k < 31; ++k) U[k] = U[k + 1];
-        U[31] = 0;
-        for (int k = 0; k < 32; ++k) U[k] ^= bs::gm(top, U32[k]);
-    }
-    return t;
-}
-
 bool rs256_fast_init(Rs256Code &c) {
     if (c.primitive != 2 || (c.polynomial & 0xff) != 0x1d) return false;
     if (c.ecc != 32 && c.ecc != 16 && c.ecc != 8 && c.ecc != 4 && c.ecc != 2) return false;
@@ -1802,19 +1690,20 @@ bool rs256_fast_encode(const Rs256Code &c, const uint8_t *data, size_t nblocks, 
         // proportion to the blocks and are faster below about 1,365 per SM
         auto *fs = static_cast<FastState *>(c.fast_state);
         std::call_once(fs->nib_once, [&] {
-            const std::vector<uint32_t> t = nib_tables();
+            constexpr bs::Poly<32> g = bs::factor_poly<32>(0);
+            const std::vector<uint32_t> t = nib_tables(g.c + 1);  // x^32 mod g
             FFGPU_CHECK_CUDA(cudaMalloc(&fs->nib_tab, t.size() * 4));
             FFGPU_CHECK_CUDA(cudaMemcpy(fs->nib_tab, t.data(), t.size() * 4, cudaMemcpyHostToDevice));
             FFGPU_CHECK_CUDA(cudaFuncSetAttribute(bs::rs256_encode_nib_kernel,
                                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                  bs::kNibWords * 16));
+                                                  kNibWords * 16));
         });
         // four blocks per warp, one CTA per SM
         const size_t warps = (nblocks + 3) / 4, sms = (size_t)sm_count();
         const unsigned threads = (unsigned)std::min<size_t>(1024, (warps + sms - 1) / sms * 32);
         const unsigned grid = (unsigned)std::min(sms, (warps * 32 + threads - 1) / threads);
         KernelTimer kt_timer("rs256_encode_nib_kernel", st);
-        bs::rs256_encode_nib_kernel<<<grid, threads, (size_t)(msg_len + 3) / 4 * bs::kNibGroupQ * 16, st>>>(
+        bs::rs256_encode_nib_kernel<<<grid, threads, (size_t)(msg_len + 3) / 4 * kNibGroupQ * 16, st>>>(
             data, nblocks, msg_len, fs->nib_tab, parity);
         check_launch("rs256_encode_nib_kernel");
         return true;

@@ -12,7 +12,8 @@ the oracle: CPU parity checks of the GPU code itself.
   in lock step.
 * The lazily reduced arithmetic of the one-block-per-thread RSi16 kernels
   (rsi16_bt.cuh, ecc 32 and 64): parity, syndromes and the lane
-  Berlekamp-Massey."""
+  Berlekamp-Massey.
+* The nibble-table RS256 encoder (rs256_nib.cuh): its tables and lane code."""
 
 import os
 import shutil
@@ -106,5 +107,23 @@ def test_rsi16_block_per_thread_arithmetic_on_host(tmp_path):
                     os.path.join(REPO, "tests", "host", "rsi16_bt_check.cpp"), str(obj), "-o", str(exe)],
                    check=True)
     r = subprocess.run([str(exe), "23", "96"], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True,
+                       timeout=600)
+    assert r.returncode == 0 and r.stdout.strip().endswith("bad 0"), r.stdout[-2000:]
+
+
+@pytest.mark.skipif(shutil.which("g++") is None or shutil.which("gcc") is None, reason="needs gcc/g++")
+def test_rs256_nibble_encoder_on_host(tmp_path):
+    """The nibble-table RS256 encoder's tables and lane code (rs256_nib.cuh)
+    against the oracle's encode: message lengths 1..223, buffers 0/4/8/12
+    bytes past a 16-byte boundary, poison around the staged table and the
+    buffer."""
+    obj = tmp_path / "ffrs_oracle.o"
+    exe = tmp_path / "rs256_nib_check"
+    subprocess.run(["gcc", "-O2", "-c", os.path.join(REPO, "oracle", "ffrs_oracle.c"), "-o", str(obj)], check=True)
+    subprocess.run(["g++", "-O2", "-std=c++17", "-I", os.path.join(REPO, "tests", "host", "stub"),
+                    "-I", os.path.join(REPO, "libffrs_gb300", "csrc"), "-I", os.path.join(REPO, "oracle"),
+                    os.path.join(REPO, "tests", "host", "rs256_nib_check.cpp"), str(obj), "-o", str(exe)],
+                   check=True)
+    r = subprocess.run([str(exe), "29", "96"], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True,
                        timeout=600)
     assert r.returncode == 0 and r.stdout.strip().endswith("bad 0"), r.stdout[-2000:]
