@@ -1736,29 +1736,14 @@ size_t rs256_fast_scratch_bytes(int ecc, size_t nblocks) {
     return ntiles * (size_t)(ecc == 32 ? bs::kTileWords<32> : bs::kTileWords<16>) * 4;
 }
 
+// the decode kernels' shared-memory attributes, set once per process (a
+// thread-safe static initialiser)
 template <int E>
-static void launch_bs_decode(const Rs256Code &c, uint8_t *data, uint8_t *parity, size_t nblocks, int msg_len,
-                             uint8_t *status, uint32_t *planes, cudaStream_t st) {
-    constexpr int T = bs::SyndCode<E>::T;
-    const size_t ntiles = ((nblocks + 31) / 32 + 31) / 32;
-    if constexpr (E == 32) {
-        static const bool synd_attrs = [] {
+static void bs_decode_attrs() {
+    static const bool attrs = [] {
+        if constexpr (E == 32)
             cudaFuncSetAttribute(bs::bs_synd32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)bs::Synd32Geom::smem);
-            return true;
-        }();
-        (void)synd_attrs;
-        KernelTimer kt_timer("bs_synd32_kernel", st);
-        bs::bs_synd32_kernel<<<(unsigned)ntiles, 256, bs::Synd32Geom::smem, st>>>(data, parity, nblocks, msg_len,
-                                                                                  planes);
-        check_launch("bs_synd32_kernel");
-    } else {
-        KernelTimer kt_timer("bs_synd_kernel", st);
-        bs::bs_synd_kernel<E, true><<<synd_grid(nblocks, T), bs::kSyndGroups * T, 0, st>>>(
-            data, parity, nblocks, msg_len, reinterpret_cast<uint8_t *>(planes));
-        check_launch("bs_synd_kernel");
-    }
-    static const bool attrs = [] {  // once per process (a thread-safe static initialiser)
         cudaFuncSetAttribute(bs::bs_bm_kernel<E>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)bs::SolveGeom<E>::smem);
         cudaFuncSetAttribute(bs::bs_chien_kernel<E>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1769,6 +1754,25 @@ static void launch_bs_decode(const Rs256Code &c, uint8_t *data, uint8_t *parity,
         return true;
     }();
     (void)attrs;
+}
+
+template <int E>
+static void launch_bs_decode(const Rs256Code &c, uint8_t *data, uint8_t *parity, size_t nblocks, int msg_len,
+                             uint8_t *status, uint32_t *planes, cudaStream_t st) {
+    constexpr int T = bs::SyndCode<E>::T;
+    const size_t ntiles = ((nblocks + 31) / 32 + 31) / 32;
+    bs_decode_attrs<E>();
+    if constexpr (E == 32) {
+        KernelTimer kt_timer("bs_synd32_kernel", st);
+        bs::bs_synd32_kernel<<<(unsigned)ntiles, 256, bs::Synd32Geom::smem, st>>>(data, parity, nblocks, msg_len,
+                                                                                  planes);
+        check_launch("bs_synd32_kernel");
+    } else {
+        KernelTimer kt_timer("bs_synd_kernel", st);
+        bs::bs_synd_kernel<E, true><<<synd_grid(nblocks, T), bs::kSyndGroups * T, 0, st>>>(
+            data, parity, nblocks, msg_len, reinterpret_cast<uint8_t *>(planes));
+        check_launch("bs_synd_kernel");
+    }
     {
         KernelTimer kt_timer("bs_bm_kernel", st);
         bs::bs_bm_kernel<E><<<(unsigned)ntiles, 128, bs::SolveGeom<E>::smem, st>>>(nblocks, planes);
