@@ -102,8 +102,8 @@ __device__ __forceinline__ void nib_chunk(const uint4 *T, const uint4 *Tb, int m
 }
 
 // the 16-byte chunk at address ac as four words; chunks that reach past
-// either end of the buffer [d0, d1) are read by 4-byte words (the buffer is
-// 4-byte aligned), zero outside it
+// either end of the buffer [d0, d1) (d0 4-byte aligned) are read by 4-byte
+// words, the word holding d1 byte by byte, zero outside the buffer
 __device__ __forceinline__ void nib_load(uintptr_t ac, uintptr_t d0, uintptr_t d1, uint32_t (&w)[4]) {
     if (ac >= d0 && ac + 16 <= d1) {
         const uint4 q = __ldg(reinterpret_cast<const uint4 *>(ac));
@@ -112,7 +112,14 @@ __device__ __forceinline__ void nib_load(uintptr_t ac, uintptr_t d0, uintptr_t d
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
             const uintptr_t aw = ac + 4 * i;
-            w[i] = (aw >= d0 && aw < d1) ? __ldg(reinterpret_cast<const uint32_t *>(aw)) : 0u;
+            uint32_t v = 0u;
+            if (aw >= d0 && aw + 4 <= d1) {
+                v = __ldg(reinterpret_cast<const uint32_t *>(aw));
+            } else if (aw >= d0 && aw < d1) {
+                for (uintptr_t k = aw; k < d1; ++k)
+                    v |= (uint32_t)__ldg(reinterpret_cast<const uint8_t *>(k)) << (8 * (k - aw));
+            }
+            w[i] = v;
         }
     }
 }

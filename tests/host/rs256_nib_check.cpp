@@ -5,7 +5,8 @@
 // shuffles do.  The staged table is exactly the kernel's shared-memory part
 // (the line groups of degree indices 0 .. ml - 1) with poison on both sides,
 // and the message buffer starts at 0, 4, 8 or 12 bytes past a 16-byte
-// boundary with poison around it, so a read outside either shows up as a
+// boundary with poison around it (for 4 and 12 and an odd message length it
+// also ends inside a 4-byte word), so a read outside either shows up as a
 // wrong parity byte.
 // Usage: rs256_nib_check <seed> <blocks per case>; prints "bad N", exits 1 if
 // N > 0.
@@ -21,8 +22,11 @@ extern "C" {
 }
 using namespace ffgpu;
 
-static int run(const orc_rs256 *o, const std::vector<uint32_t> &tab, int ml, size_t nb, int offset,
+static int run(const orc_rs256 *o, const std::vector<uint32_t> &tab, int ml, size_t nb_even, int offset,
                std::mt19937 &g) {
+    // an odd block count for offsets 4 and 12: with an odd ml the buffer then
+    // ends inside a 4-byte word
+    const size_t nb = nb_even - ((offset & 4) ? 1 : 0);
     // staged table: ceil(ml / 4) line groups between poisoned guards
     const size_t groups = (size_t)(ml + 3) / 4, guard = kNibGroupQ;
     std::vector<uint4> stage(guard + groups * kNibGroupQ + guard);
