@@ -488,6 +488,15 @@ struct RecLayout {
 // shared-memory access below touches 32 different banks.
 __device__ __forceinline__ int swz(int g) { return g & 31; }
 
+// the n < 4 bytes at p (the last of an array) as the low bytes of a word,
+// the rest zero; out of line, so that the loads around it keep their
+// registers
+static __device__ __noinline__ uint32_t ldg_tail(const uint8_t *p, size_t n) {
+    uint32_t v = 0u;
+    for (size_t q = 0; q < n; ++q) v |= (uint32_t)__ldg(p + q) << (8 * q);
+    return v;
+}
+
 // Load window bytes [p0, p0 + 32) of every block of the tile from the segment
 // `base` (block b at base + b * seg_len; total bytes of the segment array in
 // `total`).  Positions at or beyond seg_len are never consumed.
@@ -507,8 +516,11 @@ __device__ __forceinline__ void load_window(uint32_t *buf, const uint8_t *__rest
                 const size_t a0 = start & ~(size_t)3;
                 sh[r] = (uint32_t)(start & 3) * 8;
 #pragma unroll
-                for (int i = 0; i < 9; ++i)
-                    w[r][i] = (a0 + 4 * i < total) ? __ldg(reinterpret_cast<const uint32_t *>(base + a0 + 4 * i)) : 0u;
+                for (int i = 0; i < 9; ++i) {
+                    const size_t aw = a0 + 4 * i;
+                    w[r][i] = aw + 4 <= total ? __ldg(reinterpret_cast<const uint32_t *>(base + aw))
+                                              : (aw < total ? ldg_tail(base + aw, total - aw) : 0u);
+                }
             } else {
 #pragma unroll
                 for (int i = 0; i < 9; ++i) w[r][i] = 0u;
@@ -1141,8 +1153,8 @@ struct Synd32Geom {
 };
 
 // cp.async of window w's words of the tile into raw: block b's word k at
-// raw[(b / 32) * kRawStride + (b % 32) * 9 + k].  Words outside the array
-// are zero-filled (no read).
+// raw[(b / 32) * kRawStride + (b % 32) * 9 + k].  Bytes outside the array
+// are zero-filled (not read).
 __device__ __forceinline__ void synd32_load(uint32_t *raw, const uint8_t *__restrict__ data,
                                             const uint8_t *__restrict__ parity, size_t nblocks, int msg_len,
                                             size_t first, int w) {
@@ -1152,18 +1164,25 @@ __device__ __forceinline__ void synd32_load(uint32_t *raw, const uint8_t *__rest
         // offsets relative to the tile's first data byte fit in 32 bits;
         // word q = 9 b + k of the window goes to thread q % 256, so that a
         // warp reads whole consecutive stretches of the tile
+        // bytes from tile0 to the end of the array, clamped: a window's
+        // offsets stay below 2^18.  Offsets precede the array only in the
+        // first tile (elsewhere tile0 >= 1024 > 224 bytes back).
         const long long tile0 = (long long)first * msg_len;
-        const long long total = (long long)(nblocks * (size_t)msg_len) - tile0;  // bytes from tile0 to the end
+        const long long left = (long long)(nblocks * (size_t)msg_len) - tile0;
+        const int total = left < (1 << 30) ? (int)left : (1 << 30);
+        const int lo = first == 0 ? 0 : -(1 << 30);
         const int c = msg_len - 224 + 32 * w;
         const uint8_t *tb = data + tile0;
         int b = t / 9, k = t - 9 * (t / 9);
 #pragma unroll 4
         for (int i = 0; i < 36; ++i) {
-            const long long ak = (long long)((b * msg_len + c) & ~3) + 4 * k;  // may precede the array
-            const bool in = ak >= -tile0 && ak < total;
+            const int ak = ((b * msg_len + c) & ~3) + 4 * k;  // may precede the array
+            const bool in = ak >= lo && ak < total;
+            // the word holding the array's last byte is read only up to it
+            const int nbytes = in ? min(4, total - ak) : 0;
             const uint32_t dst = sbase + (uint32_t)(((b >> 5) * Synd32Geom::kRawStride + (b & 31) * 9 + k) * 4);
             asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(in ? tb + ak : data),
-                         "r"(in ? 4 : 0)
+                         "r"(nbytes)
                          : "memory");
             // q += 256 = 9 * 28 + 4
             b += 28;
