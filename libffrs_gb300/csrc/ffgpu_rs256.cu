@@ -472,12 +472,23 @@ int ffgpu_rs256_encode_host(const ffgpu_rs256 *code, const uint8_t *buf, size_t 
         for (size_t b0 = 0; b0 < full || (k == 0 && tail); b0 += chunk, ++k) {
             const size_t n = std::min(chunk, full - b0);
             const bool last = b0 + n >= full;
-            const size_t in_bytes = n * message_len + (last ? tail : 0);
             const size_t out_bytes = (n + (last && tail ? 1 : 0)) * (size_t)c.ecc;
             const size_t i0 = b0 * message_len, o0 = b0 * (size_t)c.ecc;
-            FFGPU_CHECK_CUDA(cudaMemcpyAsync(d_in + i0, buf + i0, in_bytes, cudaMemcpyHostToDevice, pl.up()));
-            st = pl.compute(k);
-            if (n) rs256_encode(c, d_in + i0, n, (int)message_len, d_out + o0, st);
+            // within a chunk of 32 K blocks or more, the upload goes in four
+            // pieces and each piece's encode waits only for its own copy (the
+            // encode takes time in proportion to its blocks); the output
+            // stays one copy
+            const size_t nsub = n >= 32768 ? 4 : 1;
+            for (size_t q = 0; q < nsub; ++q) {
+                const size_t s0 = n * q / nsub, s1 = n * (q + 1) / nsub;
+                const size_t bytes = (s1 - s0) * message_len + (q + 1 == nsub && last ? tail : 0);
+                FFGPU_CHECK_CUDA(cudaMemcpyAsync(d_in + i0 + s0 * message_len, buf + i0 + s0 * message_len, bytes,
+                                                 cudaMemcpyHostToDevice, pl.up()));
+                st = pl.compute(k);  // waits for the copies issued so far
+                if (s1 > s0)
+                    rs256_encode(c, d_in + i0 + s0 * message_len, s1 - s0, (int)message_len,
+                                 d_out + o0 + s0 * (size_t)c.ecc, st);
+            }
             if (last && tail)
                 rs256_encode(c, d_in + full * message_len, 1, (int)tail, d_out + full * (size_t)c.ecc, st);
             st = pl.to_down(k);
