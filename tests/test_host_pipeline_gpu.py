@@ -114,3 +114,20 @@ def test_rsi16_host_chunks(ffrs_gpu, chunk, forced, bl, ecc):
     np.testing.assert_array_equal(st.astype(np.int16), np.where(so < 0, 255, so.astype(np.int16)))
     np.testing.assert_array_equal(np.frombuffer(bytes(mb), np.uint16).reshape(nb, ml), mo)
     np.testing.assert_array_equal(np.frombuffer(bytes(eb), np.uint16).reshape(nb, ecc), eo)
+
+
+def test_rs256_host_encode_split_upload(ffrs_gpu):
+    """An encode of 32,768 blocks or more in one chunk uploads in four pieces,
+    each encoded once its copy is in; with a ragged tail, from a pageable and
+    from a page-locked buffer, against the oracle."""
+    rng = np.random.Generator(np.random.PCG64(4242))
+    ecc, ml, nb, tail = 32, 223, 40003, 150
+    o = O.RS256(ecc, block_len=ml + ecc)
+    rs = ffrs_gpu.RS256(ecc_len=ecc)
+    buf = rng.integers(0, 256, size=nb * ml + tail, dtype=np.uint8)
+    want = np.concatenate([o.encode_blocks(buf[:nb * ml].reshape(nb, ml), threads=8).ravel(),
+                           O.RS256(ecc, block_len=tail + ecc).encode_blocks(buf[nb * ml:].reshape(1, tail)).ravel()])
+    np.testing.assert_array_equal(np.frombuffer(bytes(rs.encode(buf.tobytes())), np.uint8), want)
+    pinned = ffrs_gpu.create_buffer(buf.size)
+    np.frombuffer(pinned, np.uint8)[:] = buf
+    np.testing.assert_array_equal(np.frombuffer(bytes(rs.encode(pinned)), np.uint8), want)
