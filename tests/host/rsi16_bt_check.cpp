@@ -8,7 +8,8 @@
 //     the oracle's syndromes;
 //   bt_rev_bm: the lane Berlekamp-Massey on lazy values, against the
 //     canonical one of the warp-batch path (rsi16_rev_bm_lane): same length,
-//     same connection polynomial.
+//     same connection polynomial, on the syndromes of the received words and
+//     on synthetic syndrome columns.
 // ecc 32 and 64, block lengths from two chunks to 65536 words, random words
 // and words of all 65535 (the largest lazy sums).  The largest accumulator
 // seen is checked against the bound the code assumes (below 2^28 before the
@@ -146,6 +147,57 @@ static int run(size_t block_len, size_t nb, std::mt19937 &g) {
     return bad;
 }
 
+// bt_rev_bm against rsi16_rev_bm_lane on synthetic syndrome columns, not
+// only those of error patterns: random values, values that are zero with
+// probability 1/2 or 7/8, zero runs at either end, one non-zero value, and
+// values 0 / 65536 only; these reach the stalled and abnormal branches
+template <int N>
+static int run_bm_synthetic(size_t count, std::mt19937 &g) {
+    constexpr int T = N / 2;
+    char err[256];
+    orc_rsi16 *o = orc_rsi16_new(N * 4, N, 3, err, sizeof err);
+    if (!o) {
+        std::printf("oracle: %s\n", err);
+        return 1;
+    }
+    const uint32_t *ex = tab(o, 9), *lg = tab(o, 10);
+    std::vector<uint32_t> inv(65537);
+    for (uint32_t a = 0; a < 65537; ++a) inv[a] = ex[65536u - lg[a]];
+    std::vector<uint32_t> Scol(N * 33);
+    int bad = 0, abnormal = 0;
+    for (size_t t = 0; t < count; ++t) {
+        const int kind = (int)(t % 6);
+        for (int k = 0; k < N; ++k) {
+            uint32_t v = g() % 65537u;
+            if (kind == 1 && (g() & 1)) v = 0;
+            if (kind == 2 && (g() & 7)) v = 0;
+            if (kind == 3) {
+                const int cut = (int)(g() % N);
+                if ((t / 6) & 1 ? k < cut : k >= cut) v = 0;
+            }
+            if (kind == 4) v = k == (int)(t / 6 % N) ? v : 0;
+            if (kind == 5) v = (g() & 1) ? 65536u : 0u;
+            Scol[k * 33] = v;
+        }
+        int32_t Cl[T + 1];
+        uint32_t Cc[T + 1];
+        const uint32_t Ll = bt_rev_bm<T, N>(Scol.data(), inv.data(), Cl);
+        const uint32_t Lc = rsi16_rev_bm_lane<T>(Scol.data(), inv.data(), N, Cc);
+        abnormal += Lc == 0;
+        bool ok = Ll == Lc;
+        if (ok && Lc)
+            for (int i = 0; i <= T; ++i) ok &= (uint32_t)Cl[i] == Cc[i];
+        if (!ok) {
+            if (bad < 3) std::printf("synthetic berlekamp-massey: ecc %d case %zu kind %d: L %u, canonical %u\n", N, t,
+                                     kind, Ll, Lc);
+            ++bad;
+        }
+    }
+    std::printf("ecc %d: %zu synthetic columns, %d declined by both\n", N, count, abnormal);
+    orc_rsi16_free(o);
+    return bad;
+}
+
 int main(int argc, char **argv) {
     std::mt19937 g(argc > 1 ? (unsigned)std::atoi(argv[1]) : 1u);
     const size_t nb = argc > 2 ? (size_t)std::atoi(argv[2]) : 64;
@@ -154,6 +206,8 @@ int main(int argc, char **argv) {
     for (size_t bl : {128, 1024, 4096}) bad += run<64>(bl, nb, g);
     bad += run<32>(65536, 8, g);
     bad += run<64>(65536, 8, g);
+    bad += run_bm_synthetic<32>(nb * 200, g);
+    bad += run_bm_synthetic<64>(nb * 200, g);
     if (acc_max >= (1u << 28)) {
         std::printf("accumulator %u reached 2^28\n", acc_max);
         ++bad;
